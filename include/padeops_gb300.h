@@ -1,0 +1,162 @@
+/*
+ * padeops_gb300.h -- C ABI of the GB300 compact-operator library.
+ *
+ * Drop-in boundary for the PadeOps derivative/filter objects.  Each reference Fortran
+ * type (cd06, cd10, cf90, gaussian, cd06stagg) becomes an opaque `pade_op` handle; each
+ * type-bound procedure becomes one function with the same argument meaning.  A Fortran
+ * shim keeps the reference's module/type names, stores the handle as type(c_ptr) and
+ * calls these functions through ISO_C_BINDING.
+ *
+ * Conventions
+ *  - Arrays are column-major (Fortran order, x fastest), FP64, as in the reference.
+ *  - Field pointers may be DEVICE pointers (the call is asynchronous on `stream`, safe
+ *    to capture in a CUDA graph) or HOST pointers (the library stages the data through
+ *    device memory and returns after the result is back in host memory).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ *  - Complex arrays (`*_cmplx`) are complex(rkind): interleaved (re, im) FP64 pairs.
+ *  - Every function returns a status.  Positive values below 1000 are the reference's own
+ *    init `ierr` / GracefulExit codes, so a shim can forward them unchanged; values from
+ *    1000 up are library errors.  The library never aborts the process.
+ */
+#ifndef PADEOPS_GB300_H
+#define PADEOPS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PADE_OK 0
+#define PADE_EREF_NONPERIODIC_N 2 /* cd06/cd10 init: n < 8 (cd06.F90:181, cd10.F90:224, 270) */
+#define PADE_EREF_PERIODIC_N 3    /* cd06 init periodic: n < 6 (cd06.F90:158) */
+#define PADE_EREF_FILTER_N 7      /* cf90 init: n < 10 (cf90.F90:128, 166) */
+#define PADE_EREF_STAGG_N 21      /* cd06stagg init: n <= 4 (cd06stagg.F90:183, 218) */
+#define PADE_EREF_BC 324          /* boundary code outside {0,1,-1} (cd10.F90:2045; cf90.F90:1036) */
+#define PADE_EINVAL 1001
+#define PADE_ENOMEM 1002
+#define PADE_ECUDA 1003
+#define PADE_ENOTSUP 1004
+#define PADE_ETIMEOUT 1005
+#define PADE_ERANGE 1006 /* an input left the double-float path's range (|f| in [2^-74, 2^127)) */
+
+/* ---- arithmetic paths (pade_set_path) ---- */
+#define PADE_PATH_DF 0     /* default: double-float arithmetic on the FP32 pipes, FP64 in/out */
+#define PADE_PATH_NATIVE 1 /* native FP64 arithmetic, one thread per line */
+#define PADE_PATH_FP32 2   /* FP32 in/out (pade_apply only) */
+
+typedef struct pade_op_s* pade_op;
+
+/* ---- cd06: 6th-order collocated compact derivative (src/derivatives/cd06.F90) ---- */
+/* replaces cd06%init(n, dx, periodic, bc1, bcn) -> ierr   (cd06.F90:129-201) */
+int pade_cd06_init(pade_op* op, int n, double dx, int periodic, int bc1, int bcn);
+/* replace cd06%dd1/dd2/dd3(f, df, na, nb)   (cd06.F90:775-839) */
+int pade_cd06_dd1(pade_op op, const double* f, double* df, int na, int nb, void* stream);
+int pade_cd06_dd2(pade_op op, const double* f, double* df, int na, int nb, void* stream);
+int pade_cd06_dd3(pade_op op, const double* f, double* df, int na, int nb, void* stream);
+/* periodic second derivative; upstream cd06.F90:745-773 and 492-513 leave it incomplete
+ * (derivatives.F90:525 GracefulExit); here completed with 1/dx^2 and the LU2 solve.
+ * Non-periodic objects return PADE_ENOTSUP like the reference's GracefulExit. */
+int pade_cd06_d2d1(pade_op op, const double* f, double* df, int na, int nb, void* stream);
+int pade_cd06_d2d2(pade_op op, const double* f, double* df, int na, int nb, void* stream);
+int pade_cd06_d2d3(pade_op op, const double* f, double* df, int na, int nb, void* stream);
+
+/* ---- cd10: 10th-order collocated compact derivative (src/derivatives/cd10.F90) ---- */
+/* replaces cd10%init(n, dx, periodic, bc1, bcn) -> ierr   (cd10.F90:195-315) */
+int pade_cd10_init(pade_op* op, int n, double dx, int periodic, int bc1, int bcn);
+/* replace cd10%dd1..dd3(f, df, na, nb, bc1_, bcn_)   (cd10.F90:2029-2237);
+ * the reference's omitted optional bc arguments are 0 */
+int pade_cd10_dd1(pade_op op, const double* f, double* df, int na, int nb, int bc1, int bcn, void* stream);
+int pade_cd10_dd2(pade_op op, const double* f, double* df, int na, int nb, int bc1, int bcn, void* stream);
+int pade_cd10_dd3(pade_op op, const double* f, double* df, int na, int nb, int bc1, int bcn, void* stream);
+/* replace cd10%d2d1..d2d3(f, df, na, nb, bc1_, bcn_)   (cd10.F90:2239-2447) */
+int pade_cd10_d2d1(pade_op op, const double* f, double* df, int na, int nb, int bc1, int bcn, void* stream);
+int pade_cd10_d2d2(pade_op op, const double* f, double* df, int na, int nb, int bc1, int bcn, void* stream);
+int pade_cd10_d2d3(pade_op op, const double* f, double* df, int na, int nb, int bc1, int bcn, void* stream);
+
+/* ---- cf90: 8th-order compact filter (src/filters/cf90.F90) ---- */
+/* replaces cf90%init(n, periodic) -> ierr   (cf90.F90:107-175) */
+int pade_cf90_init(pade_op* op, int n, int periodic);
+/* replace cf90%filter1/filter2/filter3(f, ff, na, nb, bc1_, bcn_)   (cf90.F90:1020-1228) */
+int pade_cf90_filter1(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn, void* stream);
+int pade_cf90_filter2(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn, void* stream);
+int pade_cf90_filter3(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn, void* stream);
+/* replaces cf90%filter3 on complex(rkind) (cf90.F90:1230-1251); the reference always
+ * solves with penta_nn here, this entry uses the factorisation of (bc1, bcn) */
+int pade_cf90_filter3_cmplx(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn,
+                            void* stream);
+
+/* ---- gaussian: explicit 9-point filter of width 4 dx (src/filters/gaussian.F90) ---- */
+/* replaces gaussian%init(n, periodic) -> ierr   (gaussian.F90:74-93) */
+int pade_gaussian_init(pade_op* op, int n, int periodic);
+/* replace gaussian%filter1/filter2/filter3 (gaussian.F90:104-582) */
+int pade_gaussian_filter1(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn, void* stream);
+int pade_gaussian_filter2(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn, void* stream);
+int pade_gaussian_filter3(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn, void* stream);
+int pade_gaussian_filter3_cmplx(pade_op op, const double* f, double* ff, int na, int nb, int bc1, int bcn,
+                                void* stream);
+
+/* ---- cd06stagg: staggered 6th-order compact operators (src/derivatives/cd06stagg.F90) ---- */
+/* replace the generic cd06stagg%init: init_periodic(n, dx) (cd06stagg.F90:170-195) and
+ * init_nonperiodic(n, dx, isTopEven, isBotEven, isTopSided, isBotSided) (197-232) */
+int pade_cd06stagg_init_periodic(pade_op* op, int n, double dx);
+int pade_cd06stagg_init_nonperiodic(pade_op* op, int n, double dx, int isTopEven, int isBotEven, int isTopSided,
+                                    int isBotSided);
+/* replace ddz_E2C/C2E/C2C/E2E, d2dz2_C2C/E2E, InterpZ_E2C/C2E, REAL overloads
+ * (cd06stagg.F90:820-1059).  Input (n1,n2,nin), output (n1,n2,nout); E = n+1 points. */
+int pade_cd06stagg_ddz_E2C(pade_op op, const double* fE, double* dfC, int n1, int n2, void* stream);
+int pade_cd06stagg_ddz_C2E(pade_op op, const double* fC, double* dfE, int n1, int n2, void* stream);
+int pade_cd06stagg_ddz_C2C(pade_op op, const double* fC, double* dfC, int n1, int n2, void* stream);
+int pade_cd06stagg_ddz_E2E(pade_op op, const double* fE, double* dfE, int n1, int n2, void* stream);
+int pade_cd06stagg_d2dz2_C2C(pade_op op, const double* fC, double* d2fC, int n1, int n2, void* stream);
+int pade_cd06stagg_d2dz2_E2E(pade_op op, const double* fE, double* d2fE, int n1, int n2, void* stream);
+int pade_cd06stagg_InterpZ_E2C(pade_op op, const double* fE, double* IfC, int n1, int n2, void* stream);
+int pade_cd06stagg_InterpZ_C2E(pade_op op, const double* fC, double* IfE, int n1, int n2, void* stream);
+/* CMPLX overloads of the same eight procedures (complex(rkind) arrays) */
+int pade_cd06stagg_ddz_E2C_cmplx(pade_op op, const double* fE, double* dfC, int n1, int n2, void* stream);
+int pade_cd06stagg_ddz_C2E_cmplx(pade_op op, const double* fC, double* dfE, int n1, int n2, void* stream);
+int pade_cd06stagg_ddz_C2C_cmplx(pade_op op, const double* fC, double* dfC, int n1, int n2, void* stream);
+int pade_cd06stagg_ddz_E2E_cmplx(pade_op op, const double* fE, double* dfE, int n1, int n2, void* stream);
+int pade_cd06stagg_d2dz2_C2C_cmplx(pade_op op, const double* fC, double* d2fC, int n1, int n2, void* stream);
+int pade_cd06stagg_d2dz2_E2E_cmplx(pade_op op, const double* fE, double* d2fE, int n1, int n2, void* stream);
+int pade_cd06stagg_InterpZ_E2C_cmplx(pade_op op, const double* fE, double* IfC, int n1, int n2, void* stream);
+int pade_cd06stagg_InterpZ_C2E_cmplx(pade_op op, const double* fC, double* IfE, int n1, int n2, void* stream);
+
+/* ---- common ---- */
+/* replaces the destroy procedure of every type above */
+int pade_destroy(pade_op op);
+/* arithmetic path for the FP64 entry points of this object (PADE_PATH_DF or _NATIVE) */
+int pade_set_path(pade_op op, int path);
+/* Generic entry: family operation `opcode` (cd06/cd10: 1 = first, 2 = second derivative;
+ * cf90/gaussian: 0; cd06stagg: 0 ddz_E2C, 1 ddz_C2E, 2 ddz_C2C, 3 ddz_E2E, 4 d2dz2_C2C,
+ * 5 d2dz2_E2E, 6 InterpZ_E2C, 7 InterpZ_C2E) along direction `dir` (1, 2, 3) of an array
+ * whose other two extents are na, nb.  path PADE_PATH_FP32 takes float arrays. */
+int pade_apply(pade_op op, int opcode, int dir, int is_complex, const void* f, void* out, int na, int nb, int bc1,
+               int bcn, int path, void* stream);
+/* Read and clear the sticky error flags raised by asynchronous device-pointer calls
+ * (synchronises the device).  *flags != 0 means some input left the df range. */
+int pade_get_status(pade_op op, int* flags);
+/* line lengths of an operation: input and output points along the operated direction */
+int pade_get_lengths(pade_op op, int opcode, int* n_in, int* n_out);
+const char* pade_strerror(int status);
+
+/* ---- host-only plan inspection (no GPU needed; never called by the entry points above) ----
+ * family: 0 cd06, 1 cd10, 2 cf90, 3 gaussian, 4 cd06stagg.
+ * params: cd06/cd10 {n, dx, periodic}; cf90/gaussian {n, periodic};
+ *         cd06stagg {n, dx, periodic, isTopEven, isBotEven, isTopSided, isBotSided}. */
+#define PADE_FAMILY_CD06 0
+#define PADE_FAMILY_CD10 1
+#define PADE_FAMILY_CF90 2
+#define PADE_FAMILY_GAUSSIAN 3
+#define PADE_FAMILY_CD06STAGG 4
+/* Apply the device plan's arithmetic (banded LU + cyclic correction) in FP64 on the CPU to
+ * `nlines` contiguous lines; lets tests validate operator plans without a GPU. */
+int pade_plan_check(int family, const double* params, int opcode, int bc1, int bcn, const double* f, double* out,
+                    int nlines);
+/* Dense n_out x n_in matrix of the operator (row-major), for tests and the dense path. */
+int pade_plan_dense(int family, const double* params, int opcode, int bc1, int bcn, double* mat, int* n_in,
+                    int* n_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PADEOPS_GB300_H */

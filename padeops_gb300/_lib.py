@@ -1,0 +1,107 @@
+"""ctypes binding of ``libpadeops_gb300.so`` (the C ABI in include/padeops_gb300.h).
+
+The compute path is the native library; there is no Python or CPU fallback.  Loading
+fails loudly when the library is missing: run ``padeops_gb300.build.build()`` (or
+``__graft_entry__.build()``) first.
+"""
+import ctypes
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libpadeops_gb300.so")
+HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "padeops_gb300.h")
+
+PADE_OK = 0
+PADE_EREF_NONPERIODIC_N = 2
+PADE_EREF_PERIODIC_N = 3
+PADE_EREF_FILTER_N = 7
+PADE_EREF_STAGG_N = 21
+PADE_EREF_BC = 324
+PADE_EINVAL = 1001
+PADE_ENOMEM = 1002
+PADE_ECUDA = 1003
+PADE_ENOTSUP = 1004
+PADE_ETIMEOUT = 1005
+PADE_ERANGE = 1006
+
+PATH_DF = 0
+PATH_NATIVE = 1
+PATH_FP32 = 2
+
+FAMILY = {"cd06": 0, "cd10": 1, "cf90": 2, "gaussian": 3, "cd06stagg": 4}
+STAGG_OPS = ("ddz_E2C", "ddz_C2E", "ddz_C2C", "ddz_E2E", "d2dz2_C2C", "d2dz2_E2E", "InterpZ_E2C", "InterpZ_C2E")
+
+_lib = None
+
+
+class PadeError(RuntimeError):
+    """A non-zero status from the library (the reference would GracefulExit here)."""
+
+    def __init__(self, code, where=""):
+        self.code = code
+        msg = strerror(code) if _lib is not None else str(code)
+        super().__init__(f"{where}: status {code} ({msg})" if where else f"status {code} ({msg})")
+
+
+def exported_symbols():
+    """Names of the functions declared in include/padeops_gb300.h."""
+    txt = open(HEADER_PATH).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\bint\s+(pade_\w+)\s*\(", txt)) | set(re.findall(r"char\*\s+(pade_\w+)\s*\(", txt)))
+
+
+def lib():
+    """Load the library and declare argument types (once)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} not built; run padeops_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    pop = ctypes.POINTER(ctypes.c_void_p)
+    pi = ctypes.POINTER(ctypes.c_int)
+    dp = ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "pade_cd06_init": [pop, i, d, i, i, i],
+        "pade_cd10_init": [pop, i, d, i, i, i],
+        "pade_cf90_init": [pop, i, i],
+        "pade_gaussian_init": [pop, i, i],
+        "pade_cd06stagg_init_periodic": [pop, i, d],
+        "pade_cd06stagg_init_nonperiodic": [pop, i, d, i, i, i, i],
+        "pade_destroy": [vp],
+        "pade_set_path": [vp, i],
+        "pade_apply": [vp, i, i, i, vp, vp, i, i, i, i, i, vp],
+        "pade_get_status": [vp, pi],
+        "pade_get_lengths": [vp, i, pi, pi],
+        "pade_plan_check": [i, dp, i, i, i, dp, dp, i],
+        "pade_plan_dense": [i, dp, i, i, i, dp, pi, pi],
+    }
+    for nm in ("dd1", "dd2", "dd3", "d2d1", "d2d2", "d2d3"):
+        sig[f"pade_cd06_{nm}"] = [vp, vp, vp, i, i, vp]
+        sig[f"pade_cd10_{nm}"] = [vp, vp, vp, i, i, i, i, vp]
+    for fam in ("cf90", "gaussian"):
+        for nm in ("filter1", "filter2", "filter3", "filter3_cmplx"):
+            sig[f"pade_{fam}_{nm}"] = [vp, vp, vp, i, i, i, i, vp]
+    for nm in STAGG_OPS:
+        sig[f"pade_cd06stagg_{nm}"] = [vp, vp, vp, i, i, vp]
+        sig[f"pade_cd06stagg_{nm}_cmplx"] = [vp, vp, vp, i, i, vp]
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.pade_strerror.argtypes = [i]
+    L.pade_strerror.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def strerror(code):
+    return lib().pade_strerror(int(code)).decode()
+
+
+def check(rc, where=""):
+    if rc != PADE_OK:
+        raise PadeError(rc, where)
+    return rc

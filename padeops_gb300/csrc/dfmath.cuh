@@ -1,0 +1,96 @@
+// Double-float ("df") arithmetic on the FP32 pipes.
+//
+// A df value is an unevaluated sum h + l of two floats.  GB300 runs FP64 (and the
+// FP64<->FP32 conversions) at 1/56 of the FP32 rate, so the FP64 operator path keeps its
+// arithmetic in df: inputs are split with integer instructions, sums and products use
+// the classical error-free transformations (Knuth's TwoSum, FMA-based TwoProduct), and
+// results go back to FP64 with integer instructions plus one FP64 add.  All float
+// operations use the _rn intrinsics so the compiler cannot contract them into FMAs,
+// which would break the error-free transformations.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace pade {
+
+struct dfv {
+    float h, l;
+};
+
+// Split an FP64 value into (hi, lo): hi keeps the leading 24 significant bits
+// (truncated), lo the remaining 29 bits rounded to float.  Exact to 2^-47 relative.
+// Full precision needs the biased FP64 exponent in [949, 1150] (|d| in [2^-74, 2^127));
+// other non-zero values set `bad` and are flushed (the host reports PADE_ERANGE).
+__device__ __forceinline__ dfv df_from_double(double d, unsigned& bad) {
+    const unsigned lo32 = (unsigned)__double2loint(d);
+    const unsigned hi32 = (unsigned)__double2hiint(d);
+    const unsigned ex = hi32 & 0x7FF00000u;
+    const unsigned sign = hi32 & 0x80000000u;
+    const bool ok = (ex - (949u << 20)) <= ((1150u - 949u) << 20);
+    const bool zero = ((hi32 & 0x7FFFFFFFu) | lo32) == 0u;
+    bad |= (unsigned)(!ok && !zero);
+    const unsigned hb = (((hi32 - (896u << 20)) << 3) & 0x7FFFFFF8u) | (lo32 >> 29) | sign;
+    const float lf = __uint2float_rn(lo32 & 0x1FFFFFFFu);
+    const unsigned sb = (ex - (948u << 20)) << 3;
+    float lo = __fmul_rn(lf, __uint_as_float(sb));
+    lo = __uint_as_float(__float_as_uint(lo) ^ sign);
+    dfv r;
+    r.h = ok ? __uint_as_float(hb) : 0.0f;
+    r.l = ok ? lo : 0.0f;
+    return r;
+}
+
+// Exact float -> double with integer instructions (zero and subnormal floats map to 0).
+__device__ __forceinline__ double float_bits_to_double(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned mag = b & 0x7FFFFFFFu;
+    const unsigned sg = b & 0x80000000u;
+    const bool z = mag < 0x00800000u;
+    const unsigned hi = z ? sg : (((mag >> 3) + (896u << 20)) | sg);
+    const unsigned lo = z ? 0u : (b << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// (h + l) rounded once to FP64: two exact conversions and one FP64 add.
+__device__ __forceinline__ double df_to_double(dfv a) {
+    return __dadd_rn(float_bits_to_double(a.h), float_bits_to_double(a.l));
+}
+
+__device__ __forceinline__ dfv df_zero() { return dfv{0.0f, 0.0f}; }
+
+// a + b, high parts by TwoSum (exact), low parts by one rounded add; not renormalised
+__device__ __forceinline__ dfv df_add(dfv a, dfv b) {
+    const float s = __fadd_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    return dfv{s, __fadd_rn(e, __fadd_rn(a.l, b.l))};
+}
+
+__device__ __forceinline__ dfv df_neg(dfv a) { return dfv{-a.h, -a.l}; }
+__device__ __forceinline__ dfv df_sub(dfv a, dfv b) { return df_add(a, df_neg(b)); }
+
+// FastTwoSum renormalisation (|h| >= |l| holds for every value this code produces)
+__device__ __forceinline__ dfv df_norm(dfv a) {
+    const float s = __fadd_rn(a.h, a.l);
+    return dfv{s, __fsub_rn(a.l, __fsub_rn(s, a.h))};
+}
+
+// a * c (TwoProduct of the high parts, cross terms in FP32); not renormalised
+__device__ __forceinline__ dfv df_mul(dfv a, dfv c) {
+    const float ph = __fmul_rn(a.h, c.h);
+    float pe = __fmaf_rn(a.h, c.h, -ph);
+    pe = __fmaf_rn(a.h, c.l, pe);
+    pe = __fmaf_rn(a.l, c.h, pe);
+    return dfv{ph, pe};
+}
+
+__device__ __forceinline__ dfv df_shfl_up(dfv v, unsigned d, int w) {
+    return dfv{__shfl_up_sync(0xffffffffu, v.h, d, w), __shfl_up_sync(0xffffffffu, v.l, d, w)};
+}
+__device__ __forceinline__ dfv df_shfl_down(dfv v, unsigned d, int w) {
+    return dfv{__shfl_down_sync(0xffffffffu, v.h, d, w), __shfl_down_sync(0xffffffffu, v.l, d, w)};
+}
+__device__ __forceinline__ dfv df_shfl_idx(dfv v, int src, int w) {
+    return dfv{__shfl_sync(0xffffffffu, v.h, src, w), __shfl_sync(0xffffffffu, v.l, src, w)};
+}
+
+}  // namespace pade

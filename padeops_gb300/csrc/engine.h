@@ -1,0 +1,70 @@
+// Device side of the compact line operators: plan upload and kernel launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "chunkplan.h"
+#include "plan.h"
+
+namespace pade {
+
+// Arithmetic path used for an operator application.
+enum Path : int {
+    PATH_DF = 0,      // double-float arithmetic on the FP32 pipes, FP64 in/out (default)
+    PATH_NATIVE = 1,  // native FP64 arithmetic, one thread per line (reference-order baseline)
+    PATH_FP32 = 2,    // FP32 in/out, FP32 arithmetic, chunked engine
+};
+
+// Strided description of the lines of one array: line l = a + na*b, element i of line l at
+// a*fa + b*fb + i*fp (input) and a*oa + b*ob + i*op (output), in elements.
+struct LineSet {
+    long nlines, na;
+    long fa, fb, fp;
+    long oa, ob, op;
+};
+
+// Parameters of the chunked kernel, passed by value.
+struct ChunkParams {
+    int m, nout, ns, P, Pp, nsteps, L, LS;
+    int has_center, center_off, npair, nlo, nhi, tw;
+    int pair_op[kMaxPairs], pair_om[kMaxPairs], pair_sign[kMaxPairs];
+    F2 center_c, pair_c[kMaxPairs];
+    F2 ca1, ca2;
+    const int* tidx;
+    const F2* tc;
+    const F2* rc;  // ns x 5 : g, a1, a2, b1, b2
+    const F2* fscan;
+    const F2* bscan;
+    const F2* fwrap;
+    const F2* bwrap;
+};
+
+class DevicePlan {
+   public:
+    DevicePlan() = default;
+    DevicePlan(const DevicePlan&) = delete;
+    DevicePlan& operator=(const DevicePlan&) = delete;
+    ~DevicePlan();
+    int upload(const HostPlan& hp);  // allocates device memory (not graph-capturable)
+    const HostPlan& host() const { return hp_; }
+    PlanView<double> view_d() const { return vd_; }
+    bool chunk_ok() const { return cok_; }
+    const ChunkPlanHost& chunk_host() const { return ch_; }
+    ChunkParams chunk_df() const { return cdf_; }
+    ChunkParams chunk_f32() const { return cf32_; }
+    int chunk_M() const { return ch_.M; }
+
+   private:
+    HostPlan hp_;
+    ChunkPlanHost ch_;
+    bool cok_ = false;
+    void* dev_ = nullptr;
+    PlanView<double> vd_{};
+    ChunkParams cdf_{}, cf32_{};
+};
+
+// Launch the operator on a set of lines.  f/out are device pointers to double (FP64 paths)
+// or float (PATH_FP32).  status (device word) collects out-of-range flags of the df path.
+int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const LineSet& ls, unsigned* status,
+                 cudaStream_t s);
+
+}  // namespace pade
