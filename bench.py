@@ -1,0 +1,332 @@
+"""Benchmark of the compact-operator hot path on GB300.
+
+Workload (a "step"): CD10 first and second derivatives plus the CF90 compact filter along
+x, y (periodic) and z (non-periodic, one-sided closures, bc 0) of a 256^3 FP64 field --
+nine operator applications.  Fields are seeded random-mode sums (32 modes, |k_i| <= 64,
+amplitudes N(0,1)|k|^-5/6, tanh(4(z-0.5)) profile in z), standing in for the reference's
+data.  Metric: operator throughput in Gpts/s (points x operator applications per second).
+
+  value     device throughput: inputs resident in HBM, CUDA events around K steps
+  e2e       the same step through the reference-named C-ABI entry points with pinned
+            HOST buffers (host->device copy, kernel, device->host copy per call)
+  roofline  the chunked double-float kernel (every launch of the step), algorithmic
+            16 B/point (read f once, write the result once) against the measured HBM copy
+            bandwidth in MEASURED_PEAKS.json
+  cpu_baseline  the oracle port of the reference algorithm on the host cores (OpenMP over
+            lines), on the same workload
+
+`--impl reference` times the oracle port alone (the Fortran reference cannot be built on
+this hardware: no Fortran compiler or MPI) and prints its line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 256
+NMODES, KMAX, SEED = 32, 64, 2
+OPS = [("cd10 d1", 1), ("cd10 d2", 2), ("cf90", 0)]  # (name, opcode)
+DIRS = (1, 2, 3)
+BYTES_PER_POINT = 16  # FP64 read + write
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_field():
+    from tests.fields import random_modes
+
+    return random_modes((N, N, N), NMODES, KMAX, SEED, z_nonperiodic=True, profile=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if len(r) >= 8 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 8 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) < 8:
+                continue
+            for nm, v in zip(names, r[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def setup_objects(P):
+    dx = 2 * np.pi / N
+    dz = 1.0 / (N - 1)
+    cx = P.cd10()
+    assert cx.init(N, dx, True) == 0
+    cz = P.cd10()
+    assert cz.init(N, dz, False) == 0
+    fx = P.cf90()
+    assert fx.init(N, True) == 0
+    fz = P.cf90()
+    assert fz.init(N, False) == 0
+    return {("cd10", 1): cx, ("cd10", 2): cx, ("cd10", 3): cz, ("cf90", 1): fx, ("cf90", 2): fx, ("cf90", 3): fz}
+
+
+def step_plan(objs):
+    """The nine (object, opcode, dir) applications of one step."""
+    plan = []
+    for name, opc in OPS:
+        fam = name.split()[0]
+        for d in DIRS:
+            plan.append((objs[(fam, d)], opc, d, f"{name} dir{d}"))
+    return plan
+
+
+def run_device(args, P, torch):
+    dev = torch.device("cuda", 0)
+    f_host = make_field()
+    plan = step_plan(setup_objects(P))
+    nops = len(plan)
+    # one input and one output field per application: 2.4 GB per step >> L2 (no reuse)
+    base = torch.from_numpy(np.ascontiguousarray(f_host.T)).to(dev)
+    ins = [base.clone() for _ in range(nops)]
+    outs = [torch.empty_like(base) for _ in range(nops)]
+    del base
+    stream = torch.cuda.current_stream(dev)
+    npts = N ** 3
+
+    def one_step(ev=None):
+        for k, (obj, opc, d, _) in enumerate(plan):
+            if ev is not None:
+                ev[k][0].record(stream)
+            obj.apply(opc, d, ins[k], outs[k], N, N, 0, 0)
+            if ev is not None:
+                ev[k][1].record(stream)
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    # device-timed region (events on the launching stream) with per-launch events
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nops)]
+           for _ in range(args.steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(0)
+    clk.start()
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for s in range(args.steps):
+        one_step(evs[s])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = t0.elapsed_time(t1)
+    per_launch = np.zeros(nops)
+    for s in range(args.steps):
+        for k in range(nops):
+            per_launch[k] += evs[s][k][0].elapsed_time(evs[s][k][1])
+    per_launch /= args.steps
+    return ms / args.steps, per_launch, clocks, plan, f_host
+
+
+def run_e2e(args, P, torch, f_host):
+    """Same step through the reference-named entry points with pinned host buffers."""
+    objs = setup_objects(P)
+    plan = step_plan(objs)
+    host_in = torch.from_numpy(np.ascontiguousarray(f_host.T)).pin_memory()
+    host_out = [torch.empty_like(host_in).pin_memory() for _ in range(3)]
+    calls = []
+    for k, (obj, opc, d, name) in enumerate(plan):
+        fam = name.split()[0]
+        out = host_out[k % 3]
+        if fam == "cd10":
+            fn = getattr(obj, ("dd" if opc == 1 else "d2d") + str(d))
+            bc = (0, 0)
+            calls.append(lambda fn=fn, out=out, bc=bc: fn(host_in, out, N, N, *bc))
+        else:
+            fn = getattr(obj, f"filter{d}")
+            calls.append(lambda fn=fn, out=out: fn(host_in, out, N, N, 0, 0))
+    for _ in range(max(1, args.warmup)):
+        for c in calls:
+            c()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        for c in calls:
+            c()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t) / args.steps
+    nb = N ** 3 * 8 * len(calls)
+    return dt, nb, nb
+
+
+def cpu_baseline(args, f_host, steps=None):
+    """The oracle port (reference algorithm, OpenMP over lines) on the same workload."""
+    from oracle import oracle as O
+
+    O.build()
+    dx = 2 * np.pi / N
+    dz = 1.0 / (N - 1)
+    work = []
+    for name, opc in OPS:
+        for d in DIRS:
+            per = d != 3
+            h = dx if per else dz
+            if name.startswith("cd10"):
+                work.append(lambda d=d, per=per, h=h, o=opc: O.cd10(f_host, h, periodic=per, order=o, dir=d))
+            else:
+                work.append(lambda d=d, per=per: O.cf90(f_host, periodic=per, dir=d))
+    work[0]()  # warm-up (page-in)
+    n = steps or 1
+    t = time.perf_counter()
+    for _ in range(n):
+        for w in work:
+            w()
+    dt = (time.perf_counter() - t) / n
+    gpts = len(work) * N ** 3 / dt / 1e9
+    return gpts, O.threads(), dt
+
+
+def traffic_per_launch():
+    p = os.path.join(ROOT, "profiles", "chunk_kernel_traffic.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return d.get("dram_bytes_per_launch_256cubed")
+        except Exception:
+            return None
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    metric = "CD10 d1+d2 and CF90 operator throughput, 256^3 FP64 (x,y periodic, z one-sided)"
+    config = {"workload": "cd10 d1, cd10 d2, cf90 along x, y (periodic) and z (non-periodic, bc 0) on a "
+                          "256^3 FP64 field; 9 operator applications per step",
+              "grid": [N, N, N], "ops_per_step": 9, "fields": "seeded 32-mode sum, |k|<=64, tanh z profile",
+              "l2": "each application reads its own 134 MB field and writes its own output (2.4 GB per step, "
+                    "larger than the 126 MB L2); no flush needed",
+              "parallelism": "replicas" if world > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        f_host = make_field()
+        gpts, cores, dt = cpu_baseline(args, f_host, steps=max(1, min(args.steps, 3)))
+        line = {"metric": metric, "value": gpts, "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
+                "cpu_baseline": {"value": gpts, "unit": "Gpts/s", "cores": cores, "kind": "port",
+                                 "sample": "full 256^3 step (9 applications), oracle C port with OpenMP over lines"},
+                "e2e": {"value": gpts, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    import padeops_gb300 as P
+    from padeops_gb300 import build as B
+
+    B.build()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    ms_step, per_launch, clocks, plan, f_host = run_device(args, P, torch)
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+        dist.barrier()
+    npts = N ** 3
+    value = world * len(plan) * npts / (ms_step * 1e-3) / 1e9
+    e2e = None
+    if not args.no_e2e:
+        dt, hb, db = run_e2e(args, P, torch, f_host)
+        e2e = {"value": world * len(plan) * npts / dt / 1e9, "unit": "Gpts/s", "h2d_bytes_per_step": hb,
+               "d2h_bytes_per_step": db}
+    peak, src = peaks()
+    t_kern = float(per_launch.sum())
+    achieved = len(plan) * npts * BYTES_PER_POINT / (t_kern * 1e-3) / 1e9
+    tr = traffic_per_launch()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": tr, "peak_source": src,
+            "kernel": "k_chunk<ArDF> (double-float chunked scan), mean over the 9 launches",
+            "algorithmic_bytes_per_launch": npts * BYTES_PER_POINT,
+            "per_launch_ms": {p[3]: round(float(v), 4) for p, v in zip(plan, per_launch)}}
+    cb = None
+    if rank == 0:
+        gpts, cores, dt = cpu_baseline(args, f_host, steps=1)
+        cb = {"value": gpts, "unit": "Gpts/s", "cores": cores, "kind": "port",
+              "sample": "one full 256^3 step (9 applications), oracle C port with OpenMP over lines"}
+    if rank == 0:
+        line = {"metric": metric, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64 (double-float arithmetic)", "data": "synthetic",
+                "config": config, "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": len(plan) * args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

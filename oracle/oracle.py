@@ -41,9 +41,16 @@ def lib():
         _lib.oracle_cf90.argtypes = [i, i, i, i, i, dp, dp, i, i, i]
         _lib.oracle_gaussian.argtypes = [i, i, i, i, i, dp, dp, i, i, i]
         _lib.oracle_stagg.argtypes = [i, d, i, i, i, i, i, i, i, dp, dp, i, i, i]
+        _lib.oracle_threads.argtypes = []
+        _lib.oracle_threads.restype = ctypes.c_int
         for fn in ("oracle_cd06", "oracle_cd10", "oracle_cf90", "oracle_gaussian", "oracle_stagg"):
             getattr(_lib, fn).restype = ctypes.c_int
     return _lib
+
+
+def threads():
+    """Host threads the oracle's line loops use (OpenMP)."""
+    return lib().oracle_threads()
 
 
 def _as_f3(f):

@@ -23,6 +23,9 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define ORACLE_API __attribute__((visibility("default")))
 
@@ -1422,6 +1425,8 @@ static void for_lines(int dir, const int *sin, const int *sout, const double *f,
     long fps, las, lbs, gps, glas, glbs, fla_n, gla_n;
     long nl = lines_of(dir, sin[0], sin[1], sin[2], &fps, &fla_n, &las, &lbs);
     lines_of(dir, sout[0], sout[1], sout[2], &gps, &gla_n, &glas, &glbs);
+    /* lines are independent: threads over lines mirror the reference's pencil ranks */
+#pragma omp parallel for schedule(static)
     for (long l = 0; l < nl; l++) {
         long a = l % fla_n, b = l / fla_n;
         fn(ctx, f + a * las + b * lbs, fps, g + a * glas + b * glbs, gps);
@@ -1511,6 +1516,15 @@ static void stagg_fn(const void *c, const double *f, long fs, double *g, long gs
 /* op: 0 ddz_E2C, 1 ddz_C2E, 2 ddz_C2C, 3 ddz_E2E, 4 d2dz2_C2C, 5 d2dz2_E2E, 6 InterpZ_E2C,
  * 7 InterpZ_C2E.  f is (n1,n2,in_len) and df (n1,n2,out_len) for dir=3; the line length
  * sits in the dir-th extent of each shape. */
+/* number of host threads the oracle drivers use */
+ORACLE_API int oracle_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 ORACLE_API int oracle_stagg(int n, double dx, int periodic, int topEven, int botEven, int topSided, int botSided,
                             int op, int dir, const double *f, double *df, int n1, int n2, int n3) {
     if (op < 0 || op >= ST_NOPS) return 99;

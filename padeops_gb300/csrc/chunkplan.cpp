@@ -80,6 +80,7 @@ int build_chunk_plan(const HostPlan& hp, int M, ChunkPlanHost& cp) {
     cp.m = d.m;
     cp.nout = d.nout;
     cp.ns = d.ns;
+    cp.resid = d.resid ? 1 : 0;
     cp.Q = d.q;
     cp.M = M;
     cp.P = (d.ns + M - 1) / M;
@@ -142,13 +143,8 @@ int build_chunk_plan(const HostPlan& hp, int M, ChunkPlanHost& cp) {
     cp.tw = hp.tw;
     cp.tidx = hp.tidx;
     cp.tc = hp.tc;
-    if (cp.nlo > M || cp.nhi > M) return PS_ENOTSUP;  // edge rows must sit in the first/last chunk
-    if (cp.P > 1 && (d.ns - (cp.P - 1) * M) < cp.nhi) return PS_ENOTSUP;
 
     if (d.q == 0) { cp.ok = 1; return PS_OK; }
-    if (d.ns < 2 * M && cp.P < 2) {
-        // single chunk: still fine (scan degenerates)
-    }
 
     // ---- recurrence coefficients ----
     const int ns = d.ns;

@@ -33,7 +33,7 @@ struct ChunkPlanHost {
     int M = 16, P = 1, Pp = 1, nsteps = 0, L = 16;
     int Q = 0;          // 0 explicit, 1 tri, 2 penta
     int circ = 0;       // circulant (constant coefficients, ring wrap)
-    int m = 0, nout = 0, ns = 0;
+    int m = 0, nout = 0, ns = 0, resid = 0;
     int LS = 0;         // shared-memory line stride in elements (odd)
     // interior stencil as center + (antisymmetric or symmetric) pairs
     int has_center = 0, center_off = 0;

@@ -25,7 +25,7 @@ struct LineSet {
 // Parameters of the chunked kernel, passed by value.
 struct ChunkParams {
     int m, nout, ns, P, Pp, nsteps, L, LS;
-    int has_center, center_off, npair, nlo, nhi, tw;
+    int has_center, center_off, npair, nlo, nhi, tw, resid;
     int pair_op[kMaxPairs], pair_om[kMaxPairs], pair_sign[kMaxPairs];
     F2 center_c, pair_c[kMaxPairs];
     F2 ca1, ca2;

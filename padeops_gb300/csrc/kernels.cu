@@ -1,73 +1,16 @@
-// CUDA kernels of the compact line operators (sm_103a) and their launchers.
+// CUDA kernels of the compact line operators (sm_103a), plan upload and launch dispatch.
 //
 //  * k_seq     one thread per line, native FP64, the plan's banded LU + cyclic Woodbury
 //              correction; the reference-order baseline (FP64-pipe bound on GB300).
-//  * k_chunk   the fast path: a CTA stages L lines in shared memory, P lanes per line
-//              (adjacent lanes) each own a chunk of M rows, the recurrences run twice per
-//              chunk around a log-step shuffle scan of the chunk transfers.  Arithmetic is
-//              double-float (ArDF, FP64 in/out) or FP32 (ArF32).
+//  * k_chunk   the fast path, see chunk_kernel.cuh.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 
-#include "dfmath.cuh"
-#include "engine.h"
+#include "chunk_kernel.cuh"
 
 namespace pade {
-
-// ------------------------------------------------------------------------------------
-// arithmetic policies
-// ------------------------------------------------------------------------------------
-struct ArDF {
-    using V = dfv;
-    using IO = double;
-    static __device__ __forceinline__ V load(double x, unsigned& bad) { return df_from_double(x, bad); }
-    static __device__ __forceinline__ double store(V v) { return df_to_double(v); }
-    static __device__ __forceinline__ V coef(F2 c) { return dfv{c.h, c.l}; }
-    static __device__ __forceinline__ V zero() { return df_zero(); }
-    static __device__ __forceinline__ V add(V a, V b) { return df_add(a, b); }
-    static __device__ __forceinline__ V sub(V a, V b) { return df_sub(a, b); }
-    static __device__ __forceinline__ V mul(V a, V c) { return df_mul(a, c); }
-    static __device__ __forceinline__ V norm(V a) { return df_norm(a); }
-    // base - c1*x1 - c2*x2
-    static __device__ __forceinline__ V fms2(V base, V c1, V x1, V c2, V x2) {
-        return df_norm(df_sub(df_sub(base, df_mul(x1, c1)), df_mul(x2, c2)));
-    }
-    static __device__ __forceinline__ V fms1(V base, V c1, V x1) { return df_norm(df_sub(base, df_mul(x1, c1))); }
-    // acc + M * v for a 2x2 matrix m (row-major) acting on (v1, v2)
-    static __device__ __forceinline__ V mac2(V acc, V m0, V v1, V m1, V v2) {
-        return df_norm(df_add(df_add(acc, df_mul(v1, m0)), df_mul(v2, m1)));
-    }
-    static __device__ __forceinline__ V mac1(V acc, V m0, V v1) { return df_norm(df_add(acc, df_mul(v1, m0))); }
-    static __device__ __forceinline__ V shfl_up(V v, unsigned d, int w) { return df_shfl_up(v, d, w); }
-    static __device__ __forceinline__ V shfl_down(V v, unsigned d, int w) { return df_shfl_down(v, d, w); }
-    static __device__ __forceinline__ V shfl_idx(V v, int s, int w) { return df_shfl_idx(v, s, w); }
-};
-
-struct ArF32 {
-    using V = float;
-    using IO = float;
-    static __device__ __forceinline__ V load(float x, unsigned&) { return x; }
-    static __device__ __forceinline__ float store(V v) { return v; }
-    static __device__ __forceinline__ V coef(F2 c) { return c.h; }
-    static __device__ __forceinline__ V zero() { return 0.0f; }
-    static __device__ __forceinline__ V add(V a, V b) { return a + b; }
-    static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
-    static __device__ __forceinline__ V mul(V a, V c) { return a * c; }
-    static __device__ __forceinline__ V norm(V a) { return a; }
-    static __device__ __forceinline__ V fms2(V base, V c1, V x1, V c2, V x2) {
-        return __fmaf_rn(-c2, x2, __fmaf_rn(-c1, x1, base));
-    }
-    static __device__ __forceinline__ V fms1(V base, V c1, V x1) { return __fmaf_rn(-c1, x1, base); }
-    static __device__ __forceinline__ V mac2(V acc, V m0, V v1, V m1, V v2) {
-        return __fmaf_rn(m1, v2, __fmaf_rn(m0, v1, acc));
-    }
-    static __device__ __forceinline__ V mac1(V acc, V m0, V v1) { return __fmaf_rn(m0, v1, acc); }
-    static __device__ __forceinline__ V shfl_up(V v, unsigned d, int w) { return __shfl_up_sync(0xffffffffu, v, d, w); }
-    static __device__ __forceinline__ V shfl_down(V v, unsigned d, int w) { return __shfl_down_sync(0xffffffffu, v, d, w); }
-    static __device__ __forceinline__ V shfl_idx(V v, int s, int w) { return __shfl_sync(0xffffffffu, v, s, w); }
-};
 
 // ------------------------------------------------------------------------------------
 // k_seq: one thread per line, native FP64
@@ -134,6 +77,8 @@ __global__ void k_seq(const PlanView<double> P, const double* __restrict__ f, do
             }
         }
     }
+    if (P.resid)
+        for (int i = 0; i < ns; i++) ol[i * op] = fl[i * fp] - ol[i * op];
     for (int i = ns; i < P.nout; i++) ol[i * op] = ol[(i - ns) * op];
 }
 
@@ -145,281 +90,6 @@ __global__ void k_trivial(int zero, int nout, const IO* __restrict__ f, IO* __re
     const long a = l % ls.na, b = l / ls.na;
     for (int i = 0; i < nout; i++)
         out[a * ls.oa + b * ls.ob + i * ls.op] = zero ? (IO)0 : f[a * ls.fa + b * ls.fb + i * ls.fp];
-}
-
-// ------------------------------------------------------------------------------------
-// k_chunk: the chunked scan engine
-// ------------------------------------------------------------------------------------
-template <int M>
-__device__ __forceinline__ int spos(int p) {
-    return p + p / M;
-}
-
-template <class AR, int Q, int M, bool CIRC>
-__global__ void __launch_bounds__(256, 2)
-    k_chunk(const ChunkParams cp, const typename AR::IO* __restrict__ f, typename AR::IO* __restrict__ out,
-            const LineSet ls, unsigned* __restrict__ status) {
-    using V = typename AR::V;
-    using IO = typename AR::IO;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    long* base_in = reinterpret_cast<long*>(smem_raw);
-    long* base_out = base_in + cp.L;
-    V* tile = reinterpret_cast<V*>(smem_raw + 16 * cp.L);
-    IO* tio = reinterpret_cast<IO*>(tile);
-
-    const int tid = threadIdx.x, nth = blockDim.x;
-    const long line0 = (long)blockIdx.x * cp.L;
-    const int nl = (int)min((long)cp.L, ls.nlines - line0);
-    if (tid < cp.L) {
-        const long lg = line0 + tid;
-        const long a = lg % ls.na, b = lg / ls.na;
-        base_in[tid] = a * ls.fa + b * ls.fb;
-        base_out[tid] = a * ls.oa + b * ls.ob;
-    }
-    __syncthreads();
-
-    // ---- stage the input lines (converted once) in shared memory ----
-    unsigned bad = 0;
-    if (ls.fp == 1) {
-        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
-        for (int l = warp; l < nl; l += nw) {
-            const IO* src = f + base_in[l];
-            V* dst = tile + l * cp.LS;
-            for (int p = lane; p < cp.m; p += 32) dst[spos<M>(p)] = AR::load(src[p], bad);
-        }
-    } else {
-        const int l = tid % cp.L, p0 = tid / cp.L, ps = nth / cp.L;
-        if (l < nl) {
-            const IO* src = f + base_in[l];
-            V* dst = tile + l * cp.LS;
-            for (int p = p0; p < cp.m; p += ps) dst[spos<M>(p)] = AR::load(src[(long)p * ls.fp], bad);
-        }
-    }
-    __syncthreads();
-
-    // ---- per-lane chunk ----
-    const int t = tid % cp.Pp, l = tid / cp.Pp;
-    const bool active = (l < nl) && (t < cp.P);
-    const int r0 = t * M;
-    const V* line = tile + l * cp.LS;
-    const int ns = cp.ns;
-    V r[M];
-
-#pragma unroll
-    for (int j = 0; j < M; j++) {
-        const int i = r0 + j;
-        V acc = AR::zero();
-        if (active && i < ns) {
-            if (i < cp.nlo || i >= ns - cp.nhi) {
-                const int tr = i < cp.nlo ? i : cp.nlo + (i - (ns - cp.nhi));
-                for (int k = 0; k < cp.tw; k++) {
-                    const int idx = __ldg(cp.tidx + tr * cp.tw + k);
-                    const F2 c = cp.tc[tr * cp.tw + k];
-                    acc = AR::add(acc, AR::mul(line[spos<M>(idx)], AR::coef(c)));
-                }
-            } else {
-                if (cp.has_center) acc = AR::mul(line[spos<M>(i + cp.center_off)], AR::coef(cp.center_c));
-#pragma unroll
-                for (int k = 0; k < kMaxPairs; k++) {
-                    if (k < cp.npair) {
-                        const V fp = line[spos<M>(i + cp.pair_op[k])];
-                        V fm = line[spos<M>(i + cp.pair_om[k])];
-                        const V d = cp.pair_sign[k] < 0 ? AR::sub(fp, fm) : AR::add(fp, fm);
-                        acc = AR::add(acc, AR::mul(d, AR::coef(cp.pair_c[k])));
-                    }
-                }
-            }
-            acc = AR::norm(acc);
-        }
-        r[j] = acc;
-    }
-
-    if constexpr (Q > 0) {
-        const int Pp = cp.Pp;
-        // coefficient access
-        auto fcoef = [&](int i, V& g, V& a1, V& a2) {
-            if constexpr (CIRC) {
-                g = AR::coef(F2{1.0f, 0.0f});
-                a1 = AR::coef(cp.ca1);
-                a2 = AR::coef(cp.ca2);
-            } else {
-                g = AR::coef(cp.rc[i * 5 + 0]);
-                a1 = AR::coef(cp.rc[i * 5 + 1]);
-                a2 = AR::coef(cp.rc[i * 5 + 2]);
-            }
-        };
-        auto bcoef = [&](int i, V& b1, V& b2) {
-            if constexpr (CIRC) {
-                b1 = AR::coef(cp.ca1);
-                b2 = AR::coef(cp.ca2);
-            } else {
-                b1 = AR::coef(cp.rc[i * 5 + 3]);
-                b2 = AR::coef(cp.rc[i * 5 + 4]);
-            }
-        };
-        // ---------------- forward ----------------
-        V s1 = AR::zero(), s2 = AR::zero();
-#pragma unroll
-        for (int j = 0; j < M; j++) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V g, a1, a2;
-                fcoef(i, g, a1, a2);
-                const V gr = CIRC ? r[j] : AR::mul(r[j], g);
-                const V y = (Q == 2) ? AR::fms2(gr, a1, s1, a2, s2) : AR::fms1(gr, a1, s1);
-                s2 = s1;
-                s1 = y;
-            }
-        }
-        for (int k = 0; k < cp.nsteps; k++) {
-            const unsigned dlt = 1u << k;
-            const V o1 = AR::shfl_up(s1, dlt, Pp);
-            const V o2 = (Q == 2) ? AR::shfl_up(s2, dlt, Pp) : AR::zero();
-            if (t >= (int)dlt) {
-                const F2* Fm = cp.fscan + ((size_t)t * kMaxSteps + k) * 4;
-                if constexpr (Q == 2) {
-                    const V n1 = AR::mac2(s1, AR::coef(Fm[0]), o1, AR::coef(Fm[1]), o2);
-                    const V n2 = AR::mac2(s2, AR::coef(Fm[2]), o1, AR::coef(Fm[3]), o2);
-                    s1 = n1;
-                    s2 = n2;
-                } else {
-                    s1 = AR::mac1(s1, AR::coef(Fm[0]), o1);
-                }
-            }
-        }
-        {
-            V i1 = AR::shfl_up(s1, 1, Pp);
-            V i2 = (Q == 2) ? AR::shfl_up(s2, 1, Pp) : AR::zero();
-            if (t == 0) {
-                i1 = AR::zero();
-                i2 = AR::zero();
-            }
-            if constexpr (CIRC) {
-                const V E1 = AR::shfl_idx(s1, cp.P - 1, Pp);
-                const V E2 = (Q == 2) ? AR::shfl_idx(s2, cp.P - 1, Pp) : AR::zero();
-                const F2* W = cp.fwrap + (size_t)t * 4;
-                if (t < cp.P) {
-                    if constexpr (Q == 2) {
-                        const V n1 = AR::mac2(i1, AR::coef(W[0]), E1, AR::coef(W[1]), E2);
-                        const V n2 = AR::mac2(i2, AR::coef(W[2]), E1, AR::coef(W[3]), E2);
-                        i1 = n1;
-                        i2 = n2;
-                    } else {
-                        i1 = AR::mac1(i1, AR::coef(W[0]), E1);
-                    }
-                }
-            }
-            s1 = i1;
-            s2 = i2;
-        }
-#pragma unroll
-        for (int j = 0; j < M; j++) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V g, a1, a2;
-                fcoef(i, g, a1, a2);
-                const V gr = CIRC ? r[j] : AR::mul(r[j], g);
-                const V y = (Q == 2) ? AR::fms2(gr, a1, s1, a2, s2) : AR::fms1(gr, a1, s1);
-                r[j] = y;
-                s2 = s1;
-                s1 = y;
-            }
-        }
-        // ---------------- backward ----------------
-        V u1 = AR::zero(), u2 = AR::zero();
-#pragma unroll
-        for (int j = M - 1; j >= 0; j--) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V b1, b2;
-                bcoef(i, b1, b2);
-                const V x = (Q == 2) ? AR::fms2(r[j], b1, u1, b2, u2) : AR::fms1(r[j], b1, u1);
-                u2 = u1;
-                u1 = x;
-            }
-        }
-        for (int k = 0; k < cp.nsteps; k++) {
-            const unsigned dlt = 1u << k;
-            const V o1 = AR::shfl_down(u1, dlt, Pp);
-            const V o2 = (Q == 2) ? AR::shfl_down(u2, dlt, Pp) : AR::zero();
-            if (t + (int)dlt < Pp) {
-                const F2* Bm = cp.bscan + ((size_t)t * kMaxSteps + k) * 4;
-                if constexpr (Q == 2) {
-                    const V n1 = AR::mac2(u1, AR::coef(Bm[0]), o1, AR::coef(Bm[1]), o2);
-                    const V n2 = AR::mac2(u2, AR::coef(Bm[2]), o1, AR::coef(Bm[3]), o2);
-                    u1 = n1;
-                    u2 = n2;
-                } else {
-                    u1 = AR::mac1(u1, AR::coef(Bm[0]), o1);
-                }
-            }
-        }
-        {
-            V i1 = AR::shfl_down(u1, 1, Pp);
-            V i2 = (Q == 2) ? AR::shfl_down(u2, 1, Pp) : AR::zero();
-            if (t >= cp.P - 1) {
-                i1 = AR::zero();
-                i2 = AR::zero();
-            }
-            if constexpr (CIRC) {
-                const V F1 = AR::shfl_idx(u1, 0, Pp);
-                const V F2v = (Q == 2) ? AR::shfl_idx(u2, 0, Pp) : AR::zero();
-                const F2* W = cp.bwrap + (size_t)t * 4;
-                if (t < cp.P) {
-                    if constexpr (Q == 2) {
-                        const V n1 = AR::mac2(i1, AR::coef(W[0]), F1, AR::coef(W[1]), F2v);
-                        const V n2 = AR::mac2(i2, AR::coef(W[2]), F1, AR::coef(W[3]), F2v);
-                        i1 = n1;
-                        i2 = n2;
-                    } else {
-                        i1 = AR::mac1(i1, AR::coef(W[0]), F1);
-                    }
-                }
-            }
-            u1 = i1;
-            u2 = i2;
-        }
-#pragma unroll
-        for (int j = M - 1; j >= 0; j--) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V b1, b2;
-                bcoef(i, b1, b2);
-                const V x = (Q == 2) ? AR::fms2(r[j], b1, u1, b2, u2) : AR::fms1(r[j], b1, u1);
-                r[j] = x;
-                u2 = u1;
-                u1 = x;
-            }
-        }
-    }
-
-    // ---- write back through shared memory (coalesced global stores) ----
-    __syncthreads();
-    if (active) {
-        IO* dst = tio + l * cp.LS;
-#pragma unroll
-        for (int j = 0; j < M; j++) {
-            const int i = r0 + j;
-            if (i < ns) dst[spos<M>(i)] = AR::store(r[j]);
-        }
-    }
-    __syncthreads();
-    if (ls.op == 1) {
-        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
-        for (int ll = warp; ll < nl; ll += nw) {
-            IO* o = out + base_out[ll];
-            const IO* src = tio + ll * cp.LS;
-            for (int p = lane; p < cp.nout; p += 32) o[p] = src[spos<M>(p < ns ? p : p - ns)];
-        }
-    } else {
-        const int ll = tid % cp.L, p0 = tid / cp.L, ps = nth / cp.L;
-        if (ll < nl) {
-            IO* o = out + base_out[ll];
-            const IO* src = tio + ll * cp.LS;
-            for (int p = p0; p < cp.nout; p += ps) o[(long)p * ls.op] = src[spos<M>(p < ns ? p : p - ns)];
-        }
-    }
-    if (bad) atomicOr(status, 1u);
 }
 
 // ------------------------------------------------------------------------------------
@@ -514,6 +184,7 @@ int DevicePlan::upload(const HostPlan& hp) {
     vd_.cyclic = d.cyclic;
     vd_.zero = d.zero;
     vd_.identity = d.identity;
+    vd_.resid = d.resid;
     vd_.ntap = hp.ntap;
     vd_.nlo = hp.nlo;
     vd_.nhi = hp.nhi;
@@ -548,6 +219,7 @@ int DevicePlan::upload(const HostPlan& hp) {
             c.nlo = ch_.nlo;
             c.nhi = ch_.nhi;
             c.tw = ch_.tw;
+            c.resid = ch_.resid;
             for (int k = 0; k < kMaxPairs; k++) {
                 c.pair_op[k] = ch_.pair_op[k];
                 c.pair_om[k] = ch_.pair_om[k];
@@ -579,36 +251,6 @@ int DevicePlan::upload(const HostPlan& hp) {
 // ------------------------------------------------------------------------------------
 // launch
 // ------------------------------------------------------------------------------------
-namespace {
-
-template <class AR, int Q, int M, bool CIRC>
-int launch_chunk_t(const ChunkParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
-                   cudaStream_t s) {
-    using IO = typename AR::IO;
-    const int threads = c.L * c.Pp;
-    const long blocks = (ls.nlines + c.L - 1) / c.L;
-    const size_t smem = 16 * (size_t)c.L + sizeof(typename AR::V) * (size_t)c.L * c.LS;
-    auto kern = k_chunk<AR, Q, M, CIRC>;
-    if (smem > 48 * 1024) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return PS_ECUDA;
-    }
-    kern<<<(unsigned)blocks, threads, smem, s>>>(c, (const IO*)f, (IO*)out, ls, status);
-    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
-}
-
-template <class AR, int M>
-int launch_chunk_m(const ChunkPlanHost& h, const ChunkParams& c, const void* f, void* out, const LineSet& ls,
-                   unsigned* status, cudaStream_t s) {
-    if (h.Q == 0) return launch_chunk_t<AR, 0, M, false>(c, f, out, ls, status, s);
-    if (h.Q == 1) return h.circ ? launch_chunk_t<AR, 1, M, true>(c, f, out, ls, status, s)
-                                : launch_chunk_t<AR, 1, M, false>(c, f, out, ls, status, s);
-    return h.circ ? launch_chunk_t<AR, 2, M, true>(c, f, out, ls, status, s)
-                  : launch_chunk_t<AR, 2, M, false>(c, f, out, ls, status, s);
-}
-
-}  // namespace
-
 int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const LineSet& ls, unsigned* status,
                  cudaStream_t s) {
     if (ls.nlines <= 0) return PS_OK;

@@ -415,6 +415,7 @@ int def_cf90(int n, bool periodic, int bc1, int bcn, OpDef& o) {
         o.lhs[0][0] = o.lhs[0][1] = o.lhs[1][0] = 0.0;
         o.lhs[n - 1][3] = o.lhs[n - 1][4] = o.lhs[n - 2][4] = 0.0;
     }
+    o.resid = true;
     return PS_OK;
 }
 

@@ -32,6 +32,11 @@ struct OpDef {
     bool cyclic = false;
     bool zero = false;      // n == 1 derivative: output is zero
     bool identity = false;  // n == 1 filter: output equals input
+    // residual form: out = f - A^-1 ((A - B) f), identical to A^-1 B f for square operators.
+    // Used for near-identity filters (cf90): (A - B) has coefficients ~1e-4, so the
+    // rounding that the solve amplifies at the poorly conditioned Nyquist mode shrinks by
+    // the same factor.
+    bool resid = false;
     std::vector<LinForm> rhs;                 // ns rows
     std::vector<std::array<double, 5>> lhs;   // ns rows, coefficients at offsets -2..2
     // Interior stencil used by the device fast path: out_i = sum_t ic[t] * f[i + io[t]]

@@ -53,13 +53,43 @@ int build_plan(const OpDef& d, HostPlan& p) {
     p.ntap = (int)d.io.size();
     p.io = d.io;
     p.ic = d.ic;
+    std::vector<LinForm> rhs = d.rhs;
+    if (d.resid) {
+        // residual form: rows of R = A - B and the interior stencil of A - B
+        if (d.m != ns || d.nout != ns) return PS_EINVAL;
+        for (int i = 0; i < ns; i++) {
+            LinForm a;
+            for (int o = -2; o <= 2; o++) {
+                double v = d.lhs[i][o + 2];
+                if (v == 0.0) continue;
+                int j = i + o;
+                if (d.cyclic) j = ((j % ns) + ns) % ns;
+                else if (j < 0 || j >= ns) continue;
+                a = a + LinForm(j, v);
+            }
+            rhs[i] = a - d.rhs[i];
+        }
+        const auto& mid = d.lhs[ns / 2];
+        std::map<int, double> st;
+        for (int t = 0; t < p.ntap; t++) st[d.io[t]] -= d.ic[t];
+        for (int o = -2; o <= 2; o++)
+            if (mid[o + 2] != 0.0) st[o] += mid[o + 2];
+        p.io.clear();
+        p.ic.clear();
+        for (auto& kv : st) {
+            p.io.push_back(kv.first);
+            p.ic.push_back(kv.second);
+        }
+        p.ntap = (int)p.io.size();
+        if (p.ntap > kMaxTap) return PS_EINVAL;
+    }
 
     // ---- RHS: which rows follow the interior stencil with direct indexing ----
     std::vector<char> reg(ns, 0);
     std::vector<std::vector<std::pair<int, double>>> rows(ns);
     std::vector<std::pair<int, double>> st;
     for (int i = 0; i < ns; i++) {
-        rows[i] = canon(d.rhs[i]);
+        rows[i] = canon(rhs[i]);
         reg[i] = stencil_direct(p, i, st) && same_row(rows[i], st);
     }
     int first = -1, last = -1;
@@ -240,6 +270,8 @@ void host_apply_line(const HostPlan& p, const double* f, long fs, double* out, l
             }
         }
     }
+    if (d.resid)
+        for (int i = 0; i < ns; i++) out[i * os] = f[i * fs] - out[i * os];
     for (int i = ns; i < d.nout; i++) out[i * os] = out[(i - ns) * os];
 }
 

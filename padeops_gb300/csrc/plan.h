@@ -18,7 +18,7 @@ constexpr int kMaxNc = 4;    // cyclic corner rows (2q)
 // Plain-old-data view passed to kernels by value.  Coefficient arrays are of type C.
 template <class C>
 struct PlanView {
-    int m, nout, ns, q, cyclic, zero, identity;
+    int m, nout, ns, q, cyclic, zero, identity, resid;
     int ntap, nlo, nhi, tw, nc;
     int io[kMaxTap];
     C ic[kMaxTap];

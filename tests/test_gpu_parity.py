@@ -5,7 +5,11 @@ ABI on seeded fields and is compared with the oracle's restatement of the refere
 the same input.  Tolerances (normwise relative, max|a-b|/max|b|):
   FP64 paths (double-float and native)  1e-12 for first derivatives and filters;
       second derivatives allow the FP64 conditioning of the second difference,
-      50*eps*max|f|/(h^2 max|f''|), when that is larger
+      50*eps*max|f|/(h^2 max|f''|), when that is larger.  CF90 on the double-float path
+      with white-noise input: the CF90 matrix has condition ~2.1e3 (its symbol is 1.3e-3
+      at the Nyquist wavenumber) and double-float carries 48 significant bits, so the
+      bound is cond * 2^-48 ~ 7e-12; such inputs are checked at 1e-11 (smooth fields like
+      the benchmark's still at 1e-12, and the native FP64 path always at 1e-12)
   FP32 path                             3e-5 (5e-4 for cf90, whose matrix is near
       singular at the Nyquist mode)
 """
@@ -23,6 +27,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 BCS = [0, 1, -1]
 EPS = np.finfo(np.float64).eps
+CF90_DF_NOISE_TOL = 1e-11  # cond(A_cf90) * 2^-48, see the module docstring
 
 
 def to_dev(a, dtype=torch.float64):
@@ -134,7 +139,7 @@ def test_cf90(oracle, periodic, bc1, bcn, dir):
     for path in PATHS:
         out = run(o, 0, dir, f, shape, bc1, bcn, path)
         ref = oracle.cf90(f, periodic=periodic, bc1=bc1, bcn=bcn, dir=dir)
-        assert relerr(out, ref) < 1e-12, path
+        assert relerr(out, ref) < (CF90_DF_NOISE_TOL if path == L.PATH_DF else 1e-12), path
 
 
 @pytest.mark.parametrize("periodic", [True, False])
@@ -227,7 +232,7 @@ def test_named_entry_points_and_complex(oracle):
     gf = np.zeros_like(g, order="F")
     cf.filter3(g, gf, n1, n2, 0, 0)
     refc = oracle.cf90(g.real, periodic=False, dir=3) + 1j * oracle.cf90(g.imag, periodic=False, dir=3)
-    assert relerr(gf, refc) < 1e-12
+    assert relerr(gf, refc) < CF90_DF_NOISE_TOL  # white-noise input, see the module docstring
 
 
 @pytest.mark.parametrize("fam", ["cd10", "cf90", "cd06"])
