@@ -73,8 +73,11 @@ __device__ __forceinline__ int spos(int p) {
     return p + p / M;
 }
 
+// Staging loads keep up to kLoadUnroll loads in flight per thread before converting.
+constexpr int kLoadUnroll = 8;
+
 template <class AR, int Q, int M, bool CIRC>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, 3)
     k_chunk(const ChunkParams cp, const typename AR::IO* __restrict__ f, typename AR::IO* __restrict__ out,
             const LineSet ls, unsigned* __restrict__ status) {
     using V = typename AR::V;
@@ -82,8 +85,9 @@ __global__ void __launch_bounds__(256, 2)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     long* base_in = reinterpret_cast<long*>(smem_raw);
     long* base_out = base_in + cp.L;
-    V* tile = reinterpret_cast<V*>(smem_raw + 16 * cp.L);
-    IO* tio = reinterpret_cast<IO*>(tile);
+    V* tile = reinterpret_cast<V*>(smem_raw + 16 * cp.L);  // input lines (converted), L x LS
+    V* work = tile + (size_t)cp.L * cp.LS;                  // per-row RHS / solution, L x LS
+    IO* wio = reinterpret_cast<IO*>(work);                  // same storage, output values
 
     const int tid = threadIdx.x, nth = blockDim.x;
     const long line0 = (long)blockIdx.x * cp.L;
@@ -96,99 +100,126 @@ __global__ void __launch_bounds__(256, 2)
     }
     __syncthreads();
 
-    // ---- stage the input lines (converted once) in shared memory ----
+    // ---- A: stage the input lines in shared memory, converted once ----
     unsigned bad = 0;
     if (ls.fp == 1) {
+        // contiguous lines: one warp per line, kLoadUnroll loads in flight per lane
         const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
         for (int l = warp; l < nl; l += nw) {
             const IO* src = f + base_in[l];
             V* dst = tile + l * cp.LS;
-            for (int p = lane; p < cp.m; p += 32) dst[spos<M>(p)] = AR::load(src[p], bad);
+            for (int p0 = lane; p0 < cp.m; p0 += 32 * kLoadUnroll) {
+                IO v[kLoadUnroll];
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int p = p0 + 32 * u;
+                    v[u] = p < cp.m ? __ldg(src + p) : (IO)0;
+                }
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int p = p0 + 32 * u;
+                    if (p < cp.m) dst[spos<M>(p)] = AR::load(v[u], bad);
+                }
+            }
         }
     } else {
-        const int l = tid % cp.L, p0 = tid / cp.L, ps = nth / cp.L;
+        // strided lines: consecutive threads take consecutive lines (coalesced rows)
+        const int l = tid % cp.L, pstep = nth / cp.L;
         if (l < nl) {
             const IO* src = f + base_in[l];
             V* dst = tile + l * cp.LS;
-            for (int p = p0; p < cp.m; p += ps) dst[spos<M>(p)] = AR::load(src[(long)p * ls.fp], bad);
+            for (int p0 = tid / cp.L; p0 < cp.m; p0 += pstep * kLoadUnroll) {
+                IO v[kLoadUnroll];
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int p = p0 + pstep * u;
+                    v[u] = p < cp.m ? __ldg(src + (long)p * ls.fp) : (IO)0;
+                }
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int p = p0 + pstep * u;
+                    if (p < cp.m) dst[spos<M>(p)] = AR::load(v[u], bad);
+                }
+            }
         }
     }
     __syncthreads();
 
-    // ---- per-lane chunk ----
+    // ---- per-lane chunk: rows r0 .. r1-1 of line l ----
     const int t = tid % cp.Pp, l = tid / cp.Pp;
     const bool active = (l < nl) && (t < cp.P);
-    const int r0 = t * M;
-    const V* line = tile + l * cp.LS;
     const int ns = cp.ns;
-    V r[M];
-
+    const int r0 = t * M, r1 = active ? min(ns, r0 + M) : r0;
+    const V* line = tile + l * cp.LS;
+    V* wl = work + l * cp.LS;
+    // non-circulant coefficient tables, staged once per CTA (chunk-padded like the lines)
+    V* ctab = work + (size_t)cp.L * cp.LS;  // 9 tables of LSc entries: g a1 a2 b1 b2 pf1 pf2 pb1 pb2
+    const int LSc = spos<M>(ns - 1) + 1;
+    if constexpr (!CIRC && Q > 0) {
+        for (int i = tid; i < ns; i += nth) {
+            const int ps = spos<M>(i);
 #pragma unroll
-    for (int j = 0; j < M; j++) {
-        const int i = r0 + j;
-        V acc = AR::zero();
-        if (active && i < ns) {
-            if (i < cp.nlo || i >= ns - cp.nhi) {
-                const int tr = i < cp.nlo ? i : cp.nlo + (i - (ns - cp.nhi));
-                for (int k = 0; k < cp.tw; k++) {
-                    const int idx = __ldg(cp.tidx + tr * cp.tw + k);
-                    const F2 c = cp.tc[tr * cp.tw + k];
-                    acc = AR::add(acc, AR::mul(line[spos<M>(idx)], AR::coef(c)));
-                }
-            } else {
-                if (cp.has_center) acc = AR::mul(line[spos<M>(i + cp.center_off)], AR::coef(cp.center_c));
-#pragma unroll
-                for (int k = 0; k < kMaxPairs; k++) {
-                    if (k < cp.npair) {
-                        const V fp = line[spos<M>(i + cp.pair_op[k])];
-                        V fm = line[spos<M>(i + cp.pair_om[k])];
-                        const V d = cp.pair_sign[k] < 0 ? AR::sub(fp, fm) : AR::add(fp, fm);
-                        acc = AR::add(acc, AR::mul(d, AR::coef(cp.pair_c[k])));
-                    }
-                }
-            }
-            acc = AR::norm(acc);
+            for (int k = 0; k < 5; k++) ctab[k * LSc + ps] = AR::coef(cp.rc[i * 5 + k]);
+            ctab[5 * LSc + ps] = AR::coef(cp.phf[i * 2]);
+            ctab[6 * LSc + ps] = AR::coef(cp.phf[i * 2 + 1]);
+            ctab[7 * LSc + ps] = AR::coef(cp.phb[i * 2]);
+            ctab[8 * LSc + ps] = AR::coef(cp.phb[i * 2 + 1]);
         }
-        r[j] = acc;
+        __syncthreads();
     }
 
-    if constexpr (Q > 0) {
-        const int Pp = cp.Pp;
-        // coefficient access
-        auto fcoef = [&](int i, V& g, V& a1, V& a2) {
-            if constexpr (CIRC) {
-                g = AR::coef(F2{1.0f, 0.0f});
-                a1 = AR::coef(cp.ca1);
-                a2 = AR::coef(cp.ca2);
-            } else {
-                g = AR::coef(cp.rc[i * 5 + 0]);
-                a1 = AR::coef(cp.rc[i * 5 + 1]);
-                a2 = AR::coef(cp.rc[i * 5 + 2]);
+    auto rhs_row = [&](int i) -> V {
+        V acc = AR::zero();
+        if (i < cp.nlo || i >= ns - cp.nhi) {
+            const int tr = i < cp.nlo ? i : cp.nlo + (i - (ns - cp.nhi));
+#pragma unroll 1
+            for (int k = 0; k < cp.tw; k++) {
+                const int idx = __ldg(cp.tidx + tr * cp.tw + k);
+                acc = AR::add(acc, AR::mul(line[spos<M>(idx)], AR::coef(cp.tc[tr * cp.tw + k])));
             }
-        };
-        auto bcoef = [&](int i, V& b1, V& b2) {
-            if constexpr (CIRC) {
-                b1 = AR::coef(cp.ca1);
-                b2 = AR::coef(cp.ca2);
-            } else {
-                b1 = AR::coef(cp.rc[i * 5 + 3]);
-                b2 = AR::coef(cp.rc[i * 5 + 4]);
-            }
-        };
-        // ---------------- forward ----------------
-        V s1 = AR::zero(), s2 = AR::zero();
-#pragma unroll
-        for (int j = 0; j < M; j++) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V g, a1, a2;
-                fcoef(i, g, a1, a2);
-                const V gr = CIRC ? r[j] : AR::mul(r[j], g);
-                const V y = (Q == 2) ? AR::fms2(gr, a1, s1, a2, s2) : AR::fms1(gr, a1, s1);
-                s2 = s1;
-                s1 = y;
+        } else {
+            if (cp.has_center) acc = AR::mul(line[spos<M>(i + cp.center_off)], AR::coef(cp.center_c));
+#pragma unroll 1
+            for (int k = 0; k < cp.npair; k++) {
+                const V a = line[spos<M>(i + cp.pair_op[k])];
+                const V b = line[spos<M>(i + cp.pair_om[k])];
+                const V d = cp.pair_sign[k] < 0 ? AR::sub(a, b) : AR::add(a, b);
+                acc = AR::add(acc, AR::mul(d, AR::coef(cp.pair_c[k])));
             }
         }
+        return AR::norm(acc);
+    };
+
+    if constexpr (Q == 0) {
+        // explicit operator: the right-hand side is the result
+        IO* wlio = reinterpret_cast<IO*>(wl);
+#pragma unroll 1
+        for (int i = r0; i < r1; i++) {
+            V x = rhs_row(i);
+            if (cp.resid) x = AR::norm(AR::sub(line[spos<M>(i)], x));
+            wlio[spos<M>(i)] = AR::store(x);
+        }
+    } else {
+        const int Pp = cp.Pp;
+        const V ca1 = AR::coef(cp.ca1), ca2 = AR::coef(cp.ca2);
+        // ---- B+C: right-hand side and forward recurrence from a zero state ----
+        V s1 = AR::zero(), s2 = AR::zero();
+#pragma unroll 1
+        for (int i = r0; i < r1; i++) {
+            V r = rhs_row(i);
+            V a1 = ca1, a2 = ca2;
+            if constexpr (!CIRC) {
+                const int ps = spos<M>(i);
+                r = AR::mul(r, ctab[ps]);
+                a1 = ctab[LSc + ps];
+                a2 = ctab[2 * LSc + ps];
+            }
+            const V y = (Q == 2) ? AR::fms2(r, a1, s1, a2, s2) : AR::fms1(r, a1, s1);
+            wl[spos<M>(i)] = y;
+            s2 = s1;
+            s1 = y;
+        }
+        // ---- D: log-step scan of the chunk transfers -> incoming state ----
         for (int k = 0; k < cp.nsteps; k++) {
             const unsigned dlt = 1u << k;
             const V o1 = AR::shfl_up(s1, dlt, Pp);
@@ -205,57 +236,50 @@ __global__ void __launch_bounds__(256, 2)
                 }
             }
         }
-        {
-            V i1 = AR::shfl_up(s1, 1, Pp);
-            V i2 = (Q == 2) ? AR::shfl_up(s2, 1, Pp) : AR::zero();
-            if (t == 0) {
-                i1 = AR::zero();
-                i2 = AR::zero();
-            }
-            if constexpr (CIRC) {
-                const V E1 = AR::shfl_idx(s1, cp.P - 1, Pp);
-                const V E2 = (Q == 2) ? AR::shfl_idx(s2, cp.P - 1, Pp) : AR::zero();
+        V i1 = AR::shfl_up(s1, 1, Pp);
+        V i2 = (Q == 2) ? AR::shfl_up(s2, 1, Pp) : AR::zero();
+        if (t == 0) {
+            i1 = AR::zero();
+            i2 = AR::zero();
+        }
+        if constexpr (CIRC) {
+            const V E1 = AR::shfl_idx(s1, cp.P - 1, Pp);
+            const V E2 = (Q == 2) ? AR::shfl_idx(s2, cp.P - 1, Pp) : AR::zero();
+            if (t < cp.P) {
                 const F2* W = cp.fwrap + (size_t)t * 4;
-                if (t < cp.P) {
-                    if constexpr (Q == 2) {
-                        const V n1 = AR::mac2(i1, AR::coef(W[0]), E1, AR::coef(W[1]), E2);
-                        const V n2 = AR::mac2(i2, AR::coef(W[2]), E1, AR::coef(W[3]), E2);
-                        i1 = n1;
-                        i2 = n2;
-                    } else {
-                        i1 = AR::mac1(i1, AR::coef(W[0]), E1);
-                    }
+                if constexpr (Q == 2) {
+                    const V n1 = AR::mac2(i1, AR::coef(W[0]), E1, AR::coef(W[1]), E2);
+                    const V n2 = AR::mac2(i2, AR::coef(W[2]), E1, AR::coef(W[3]), E2);
+                    i1 = n1;
+                    i2 = n2;
+                } else {
+                    i1 = AR::mac1(i1, AR::coef(W[0]), E1);
                 }
             }
-            s1 = i1;
-            s2 = i2;
         }
-#pragma unroll
-        for (int j = 0; j < M; j++) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V g, a1, a2;
-                fcoef(i, g, a1, a2);
-                const V gr = CIRC ? r[j] : AR::mul(r[j], g);
-                const V y = (Q == 2) ? AR::fms2(gr, a1, s1, a2, s2) : AR::fms1(gr, a1, s1);
-                r[j] = y;
-                s2 = s1;
-                s1 = y;
-            }
-        }
-        // ---------------- backward ----------------
+        // ---- E+F: forward correction y = y~ + phi . state, backward recurrence from zero ----
         V u1 = AR::zero(), u2 = AR::zero();
-#pragma unroll
-        for (int j = M - 1; j >= 0; j--) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V b1, b2;
-                bcoef(i, b1, b2);
-                const V x = (Q == 2) ? AR::fms2(r[j], b1, u1, b2, u2) : AR::fms1(r[j], b1, u1);
-                u2 = u1;
-                u1 = x;
+#pragma unroll 1
+        for (int i = r1 - 1; i >= r0; i--) {
+            const int ps = spos<M>(i);
+            V p1, p2, b1 = ca1, b2 = ca2;
+            if constexpr (CIRC) {
+                const F2* ph = cp.phf + (size_t)(i - r0) * 2;
+                p1 = AR::coef(ph[0]);
+                p2 = AR::coef(ph[1]);
+            } else {
+                p1 = ctab[5 * LSc + ps];
+                p2 = ctab[6 * LSc + ps];
+                b1 = ctab[3 * LSc + ps];
+                b2 = ctab[4 * LSc + ps];
             }
+            const V y = (Q == 2) ? AR::mac2(wl[ps], p1, i1, p2, i2) : AR::mac1(wl[ps], p1, i1);
+            const V x = (Q == 2) ? AR::fms2(y, b1, u1, b2, u2) : AR::fms1(y, b1, u1);
+            wl[ps] = x;
+            u2 = u1;
+            u1 = x;
         }
+        // ---- G: reverse scan -> state entering from above ----
         for (int k = 0; k < cp.nsteps; k++) {
             const unsigned dlt = 1u << k;
             const V o1 = AR::shfl_down(u1, dlt, Pp);
@@ -272,73 +296,62 @@ __global__ void __launch_bounds__(256, 2)
                 }
             }
         }
-        {
-            V i1 = AR::shfl_down(u1, 1, Pp);
-            V i2 = (Q == 2) ? AR::shfl_down(u2, 1, Pp) : AR::zero();
-            if (t >= cp.P - 1) {
-                i1 = AR::zero();
-                i2 = AR::zero();
-            }
-            if constexpr (CIRC) {
-                const V F1 = AR::shfl_idx(u1, 0, Pp);
-                const V F2v = (Q == 2) ? AR::shfl_idx(u2, 0, Pp) : AR::zero();
+        V j1 = AR::shfl_down(u1, 1, Pp);
+        V j2 = (Q == 2) ? AR::shfl_down(u2, 1, Pp) : AR::zero();
+        if (t >= cp.P - 1) {
+            j1 = AR::zero();
+            j2 = AR::zero();
+        }
+        if constexpr (CIRC) {
+            const V F1 = AR::shfl_idx(u1, 0, Pp);
+            const V F2v = (Q == 2) ? AR::shfl_idx(u2, 0, Pp) : AR::zero();
+            if (t < cp.P) {
                 const F2* W = cp.bwrap + (size_t)t * 4;
-                if (t < cp.P) {
-                    if constexpr (Q == 2) {
-                        const V n1 = AR::mac2(i1, AR::coef(W[0]), F1, AR::coef(W[1]), F2v);
-                        const V n2 = AR::mac2(i2, AR::coef(W[2]), F1, AR::coef(W[3]), F2v);
-                        i1 = n1;
-                        i2 = n2;
-                    } else {
-                        i1 = AR::mac1(i1, AR::coef(W[0]), F1);
-                    }
+                if constexpr (Q == 2) {
+                    const V n1 = AR::mac2(j1, AR::coef(W[0]), F1, AR::coef(W[1]), F2v);
+                    const V n2 = AR::mac2(j2, AR::coef(W[2]), F1, AR::coef(W[3]), F2v);
+                    j1 = n1;
+                    j2 = n2;
+                } else {
+                    j1 = AR::mac1(j1, AR::coef(W[0]), F1);
                 }
             }
-            u1 = i1;
-            u2 = i2;
         }
-#pragma unroll
-        for (int j = M - 1; j >= 0; j--) {
-            const int i = r0 + j;
-            if (active && i < ns) {
-                V b1, b2;
-                bcoef(i, b1, b2);
-                const V x = (Q == 2) ? AR::fms2(r[j], b1, u1, b2, u2) : AR::fms1(r[j], b1, u1);
-                r[j] = x;
-                u2 = u1;
-                u1 = x;
+        // ---- H+I: backward correction, residual form, FP64 conversion (in place) ----
+        IO* wlio = reinterpret_cast<IO*>(wl);
+#pragma unroll 2
+        for (int i = r0; i < r1; i++) {
+            const int ps = spos<M>(i);
+            V p1, p2;
+            if constexpr (CIRC) {
+                const F2* ph = cp.phb + (size_t)(r1 - 1 - i) * 2;
+                p1 = AR::coef(ph[0]);
+                p2 = AR::coef(ph[1]);
+            } else {
+                p1 = ctab[7 * LSc + ps];
+                p2 = ctab[8 * LSc + ps];
             }
+            V x = (Q == 2) ? AR::mac2(wl[ps], p1, j1, p2, j2) : AR::mac1(wl[ps], p1, j1);
+            if (cp.resid) x = AR::norm(AR::sub(line[ps], x));
+            wlio[ps] = AR::store(x);
         }
     }
+    __syncthreads();
 
-    // ---- write back through shared memory (coalesced global stores) ----
-    __syncthreads();
-    if (active) {
-        IO* dst = tio + l * cp.LS;
-#pragma unroll
-        for (int j = 0; j < M; j++) {
-            const int i = r0 + j;
-            if (i < ns) {
-                // residual-form operators return f - x; each lane reads then overwrites its own rows
-                const V x = cp.resid ? AR::norm(AR::sub(line[spos<M>(i)], r[j])) : r[j];
-                dst[spos<M>(i)] = AR::store(x);
-            }
-        }
-    }
-    __syncthreads();
+    // ---- J: coalesced stores ----
     if (ls.op == 1) {
         const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
         for (int ll = warp; ll < nl; ll += nw) {
             IO* o = out + base_out[ll];
-            const IO* src = tio + ll * cp.LS;
+            const IO* src = wio + ll * cp.LS;
             for (int p = lane; p < cp.nout; p += 32) o[p] = src[spos<M>(p < ns ? p : p - ns)];
         }
     } else {
-        const int ll = tid % cp.L, p0 = tid / cp.L, ps = nth / cp.L;
+        const int ll = tid % cp.L, pstep = nth / cp.L;
         if (ll < nl) {
             IO* o = out + base_out[ll];
-            const IO* src = tio + ll * cp.LS;
-            for (int p = p0; p < cp.nout; p += ps) o[(long)p * ls.op] = src[spos<M>(p < ns ? p : p - ns)];
+            const IO* src = wio + ll * cp.LS;
+            for (int p = tid / cp.L; p < cp.nout; p += pstep) o[(long)p * ls.op] = src[spos<M>(p < ns ? p : p - ns)];
         }
     }
     if (bad) atomicOr(status, 1u);
@@ -350,7 +363,9 @@ int launch_chunk_t(const ChunkParams& c, const void* f, void* out, const LineSet
     using IO = typename AR::IO;
     const int threads = c.L * c.Pp;
     const long blocks = (ls.nlines + c.L - 1) / c.L;
-    const size_t smem = 16 * (size_t)c.L + sizeof(typename AR::V) * (size_t)c.L * c.LS;
+    const int LSc = c.ns - 1 + (c.ns - 1) / M + 1;
+    const size_t smem = 16 * (size_t)c.L + 2 * sizeof(typename AR::V) * (size_t)c.L * c.LS +
+                        ((!CIRC && Q > 0) ? 9 * sizeof(typename AR::V) * (size_t)LSc : 0);
     auto kern = k_chunk<AR, Q, M, CIRC>;
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -227,6 +227,42 @@ int build_chunk_plan(const HostPlan& hp, int M, ChunkPlanHost& cp) {
                 cp.bscan[((size_t)t * kMaxSteps + k) * 4 + x] = (double)B[x];
             }
         }
+    // fundamental solutions within chunks
+    if (cp.circ) {
+        cp.phf.assign((size_t)M * 2, 0.0);
+        cp.phb.assign((size_t)M * 2, 0.0);
+        Mat F = eye(), B = eye();
+        for (int j = 0; j < M; j++) {
+            Mat Ci = {-rc[0][1], -rc[0][2], 1.0L, 0.0L};
+            F = mul(Ci, F);
+            cp.phf[(size_t)j * 2] = (double)F[0];
+            cp.phf[(size_t)j * 2 + 1] = (double)F[1];
+            Mat Di = {-rc[0][3], -rc[0][4], 1.0L, 0.0L};
+            B = mul(Di, B);
+            cp.phb[(size_t)j * 2] = (double)B[0];
+            cp.phb[(size_t)j * 2 + 1] = (double)B[1];
+        }
+    } else {
+        cp.phf.assign((size_t)ns * 2, 0.0);
+        cp.phb.assign((size_t)ns * 2, 0.0);
+        for (int t = 0; t < P; t++) {
+            int s0 = t * M, e0 = std::min(ns, s0 + M);
+            Mat F = eye();
+            for (int i = s0; i < e0; i++) {
+                Mat Ci = {-rc[i][1], -rc[i][2], 1.0L, 0.0L};
+                F = mul(Ci, F);
+                cp.phf[(size_t)i * 2] = (double)F[0];
+                cp.phf[(size_t)i * 2 + 1] = (double)F[1];
+            }
+            Mat B = eye();
+            for (int i = e0 - 1; i >= s0; i--) {
+                Mat Di = {-rc[i][3], -rc[i][4], 1.0L, 0.0L};
+                B = mul(Di, B);
+                cp.phb[(size_t)i * 2] = (double)B[0];
+                cp.phb[(size_t)i * 2 + 1] = (double)B[1];
+            }
+        }
+    }
     cp.fwrap.assign((size_t)Pp * 4, 0.0);
     cp.bwrap.assign((size_t)Pp * 4, 0.0);
     if (cp.circ) {

@@ -10,7 +10,8 @@
 // (periodic; then the coefficients are constants and the recurrences wrap around the
 // ring).  Each lane runs its chunk from a zero state, the lanes combine the chunk end
 // states with a log-step shuffle scan of the affine chunk transfers (precomputed here),
-// and each lane reruns its chunk from the exact incoming state.  No step truncates.
+// and each lane adds the response of its rows to the exact incoming state (precomputed
+// fundamental solutions, phf/phb).  No step truncates.
 #pragma once
 #include <vector>
 
@@ -53,6 +54,10 @@ struct ChunkPlanHost {
     double cg = 1.0, ca1 = 0.0, ca2 = 0.0;
     // scan matrices: fwd/bwd [lane][step] 2x2 (row-major), cyclic wrap [lane] 2x2
     std::vector<double> fscan, bscan, fwrap, bwrap;
+    // fundamental solutions inside a chunk: the response of row i to a unit incoming state,
+    // (phi1, phi2) per row (non-circulant, ns rows) or per position in the chunk counted
+    // from the chunk start (forward) / end (backward) (circulant, M positions)
+    std::vector<double> phf, phb;
 };
 
 int build_chunk_plan(const HostPlan& hp, int M, ChunkPlanHost& cp);

@@ -36,6 +36,8 @@ struct ChunkParams {
     const F2* bscan;
     const F2* fwrap;
     const F2* bwrap;
+    const F2* phf;  // fundamental solutions (see ChunkPlanHost)
+    const F2* phb;
 };
 
 class DevicePlan {

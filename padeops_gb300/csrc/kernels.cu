@@ -140,7 +140,7 @@ int DevicePlan::upload(const HostPlan& hp) {
     int rc = d.zero || d.identity ? PS_OK : build_chunk_plan(hp, M, ch_);
     cok_ = (rc == PS_OK && ch_.ok && ch_.use_pairs);
     size_t o_ctidx = 0, o_ctc[2] = {0, 0}, o_rc[2] = {0, 0}, o_fs[2] = {0, 0}, o_bs[2] = {0, 0}, o_fw[2] = {0, 0},
-           o_bw[2] = {0, 0};
+           o_bw[2] = {0, 0}, o_pf[2] = {0, 0}, o_pb[2] = {0, 0};
     // circulant: fold the forward scale 1/c into the stencil and edge rows
     const double cg = (cok_ && ch_.circ) ? ch_.rc[0] : 1.0;
     if (cok_) {
@@ -166,6 +166,10 @@ int DevicePlan::upload(const HostPlan& hp) {
             o_fw[v] = A.put(fw.data(), fw.size() * sizeof(F2));
             auto bw = conv(ch_.bwrap, 1.0);
             o_bw[v] = A.put(bw.data(), bw.size() * sizeof(F2));
+            auto pf = conv(ch_.phf, 1.0);
+            o_pf[v] = A.put(pf.data(), pf.size() * sizeof(F2));
+            auto pb = conv(ch_.phb, 1.0);
+            o_pb[v] = A.put(pb.data(), pb.size() * sizeof(F2));
         }
     }
     const cudaError_t me = cudaMalloc(&dev_, A.host.size());
@@ -242,6 +246,8 @@ int DevicePlan::upload(const HostPlan& hp) {
             c.bscan = (const F2*)(base + o_bs[v]);
             c.fwrap = (const F2*)(base + o_fw[v]);
             c.bwrap = (const F2*)(base + o_bw[v]);
+            c.phf = (const F2*)(base + o_pf[v]);
+            c.phb = (const F2*)(base + o_pb[v]);
             (v == 0 ? cdf_ : cf32_) = c;
         }
     }
