@@ -38,6 +38,7 @@ extern "C" {
 #define PADE_ENOTSUP 1004
 #define PADE_ETIMEOUT 1005
 #define PADE_ERANGE 1006 /* an input left the double-float path's range (|f| in [2^-74, 2^127)) */
+#define PADE_ESCRATCH 1007 /* pade_apply_noalloc: a host buffer exceeds its static staging capacity */
 
 /* ---- arithmetic paths (pade_set_path) ---- */
 #define PADE_PATH_DF 0     /* default: double-float arithmetic on the FP32 pipes, FP64 in/out */
@@ -132,6 +133,18 @@ int pade_set_path(pade_op op, int path);
  * whose other two extents are na, nb.  path PADE_PATH_FP32 takes float arrays. */
 int pade_apply(pade_op op, int opcode, int dir, int is_complex, const void* f, void* out, int na, int nb, int bc1,
                int bcn, int path, void* stream);
+/* No counterpart in the reference.  The FP64 operator application of pade_apply (the
+ * object's arithmetic path; device or host buffers) for callers that cannot allocate
+ * device memory once their time loop runs: it calls no cudaMalloc, cudaFree or other
+ * allocating routine.  Host-buffer staging and the error flag live in one file-scope
+ * device array of PADE_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the library
+ * until exit; host buffers larger than half of it return PADE_ESCRATCH.  All calls share
+ * the array (the flag is cleared per call), so calls whose GPU work overlaps race.  The
+ * first call on a device resolves the array's address (make it before any stream
+ * capture).  Device-pointer calls are asynchronous and do not report PADE_ERANGE. */
+#define PADE_NOALLOC_SCRATCH_BYTES (32u << 20)
+int pade_apply_noalloc(pade_op op, int opcode, int dir, int is_complex, const void* f, void* out, int na, int nb,
+                       int bc1, int bcn, void* stream);
 /* Read and clear the sticky error flags raised by asynchronous device-pointer calls
  * (synchronises the device).  *flags != 0 means some input left the df range. */
 int pade_get_status(pade_op op, int* flags);

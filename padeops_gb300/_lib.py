@@ -24,6 +24,8 @@ PADE_ECUDA = 1003
 PADE_ENOTSUP = 1004
 PADE_ETIMEOUT = 1005
 PADE_ERANGE = 1006
+PADE_ESCRATCH = 1007
+NOALLOC_SCRATCH_BYTES = 32 << 20
 
 PATH_DF = 0
 PATH_NATIVE = 1
@@ -73,6 +75,7 @@ def lib():
         "pade_destroy": [vp],
         "pade_set_path": [vp, i],
         "pade_apply": [vp, i, i, i, vp, vp, i, i, i, i, i, vp],
+        "pade_apply_noalloc": [vp, i, i, i, vp, vp, i, i, i, i, vp],
         "pade_get_status": [vp, pi],
         "pade_get_lengths": [vp, i, pi, pi],
         "pade_plan_check": [i, dp, i, i, i, dp, dp, i],

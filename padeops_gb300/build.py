@@ -16,8 +16,8 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libpadeops_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["operators.cpp", "plan.cpp", "chunkplan.cpp", "capi.cpp"]
-CUDA_SOURCES = ["kernels.cu", "kernels_df16.cu", "kernels_df32.cu", "kernels_f32.cu"]
-HEADERS = ["operators.h", "plan.h", "chunkplan.h", "engine.h", "dfmath.cuh", "chunk_kernel.cuh"]
+CUDA_SOURCES = ["kernels.cu", "kernels_df16.cu", "kernels_df32.cu", "kernels_f32.cu", "noalloc.cu"]
+HEADERS = ["operators.h", "plan.h", "chunkplan.h", "engine.h", "dfmath.cuh", "chunk_kernel.cuh", "capi_internal.h"]
 
 
 def _nvcc():

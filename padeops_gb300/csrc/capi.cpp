@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/padeops_gb300.h"
+#include "capi_internal.h"
 #include "engine.h"
 #include "operators.h"
 #include "plan.h"
@@ -16,40 +17,12 @@ using namespace pade;
 
 namespace {
 
-enum Family { F_CD06 = 0, F_CD10 = 1, F_CF90 = 2, F_GAUSS = 3, F_STAGG = 4 };
-
-int bcid(int bc) { return bc == 0 ? 0 : (bc == 1 ? 1 : 2); }
-bool bc_valid(int bc) { return bc == 0 || bc == 1 || bc == -1; }
 const int kBC[3] = {0, 1, -1};
 
 }  // namespace
 
-struct pade_op_s {
-    int family = 0;
-    int n = 0;
-    double dx = 1.0;
-    int periodic = 1, bc1 = 0, bcn = 0;
-    StaggCfg sc;
-    int path = PATH_DF;
-    // plans keyed by opcode * 16 + bc index (bcid(bc1) * 3 + bcid(bcn))
-    std::map<int, std::unique_ptr<DevicePlan>> plans;
-    std::map<int, int> plan_err;  // opcodes the reference refuses (e.g. cd06 non-periodic d2)
-    unsigned* status = nullptr;   // device flag word
-    // staging for host-pointer calls
-    std::mutex mu;
-    void* stage_in = nullptr;
-    void* stage_out = nullptr;
-    size_t stage_in_bytes = 0, stage_out_bytes = 0;
-    ~pade_op_s() {
-        if (status) cudaFree(status);
-        if (stage_in) cudaFree(stage_in);
-        if (stage_out) cudaFree(stage_out);
-    }
-};
 
 namespace {
-
-int key(int opcode, int bc1, int bcn) { return opcode * 16 + bcid(bc1) * 3 + bcid(bcn); }
 
 int define(int family, int n, double dx, int periodic, const StaggCfg& sc, int opcode, int bc1, int bcn,
            OpDef& d) {
@@ -69,7 +42,7 @@ int add_plan(pade_op_s* h, int opcode, int bc1, int bcn) {
     const int dbc1 = h->family == F_CD06 ? h->bc1 : bc1, dbcn = h->family == F_CD06 ? h->bcn : bcn;
     int rc = define(h->family, h->n, h->dx, h->periodic, h->sc, opcode, dbc1, dbcn, d);
     if (rc != PS_OK) {
-        h->plan_err[key(opcode, bc1, bcn)] = rc;
+        h->plan_err[plan_key(opcode, bc1, bcn)] = rc;
         return rc;
     }
     HostPlan hp;
@@ -78,7 +51,7 @@ int add_plan(pade_op_s* h, int opcode, int bc1, int bcn) {
     auto dp = std::make_unique<DevicePlan>();
     rc = dp->upload(hp);
     if (rc != PS_OK) return rc;
-    h->plans[key(opcode, bc1, bcn)] = std::move(dp);
+    h->plans[plan_key(opcode, bc1, bcn)] = std::move(dp);
     return PS_OK;
 }
 
@@ -158,9 +131,9 @@ int apply(pade_op h, int opcode, int dir, int cplx, const void* f, void* out, in
     } else {
         bc1 = bcn = 0;
     }
-    auto e = h->plan_err.find(key(opcode, bc1, bcn));
+    auto e = h->plan_err.find(plan_key(opcode, bc1, bcn));
     if (e != h->plan_err.end()) return e->second;
-    auto it = h->plans.find(key(opcode, bc1, bcn));
+    auto it = h->plans.find(plan_key(opcode, bc1, bcn));
     if (it == h->plans.end()) return PS_EINVAL;
     const DevicePlan& P = *it->second;
     const OpDef& d = P.host().def;
@@ -428,6 +401,7 @@ const char* pade_strerror(int s) {
     case PS_ENOTSUP: return "operation not supported for this object";
     case PS_ETIMEOUT: return "timed out";
     case PS_ERANGE: return "input outside the double-float range";
+    case PADE_ESCRATCH: return "buffer larger than the static staging capacity of pade_apply_noalloc";
     }
     return "unknown status";
 }
