@@ -152,6 +152,74 @@ int pade_get_status(pade_op op, int* flags);
 int pade_get_lengths(pade_op op, int opcode, int* n_in, int* n_out);
 const char* pade_strerror(int status);
 
+/* ==== spectral layer, Poisson solvers and pencil transposes (device pointers only) ====
+ * One GPU holds the whole grid: the reference's x/y/z pencils are the same (i,j,k)
+ * Fortran-ordered array.  FFT lengths must be powers of two from 2 to 8192 (otherwise
+ * PADE_ENOTSUP); transforms are FFTW-convention (forward exp(-i..), unnormalised).
+ * Calls on one handle share its workspace: order them on one stream. */
+typedef struct pade_spectral_s* pade_spectral;
+typedef struct pade_poisson_s* pade_poisson;
+typedef struct pade_poisson3d_s* pade_poisson3d;
+/* modified-wavenumber callback: maps k*d to k'*d in place (PoissonPeriodic.F90:11-16) */
+typedef void (*pade_modk_fn)(double* kd, int n);
+
+/* GetWaveNums (src/incompressible/spectral.F90:1748-1764 = src/utilities/PoissonPeriodic.F90:
+ * 226-242): ifftshifted wavenumbers of n points at spacing dx.  Host only. */
+int pade_wavenumbers(int n, double dx, double* k);
+/* getmodCD06stagg (src/incompressible/PadeDerOps.F90:1034-1053).  Host only. */
+int pade_modified_wavenumbers_cd06stagg(const double* k, int n, double dz, double* kp);
+
+/* spectral (src/incompressible/spectral.F90:867-1215 init for two periodic directions,
+ * fft/ifft 1413-1452 -> fft_3d.F90:616-663 fft2_x2y / ifft2_y2x).  fix_oddball zeroes the
+ * Nyquist wavenumbers k1(nx/2+1), k2(ny/2+1) (the reference default). */
+int pade_spectral_init(pade_spectral* sp, int nx, int ny, int nz, double dx, double dy, int fix_oddball);
+int pade_spectral_destroy(pade_spectral sp);
+/* k1 (nx/2+1 entries) and k2 (ny entries) as the spectral type stores them */
+int pade_spectral_get_wavenumbers(pade_spectral sp, double* k1, double* k2);
+/* real (nx,ny,nz) -> complex (nx/2+1,ny,nz): r2c along x, forward c2c along y */
+int pade_spectral_fft(pade_spectral sp, const double* in, void* out, void* stream);
+/* complex (nx/2+1,ny,nz) -> real (nx,ny,nz): backward c2c y, c2r x, times 1/(nx ny);
+ * set_oddball zeroes the x-Nyquist modes first (fft_3d.F90:633-635).  `in` is not modified. */
+int pade_spectral_ifft(pade_spectral sp, const void* in, double* out, int set_oddball, void* stream);
+
+/* padepoisson with PeriodicInZ (src/incompressible/PadePoisson.F90:130-200, 76-128): the
+ * periodic staggered-CD06 projection.  Keeps a pointer to `sp` (which must outlive it). */
+int pade_poisson_periodic_init(pade_poisson* p, pade_spectral sp, double dx, double dy, double dz);
+int pade_poisson_destroy(pade_poisson p);
+/* k3 modified wavenumbers used in |k|^2 (nz entries) */
+int pade_poisson_get_modified_k3(pade_poisson p, double* k3mod);
+/* PressureProjection -> PeriodicProjection (PadePoisson.F90:386-441): uhat, vhat complex
+ * (nx/2+1,ny,nz), what complex (nx/2+1,ny,nz+1), all updated in place. */
+int pade_poisson_projection(pade_poisson p, void* uhat, void* vhat, void* what, void* stream);
+/* DivergenceCheck (PadePoisson.F90:1165-1246): divergence real (nx,ny,nz).  fix_div
+ * re-projects when max(divergence) > 1e-13 (and again above 1e-10).  maxdiv (host, may be
+ * NULL when fix_div is 0) receives the signed maximum of the last divergence computed;
+ * asking for it synchronises the stream. */
+int pade_poisson_divergence_check(pade_poisson p, void* uhat, void* vhat, void* what, double* divergence,
+                                  int fix_div, double* maxdiv, void* stream);
+
+/* PoissonPeriodic (src/utilities/PoissonPeriodic.F90:120-210 init, 37-111 poisson_solve):
+ * triply periodic solve of lap f = rhs, f and rhs real (nx,ny,nz); rhs == f solves in
+ * place.  dir_id 1..3 names the input pencil (all the same array here); the callbacks
+ * (may be NULL) modify k*dx, k*dy, k*dz. */
+int pade_poisson3d_init(pade_poisson3d* p, int nx, int ny, int nz, double dx, double dy, double dz, int dir_id,
+                        pade_modk_fn modkx, pade_modk_fn modky, pade_modk_fn modkz);
+int pade_poisson3d_destroy(pade_poisson3d p);
+int pade_poisson3d_solve(pade_poisson3d p, const double* rhs, double* f, void* stream);
+
+/* FFT building blocks (the FFTW plans of fft_3d.F90:198-350): c2c along dir of complex
+ * (n1,n2,n3), sign -1 forward / +1 backward, times scale; r2c along x (nx,ny,nz) ->
+ * (nx/2+1,ny,nz); c2r along x, times scale.  in == out is allowed for c2c. */
+int pade_fft_c2c(int dir, int sign, const void* in, void* out, int n1, int n2, int n3, double scale, void* stream);
+int pade_fft_r2c_x(const double* in, void* out, int nx, int ny, int nz, void* stream);
+int pade_fft_c2r_x(const void* in, double* out, int nx, int ny, int nz, double scale, void* stream);
+
+/* 2DECOMP transpose_x_to_y / y_to_z / z_to_y / y_to_x (pencil 1 = x, 2 = y, 3 = z) for
+ * one rank: the pencils share the (i,j,k) layout, so this is a device copy of n1*n2*n3
+ * elements of elem_bytes (8 real, 16 complex). */
+int pade_transpose(int from_pencil, int to_pencil, const void* in, void* out, int n1, int n2, int n3,
+                   int elem_bytes, void* stream);
+
 /* ---- host-only plan inspection (no GPU needed; never called by the entry points above) ----
  * family: 0 cd06, 1 cd10, 2 cf90, 3 gaussian, 4 cd06stagg.
  * params: cd06/cd10 {n, dx, periodic}; cf90/gaussian {n, periodic};

@@ -36,6 +36,9 @@ STAGG_OPS = ("ddz_E2C", "ddz_C2E", "ddz_C2C", "ddz_E2E", "d2dz2_C2C", "d2dz2_E2E
 
 _lib = None
 
+# void (*)(double* kd, int n): modified-wavenumber callback of pade_poisson3d_init
+MODK_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_double), ctypes.c_int)
+
 
 class PadeError(RuntimeError):
     """A non-zero status from the library (the reference would GracefulExit here)."""
@@ -90,6 +93,27 @@ def lib():
     for nm in STAGG_OPS:
         sig[f"pade_cd06stagg_{nm}"] = [vp, vp, vp, i, i, vp]
         sig[f"pade_cd06stagg_{nm}_cmplx"] = [vp, vp, vp, i, i, vp]
+    sig.update({
+        "pade_wavenumbers": [i, d, dp],
+        "pade_modified_wavenumbers_cd06stagg": [dp, i, d, dp],
+        "pade_spectral_init": [pop, i, i, i, d, d, i],
+        "pade_spectral_destroy": [vp],
+        "pade_spectral_get_wavenumbers": [vp, dp, dp],
+        "pade_spectral_fft": [vp, vp, vp, vp],
+        "pade_spectral_ifft": [vp, vp, vp, i, vp],
+        "pade_poisson_periodic_init": [pop, vp, d, d, d],
+        "pade_poisson_destroy": [vp],
+        "pade_poisson_get_modified_k3": [vp, dp],
+        "pade_poisson_projection": [vp, vp, vp, vp, vp],
+        "pade_poisson_divergence_check": [vp, vp, vp, vp, vp, i, dp, vp],
+        "pade_poisson3d_init": [pop, i, i, i, d, d, d, i, MODK_FN, MODK_FN, MODK_FN],
+        "pade_poisson3d_destroy": [vp],
+        "pade_poisson3d_solve": [vp, vp, vp, vp],
+        "pade_fft_c2c": [i, i, vp, vp, i, i, i, d, vp],
+        "pade_fft_r2c_x": [vp, vp, i, i, i, vp],
+        "pade_fft_c2r_x": [vp, vp, i, i, i, d, vp],
+        "pade_transpose": [i, i, vp, vp, i, i, i, i, vp],
+    })
     for name, args in sig.items():
         fn = getattr(L, name)
         fn.argtypes = args

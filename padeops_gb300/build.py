@@ -16,8 +16,10 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libpadeops_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["operators.cpp", "plan.cpp", "chunkplan.cpp", "capi.cpp"]
-CUDA_SOURCES = ["kernels.cu", "kernels_df16.cu", "kernels_df32.cu", "kernels_f32.cu", "noalloc.cu"]
-HEADERS = ["operators.h", "plan.h", "chunkplan.h", "engine.h", "dfmath.cuh", "chunk_kernel.cuh", "capi_internal.h"]
+CUDA_SOURCES = ["kernels.cu", "kernels_df16.cu", "kernels_df32.cu", "kernels_f32.cu", "noalloc.cu", "fft.cu",
+                "spectral.cu"]
+HEADERS = ["operators.h", "plan.h", "chunkplan.h", "engine.h", "dfmath.cuh", "chunk_kernel.cuh", "capi_internal.h",
+           "fft.h"]
 
 
 def _nvcc():
@@ -46,7 +48,9 @@ def build(force=False, verbose=False):
     if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == dig:
         return LIB
     nvcc = _nvcc()
-    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+    # host code: no floating-point contraction, so x86 and Arm builds round alike
+    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I",
+              os.path.join(ROOT, "include")]
     procs = []
     objs = []
     for name in HOST_SOURCES + CUDA_SOURCES:

@@ -1,0 +1,51 @@
+// Batched FP64 line FFTs (fft.cu) used by the spectral and Poisson layers (spectral.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace pade {
+
+// Lines of a 3-D array: line l has a = l % na, b = l / na and point p at
+// a * fa + b * fb + p * fp (input) and a * oa + b * ob + p * op (output), in elements of
+// the respective input/output type (double2 for complex, double for real).
+struct FftLines {
+    long nlines, na;
+    long fa, fb, fp;
+    long oa, ob, op;
+};
+
+enum FftIn { IN_COMPLEX = 0, IN_REAL = 1, IN_HALF = 2 };
+enum FftOut { OUT_COMPLEX = 0, OUT_HALF = 1, OUT_REAL = 2 };
+
+// What happens between loading and storing a line.
+enum FftKind {
+    FK_PLAIN = 0,      // one transform with the given sign
+    FK_PROJECT = 1,    // PadePoisson periodic projection along z (see FftExtra)
+    FK_POISSON3D = 2,  // PoissonPeriodic: forward, multiply, backward along z
+};
+
+// Extra operands of FK_PROJECT / FK_POISSON3D.  Lines run along z through complex
+// (nxh, ny, nz) arrays: line l = i + nxh * j, point stride plane = nxh * ny.
+struct FftExtra {
+    const double* ka;  // per i: wavenumber entering |k|^2
+    const double* kb;  // per j
+    const double* kc;  // per point along the line
+    const double* k1;  // FK_PROJECT: spectral wavenumbers of d/dx, d/dy (per i, per j)
+    const double* k2;
+    double2* u;        // FK_PROJECT: uhat, vhat, read for the divergence, updated in place
+    double2* v;
+    long nxh;
+    long plane;
+};
+
+FftLines fft_lines(int dir, long n1, long n2, long n3, long in_len, long out_len);
+
+// Launch one batched transform of length n (a power of two, 2..8192).  sign -1 is the
+// forward (exp(-i...)) transform, +1 the backward one; outputs are multiplied by scale.
+// oddball (IN_HALF only) zeroes the Nyquist entry before the complex-to-real transform.
+int fft_launch(int in_mode, int out_mode, int kind, int n, int sign, double scale, int oddball, const void* in,
+               void* out, const FftLines& ls, const FftExtra& ex, cudaStream_t s);
+
+// Number of kernels fft_launch starts per call (for launch accounting).
+constexpr int kFftKernelsPerLaunch = 1;
+
+}  // namespace pade

@@ -1,0 +1,89 @@
+"""Mirror of module spectralMod (src/incompressible/spectral.F90): type spectral.
+
+The x-y Fourier layer of the incompressible solver for grids periodic in x and y:
+``fft`` = r2c along x then forward c2c along y, ``ifft`` = backward c2c along y, optional
+oddball zeroing, c2r along x, times 1/(nx ny) (fft_3d.F90:616-663).  Arrays are CUDA
+torch tensors in Fortran order (x fastest): physical (nx, ny, nz) float64, spectral
+(nx/2+1, ny, nz) complex128.  Transform lengths must be powers of two.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from ._base import buffer
+
+
+def GetWaveNums(n, dx):
+    """spectral.F90:1748-1764 (host)."""
+    k = np.empty(n)
+    L.check(L.lib().pade_wavenumbers(int(n), float(dx), k.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+            "GetWaveNums")
+    return k
+
+
+def getmodCD06stagg(k, dz):
+    """PadeDerOps.F90:1034-1053 (host)."""
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    kp = np.empty_like(k)
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.check(L.lib().pade_modified_wavenumbers_cd06stagg(k.ctypes.data_as(dp), k.size, float(dz), kp.ctypes.data_as(dp)),
+            "getmodCD06stagg")
+    return kp
+
+
+def _dev(a, what):
+    p, cplx, stream, _ = buffer(a, what, complex_ok=True)
+    if stream is None:
+        raise TypeError(f"{what} must be a CUDA tensor")
+    return p, cplx, stream
+
+
+class spectral:
+    """Two-periodic spectral type: init, fft, ifft, k1/k2 wavenumbers."""
+
+    def __init__(self):
+        self._h = ctypes.c_void_p(None)
+
+    def init(self, nx, ny, nz, dx, dy, fixOddball=True):
+        """spectral.F90:867-1215 for the x-y periodic (two-dimensional transform) case."""
+        self.destroy()
+        h = ctypes.c_void_p(None)
+        L.check(L.lib().pade_spectral_init(ctypes.byref(h), int(nx), int(ny), int(nz), float(dx), float(dy),
+                                           int(bool(fixOddball))), "spectral.init")
+        self._h = h
+        self.nx_g, self.ny_g, self.nz_g = nx, ny, nz
+        self.physical_shape = (nx, ny, nz)
+        self.spectral_shape = (nx // 2 + 1, ny, nz)
+        k1 = np.empty(nx // 2 + 1)
+        k2 = np.empty(ny)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.check(L.lib().pade_spectral_get_wavenumbers(h, k1.ctypes.data_as(dp), k2.ctypes.data_as(dp)))
+        self.k1_1d, self.k2_1d = k1, k2
+
+    @property
+    def handle(self):
+        if not self._h.value:
+            raise L.PadeError(L.PADE_EINVAL, "spectral used before init")
+        return self._h
+
+    def fft(self, arr_in, arr_out):
+        pi, _, s = _dev(arr_in, "arr_in")
+        po, _, _ = _dev(arr_out, "arr_out")
+        L.check(L.lib().pade_spectral_fft(self.handle, pi, po, s), "spectral.fft")
+
+    def ifft(self, arr_in, arr_out, setOddball=False):
+        pi, _, s = _dev(arr_in, "arr_in")
+        po, _, _ = _dev(arr_out, "arr_out")
+        L.check(L.lib().pade_spectral_ifft(self.handle, pi, po, int(bool(setOddball)), s), "spectral.ifft")
+
+    def destroy(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            L.lib().pade_spectral_destroy(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
