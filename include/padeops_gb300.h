@@ -220,6 +220,53 @@ int pade_fft_c2r_x(const void* in, double* out, int nx, int ny, int nz, double s
 int pade_transpose(int from_pencil, int to_pencil, const void* in, void* out, int n1, int n2, int n3,
                    int elem_bytes, void* stream);
 
+/* ==== LES time step of the incompressible solver (src/incompressible/igrid.F90) ====
+ * Periodic in x, y (Fourier) and z (staggered CD06), rotational advection, TVD-RK3,
+ * viscosity 1/Re, Smagorinsky / standard dynamic procedure (sgsmod_igrid.F90,
+ * standardDynamicProcedure.F90).  Fields live on the device; grid sizes are powers of two.
+ * The reference's own dynamic test filter is not available for periodic z (spectral.F90:
+ * 1338-1341); this library applies the same x-y cutoff there. */
+typedef struct pade_les_s* pade_les;
+typedef struct {
+    int nx, ny, nz;
+    double Lx, Ly, Lz;
+    double Re;             /* molecular viscosity 1/Re (addViscousTerm) */
+    int isInviscid;
+    double CFL;            /* > 0: dt from compute_deltaT (igrid.F90:1374-1403) */
+    double dt;             /* fixed time step when CFL <= 0 */
+    int useSGS, dynamic;   /* dynamic: DynamicProcedureType 1 (planar averages) */
+    double Csgs;           /* Smagorinsky constant when not dynamic */
+    double deltaRatio;     /* test-filter width ratio (default 2) */
+    int DynProcFreq;       /* dynamic procedure every DynProcFreq steps */
+    double dealiasFact;    /* 2/3 rule by default */
+    int t_DivergenceCheck; /* check/fix the divergence every t steps (0: never) */
+} pade_les_params;
+#define PADE_LES_UHAT 0
+#define PADE_LES_VHAT 1
+#define PADE_LES_WHAT 2
+#define PADE_LES_U 3
+#define PADE_LES_V 4
+#define PADE_LES_WC 5
+#define PADE_LES_W 6
+#define PADE_LES_UE 7
+#define PADE_LES_VE 8
+#define PADE_LES_NUC 30
+#define PADE_LES_NUE 31
+/* duidxjC(:,:,:,i) is field 10+i-1, duidxjE(:,:,:,i) is 20+i-1 (i = 1..9, igrid order) */
+int pade_les_init(pade_les* les, const pade_les_params* params);
+int pade_les_destroy(pade_les les);
+/* initial physical fields (device): u, v (nx,ny,nz), w on edges (nx,ny,nz+1); runs the
+ * igrid init sequence (igrid.F90:625-648) and synchronises */
+int pade_les_set_fields(pade_les les, const double* u, const double* v, const double* w, void* stream);
+/* one TVD-RK3 step on `stream`; use_graph replays a captured CUDA graph for steps without
+ * a divergence check (needs a non-NULL stream) */
+int pade_les_step(pade_les les, int use_graph, void* stream);
+/* last dt, simulated time, completed steps and the dynamic coefficient per z plane (nz
+ * entries, may be NULL); synchronises */
+int pade_les_info(pade_les les, double* dt, double* tsim, int* step, double* lambda1d);
+/* device pointer of an internal field (PADE_LES_*), valid until pade_les_destroy */
+int pade_les_field(pade_les les, int which, void** ptr);
+
 /* ---- host-only plan inspection (no GPU needed; never called by the entry points above) ----
  * family: 0 cd06, 1 cd10, 2 cf90, 3 gaussian, 4 cd06stagg.
  * params: cd06/cd10 {n, dx, periodic}; cf90/gaussian {n, periodic};

@@ -1,0 +1,98 @@
+"""Mirror of module IncompressibleGrid (src/incompressible/igrid.F90): type igrid, restricted
+to the periodic-in-z LES configuration this library provides.
+
+Fourier x/y, staggered CD06 z, rotational advection, TVD-RK3, viscosity 1/Re, and the
+Smagorinsky model with the standard dynamic procedure.  Parameters that the reference
+reads from its namelist input file are keyword arguments here; fields are CUDA torch
+tensors in Fortran order (x fastest): u, v (nx, ny, nz), w on the nz+1 edges.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from .spectralMod import _dev
+
+try:
+    import torch
+except ImportError:  # pragma: no cover
+    torch = None
+
+
+class igrid:
+    def __init__(self):
+        self._h = ctypes.c_void_p(None)
+
+    def init(self, nx, ny, nz, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, Re=1000.0, isInviscid=False, CFL=0.5,
+             dt=-1.0, useSGS=True, DynamicProcedureType=1, Csgs=0.17, deltaRatio=2.0, DynProcFreq=1,
+             dealiasFact=2.0 / 3.0, t_DivergenceCheck=10):
+        """igrid init (igrid.F90:330-660) for PeriodicInZ with SGSModelID 0 (Smagorinsky)."""
+        if DynamicProcedureType not in (0, 1):
+            raise L.PadeError(L.PADE_ENOTSUP, "only DynamicProcedureType 0 or 1")
+        self.destroy()
+        p = L.LesParams(nx, ny, nz, Lx, Ly, Lz, Re, int(bool(isInviscid)), CFL, dt, int(bool(useSGS)),
+                        int(DynamicProcedureType == 1), Csgs, deltaRatio, DynProcFreq, dealiasFact,
+                        t_DivergenceCheck)
+        h = ctypes.c_void_p(None)
+        L.check(L.lib().pade_les_init(ctypes.byref(h), ctypes.byref(p)), "igrid.init")
+        self._h = h
+        self.nx, self.ny, self.nz = nx, ny, nz
+
+    @property
+    def handle(self):
+        if not self._h.value:
+            raise L.PadeError(L.PADE_EINVAL, "igrid used before init")
+        return self._h
+
+    def set_fields(self, u, v, w):
+        pu, _, s = _dev(u, "u")
+        pv, _, _ = _dev(v, "v")
+        pw, _, _ = _dev(w, "w")
+        L.check(L.lib().pade_les_set_fields(self.handle, pu, pv, pw, s), "igrid.set_fields")
+
+    def timeAdvance(self, use_graph=True):
+        """One TVD_RK3 step (TimeSteppingScheme 1) on torch's current stream."""
+        s = torch.cuda.current_stream().cuda_stream if torch is not None else None
+        L.check(L.lib().pade_les_step(self.handle, int(bool(use_graph)), s), "igrid.timeAdvance")
+
+    def info(self):
+        dt, ts, st = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        lam = np.empty(self.nz)
+        L.check(L.lib().pade_les_info(self.handle, ctypes.byref(dt), ctypes.byref(ts), ctypes.byref(st),
+                                      lam.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return {"dt": dt.value, "tsim": ts.value, "step": st.value, "lambda": lam}
+
+    def field(self, name):
+        """A copy of an internal field as a CUDA tensor (Fortran-shaped view reversed)."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        nxh = nx // 2 + 1
+        shapes = {"uhat": ((nz, ny, nxh), True), "vhat": ((nz, ny, nxh), True), "what": ((nz + 1, ny, nxh), True),
+                  "u": ((nz, ny, nx), False), "v": ((nz, ny, nx), False), "wC": ((nz, ny, nx), False),
+                  "w": ((nz + 1, ny, nx), False), "uE": ((nz + 1, ny, nx), False), "vE": ((nz + 1, ny, nx), False),
+                  "nu_sgs_C": ((nz, ny, nx), False), "nu_sgs_E": ((nz + 1, ny, nx), False)}
+        if name.startswith("duidxjC") or name.startswith("duidxjE"):
+            idx = int(name[7:]) - 1
+            which = (10 if name[6] == "C" else 20) + idx
+            shape, cplx = ((nz if name[6] == "C" else nz + 1, ny, nx), False)
+        else:
+            which = L.LES_FIELDS[name]
+            shape, cplx = shapes[name]
+        p = ctypes.c_void_p(None)
+        L.check(L.lib().pade_les_field(self.handle, which, ctypes.byref(p)))
+        n = int(np.prod(shape)) * (2 if cplx else 1)
+        t = torch.empty(n, dtype=torch.float64, device="cuda")
+        # one-rank transpose = device copy of n doubles, ordered on the current stream
+        L.check(L.lib().pade_transpose(1, 2, p, ctypes.c_void_p(t.data_ptr()), n, 1, 1, 8,
+                                       torch.cuda.current_stream().cuda_stream))
+        return (t.view(torch.complex128) if cplx else t).view(shape)
+
+    def destroy(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            L.lib().pade_les_destroy(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

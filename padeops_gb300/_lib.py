@@ -36,6 +36,20 @@ STAGG_OPS = ("ddz_E2C", "ddz_C2E", "ddz_C2C", "ddz_E2E", "d2dz2_C2C", "d2dz2_E2E
 
 _lib = None
 
+class LesParams(ctypes.Structure):
+    """pade_les_params (include/padeops_gb300.h)."""
+
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("Lx", ctypes.c_double), ("Ly", ctypes.c_double), ("Lz", ctypes.c_double),
+                ("Re", ctypes.c_double), ("isInviscid", ctypes.c_int), ("CFL", ctypes.c_double),
+                ("dt", ctypes.c_double), ("useSGS", ctypes.c_int), ("dynamic", ctypes.c_int),
+                ("Csgs", ctypes.c_double), ("deltaRatio", ctypes.c_double), ("DynProcFreq", ctypes.c_int),
+                ("dealiasFact", ctypes.c_double), ("t_DivergenceCheck", ctypes.c_int)]
+
+
+LES_FIELDS = {"uhat": 0, "vhat": 1, "what": 2, "u": 3, "v": 4, "wC": 5, "w": 6, "uE": 7, "vE": 8,
+              "nu_sgs_C": 30, "nu_sgs_E": 31}
+
 # void (*)(double* kd, int n): modified-wavenumber callback of pade_poisson3d_init
 MODK_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_double), ctypes.c_int)
 
@@ -113,6 +127,12 @@ def lib():
         "pade_fft_r2c_x": [vp, vp, i, i, i, vp],
         "pade_fft_c2r_x": [vp, vp, i, i, i, d, vp],
         "pade_transpose": [i, i, vp, vp, i, i, i, i, vp],
+        "pade_les_init": [pop, ctypes.POINTER(LesParams)],
+        "pade_les_destroy": [vp],
+        "pade_les_set_fields": [vp, vp, vp, vp, vp],
+        "pade_les_step": [vp, i, vp],
+        "pade_les_info": [vp, dp, dp, pi, dp],
+        "pade_les_field": [vp, i, pop],
     })
     for name, args in sig.items():
         fn = getattr(L, name)

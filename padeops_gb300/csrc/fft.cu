@@ -23,6 +23,11 @@
 //  * FK_POISSON3D, the z part of PoissonPeriodic (PoissonPeriodic.F90:89-111):
 //    forward, multiply by -1/(kx^2 + ky^2 + kz^2 + 1e-20) with the zero mode set to 0,
 //    backward.
+//  * FK_DEALIAS, spectral%dealias / dealias_edgeField for periodic z (spectral.F90:
+//    314-363, mask 777-811): forward, multiply by the 0/1 mask, backward times 1/nz; for
+//    an edge field the first plane is copied to plane nz+1.
+// FK_PLAIN can multiply by i*k on load (the mtimes_ik1/ik2 pass before an inverse
+// transform, spectral.F90:235-310), with the reference's two products per point.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -125,6 +130,12 @@ __global__ void __launch_bounds__(256) k_fft(const void* in, void* out, const Ff
             if (p == 0 || p == half) v.y = 0.0;
             if (oddball && p == half) v.x = 0.0;
         }
+        if (KIND == FK_PLAIN && ex.mul == MUL_MASK_AP) {
+            if (!(fabs(ex.ka[a]) < ex.cut_a && fabs(ex.kb[p]) < ex.cut_b)) v = make_double2(0.0, 0.0);
+        } else if (KIND == FK_PLAIN && ex.mul != MUL_NONE) {
+            const double k = ex.km[ex.mul == MUL_IK_A ? a : p];
+            v = make_double2(-k * v.y, k * v.x);
+        }
         if (KIND == FK_PROJECT) {
             // f2d = dwdz + i (k1 uhat + k2 vhat), PadePoisson.F90:391-407
             const long idx = lg + p * ex.plane;
@@ -146,10 +157,12 @@ __global__ void __launch_bounds__(256) k_fft(const void* in, void* out, const Ff
             const int l = e >> logn, p = e & (n - 1);
             const long lg = l0 + l;
             const long i = lg % ex.nxh, j = lg / ex.nxh;
-            const double kr = ksq(ex.ka[i], ex.kb[j], ex.kc[p]);
+            const double kr = KIND == FK_DEALIAS ? 0.0 : ksq(ex.ka[i], ex.kb[j], ex.kc[p]);
             double m;
             if (KIND == FK_PROJECT) {
                 m = kr <= 1e-14 ? 0.0 : -(1.0 / kr);
+            } else if (KIND == FK_DEALIAS) {
+                m = (fabs(ex.ka[i]) < ex.cut_a && fabs(ex.kb[j]) < ex.cut_b && fabs(ex.kc[p]) < ex.cut_c) ? 1.0 : 0.0;
             } else {
                 m = -1.0 / __dadd_rn(kr, 1e-20);
                 if (lg == 0 && p == 0) m = 0.0;
@@ -175,6 +188,7 @@ __global__ void __launch_bounds__(256) k_fft(const void* in, void* out, const Ff
         } else {
             reinterpret_cast<double2*>(out)[o] = v;
         }
+        if (KIND == FK_DEALIAS && ex.edge_copy && p == 0) reinterpret_cast<double2*>(out)[o + (long)n * ls.op] = v;
         if (KIND == FK_PROJECT) {
             // uhat -= i k1 p ; vhat -= i k2 p  (PadePoisson.F90:422-430)
             const long idx = lg + p * ex.plane;
@@ -272,6 +286,8 @@ int fft_launch(int in_mode, int out_mode, int kind, int n, int sign, double scal
         return launch_t<IN_COMPLEX, OUT_COMPLEX, FK_PROJECT>(in, out, ls, tw, logn, lb, sign, scale, 0, ex, s);
     if (kind == FK_POISSON3D)
         return launch_t<IN_COMPLEX, OUT_COMPLEX, FK_POISSON3D>(in, out, ls, tw, logn, lb, sign, scale, 0, ex, s);
+    if (kind == FK_DEALIAS)
+        return launch_t<IN_COMPLEX, OUT_COMPLEX, FK_DEALIAS>(in, out, ls, tw, logn, lb, sign, scale, 0, ex, s);
     if (in_mode == IN_COMPLEX && out_mode == OUT_COMPLEX)
         return launch_t<IN_COMPLEX, OUT_COMPLEX, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, scale, 0, ex, s);
     if (in_mode == IN_REAL && out_mode == OUT_HALF)

@@ -21,7 +21,15 @@ enum FftKind {
     FK_PLAIN = 0,      // one transform with the given sign
     FK_PROJECT = 1,    // PadePoisson periodic projection along z (see FftExtra)
     FK_POISSON3D = 2,  // PoissonPeriodic: forward, multiply, backward along z
+    FK_DEALIAS = 3,    // spectral dealias along z: forward, 0/1 mask, backward (see FftExtra)
 };
+
+// FK_PLAIN pre-multiplication on load (mtimes_ik1 / mtimes_ik2 of spectral.F90:235-310):
+// MUL_IK_A multiplies point (a, p) by i*km[a] (km indexed by the line's first index, the
+// x wavenumber of a y line), MUL_IK_P by i*km[p] (the wavenumber along the line).
+// MUL_MASK_AP keeps point (a, p) where |ka[a]| < cut_a and |kb[p]| < cut_b and zeroes it
+// otherwise (the x-y sharp test filter on a y line).
+enum FftMul { MUL_NONE = 0, MUL_IK_A = 1, MUL_IK_P = 2, MUL_MASK_AP = 3 };
 
 // Extra operands of FK_PROJECT / FK_POISSON3D.  Lines run along z through complex
 // (nxh, ny, nz) arrays: line l = i + nxh * j, point stride plane = nxh * ny.
@@ -35,6 +43,10 @@ struct FftExtra {
     double2* v;
     long nxh;
     long plane;
+    int mul;           // FftMul (FK_PLAIN)
+    const double* km;
+    double cut_a, cut_b, cut_c;  // FK_DEALIAS: keep |ka| < cut_a and |kb| < cut_b and |kc| < cut_c
+    int edge_copy;     // FK_DEALIAS: also store point 0 at point n (periodic edge plane)
 };
 
 FftLines fft_lines(int dir, long n1, long n2, long n3, long in_len, long out_len);

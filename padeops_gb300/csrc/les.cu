@@ -1,0 +1,885 @@
+// LES time step of the incompressible solver (igrid), periodic in z, on one GPU.
+//
+// Restates src/incompressible/igrid.F90 for the configuration PeriodicInZ, Fourier x/y,
+// staggered CD06 z (Pade6stagg periodic), rotational advection, TVD-RK3, molecular
+// viscosity 1/Re, and the Smagorinsky model with the standard (planar-averaged) dynamic
+// procedure; no stratification, Coriolis, forcing, turbines, fringe or wall model:
+//   TVD_RK3            igrid.F90:1105-1174     compute_deltaT        1374-1403
+//   populate_rhs       1793-1912               addNonLinearTerm_Rot  1497-1570
+//   addViscousTerm     1914-1959               project_and_prep      1961-1991
+//   dealiasFields      1020-1037               interp_PrimitiveVars  1423-1463
+//   compute_duidxj     2553-2684               init sequence         625-648
+//   getTauSGS/getRHS_SGS            sgsmod_igrid.F90:157-265
+//   Smagorinsky kernel, Sij, nu interpolation   smagorinsky.F90, eddyViscosity.F90
+//   DoStandardDynamicProcedure      standardDynamicProcedure.F90:74-244
+// The slip-wall BC codes of the periodic configuration select d2dz2_C2C for the viscous
+// z term of u and v (igrid.F90:2651-2658).  The test filter is spectral%InitTestFilter's
+// x-y sharp cutoff at (2/3)(pi/dx)/deltaRatio (spectral.F90:1333-1367); the reference
+// itself stops there for periodic-z problems (GracefulExit 1233).
+//
+// Every step is a fixed sequence of kernels on one stream with the time step held in
+// device memory, so steps without a divergence check (which reads a maximum on the host)
+// can be replayed from a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "../../include/padeops_gb300.h"
+#include "fft.h"
+#include "operators.h"
+#include "spectral_internal.h"
+
+using namespace pade;
+
+namespace {
+
+enum { OP_DDZ_E2C = 0, OP_DDZ_C2E = 1, OP_D2_C2C = 4, OP_D2_E2E = 5, OP_I_E2C = 6, OP_I_C2E = 7 };
+
+#define GRID_STRIDE(e, n) \
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < (n); e += (long)gridDim.x * blockDim.x)
+
+// non-contracting FP64 arithmetic: the reference evaluates each product and sum separately
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+
+// Sij from duidxj (eddyViscosity.F90:1-21); d holds 9 arrays at stride n
+__device__ __forceinline__ double sij(const double* const* d, int idx, long e) {
+    switch (idx) {
+        case 0: return d[0][e];
+        case 1: return 0.5 * add(d[1][e], d[3][e]);
+        case 2: return 0.5 * add(d[2][e], d[6][e]);
+        case 3: return d[4][e];
+        case 4: return 0.5 * add(d[5][e], d[7][e]);
+        default: return d[8][e];
+    }
+}
+
+// sqrt(2 Sij Sij) in the reference's summation order (smagorinsky.F90:39-67)
+__device__ __forceinline__ double smag(double s1, double s2, double s3, double s4, double s5, double s6) {
+    double s = mul(s1, s1);
+    s = add(s, 2.0 * mul(s2, s2));
+    s = add(s, 2.0 * mul(s3, s3));
+    s = add(s, mul(s4, s4));
+    s = add(s, 2.0 * mul(s5, s5));
+    s = add(s, mul(s6, s6));
+    return sqrt(2.0 * s);
+}
+
+struct Ptr9 {
+    const double* p[9];
+};
+
+// ---- addNonLinearTerm_Rot products (igrid.F90:1530-1557)
+__global__ void k_nl_c(Ptr9 dC, const double* __restrict__ u, const double* __restrict__ v, double* __restrict__ a,
+                       double* __restrict__ b, long n) {
+    GRID_STRIDE(e, n) {
+        const double dudy = dC.p[1][e], dvdx = dC.p[3][e];
+        a[e] = mul(sub(dvdx, dudy), v[e]);
+        b[e] = mul(sub(dudy, dvdx), u[e]);
+    }
+}
+
+__global__ void k_nl_e(Ptr9 dE, const double* __restrict__ w, const double* __restrict__ uE,
+                       const double* __restrict__ vE, double* __restrict__ a, double* __restrict__ b,
+                       double* __restrict__ c, long n) {
+    GRID_STRIDE(e, n) {
+        const double dudz = dE.p[2][e], dvdz = dE.p[5][e], dwdx = dE.p[6][e], dwdy = dE.p[7][e];
+        a[e] = mul(sub(dwdx, dudz), w[e]);
+        b[e] = mul(sub(dwdy, dvdz), w[e]);
+        c[e] = add(mul(sub(dudz, dwdx), uE[e]), mul(sub(dvdz, dwdy), vE[e]));
+    }
+}
+
+// rhs = rhs + f1  [+ (1/Re)(-kabs_sq fhat + d2)]  (igrid.F90:1537-1538, 1924-1930)
+__global__ void k_rhs_finish(double2* __restrict__ rhs, const double2* __restrict__ f1,
+                             const double2* __restrict__ fhat, const double2* __restrict__ d2,
+                             const double* __restrict__ k1, const double* __restrict__ k2, long nxh, long nxy,
+                             double oneByRe, int viscous, long n) {
+    GRID_STRIDE(e, n) {
+        double2 r = rhs[e];
+        if (f1) {
+            const double2 a = f1[e];
+            r = make_double2(add(r.x, a.x), add(r.y, a.y));
+        }
+        if (viscous) {
+            const long q = e % nxy;
+            const double ka = k1[q % nxh], kb = k2[q / nxh];
+            const double ks = add(mul(ka, ka), mul(kb, kb));
+            const double2 fh = fhat[e], dd = d2[e];
+            const double tx = add(mul(-ks, fh.x), dd.x), ty = add(mul(-ks, fh.y), dd.y);
+            r = make_double2(add(r.x, mul(oneByRe, tx)), add(r.y, mul(oneByRe, ty)));
+        }
+        rhs[e] = r;
+    }
+}
+
+// |S| at cell centres (get_smagorinsky_kernel); optional copy for the dynamic procedure
+__global__ void k_nu_kernel(Ptr9 dC, double* __restrict__ nu, double* __restrict__ dsgs, long n) {
+    GRID_STRIDE(e, n) {
+        const double v = smag(sij(dC.p, 0, e), sij(dC.p, 1, e), sij(dC.p, 2, e), sij(dC.p, 3, e), sij(dC.p, 4, e),
+                              sij(dC.p, 5, e));
+        nu[e] = v;
+        if (dsgs) dsgs[e] = v;
+    }
+}
+
+// |S| of six arrays
+__global__ void k_smag6(const double* s0, const double* s1, const double* s2, const double* s3, const double* s4,
+                        const double* s5, double* __restrict__ out, long n) {
+    GRID_STRIDE(e, n) { out[e] = smag(s0[e], s1[e], s2[e], s3[e], s4[e], s5[e]); }
+}
+
+// out = [scale *] Sij(idx)
+__global__ void k_sij(Ptr9 d, int idx, const double* __restrict__ scale, double* __restrict__ out, long n) {
+    GRID_STRIDE(e, n) {
+        const double s = sij(d.p, idx, e);
+        out[e] = scale ? mul(scale[e], s) : s;
+    }
+}
+
+// M = filt - dr2 * Df * Sf  (standardDynamicProcedure.F90:102-106)
+__global__ void k_mij(const double* __restrict__ filt, const double* __restrict__ df, const double* __restrict__ sf,
+                      double dr2, double* __restrict__ m, long n) {
+    GRID_STRIDE(e, n) { m[e] = sub(filt[e], mul(mul(dr2, df[e]), sf[e])); }
+}
+
+__global__ void k_prod(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out, long n) {
+    GRID_STRIDE(e, n) { out[e] = mul(a[e], b[e]); }
+}
+
+// L = filt - a * b  (standardDynamicProcedure.F90:112-136)
+__global__ void k_lij(const double* __restrict__ filt, const double* __restrict__ a, const double* __restrict__ b,
+                      double* __restrict__ l, long n) {
+    GRID_STRIDE(e, n) { l[e] = sub(filt[e], mul(a[e], b[e])); }
+}
+
+struct Ptr6 {
+    const double* p[6];
+};
+
+// numerator / denominator of the Germano identity in the reference's order (139-154)
+__global__ void k_num_den(Ptr6 L, Ptr6 M, double* __restrict__ num, double* __restrict__ den, long n) {
+    GRID_STRIDE(e, n) {
+        double a = mul(L.p[0][e], M.p[0][e]);
+        for (int i = 1; i < 6; i++) a = add(a, mul(L.p[i][e], M.p[i][e]));
+        a = add(a, mul(L.p[1][e], M.p[1][e]));
+        a = add(a, mul(L.p[2][e], M.p[2][e]));
+        a = add(a, mul(L.p[4][e], M.p[4][e]));
+        double b = mul(M.p[0][e], M.p[0][e]);
+        for (int i = 1; i < 6; i++) b = add(b, mul(M.p[i][e], M.p[i][e]));
+        b = add(b, mul(M.p[1][e], M.p[1][e]));
+        b = add(b, mul(M.p[2][e], M.p[2][e]));
+        b = add(b, mul(M.p[4][e], M.p[4][e]));
+        num[e] = a;
+        den[e] = 2.0 * b;
+    }
+}
+
+// per-plane sums of two arrays: grid (chunks, nz); partials [nz][chunks][2]
+constexpr int kPlaneChunks = 16;
+__global__ void k_plane_sums(const double* __restrict__ a, const double* __restrict__ b, long plane,
+                             double* __restrict__ part) {
+    __shared__ double sa[8], sb[8];
+    const int k = blockIdx.y;
+    const double* pa = a + (long)k * plane;
+    const double* pb = b + (long)k * plane;
+    double x = 0.0, y = 0.0;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < plane; e += (long)gridDim.x * blockDim.x) {
+        x += pa[e];
+        y += pb[e];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sa[threadIdx.x >> 5] = x;
+        sb[threadIdx.x >> 5] = y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tx = 0.0, ty = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            tx += sa[w];
+            ty += sb[w];
+        }
+        part[((long)k * gridDim.x + blockIdx.x) * 2] = tx;
+        part[((long)k * gridDim.x + blockIdx.x) * 2 + 1] = ty;
+    }
+}
+
+// lambda(z) = max(<num> , 0) / (<den> + 1e-18)  (planarAverage_and_TakeRatio, 221-244)
+__global__ void k_lambda(const double* __restrict__ part, int chunks, double meanfact, int nz,
+                         double* __restrict__ lambda) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nz) return;
+    double x = 0.0, y = 0.0;
+    for (int c = 0; c < chunks; c++) {
+        x += part[((long)k * chunks + c) * 2];
+        y += part[((long)k * chunks + c) * 2 + 1];
+    }
+    const double nm = fmax(mul(x, meanfact), 0.0);
+    lambda[k] = nm / add(mul(y, meanfact), 1e-18);
+}
+
+// nu *= lambda(z) (dynamic) or cmodel_global
+__global__ void k_scale_nu(double* __restrict__ nu, const double* __restrict__ lambda, double c, long plane,
+                           long n) {
+    GRID_STRIDE(e, n) { nu[e] = lambda ? mul(lambda[e / plane], nu[e]) : mul(c, nu[e]); }
+}
+
+__global__ void k_clip_neg(double* __restrict__ x, long n) {
+    GRID_STRIDE(e, n) {
+        if (x[e] < 0.0) x[e] = 0.0;
+    }
+}
+
+// tau = -2 nu Sij(idx)  (sgsmod_igrid.F90:188-193)
+__global__ void k_tau(Ptr9 d, int idx, const double* __restrict__ nu, double* __restrict__ out, long n) {
+    GRID_STRIDE(e, n) { out[e] = -mul(2.0 * nu[e], sij(d.p, idx, e)); }
+}
+
+// a -= i k(a) X ; b -= i k(b) X  (mtimes_ik then subtraction, sgsmod_igrid.F90:213-260);
+// which: 1 = k1 (x index), 2 = k2 (y index)
+__global__ void k_sub_ik(double2* __restrict__ a, int wa, double2* __restrict__ b, int wb,
+                         const double2* __restrict__ X, const double* __restrict__ k1,
+                         const double* __restrict__ k2, long nxh, long nxy, long n) {
+    GRID_STRIDE(e, n) {
+        const long q = e % nxy;
+        const double2 x = X[e];
+        if (a) {
+            const double k = wa == 1 ? k1[q % nxh] : k2[q / nxh];
+            const double2 r = a[e];
+            a[e] = make_double2(sub(r.x, -mul(k, x.y)), sub(r.y, mul(k, x.x)));
+        }
+        if (b) {
+            const double k = wb == 1 ? k1[q % nxh] : k2[q / nxh];
+            const double2 r = b[e];
+            b[e] = make_double2(sub(r.x, -mul(k, x.y)), sub(r.y, mul(k, x.x)));
+        }
+    }
+}
+
+__global__ void k_csub2(double2* __restrict__ y, const double2* __restrict__ x, long n) {
+    GRID_STRIDE(e, n) {
+        const double2 a = y[e], b = x[e];
+        y[e] = make_double2(sub(a.x, b.x), sub(a.y, b.y));
+    }
+}
+
+// TVD-RK3 stage updates (igrid.F90:1128-1164); dt read from device memory
+__global__ void k_rk(int stage, double2* __restrict__ u0, double2* __restrict__ u1, const double2* __restrict__ r,
+                     const double* __restrict__ dtp, long n) {
+    const double dt = *dtp;
+    GRID_STRIDE(e, n) {
+        const double2 a = u0[e], rr = r[e];
+        if (stage == 1) {
+            u1[e] = make_double2(add(a.x, mul(dt, rr.x)), add(a.y, mul(dt, rr.y)));
+        } else if (stage == 2) {
+            const double2 b = u1[e];
+            const double c0 = 3.0 / 4.0, c1 = 1.0 / 4.0, c2 = mul(1.0 / 4.0, dt);
+            u1[e] = make_double2(add(add(mul(c0, a.x), mul(c1, b.x)), mul(c2, rr.x)),
+                                 add(add(mul(c0, a.y), mul(c1, b.y)), mul(c2, rr.y)));
+        } else {
+            const double2 b = u1[e];
+            const double c0 = 1.0 / 3.0, c1 = 2.0 / 3.0, c2 = mul(2.0 / 3.0, dt);
+            u0[e] = make_double2(add(add(mul(c0, a.x), mul(c1, b.x)), mul(c2, rr.x)),
+                                 add(add(mul(c0, a.y), mul(c1, b.y)), mul(c2, rr.y)));
+        }
+    }
+}
+
+// CFL time-step partials: max(|u/dx| + |v/dy| + |wC/dz|)  (igrid.F90:1384-1393)
+__global__ void k_cfl_partial(const double* __restrict__ u, const double* __restrict__ v,
+                              const double* __restrict__ w, double rdx, double rdy, double rdz, long n,
+                              double* __restrict__ part) {
+    __shared__ double s[8];
+    double m = 0.0;
+    GRID_STRIDE(e, n) {
+        double a = fabs(mul(rdx, u[e]));
+        a = add(a, fabs(mul(rdy, v[e])));
+        a = add(a, fabs(mul(rdz, w[e])));
+        m = fmax(m, a);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) t = fmax(t, s[i]);
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_cfl_final(const double* __restrict__ part, int np, double cfl, double tvisc, int viscous,
+                            double* __restrict__ dt) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double m = 0.0;
+    for (int i = 0; i < np; i++) m = fmax(m, part[i]);
+    double d = cfl / m;
+    if (viscous) d = fmin(d, tvisc);
+    *dt = d;
+}
+
+__global__ void k_set(double* __restrict__ p, double v) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *p = v;
+}
+
+// wrapup_timestep: tsim = tsim + dt (igrid.F90:2074)
+__global__ void k_advance(double* __restrict__ tsim, const double* __restrict__ dt) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *tsim = *tsim + *dt;
+}
+
+constexpr int kCflBlocks = 152 * 4;
+
+}  // namespace
+
+struct pade_les_s {
+    pade_les_params prm{};
+    int nx = 0, ny = 0, nz = 0, nxh = 0;
+    double dx = 0, dy = 0, dz = 0;
+    long NC = 0, NE = 0, SC = 0, SE = 0, plane = 0, splane = 0;
+    pade_spectral spC = nullptr, spE = nullptr;
+    pade_poisson po = nullptr;
+    pade_op stagg = nullptr;
+    double* d_k3 = nullptr;  // spectral k3 (oddball sign flipped) for the dealias mask
+    double cut_x = 0, cut_y = 0, cut_z = 0, tf_x = 0, tf_y = 0;
+    double cmodel_global = 0, meanfact = 0, tvisc = 0;
+    // spectral state and stage copies
+    double2 *uhat = nullptr, *vhat = nullptr, *what = nullptr;
+    double2 *uhat1 = nullptr, *vhat1 = nullptr, *what1 = nullptr;
+    double2 *urhs = nullptr, *vrhs = nullptr, *wrhs = nullptr;
+    double2 *whatC = nullptr, *uEhat = nullptr, *vEhat = nullptr;
+    double2 *d2u = nullptr, *d2v = nullptr, *d2w = nullptr;
+    double2 *tC1 = nullptr, *tE1 = nullptr;
+    double2 *uhat_cur = nullptr, *vhat_cur = nullptr, *what_cur = nullptr;  // fields project_and_prep acts on
+    // physical fields
+    double *u = nullptr, *v = nullptr, *wC = nullptr, *w = nullptr, *uE = nullptr, *vE = nullptr;
+    double* dC[9] = {nullptr};
+    double* dE[9] = {nullptr};
+    double *rC1 = nullptr, *rC2 = nullptr, *rE1 = nullptr, *rE2 = nullptr, *rE3 = nullptr;
+    double *nuC = nullptr, *nuE = nullptr, *div = nullptr;
+    // dynamic procedure
+    double *Sf[6] = {nullptr}, *M[6] = {nullptr}, *Lm[6] = {nullptr}, *uf[3] = {nullptr};
+    double *Df = nullptr, *Dsgs = nullptr, *lambda = nullptr, *part = nullptr;
+    double *d_dt = nullptr, *d_tsim = nullptr, *cflpart = nullptr;
+    std::vector<void*> allocs;
+    int step = 0, mstep = 0;
+    bool newTimeStep = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gstream = nullptr;
+};
+
+namespace {
+
+int al(pade_les h, void* p, size_t bytes) {
+    void** pp = static_cast<void**>(p);
+    int rc = dalloc(pp, bytes);
+    if (rc == PS_OK) h->allocs.push_back(*pp);
+    return rc;
+}
+
+int zop(pade_les h, int op, int cplx, const void* in, void* out, cudaStream_t s) {
+    return pade_apply(h->stagg, op, 3, cplx, in, out, cplx ? h->nxh : h->nx, h->ny, 0, 0, PADE_PATH_DF, s);
+}
+
+#define CK(x)                        \
+    do {                             \
+        const int rc_ = (x);         \
+        if (rc_ != PS_OK) return rc_; \
+    } while (0)
+#define KCHECK() CK(cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA)
+
+Ptr9 p9(double* const* a) {
+    Ptr9 r;
+    for (int i = 0; i < 9; i++) r.p[i] = a[i];
+    return r;
+}
+
+// spectral test filter of a real C field (TestFilter_Real_to_Real): fft, cutoff, ifft
+int test_filter(pade_les h, const double* in, double* out, cudaStream_t s) {
+    CK(spectral_fft(h->spC, in, h->tC1, s));
+    return spectral_ifft_masked(h->spC, h->tC1, out, h->tf_x, h->tf_y, s);
+}
+
+int dealias(pade_les h, double2* f, int edge, cudaStream_t s) {
+    FftExtra ex{};
+    ex.ka = h->spC->d_k1;
+    ex.kb = h->spC->d_k2;
+    ex.kc = h->d_k3;
+    ex.nxh = h->nxh;
+    ex.plane = h->splane;
+    ex.cut_a = h->cut_x;
+    ex.cut_b = h->cut_y;
+    ex.cut_c = h->cut_z;
+    ex.edge_copy = edge;
+    FftLines lz = fft_lines(3, h->nxh, h->ny, h->nz, h->nz, h->nz);
+    return fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_DEALIAS, h->nz, -1, 1.0 / (double)h->nz, 0, f, f, lz, ex, s);
+}
+
+int compute_duidxj(pade_les h, cudaStream_t s) {
+    pade_spectral C = h->spC, E = h->spE;
+    CK(spectral_ifft(C, h->uhat_cur, h->dC[0], 0, s, MUL_IK_A));
+    CK(spectral_ifft(E, h->uEhat, h->dE[0], 0, s, MUL_IK_A));
+    CK(spectral_ifft(C, h->uhat_cur, h->dC[1], 0, s, MUL_IK_P));
+    CK(spectral_ifft(E, h->uEhat, h->dE[1], 0, s, MUL_IK_P));
+    CK(spectral_ifft(C, h->vhat_cur, h->dC[3], 0, s, MUL_IK_A));
+    CK(spectral_ifft(E, h->vEhat, h->dE[3], 0, s, MUL_IK_A));
+    CK(spectral_ifft(C, h->vhat_cur, h->dC[4], 0, s, MUL_IK_P));
+    CK(spectral_ifft(E, h->vEhat, h->dE[4], 0, s, MUL_IK_P));
+    CK(spectral_ifft(C, h->whatC, h->dC[6], 0, s, MUL_IK_A));
+    CK(spectral_ifft(E, h->what_cur, h->dE[6], 0, s, MUL_IK_A));
+    CK(spectral_ifft(C, h->whatC, h->dC[7], 0, s, MUL_IK_P));
+    CK(spectral_ifft(E, h->what_cur, h->dE[7], 0, s, MUL_IK_P));
+    // dwdz at C and E, d2wdz2 at E
+    CK(zop(h, OP_DDZ_E2C, 1, h->what_cur, h->tC1, s));
+    CK(spectral_ifft(C, h->tC1, h->dC[8], 0, s));
+    CK(zop(h, OP_I_C2E, 1, h->tC1, h->tE1, s));
+    CK(spectral_ifft(E, h->tE1, h->dE[8], 0, s));
+    if (!h->prm.isInviscid) CK(zop(h, OP_D2_E2E, 1, h->what_cur, h->d2w, s));
+    // dudz, d2udz2; dvdz, d2vdz2
+    CK(zop(h, OP_DDZ_C2E, 1, h->uhat_cur, h->tE1, s));
+    CK(spectral_ifft(E, h->tE1, h->dE[2], 0, s));
+    if (!h->prm.isInviscid) CK(zop(h, OP_D2_C2C, 1, h->uhat_cur, h->d2u, s));
+    CK(zop(h, OP_I_E2C, 1, h->tE1, h->tC1, s));
+    CK(spectral_ifft(C, h->tC1, h->dC[2], 0, s));
+    CK(zop(h, OP_DDZ_C2E, 1, h->vhat_cur, h->tE1, s));
+    CK(spectral_ifft(E, h->tE1, h->dE[5], 0, s));
+    if (!h->prm.isInviscid) CK(zop(h, OP_D2_C2C, 1, h->vhat_cur, h->d2v, s));
+    CK(zop(h, OP_I_E2C, 1, h->tE1, h->tC1, s));
+    return spectral_ifft(C, h->tC1, h->dC[5], 0, s);
+}
+
+int prep_physical(pade_les h, cudaStream_t s) {
+    CK(spectral_ifft(h->spC, h->uhat_cur, h->u, 0, s));
+    CK(spectral_ifft(h->spC, h->vhat_cur, h->v, 0, s));
+    CK(spectral_ifft(h->spE, h->what_cur, h->w, 0, s));
+    CK(zop(h, OP_I_E2C, 1, h->what_cur, h->whatC, s));
+    CK(spectral_ifft(h->spC, h->whatC, h->wC, 0, s));
+    CK(zop(h, OP_I_C2E, 1, h->uhat_cur, h->uEhat, s));
+    CK(spectral_ifft(h->spE, h->uEhat, h->uE, 0, s));
+    CK(zop(h, OP_I_C2E, 1, h->vhat_cur, h->vEhat, s));
+    CK(spectral_ifft(h->spE, h->vEhat, h->vE, 0, s));
+    return compute_duidxj(h, s);
+}
+
+int project_and_prep(pade_les h, cudaStream_t s) {
+    CK(dealias(h, h->uhat_cur, 0, s));
+    CK(dealias(h, h->vhat_cur, 0, s));
+    CK(dealias(h, h->what_cur, 1, s));
+    CK(pade_poisson_projection(h->po, h->uhat_cur, h->vhat_cur, h->what_cur, s));
+    if (h->prm.t_DivergenceCheck > 0 && h->step % h->prm.t_DivergenceCheck == 0) {
+        double m = 0;
+        CK(pade_poisson_divergence_check(h->po, h->uhat_cur, h->vhat_cur, h->what_cur, h->div, 1, &m, s));
+    }
+    return prep_physical(h, s);
+}
+
+int dynamic_procedure(pade_les h, cudaStream_t s) {
+    const long n = h->NC;
+    const unsigned g = grid_for(n);
+    const Ptr9 dC = p9(h->dC);
+    for (int i = 0; i < 6; i++) {
+        k_sij<<<g, 256, 0, s>>>(dC, i, nullptr, h->rC1, n);
+        KCHECK();
+        CK(test_filter(h, h->rC1, h->Sf[i], s));
+    }
+    k_smag6<<<g, 256, 0, s>>>(h->Sf[0], h->Sf[1], h->Sf[2], h->Sf[3], h->Sf[4], h->Sf[5], h->Df, n);
+    KCHECK();
+    const double dr2 = h->prm.deltaRatio * h->prm.deltaRatio;
+    for (int i = 0; i < 6; i++) {
+        k_sij<<<g, 256, 0, s>>>(dC, i, h->Dsgs, h->rC1, n);
+        KCHECK();
+        CK(test_filter(h, h->rC1, h->rC2, s));
+        k_mij<<<g, 256, 0, s>>>(h->rC2, h->Df, h->Sf[i], dr2, h->M[i], n);
+        KCHECK();
+    }
+    CK(spectral_ifft_masked(h->spC, h->uhat_cur, h->uf[0], h->tf_x, h->tf_y, s));
+    CK(spectral_ifft_masked(h->spC, h->vhat_cur, h->uf[1], h->tf_x, h->tf_y, s));
+    CK(spectral_ifft_masked(h->spC, h->whatC, h->uf[2], h->tf_x, h->tf_y, s));
+    const double* U[3] = {h->u, h->v, h->wC};
+    const int pi[6] = {0, 0, 0, 1, 1, 2}, pj[6] = {0, 1, 2, 1, 2, 2};
+    for (int q = 0; q < 6; q++) {
+        k_prod<<<g, 256, 0, s>>>(U[pi[q]], U[pj[q]], h->rC1, n);
+        KCHECK();
+        CK(test_filter(h, h->rC1, h->rC2, s));
+        k_lij<<<g, 256, 0, s>>>(h->rC2, h->uf[pi[q]], h->uf[pj[q]], h->Lm[q], n);
+        KCHECK();
+    }
+    Ptr6 L, M;
+    for (int i = 0; i < 6; i++) {
+        L.p[i] = h->Lm[i];
+        M.p[i] = h->M[i];
+    }
+    k_num_den<<<g, 256, 0, s>>>(L, M, h->rC1, h->rC2, n);
+    KCHECK();
+    dim3 grid(kPlaneChunks, h->nz);
+    k_plane_sums<<<grid, 256, 0, s>>>(h->rC1, h->rC2, h->plane, h->part);
+    KCHECK();
+    k_lambda<<<(h->nz + 127) / 128, 128, 0, s>>>(h->part, kPlaneChunks, h->meanfact, h->nz, h->lambda);
+    KCHECK();
+    return PS_OK;
+}
+
+int sgs_rhs(pade_les h, cudaStream_t s) {
+    const long n = h->NC, nE = h->NE;
+    const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC), gsE = grid_for(h->SE);
+    const Ptr9 dC = p9(h->dC), dE = p9(h->dE);
+    const bool dyn = h->prm.dynamic != 0;
+    k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
+    KCHECK();
+    if (dyn && h->newTimeStep && h->mstep % std::max(1, h->prm.DynProcFreq) == 0) CK(dynamic_procedure(h, s));
+    k_scale_nu<<<g, 256, 0, s>>>(h->nuC, dyn ? h->lambda : nullptr, h->cmodel_global, h->plane, n);
+    KCHECK();
+    CK(zop(h, OP_I_C2E, 0, h->nuC, h->nuE, s));
+    if (!dyn) {
+        k_clip_neg<<<gE, 256, 0, s>>>(h->nuE, nE);
+        KCHECK();
+    }
+    if (h->newTimeStep) h->mstep++;
+    const double* k1 = h->spC->d_k1;
+    const double* k2 = h->spC->d_k2;
+    const long nxh = h->nxh, nxy = h->splane;
+    // ddx(tau11) -> urhs
+    k_tau<<<g, 256, 0, s>>>(dC, 0, h->nuC, h->rC1, n);
+    KCHECK();
+    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
+    k_sub_ik<<<gs, 256, 0, s>>>(h->urhs, 1, nullptr, 0, h->tC1, k1, k2, nxh, nxy, h->SC);
+    KCHECK();
+    // ddy(tau22) -> vrhs
+    k_tau<<<g, 256, 0, s>>>(dC, 3, h->nuC, h->rC1, n);
+    KCHECK();
+    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
+    k_sub_ik<<<gs, 256, 0, s>>>(h->vrhs, 2, nullptr, 0, h->tC1, k1, k2, nxh, nxy, h->SC);
+    KCHECK();
+    // ddz(tau33) -> wrhs
+    k_tau<<<g, 256, 0, s>>>(dC, 5, h->nuC, h->rC1, n);
+    KCHECK();
+    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
+    CK(zop(h, OP_DDZ_C2E, 1, h->tC1, h->tE1, s));
+    k_csub2<<<gsE, 256, 0, s>>>(h->wrhs, h->tE1, h->SE);
+    KCHECK();
+    // tau12: vrhs -= ik1 X, urhs -= ik2 X
+    k_tau<<<g, 256, 0, s>>>(dC, 1, h->nuC, h->rC1, n);
+    KCHECK();
+    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
+    k_sub_ik<<<gs, 256, 0, s>>>(h->vrhs, 1, h->urhs, 2, h->tC1, k1, k2, nxh, nxy, h->SC);
+    KCHECK();
+    // tau13 (edges): urhs -= ddz_E2C(X), wrhs -= ik1 X
+    k_tau<<<gE, 256, 0, s>>>(dE, 2, h->nuE, h->rE1, nE);
+    KCHECK();
+    CK(spectral_fft(h->spE, h->rE1, h->tE1, s));
+    CK(zop(h, OP_DDZ_E2C, 1, h->tE1, h->tC1, s));
+    k_csub2<<<gs, 256, 0, s>>>(h->urhs, h->tC1, h->SC);
+    KCHECK();
+    k_sub_ik<<<gsE, 256, 0, s>>>(h->wrhs, 1, nullptr, 0, h->tE1, k1, k2, nxh, nxy, h->SE);
+    KCHECK();
+    // tau23 (edges): vrhs -= ddz_E2C(X), wrhs -= ik2 X
+    k_tau<<<gE, 256, 0, s>>>(dE, 4, h->nuE, h->rE1, nE);
+    KCHECK();
+    CK(spectral_fft(h->spE, h->rE1, h->tE1, s));
+    CK(zop(h, OP_DDZ_E2C, 1, h->tE1, h->tC1, s));
+    k_csub2<<<gs, 256, 0, s>>>(h->vrhs, h->tC1, h->SC);
+    KCHECK();
+    k_sub_ik<<<gsE, 256, 0, s>>>(h->wrhs, 2, nullptr, 0, h->tE1, k1, k2, nxh, nxy, h->SE);
+    KCHECK();
+    return PS_OK;
+}
+
+int populate_rhs(pade_les h, cudaStream_t s) {
+    const long n = h->NC, nE = h->NE;
+    const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC), gsE = grid_for(h->SE);
+    const Ptr9 dC = p9(h->dC), dE = p9(h->dE);
+    k_nl_c<<<g, 256, 0, s>>>(dC, h->u, h->v, h->rC1, h->rC2, n);
+    KCHECK();
+    k_nl_e<<<gE, 256, 0, s>>>(dE, h->w, h->uE, h->vE, h->rE1, h->rE2, h->rE3, nE);
+    KCHECK();
+    const int visc = h->prm.isInviscid ? 0 : 1;
+    const double r = 1.0 / h->prm.Re;
+    const double* k1 = h->spC->d_k1;
+    const double* k2 = h->spC->d_k2;
+    // u
+    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
+    CK(spectral_fft(h->spE, h->rE1, h->tE1, s));
+    CK(zop(h, OP_I_E2C, 1, h->tE1, h->urhs, s));
+    k_rhs_finish<<<gs, 256, 0, s>>>(h->urhs, h->tC1, h->uhat_cur, h->d2u, k1, k2, h->nxh, h->splane, r, visc, h->SC);
+    KCHECK();
+    // v
+    CK(spectral_fft(h->spC, h->rC2, h->tC1, s));
+    CK(spectral_fft(h->spE, h->rE2, h->tE1, s));
+    CK(zop(h, OP_I_E2C, 1, h->tE1, h->vrhs, s));
+    k_rhs_finish<<<gs, 256, 0, s>>>(h->vrhs, h->tC1, h->vhat_cur, h->d2v, k1, k2, h->nxh, h->splane, r, visc, h->SC);
+    KCHECK();
+    // w
+    CK(spectral_fft(h->spE, h->rE3, h->wrhs, s));
+    if (visc) {
+        k_rhs_finish<<<gsE, 256, 0, s>>>(h->wrhs, nullptr, h->what_cur, h->d2w, k1, k2, h->nxh, h->splane, r, 1,
+                                          h->SE);
+        KCHECK();
+    }
+    if (h->prm.useSGS) CK(sgs_rhs(h, s));
+    return PS_OK;
+}
+
+int compute_dt(pade_les h, cudaStream_t s) {
+    if (!(h->prm.CFL > 0)) {
+        k_set<<<1, 1, 0, s>>>(h->d_dt, h->prm.dt);
+        KCHECK();
+        return PS_OK;
+    }
+    k_cfl_partial<<<kCflBlocks, 256, 0, s>>>(h->u, h->v, h->wC, 1.0 / h->dx, 1.0 / h->dy, 1.0 / h->dz, h->NC,
+                                              h->cflpart);
+    KCHECK();
+    k_cfl_final<<<1, 1, 0, s>>>(h->cflpart, kCflBlocks, h->prm.CFL, h->tvisc, h->prm.isInviscid ? 0 : 1, h->d_dt);
+    KCHECK();
+    return PS_OK;
+}
+
+int rk_stage(pade_les h, int stage, cudaStream_t s) {
+    const unsigned gs = grid_for(h->SC), gsE = grid_for(h->SE);
+    k_rk<<<gs, 256, 0, s>>>(stage, h->uhat, h->uhat1, h->urhs, h->d_dt, h->SC);
+    k_rk<<<gs, 256, 0, s>>>(stage, h->vhat, h->vhat1, h->vrhs, h->d_dt, h->SC);
+    k_rk<<<gsE, 256, 0, s>>>(stage, h->what, h->what1, h->wrhs, h->d_dt, h->SE);
+    KCHECK();
+    return PS_OK;
+}
+
+void set_cur(pade_les h, bool stagecopy) {
+    h->uhat_cur = stagecopy ? h->uhat1 : h->uhat;
+    h->vhat_cur = stagecopy ? h->vhat1 : h->vhat;
+    h->what_cur = stagecopy ? h->what1 : h->what;
+}
+
+// one TVD-RK3 step (igrid.F90:1105-1174) enqueued on s
+int enqueue_step(pade_les h, cudaStream_t s) {
+    CK(compute_dt(h, s));
+    set_cur(h, false);
+    CK(populate_rhs(h, s));
+    h->newTimeStep = false;
+    CK(rk_stage(h, 1, s));
+    set_cur(h, true);
+    CK(project_and_prep(h, s));
+    CK(populate_rhs(h, s));
+    CK(rk_stage(h, 2, s));
+    set_cur(h, true);
+    CK(project_and_prep(h, s));
+    CK(populate_rhs(h, s));
+    CK(rk_stage(h, 3, s));
+    set_cur(h, false);
+    CK(project_and_prep(h, s));
+    k_advance<<<1, 1, 0, s>>>(h->d_tsim, h->d_dt);
+    KCHECK();
+    return PS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pade_les_init(pade_les* out, const pade_les_params* p) {
+    if (!out || !p) return PS_EINVAL;
+    *out = nullptr;
+    if (p->nx < 4 || p->ny < 4 || p->nz < 6 || !(p->Lx > 0) || !(p->Ly > 0) || !(p->Lz > 0)) return PS_EINVAL;
+    if (!(p->isInviscid) && !(p->Re > 0)) return PS_EINVAL;
+    if (!(p->CFL > 0) && !(p->dt > 0)) return PS_EINVAL;
+    if (p->useSGS && p->dynamic && !(p->deltaRatio > 0)) return PS_EINVAL;
+    for (int n : {p->nx, p->ny, p->nz})
+        if (n > 8192 || (n & (n - 1)) != 0) return PS_ENOTSUP;
+    auto* h = new pade_les_s();
+    h->prm = *p;
+    h->nx = p->nx;
+    h->ny = p->ny;
+    h->nz = p->nz;
+    h->nxh = p->nx / 2 + 1;
+    h->dx = p->Lx / p->nx;
+    h->dy = p->Ly / p->ny;
+    h->dz = p->Lz / p->nz;
+    h->plane = (long)h->nx * h->ny;
+    h->splane = (long)h->nxh * h->ny;
+    h->NC = h->plane * h->nz;
+    h->NE = h->plane * (h->nz + 1);
+    h->SC = h->splane * h->nz;
+    h->SE = h->splane * (h->nz + 1);
+    const double pi = 3.141592653589793238462643383279502884;
+    const double dfact = p->dealiasFact > 0 ? p->dealiasFact : 2.0 / 3.0;
+    h->cut_x = dfact * pi / h->dx;
+    h->cut_y = dfact * pi / h->dy;
+    h->cut_z = dfact * pi / h->dz;
+    h->tf_x = ((2.0 / 3.0) * pi / h->dx) / p->deltaRatio;
+    h->tf_y = ((2.0 / 3.0) * pi / h->dy) / p->deltaRatio;
+    const double deltaLES = std::pow(1.5 * h->dx * 1.5 * h->dy * 1.5 * h->dz, 1.0 / 3.0);
+    h->cmodel_global = (p->Csgs * deltaLES) * (p->Csgs * deltaLES);
+    h->meanfact = 1.0 / ((double)h->nx * (double)h->ny);
+    const double mn = std::min(h->dx, std::min(h->dy, h->dz));
+    h->tvisc = p->CFL * p->Re * (mn * mn);
+    int rc = pade_spectral_init(&h->spC, h->nx, h->ny, h->nz, h->dx, h->dy, 0);
+    if (rc == PS_OK) rc = pade_spectral_init(&h->spE, h->nx, h->ny, h->nz + 1, h->dx, h->dy, 0);
+    if (rc == PS_OK) rc = pade_poisson_periodic_init(&h->po, h->spC, h->dx, h->dy, h->dz);
+    if (rc == PS_OK) rc = pade_cd06stagg_init_periodic(&h->stagg, h->nz, h->dz);
+    if (rc == PS_OK) {
+        std::vector<double> k3 = wavenums(h->nz, h->dz);
+        k3[h->nz / 2] = -k3[h->nz / 2];
+        rc = upload(&h->d_k3, k3);
+        if (rc == PS_OK) h->allocs.push_back(h->d_k3);
+    }
+    const size_t c16 = sizeof(double2), r8 = sizeof(double);
+    double2** cC[] = {&h->uhat, &h->vhat, &h->uhat1, &h->vhat1, &h->urhs, &h->vrhs, &h->whatC, &h->d2u, &h->d2v,
+                      &h->tC1};
+    double2** cE[] = {&h->what, &h->what1, &h->wrhs, &h->uEhat, &h->vEhat, &h->d2w, &h->tE1};
+    for (auto pp : cC)
+        if (rc == PS_OK) rc = al(h, pp, c16 * h->SC);
+    for (auto pp : cE)
+        if (rc == PS_OK) rc = al(h, pp, c16 * h->SE);
+    double** rCl[] = {&h->u, &h->v, &h->wC, &h->rC1, &h->rC2, &h->nuC, &h->div};
+    double** rEl[] = {&h->w, &h->uE, &h->vE, &h->rE1, &h->rE2, &h->rE3, &h->nuE};
+    for (auto pp : rCl)
+        if (rc == PS_OK) rc = al(h, pp, r8 * h->NC);
+    for (auto pp : rEl)
+        if (rc == PS_OK) rc = al(h, pp, r8 * h->NE);
+    for (int i = 0; i < 9 && rc == PS_OK; i++) rc = al(h, &h->dC[i], r8 * h->NC);
+    for (int i = 0; i < 9 && rc == PS_OK; i++) rc = al(h, &h->dE[i], r8 * h->NE);
+    if (p->useSGS && p->dynamic) {
+        for (int i = 0; i < 6 && rc == PS_OK; i++) rc = al(h, &h->Sf[i], r8 * h->NC);
+        for (int i = 0; i < 6 && rc == PS_OK; i++) rc = al(h, &h->M[i], r8 * h->NC);
+        for (int i = 0; i < 6 && rc == PS_OK; i++) rc = al(h, &h->Lm[i], r8 * h->NC);
+        for (int i = 0; i < 3 && rc == PS_OK; i++) rc = al(h, &h->uf[i], r8 * h->NC);
+        if (rc == PS_OK) rc = al(h, &h->Df, r8 * h->NC);
+        if (rc == PS_OK) rc = al(h, &h->Dsgs, r8 * h->NC);
+        if (rc == PS_OK) rc = al(h, &h->part, r8 * 2 * kPlaneChunks * h->nz);
+    }
+    if (rc == PS_OK) rc = al(h, &h->lambda, r8 * h->nz);
+    if (rc == PS_OK) rc = al(h, &h->d_dt, r8);
+    if (rc == PS_OK) rc = al(h, &h->d_tsim, r8);
+    if (rc == PS_OK) rc = al(h, &h->cflpart, r8 * kCflBlocks);
+    if (rc == PS_OK && cudaMemset(h->lambda, 0, r8 * h->nz) != cudaSuccess) rc = PS_ECUDA;
+    if (rc == PS_OK && cudaMemset(h->d_tsim, 0, r8) != cudaSuccess) rc = PS_ECUDA;
+    if (rc == PS_OK && cudaMemset(h->d_dt, 0, r8) != cudaSuccess) rc = PS_ECUDA;
+    if (rc != PS_OK) {
+        pade_les_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return PS_OK;
+}
+
+int pade_les_destroy(pade_les h) {
+    if (!h) return PS_OK;
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->stagg) pade_destroy(h->stagg);
+    if (h->po) pade_poisson_destroy(h->po);
+    if (h->spE) pade_spectral_destroy(h->spE);
+    if (h->spC) pade_spectral_destroy(h->spC);
+    delete h;
+    return PS_OK;
+}
+
+int pade_les_set_fields(pade_les h, const double* u, const double* v, const double* w, void* stream) {
+    if (!h || !device_ptr(u) || !device_ptr(v) || !device_ptr(w)) return PS_EINVAL;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // igrid.F90:625-648: transform, dealias, divergence report, project, prepare
+    CK(spectral_fft(h->spC, u, h->uhat, s));
+    CK(spectral_fft(h->spC, v, h->vhat, s));
+    CK(spectral_fft(h->spE, w, h->what, s));
+    set_cur(h, false);
+    CK(dealias(h, h->uhat, 0, s));
+    CK(dealias(h, h->vhat, 0, s));
+    CK(dealias(h, h->what, 1, s));
+    CK(pade_poisson_projection(h->po, h->uhat, h->vhat, h->what, s));
+    CK(prep_physical(h, s));
+    h->step = 0;
+    h->mstep = 0;
+    h->newTimeStep = true;
+    if (cudaMemsetAsync(h->d_tsim, 0, sizeof(double), s) != cudaSuccess) return PS_ECUDA;
+    return cudaStreamSynchronize(s) == cudaSuccess ? PS_OK : PS_ECUDA;
+}
+
+int pade_les_step(pade_les h, int use_graph, void* stream) {
+    if (!h) return PS_EINVAL;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool divcheck = h->prm.t_DivergenceCheck > 0 && h->step % h->prm.t_DivergenceCheck == 0;
+    const bool fixed_shape = !h->prm.useSGS || !h->prm.dynamic || h->prm.DynProcFreq <= 1;
+    if (use_graph && !divcheck && fixed_shape && s != nullptr) {
+        if (!h->gexec || h->gstream != s) {
+            if (h->gexec) cudaGraphExecDestroy(h->gexec);
+            if (h->graph) cudaGraphDestroy(h->graph);
+            h->gexec = nullptr;
+            h->graph = nullptr;
+            const int saved_m = h->mstep;
+            const bool saved_n = h->newTimeStep;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) return PS_ECUDA;
+            const int rc = enqueue_step(h, s);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(s, &g);
+            h->mstep = saved_m;
+            h->newTimeStep = saved_n;
+            if (rc != PS_OK || ce != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                return rc != PS_OK ? rc : PS_ECUDA;
+            }
+            if (cudaGraphInstantiate(&h->gexec, g, 0) != cudaSuccess) {
+                cudaGraphDestroy(g);
+                cudaGetLastError();
+                return PS_ECUDA;
+            }
+            h->graph = g;
+            h->gstream = s;
+        }
+        if (cudaGraphLaunch(h->gexec, s) != cudaSuccess) return PS_ECUDA;
+        if (h->prm.useSGS) h->mstep++;  // the captured step ran populate_rhs with newTimeStep once
+        h->newTimeStep = true;
+    } else {
+        CK(enqueue_step(h, s));
+        h->newTimeStep = true;
+    }
+    h->step++;
+    return PS_OK;
+}
+
+int pade_les_info(pade_les h, double* dt, double* tsim, int* step, double* lambda1d) {
+    if (!h) return PS_EINVAL;
+    double d[2] = {0, 0};
+    if (cudaMemcpy(&d[0], h->d_dt, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return PS_ECUDA;
+    if (cudaMemcpy(&d[1], h->d_tsim, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return PS_ECUDA;
+    if (dt) *dt = d[0];
+    if (tsim) *tsim = d[1];
+    if (step) *step = h->step;
+    if (lambda1d && cudaMemcpy(lambda1d, h->lambda, sizeof(double) * h->nz, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return PS_ECUDA;
+    return PS_OK;
+}
+
+int pade_les_field(pade_les h, int which, void** ptr) {
+    if (!h || !ptr) return PS_EINVAL;
+    void* p = nullptr;
+    if (which >= 10 && which < 19) {
+        p = h->dC[which - 10];
+    } else if (which >= 20 && which < 29) {
+        p = h->dE[which - 20];
+    } else {
+        switch (which) {
+            case PADE_LES_UHAT: p = h->uhat; break;
+            case PADE_LES_VHAT: p = h->vhat; break;
+            case PADE_LES_WHAT: p = h->what; break;
+            case PADE_LES_U: p = h->u; break;
+            case PADE_LES_V: p = h->v; break;
+            case PADE_LES_WC: p = h->wC; break;
+            case PADE_LES_W: p = h->w; break;
+            case PADE_LES_UE: p = h->uE; break;
+            case PADE_LES_VE: p = h->vE; break;
+            case PADE_LES_NUC: p = h->nuC; break;
+            case PADE_LES_NUE: p = h->nuE; break;
+            default: return PS_EINVAL;
+        }
+    }
+    *ptr = p;
+    return PS_OK;
+}
+
+}  // extern "C"

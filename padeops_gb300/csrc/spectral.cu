@@ -29,10 +29,9 @@
 #include "../../include/padeops_gb300.h"
 #include "fft.h"
 #include "operators.h"
+#include "spectral_internal.h"
 
-using namespace pade;
-
-namespace {
+namespace pade {
 
 bool device_ptr(const void* p) {
     if (!p) return false;
@@ -44,7 +43,9 @@ bool device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+namespace {
 bool pow2_len(int n) { return n >= 2 && n <= 8192 && (n & (n - 1)) == 0; }
+}  // namespace
 
 // GetWaveNums (spectral.F90:1748-1764, PoissonPeriodic.F90:226-242): k(i) =
 // (-pi + (i-1)*2*pi/dummy)/dx for i = 1..n, dummy = n - mod(n,2), then ifftshift.
@@ -77,18 +78,6 @@ void modk_cd06stagg(const double* k, int n, double dx, double* kp) {
     }
 }
 
-template <typename T>
-int upload(T** d, const std::vector<T>& h) {
-    if (cudaMalloc(d, sizeof(T) * std::max<size_t>(1, h.size())) != cudaSuccess) {
-        cudaGetLastError();
-        *d = nullptr;
-        return PS_ENOMEM;
-    }
-    if (!h.empty() && cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-        return PS_ECUDA;
-    return PS_OK;
-}
-
 int dalloc(void** p, size_t bytes) {
     if (cudaMalloc(p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
         cudaGetLastError();
@@ -102,6 +91,8 @@ unsigned grid_for(long n) {
     const long b = (n + 255) / 256;
     return (unsigned)std::max(1L, std::min(b, 152L * 16));
 }
+
+namespace {
 
 // y -= x (complex), what -= dwdzHATz_Periodic (PadePoisson.F90:415)
 __global__ void k_csub(double2* __restrict__ y, const double2* __restrict__ x, long n) {
@@ -140,44 +131,7 @@ __global__ void k_max_partial(const double* __restrict__ x, long n, double* __re
     }
 }
 
-constexpr int kMaxPartials = 152 * 8;
-
 }  // namespace
-
-struct pade_spectral_s {
-    int nx = 0, ny = 0, nz = 0, nxh = 0;
-    double dx = 0, dy = 0;
-    int fix_oddball = 1;
-    std::vector<double> k1, k2;
-    double* d_k1 = nullptr;
-    double* d_k2 = nullptr;
-    double2* work = nullptr;  // (nxh, ny, nz): the ifft's y-transform output
-};
-
-struct pade_poisson_s {
-    pade_spectral sp = nullptr;
-    int nx = 0, ny = 0, nz = 0, nxh = 0;
-    double dz = 0;
-    pade_op stagg = nullptr;
-    std::vector<double> k3mod;
-    double* d_k1r = nullptr;   // GetWaveNums(nx, dx)(1:nx/2+1)
-    double* d_k2r = nullptr;   // GetWaveNums(ny, dy)
-    double* d_k3m = nullptr;   // CD06-stagg modified z wavenumbers
-    double2* f2d = nullptr;    // (nxh, ny, nz): dwdz, then the pressure
-    double2* dwE = nullptr;    // (nxh, ny, nz+1)
-    double* part = nullptr;    // kMaxPartials
-};
-
-struct pade_poisson3d_s {
-    int nx = 0, ny = 0, nz = 0, nxh = 0, dir_id = 1;
-    std::vector<double> kx, ky, kz;
-    double* d_kx = nullptr;
-    double* d_ky = nullptr;
-    double* d_kz = nullptr;
-    double2* hat = nullptr;  // (nxh, ny, nz)
-};
-
-namespace {
 
 int spectral_fft(pade_spectral h, const double* in, void* out, cudaStream_t s) {
     const FftExtra ex{};
@@ -188,15 +142,40 @@ int spectral_fft(pade_spectral h, const double* in, void* out, cudaStream_t s) {
     return fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PLAIN, h->ny, -1, 1.0, 0, out, out, ly, ex, s);
 }
 
-int spectral_ifft(pade_spectral h, const void* in, double* out, int oddball, cudaStream_t s) {
-    const FftExtra ex{};
+int spectral_ifft(pade_spectral h, const void* in, double* out, int oddball, cudaStream_t s, int mul) {
+    FftExtra ex{};
+    ex.mul = mul;
+    ex.km = mul == MUL_IK_A ? h->d_k1 : h->d_k2;
     FftLines ly = fft_lines(2, h->nxh, h->ny, h->nz, h->ny, h->ny);
     int rc = fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PLAIN, h->ny, 1, 1.0, 0, in, h->work, ly, ex, s);
     if (rc != PS_OK) return rc;
+    ex = FftExtra{};
     FftLines lx = fft_lines(1, h->nx, h->ny, h->nz, h->nxh, h->nx);
     const double norm = 1.0 / ((double)h->nx * (double)h->ny);
     return fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, oddball, h->work, out, lx, ex, s);
 }
+
+int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s) {
+    FftExtra ex{};
+    ex.mul = MUL_MASK_AP;
+    ex.ka = h->d_k1;
+    ex.kb = h->d_k2;
+    ex.cut_a = cut1;
+    ex.cut_b = cut2;
+    FftLines ly = fft_lines(2, h->nxh, h->ny, h->nz, h->ny, h->ny);
+    int rc = fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PLAIN, h->ny, 1, 1.0, 0, in, h->work, ly, ex, s);
+    if (rc != PS_OK) return rc;
+    ex = FftExtra{};
+    FftLines lx = fft_lines(1, h->nx, h->ny, h->nz, h->nxh, h->nx);
+    const double norm = 1.0 / ((double)h->nx * (double)h->ny);
+    return fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, h->work, out, lx, ex, s);
+}
+
+}  // namespace pade
+
+using namespace pade;
+
+namespace {
 
 int projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStream_t s) {
     const int nxh = h->nxh, ny = h->ny, nz = h->nz;

@@ -1,0 +1,71 @@
+// Internal definitions shared by spectral.cu and les.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/padeops_gb300.h"
+
+struct pade_spectral_s {
+    int nx = 0, ny = 0, nz = 0, nxh = 0;
+    double dx = 0, dy = 0;
+    int fix_oddball = 1;
+    std::vector<double> k1, k2;
+    double* d_k1 = nullptr;
+    double* d_k2 = nullptr;
+    double2* work = nullptr;  // (nxh, ny, nz): the ifft's y-transform output
+};
+
+struct pade_poisson_s {
+    pade_spectral sp = nullptr;
+    int nx = 0, ny = 0, nz = 0, nxh = 0;
+    double dz = 0;
+    pade_op stagg = nullptr;
+    std::vector<double> k3mod;
+    double* d_k1r = nullptr;   // GetWaveNums(nx, dx)(1:nx/2+1)
+    double* d_k2r = nullptr;   // GetWaveNums(ny, dy)
+    double* d_k3m = nullptr;   // CD06-stagg modified z wavenumbers
+    double2* f2d = nullptr;    // (nxh, ny, nz): dwdz, then the pressure
+    double2* dwE = nullptr;    // (nxh, ny, nz+1)
+    double* part = nullptr;    // kMaxPartials
+};
+
+struct pade_poisson3d_s {
+    int nx = 0, ny = 0, nz = 0, nxh = 0, dir_id = 1;
+    std::vector<double> kx, ky, kz;
+    double* d_kx = nullptr;
+    double* d_ky = nullptr;
+    double* d_kz = nullptr;
+    double2* hat = nullptr;  // (nxh, ny, nz)
+};
+
+namespace pade {
+
+constexpr int kMaxPartials = 152 * 8;
+
+std::vector<double> wavenums(int n, double dx);
+void modk_cd06stagg(const double* k, int n, double dx, double* kp);
+bool device_ptr(const void* p);
+unsigned grid_for(long n);
+int dalloc(void** p, size_t bytes);
+// copy a host vector into a new device array
+template <typename T>
+int upload(T** d, const std::vector<T>& h) {
+    if (cudaMalloc(d, sizeof(T) * (h.empty() ? 1 : h.size())) != cudaSuccess) {
+        cudaGetLastError();
+        *d = nullptr;
+        return 1002;  // PADE_ENOMEM
+    }
+    if (!h.empty() && cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return 1003;  // PADE_ECUDA
+    return 0;
+}
+
+// spectral fft (r2c x, c2c y) and ifft (c2c y with optional i*k pre-multiplication
+// (FftMul) of the spectral input, oddball, c2r x, 1/(nx ny))
+int spectral_fft(pade_spectral h, const double* in, void* out, cudaStream_t s);
+int spectral_ifft(pade_spectral h, const void* in, double* out, int oddball, cudaStream_t s, int mul = 0);
+// ifft of fhat * G, G = 1 where |k1| < cut1 and |k2| < cut2 (the test filter's TestFilter_oop)
+int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s);
+
+}  // namespace pade

@@ -1,0 +1,83 @@
+"""Properties of the LES oracle (CPU): the reference's conservation and model identities."""
+import numpy as np
+import pytest
+
+from oracle.les_oracle import LesOracle, hit_initial_field
+
+
+@pytest.fixture(scope="module")
+def built(oracle):
+    return oracle
+
+
+def _les(n=16, **kw):
+    u, v, w = hit_initial_field(n, seed=4)
+    L_ = 2 * np.pi
+    les = LesOracle(n, n, n, L_, L_, L_, **kw)
+    les.init_fields(u, v, w)
+    return les
+
+
+def _ke(les):
+    return 0.5 * np.mean(les.u ** 2 + les.v ** 2 + les.wC ** 2)
+
+
+def test_initial_field_is_projected_and_normalised(built):
+    u, v, w = hit_initial_field(16, seed=4)
+    assert np.sqrt((u ** 2 + v ** 2 + w[:, :, :-1] ** 2).mean() / 3) == pytest.approx(1.0, rel=1e-12)
+    les = _les()
+    assert np.abs(les.divergence(les.uhat, les.vhat, les.what)).max() < 1e-13
+    # the projection removes the compressive third of an isotropic random field's energy
+    assert 0.8 < _ke(les) < 1.2
+
+
+def test_edge_planes_are_periodic(built):
+    les = _les()
+    assert np.array_equal(les.what[:, :, -1], les.what[:, :, 0])
+    assert np.abs(les.w[:, :, -1] - les.w[:, :, 0]).max() < 1e-13
+
+
+def test_energy_decays_with_viscosity_and_sgs(built):
+    les = _les()
+    e0 = _ke(les)
+    for _ in range(3):
+        les.tvd_rk3()
+    assert _ke(les) < e0
+    assert np.abs(les.divergence(les.uhat, les.vhat, les.what)).max() < 1e-12
+
+
+def test_inviscid_energy_nearly_conserved(built):
+    les = _les(useSGS=False, isInviscid=True)
+    e0 = _ke(les)
+    les.tvd_rk3(dt=1e-3)
+    assert abs(_ke(les) - e0) < 1e-4 * e0
+
+
+def test_cfl_time_step(built):
+    les = _les(CFL=0.5, Re=1e8)
+    dt = les.compute_deltaT()
+    ts = np.abs(les.u / les.dx) + np.abs(les.v / les.dy) + np.abs(les.wC / les.dz)
+    assert dt == pytest.approx(0.5 / ts.max(), rel=1e-14)
+    les2 = _les(CFL=0.5, Re=1e-3)  # viscous limit CFL*Re*min(d)^2
+    assert les2.compute_deltaT() == pytest.approx(0.5 * 1e-3 * les2.dx ** 2, rel=1e-14)
+
+
+def test_smagorinsky_kernel_is_sqrt_2SijSij(built):
+    rng = np.random.default_rng(0)
+    d = [rng.standard_normal((4, 3, 2)) for _ in range(9)]
+    S = LesOracle.sij(d)
+    full = np.zeros((4, 3, 2))
+    G = np.array(d).reshape(3, 3, 4, 3, 2)
+    for i in range(3):
+        for j in range(3):
+            sij = 0.5 * (G[i, j] + G[j, i])
+            full += sij * sij
+    assert np.allclose(LesOracle.smag_kernel(S), np.sqrt(2 * full), rtol=1e-14)
+
+
+def test_dynamic_coefficient_nonnegative_and_planar(built):
+    les = _les()
+    les.tvd_rk3()
+    assert les.lambda1d.shape == (16,)
+    assert np.all(les.lambda1d >= 0)
+    assert les.lambda1d.max() > 0
