@@ -240,6 +240,9 @@ typedef struct {
     int DynProcFreq;       /* dynamic procedure every DynProcFreq steps */
     double dealiasFact;    /* 2/3 rule by default */
     int t_DivergenceCheck; /* check/fix the divergence every t steps (0: never) */
+    int learnedSGS;        /* 1: nu from the learned closure (pade_les_set_mlp) */
+    int JudgeFreq;         /* learnedSGS: run the dynamic procedure every JudgeFreq steps as a
+                              reference for the closure (lambda1d of pade_les_info); 0: never */
 } pade_les_params;
 #define PADE_LES_UHAT 0
 #define PADE_LES_VHAT 1
@@ -266,6 +269,35 @@ int pade_les_step(pade_les les, int use_graph, void* stream);
 int pade_les_info(pade_les les, double* dt, double* tsim, int* step, double* lambda1d);
 /* device pointer of an internal field (PADE_LES_*), valid until pade_les_destroy */
 int pade_les_field(pade_les les, int which, void** ptr);
+/* attach the learned closure used when learnedSGS is set (the object must outlive the
+ * solver's use of it); drops a captured step graph, so call it again after retraining */
+typedef struct pade_mlp_s* pade_mlp;
+int pade_les_set_mlp(pade_les les, pade_mlp mlp);
+
+/* ==== learned SGS closure (no counterpart in the reference) ====
+ * MLP 10 -> 64 -> 64 -> 1 (GELU, softplus output = Cs^2) for the eddy viscosity
+ * nu = Cs^2 Delta^2 |S|; it takes the place of DoStandardDynamicProcedure's coefficient
+ * (sgsmod_igrid.F90:176-183).  Features per point: the 9 velocity gradients divided by
+ * |S| = sqrt(2 Sij Sij) and ln(1 + Delta sqrt(|S|/nu)).  Parameters are one float array:
+ * W1 (64x10 row-major), b1, W2 (64x64), b2, w3, b3.  Inference runs on the tensor cores
+ * (BF16 operands, FP32 accumulation); training is FP32 with AdamW. */
+#define PADE_MLP_NPARAM 4929
+int pade_mlp_create(pade_mlp* mlp); /* parameters zero until pade_mlp_set_params */
+int pade_mlp_destroy(pade_mlp mlp);
+int pade_mlp_set_params(pade_mlp mlp, const float* host_params); /* also resets the AdamW state */
+int pade_mlp_get_params(pade_mlp mlp, float* host_params);
+/* mean squared error of Cs^2 against y over B samples X (device, B x 10 row-major) and its
+ * gradient (host, PADE_MLP_NPARAM); synchronises */
+int pade_mlp_loss_grad(pade_mlp mlp, const float* X, const float* y, int B, float* loss, float* grad, void* stream);
+/* one AdamW step (beta 0.9/0.999, eps 1e-8, decoupled weight decay wd) on that loss;
+ * loss (host, may be NULL) synchronises */
+int pade_mlp_train_step(pade_mlp mlp, const float* X, const float* y, int B, float lr, float wd, float* loss,
+                        void* stream);
+/* features of n points from the 9 gradient arrays (device pointers) into X (n x 10) */
+int pade_mlp_features(const double* const* duidxj, long n, double delta, double nu, float* X, void* stream);
+/* nu_out = Cs^2 Delta^2 |S| per point (FP64); cs2_out (may be NULL) receives Cs^2 */
+int pade_mlp_infer_nu(pade_mlp mlp, const double* const* duidxj, long n, double delta, double nu, double* nu_out,
+                      float* cs2_out, void* stream);
 
 /* ---- host-only plan inspection (no GPU needed; never called by the entry points above) ----
  * family: 0 cd06, 1 cd10, 2 cf90, 3 gaussian, 4 cd06stagg.

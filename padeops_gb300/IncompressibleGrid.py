@@ -25,14 +25,18 @@ class igrid:
 
     def init(self, nx, ny, nz, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, Re=1000.0, isInviscid=False, CFL=0.5,
              dt=-1.0, useSGS=True, DynamicProcedureType=1, Csgs=0.17, deltaRatio=2.0, DynProcFreq=1,
-             dealiasFact=2.0 / 3.0, t_DivergenceCheck=10):
-        """igrid init (igrid.F90:330-660) for PeriodicInZ with SGSModelID 0 (Smagorinsky)."""
+             dealiasFact=2.0 / 3.0, t_DivergenceCheck=10, learnedSGS=False, JudgeFreq=0):
+        """igrid init (igrid.F90:330-660) for PeriodicInZ with SGSModelID 0 (Smagorinsky).
+
+        learnedSGS replaces the model coefficient by the learned closure (set_mlp), with the
+        dynamic procedure run every JudgeFreq steps as its reference (0: never)."""
         if DynamicProcedureType not in (0, 1):
             raise L.PadeError(L.PADE_ENOTSUP, "only DynamicProcedureType 0 or 1")
         self.destroy()
         p = L.LesParams(nx, ny, nz, Lx, Ly, Lz, Re, int(bool(isInviscid)), CFL, dt, int(bool(useSGS)),
                         int(DynamicProcedureType == 1), Csgs, deltaRatio, DynProcFreq, dealiasFact,
-                        t_DivergenceCheck)
+                        t_DivergenceCheck, int(bool(learnedSGS)), int(JudgeFreq))
+        self.Lx, self.Ly, self.Lz, self.Re = Lx, Ly, Lz, Re
         h = ctypes.c_void_p(None)
         L.check(L.lib().pade_les_init(ctypes.byref(h), ctypes.byref(p)), "igrid.init")
         self._h = h
@@ -49,6 +53,11 @@ class igrid:
         pv, _, _ = _dev(v, "v")
         pw, _, _ = _dev(w, "w")
         L.check(L.lib().pade_les_set_fields(self.handle, pu, pv, pw, s), "igrid.set_fields")
+
+    def set_mlp(self, closure):
+        """Attach a sgs_learned.LearnedClosure (kept alive by this object)."""
+        self._closure = closure
+        L.check(L.lib().pade_les_set_mlp(self.handle, closure.handle), "igrid.set_mlp")
 
     def timeAdvance(self, use_graph=True):
         """One TVD_RK3 step (TimeSteppingScheme 1) on torch's current stream."""

@@ -44,8 +44,11 @@ class LesParams(ctypes.Structure):
                 ("Re", ctypes.c_double), ("isInviscid", ctypes.c_int), ("CFL", ctypes.c_double),
                 ("dt", ctypes.c_double), ("useSGS", ctypes.c_int), ("dynamic", ctypes.c_int),
                 ("Csgs", ctypes.c_double), ("deltaRatio", ctypes.c_double), ("DynProcFreq", ctypes.c_int),
-                ("dealiasFact", ctypes.c_double), ("t_DivergenceCheck", ctypes.c_int)]
+                ("dealiasFact", ctypes.c_double), ("t_DivergenceCheck", ctypes.c_int),
+                ("learnedSGS", ctypes.c_int), ("JudgeFreq", ctypes.c_int)]
 
+
+MLP_NPARAM = 4929
 
 LES_FIELDS = {"uhat": 0, "vhat": 1, "what": 2, "u": 3, "v": 4, "wC": 5, "w": 6, "uE": 7, "vE": 8,
               "nu_sgs_C": 30, "nu_sgs_E": 31}
@@ -82,6 +85,7 @@ def lib():
     pop = ctypes.POINTER(ctypes.c_void_p)
     pi = ctypes.POINTER(ctypes.c_int)
     dp = ctypes.POINTER(ctypes.c_double)
+    fp = ctypes.POINTER(ctypes.c_float)
     sig = {
         "pade_cd06_init": [pop, i, d, i, i, i],
         "pade_cd10_init": [pop, i, d, i, i, i],
@@ -133,6 +137,15 @@ def lib():
         "pade_les_step": [vp, i, vp],
         "pade_les_info": [vp, dp, dp, pi, dp],
         "pade_les_field": [vp, i, pop],
+        "pade_les_set_mlp": [vp, vp],
+        "pade_mlp_create": [pop],
+        "pade_mlp_destroy": [vp],
+        "pade_mlp_set_params": [vp, fp],
+        "pade_mlp_get_params": [vp, fp],
+        "pade_mlp_loss_grad": [vp, vp, vp, i, fp, fp, vp],
+        "pade_mlp_train_step": [vp, vp, vp, i, ctypes.c_float, ctypes.c_float, fp, vp],
+        "pade_mlp_features": [pop, ctypes.c_long, d, d, vp, vp],
+        "pade_mlp_infer_nu": [vp, pop, ctypes.c_long, d, d, vp, vp, vp],
     })
     for name, args in sig.items():
         fn = getattr(L, name)

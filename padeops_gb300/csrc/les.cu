@@ -372,6 +372,8 @@ struct pade_les_s {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
+    pade_mlp mlp = nullptr;
+    double deltaLES = 0;
 };
 
 namespace {
@@ -529,12 +531,26 @@ int sgs_rhs(pade_les h, cudaStream_t s) {
     const long n = h->NC, nE = h->NE;
     const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC), gsE = grid_for(h->SE);
     const Ptr9 dC = p9(h->dC), dE = p9(h->dE);
-    const bool dyn = h->prm.dynamic != 0;
-    k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
-    KCHECK();
-    if (dyn && h->newTimeStep && h->mstep % std::max(1, h->prm.DynProcFreq) == 0) CK(dynamic_procedure(h, s));
-    k_scale_nu<<<g, 256, 0, s>>>(h->nuC, dyn ? h->lambda : nullptr, h->cmodel_global, h->plane, n);
-    KCHECK();
+    const bool learned = h->prm.learnedSGS != 0;
+    const bool dyn = h->prm.dynamic != 0 && !learned;
+    if (learned) {
+        if (!h->mlp) return PS_EINVAL;
+        // the dynamic procedure as a periodic reference for the closure (lambda1d)
+        if (h->newTimeStep && h->prm.JudgeFreq > 0 && h->mstep % h->prm.JudgeFreq == 0) {
+            k_nu_kernel<<<g, 256, 0, s>>>(dC, h->rC2, h->Dsgs, n);
+            KCHECK();
+            CK(dynamic_procedure(h, s));
+        }
+        const double* grads[9];
+        for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
+        CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, s));
+    } else {
+        k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
+        KCHECK();
+        if (dyn && h->newTimeStep && h->mstep % std::max(1, h->prm.DynProcFreq) == 0) CK(dynamic_procedure(h, s));
+        k_scale_nu<<<g, 256, 0, s>>>(h->nuC, dyn ? h->lambda : nullptr, h->cmodel_global, h->plane, n);
+        KCHECK();
+    }
     CK(zop(h, OP_I_C2E, 0, h->nuC, h->nuE, s));
     if (!dyn) {
         k_clip_neg<<<gE, 256, 0, s>>>(h->nuE, nE);
@@ -686,7 +702,8 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
     if (p->nx < 4 || p->ny < 4 || p->nz < 6 || !(p->Lx > 0) || !(p->Ly > 0) || !(p->Lz > 0)) return PS_EINVAL;
     if (!(p->isInviscid) && !(p->Re > 0)) return PS_EINVAL;
     if (!(p->CFL > 0) && !(p->dt > 0)) return PS_EINVAL;
-    if (p->useSGS && p->dynamic && !(p->deltaRatio > 0)) return PS_EINVAL;
+    if (p->useSGS && (p->dynamic || p->learnedSGS) && !(p->deltaRatio > 0)) return PS_EINVAL;
+    if (p->useSGS && p->learnedSGS && !(p->Re > 0)) return PS_EINVAL;  // features use the molecular 1/Re
     for (int n : {p->nx, p->ny, p->nz})
         if (n > 8192 || (n & (n - 1)) != 0) return PS_ENOTSUP;
     auto* h = new pade_les_s();
@@ -712,6 +729,7 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
     h->tf_x = ((2.0 / 3.0) * pi / h->dx) / p->deltaRatio;
     h->tf_y = ((2.0 / 3.0) * pi / h->dy) / p->deltaRatio;
     const double deltaLES = std::pow(1.5 * h->dx * 1.5 * h->dy * 1.5 * h->dz, 1.0 / 3.0);
+    h->deltaLES = deltaLES;
     h->cmodel_global = (p->Csgs * deltaLES) * (p->Csgs * deltaLES);
     h->meanfact = 1.0 / ((double)h->nx * (double)h->ny);
     const double mn = std::min(h->dx, std::min(h->dy, h->dz));
@@ -742,7 +760,7 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
         if (rc == PS_OK) rc = al(h, pp, r8 * h->NE);
     for (int i = 0; i < 9 && rc == PS_OK; i++) rc = al(h, &h->dC[i], r8 * h->NC);
     for (int i = 0; i < 9 && rc == PS_OK; i++) rc = al(h, &h->dE[i], r8 * h->NE);
-    if (p->useSGS && p->dynamic) {
+    if (p->useSGS && (p->dynamic || (p->learnedSGS && p->JudgeFreq > 0))) {
         for (int i = 0; i < 6 && rc == PS_OK; i++) rc = al(h, &h->Sf[i], r8 * h->NC);
         for (int i = 0; i < 6 && rc == PS_OK; i++) rc = al(h, &h->M[i], r8 * h->NC);
         for (int i = 0; i < 6 && rc == PS_OK; i++) rc = al(h, &h->Lm[i], r8 * h->NC);
@@ -803,7 +821,13 @@ int pade_les_step(pade_les h, int use_graph, void* stream) {
     if (!h) return PS_EINVAL;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const bool divcheck = h->prm.t_DivergenceCheck > 0 && h->step % h->prm.t_DivergenceCheck == 0;
-    const bool fixed_shape = !h->prm.useSGS || !h->prm.dynamic || h->prm.DynProcFreq <= 1;
+    bool fixed_shape;  // the same kernel sequence every step, so one captured graph serves all
+    if (!h->prm.useSGS)
+        fixed_shape = true;
+    else if (h->prm.learnedSGS)
+        fixed_shape = h->prm.JudgeFreq <= 0;
+    else
+        fixed_shape = !h->prm.dynamic || h->prm.DynProcFreq <= 1;
     if (use_graph && !divcheck && fixed_shape && s != nullptr) {
         if (!h->gexec || h->gstream != s) {
             if (h->gexec) cudaGraphExecDestroy(h->gexec);
@@ -839,6 +863,16 @@ int pade_les_step(pade_les h, int use_graph, void* stream) {
         h->newTimeStep = true;
     }
     h->step++;
+    return PS_OK;
+}
+
+int pade_les_set_mlp(pade_les h, pade_mlp mlp) {
+    if (!h) return PS_EINVAL;
+    h->mlp = mlp;
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->gexec = nullptr;
+    h->graph = nullptr;
     return PS_OK;
 }
 
