@@ -15,6 +15,10 @@ data.  Metric: operator throughput in Gpts/s (points x operator applications per
   cpu_baseline  the oracle port of the reference algorithm on the host cores (OpenMP over
             lines), on the same workload
 
+`extras` (same line): the FP32 and native-FP64 paths of the step, the 512^3 periodic
+pressure projection, and s/step of the 256^3 LES step with the dynamic procedure and with
+the learned closure.
+
 `--impl reference` times the oracle port alone (the Fortran reference cannot be built on
 this hardware: no Fortran compiler or MPI) and prints its line.
 """
@@ -44,7 +48,7 @@ def log(*a):
 
 
 def make_field():
-    from tests.fields import random_modes
+    from padeops_gb300.synthetic import random_modes
 
     return random_modes((N, N, N), NMODES, KMAX, SEED, z_nonperiodic=True, profile=True)
 
@@ -235,6 +239,118 @@ def cpu_baseline(args, f_host, steps=None):
     return gpts, O.threads(), dt
 
 
+def _time(torch, fn, reps, stream=None):
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    st = stream or torch.cuda.current_stream()
+    s.record(st)
+    for _ in range(reps):
+        fn()
+    e.record(st)
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def extras(args, P, torch, f_host):
+    """Secondary measurements of the other hot-path rows (rank 0): the FP32 and native-FP64
+    paths of the same step, the 512^3 periodic projection, and the 256^3 LES step with the
+    dynamic procedure and with the learned closure.  Errors are reported, not raised."""
+    out = {}
+    dev = torch.device("cuda", 0)
+    plan = step_plan(setup_objects(P))
+    npts = N ** 3
+    reps = max(3, min(args.steps, 10))
+    try:
+        base = torch.from_numpy(np.ascontiguousarray(f_host.T)).to(dev)
+        for path, dt, name, bpp in ((P.PATH_FP32, torch.float32, "fp32_path", 8),
+                                    (P.PATH_NATIVE, torch.float64, "native_fp64_path", 16)):
+            ins = [base.to(dt).clone() for _ in range(len(plan))]
+            outs = [torch.empty_like(x) for x in ins]
+
+            def step(ins=ins, outs=outs, path=path):
+                for k, (obj, opc, d, _) in enumerate(plan):
+                    obj.apply(opc, d, ins[k], outs[k], N, N, 0, 0, path)
+
+            ms = _time(torch, step, reps if path == P.PATH_FP32 else 2)
+            out[name] = {"value": len(plan) * npts / (ms * 1e-3) / 1e9, "unit": "Gpts/s", "ms_per_step": ms,
+                         "achieved_GBps": len(plan) * npts * bpp / (ms * 1e-3) / 1e9, "bytes_per_point": bpp}
+            del ins, outs
+        del base
+        torch.cuda.empty_cache()
+    except Exception as ex:  # pragma: no cover - reported in the JSON line
+        out["paths_error"] = repr(ex)
+    try:
+        n = 512
+        d = 2 * np.pi / n
+        sp = P.spectral()
+        sp.init(n, n, n, d, d, fixOddball=False)
+        po = P.padepoisson()
+        po.init(d, d, d, sp)
+        g = torch.Generator(device=dev).manual_seed(3)
+        U = torch.randn((n, n, n // 2 + 1), dtype=torch.complex128, device=dev, generator=g)
+        V = torch.randn_like(U)
+        W = torch.randn((n + 1, n, n // 2 + 1), dtype=torch.complex128, device=dev, generator=g)
+        ms_p = _time(torch, lambda: po.PressureProjection(U, V, W), 3)
+        div = torch.empty((n, n, n), dtype=torch.float64, device=dev)
+        ms_d = _time(torch, lambda: po.DivergenceCheck(U, V, W, div), 3)
+        phys = torch.randn((n, n, n), dtype=torch.float64, device=dev, generator=g)
+        ms_f = _time(torch, lambda: sp.fft(phys, U), 3)
+        ms_i = _time(torch, lambda: sp.ifft(U, phys), 3)
+        cbytes = 16 * (n // 2 + 1) * n * n
+        out["projection_512"] = {"PressureProjection_ms": ms_p, "DivergenceCheck_ms": ms_d,
+                                 "spectral_fft_ms": ms_f, "spectral_ifft_ms": ms_i,
+                                 "projection_compulsory_GBps": 6 * cbytes / (ms_p * 1e-3) / 1e9,
+                                 "note": "FP64 radix-2 FFTs; FP64-pipe bound (4 n log2 n FP64 ops per line)"}
+        del U, V, W, div, phys, sp, po
+        torch.cuda.empty_cache()
+    except Exception as ex:  # pragma: no cover
+        out["projection_error"] = repr(ex)
+    try:
+        from padeops_gb300.sgs_learned import LearnedClosure, init_params, train, training_set
+        from padeops_gb300.synthetic import hit_initial_field
+
+        def tdev(a):
+            return torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
+
+        n0 = 64
+        u, v, w = hit_initial_field(n0, seed=4)
+        g0 = P.igrid()
+        g0.init(n0, n0, n0)
+        g0.set_fields(tdev(u), tdev(v), tdev(w))
+        clo = LearnedClosure(init_params(0))
+        X, y = training_set(g0, clo, nsteps=8, every=2)
+        hist = train(clo, X, y, epochs=10, batch=4096, lr=3e-3)
+        del g0, X, y
+        n = 256
+        u, v, w = hit_initial_field(n, seed=4)
+        res = {}
+        for mode in ("dynamic", "learned"):
+            g1 = P.igrid()
+            if mode == "learned":
+                g1.init(n, n, n, learnedSGS=True, JudgeFreq=0)
+                g1.set_mlp(clo)
+            else:
+                g1.init(n, n, n)
+            g1.set_fields(tdev(u), tdev(v), tdev(w))
+            side = torch.cuda.Stream()
+            with torch.cuda.stream(side):
+                g1.timeAdvance(use_graph=False)  # step 0 carries the divergence check
+                ms = _time(torch, lambda g1=g1: g1.timeAdvance(use_graph=True), 3, stream=side)
+            res[mode] = ms
+            del g1
+            torch.cuda.empty_cache()
+        out["les_256"] = {"s_per_step_dynamic": res["dynamic"] / 1e3, "s_per_step_learned": res["learned"] / 1e3,
+                          "learned_speedup": res["dynamic"] / res["learned"],
+                          "config": "256^3 periodic, Re 1000, CFL 0.5, TVD-RK3, Smagorinsky (dynamic, deltaRatio 2)"
+                                    " vs learned closure trained on a 64^3 dynamic run; CUDA-graph steps",
+                          "training_loss": [hist[0], hist[-1]]}
+    except Exception as ex:  # pragma: no cover
+        out["les_error"] = repr(ex)
+    return out
+
+
 def traffic_per_launch():
     p = os.path.join(ROOT, "profiles", "chunk_kernel_traffic.json")
     if os.path.exists(p):
@@ -253,6 +369,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the secondary measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -317,12 +434,15 @@ def main():
         gpts, cores, dt = cpu_baseline(args, f_host, steps=1)
         cb = {"value": gpts, "unit": "Gpts/s", "cores": cores, "kind": "port",
               "sample": "one full 256^3 step (9 applications), oracle C port with OpenMP over lines"}
+    ext = extras(args, P, torch, f_host) if (rank == 0 and not args.no_extras) else None
     if rank == 0:
         line = {"metric": metric, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64 (double-float arithmetic)", "data": "synthetic",
                 "config": config, "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": len(plan) * args.steps}
+        if ext is not None:
+            line["extras"] = ext
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

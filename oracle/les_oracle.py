@@ -305,29 +305,3 @@ class LesOracle:
         self.tsim += dt
         self.newTimeStep = True
         return dt
-
-
-def hit_initial_field(n, seed=4, kp=4.0, urms=1.0):
-    """Seeded solenoidal-spectrum field on [0, 2pi)^3: E(k) ~ k^4 exp(-2 (k/kp)^2), random
-    phases, scaled to u_rms; w returned on nz+1 edge planes (plane nz+1 = plane 1).  The
-    projection inside init_fields makes it discretely divergence free."""
-    rng = np.random.default_rng(seed)
-    k = np.fft.fftfreq(n, 1.0 / n)
-    KX, KY, KZ = np.meshgrid(k, k, k, indexing="ij")
-    kk = np.sqrt(KX ** 2 + KY ** 2 + KZ ** 2)
-    kk[0, 0, 0] = 1.0
-    E = kk ** 4 * np.exp(-2.0 * (kk / kp) ** 2)
-    amp = np.sqrt(E / (4 * np.pi * kk ** 2))
-    amp[0, 0, 0] = 0.0
-    amp[np.abs(KX) >= n // 3] = 0.0
-    amp[np.abs(KY) >= n // 3] = 0.0
-    amp[np.abs(KZ) >= n // 3] = 0.0
-    comps = []
-    for _ in range(3):
-        ph = rng.uniform(0, 2 * np.pi, (n, n, n))
-        comps.append(np.real(np.fft.ifftn(amp * np.exp(1j * ph))) * n ** 3)
-    u, v, w = comps
-    s = urms / np.sqrt((u ** 2 + v ** 2 + w ** 2).mean() / 3.0)
-    u, v, w = (np.asfortranarray(c * s) for c in (u, v, w))
-    wE = np.asfortranarray(np.concatenate([w, w[:, :, :1]], axis=2))
-    return u, v, wE

@@ -121,12 +121,3 @@ def infer_bf16(p, X):
     h2 = gelu(z2)
     z3 = h2 @ np.asarray(w["w3"], dtype=np.float32) + np.float32(w["b3"][0])
     return softplus(z3)
-
-
-def init_params(seed):
-    """Seeded initialisation (uniform +-1/sqrt(fan_in), biases 0, b3 = ln(e^0.02 - 1))."""
-    rng = np.random.default_rng(seed)
-    d = {"W1": rng.uniform(-1, 1, (NH, NIN)) / np.sqrt(NIN), "b1": np.zeros(NH),
-         "W2": rng.uniform(-1, 1, (NH, NH)) / np.sqrt(NH), "b2": np.zeros(NH),
-         "w3": rng.uniform(-1, 1, NH) / np.sqrt(NH), "b3": np.array([np.log(np.expm1(0.02))])}
-    return pack(d).astype(np.float32)

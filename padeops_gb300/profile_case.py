@@ -2,6 +2,9 @@
 
     python -m padeops_gb300.profile_case --family cd10 --opcode 1 --dir 1 --n 256 \
         --other 256 320 --repeat 3 --path df
+    python -m padeops_gb300.profile_case --family spectral --n 256 --repeat 3   # fft + ifft
+    python -m padeops_gb300.profile_case --family projection --n 256 --repeat 3
+    python -m padeops_gb300.profile_case --family les --n 128 --repeat 2        # TVD-RK3 steps
 
 Used for Nsight Compute captures of a single kernel on a bounded case; prints the mean
 CUDA-event time per application and the implied HBM throughput at 16 B/point.
@@ -15,7 +18,8 @@ import numpy as np
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--family", default="cd10", choices=["cd06", "cd10", "cf90", "gaussian"])
+    ap.add_argument("--family", default="cd10",
+                    choices=["cd06", "cd10", "cf90", "gaussian", "spectral", "projection", "les"])
     ap.add_argument("--opcode", type=int, default=1)
     ap.add_argument("--dir", type=int, default=1)
     ap.add_argument("--n", type=int, default=256)
@@ -33,6 +37,8 @@ def main(argv=None):
     from padeops_gb300 import build as B
 
     B.build()
+    if a.family in ("spectral", "projection", "les"):
+        return spectral_case(a, torch, P)
     path = {"df": L.PATH_DF, "native": L.PATH_NATIVE, "fp32": L.PATH_FP32}[a.path]
     dt = torch.float32 if path == L.PATH_FP32 else torch.float64
     n = a.n
@@ -58,6 +64,49 @@ def main(argv=None):
     bpp = 2 * f.element_size()
     print(f"{a.family} op{a.opcode} dir{a.dir} n={n} lines={na}x{nb} path={a.path}: {ms:.4f} ms/app, "
           f"{total / ms / 1e6:.1f} Gpts/s, {total * bpp / ms / 1e6:.1f} GB/s")
+
+
+def _timed(torch, fn, repeat):
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(repeat):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / repeat
+
+
+def spectral_case(a, torch, P):
+    n = a.n
+    d = 2 * np.pi / n
+    g = torch.Generator(device="cuda").manual_seed(0)
+    if a.family == "les":
+        from padeops_gb300.synthetic import hit_initial_field
+
+        u, v, w = hit_initial_field(n, seed=4)
+        grid = P.igrid()
+        grid.init(n, n, n)
+        dev = lambda x: torch.from_numpy(np.ascontiguousarray(x.T)).cuda()  # noqa: E731
+        grid.set_fields(dev(u), dev(v), dev(w))
+        ms = _timed(torch, lambda: grid.timeAdvance(use_graph=False), a.repeat)
+        print(f"les n={n}: {ms:.3f} ms/step")
+        return
+    sp = P.spectral()
+    sp.init(n, n, n, d, d)
+    U = torch.randn((n, n, n // 2 + 1), dtype=torch.complex128, device="cuda", generator=g)
+    if a.family == "spectral":
+        f = torch.randn((n, n, n), dtype=torch.float64, device="cuda", generator=g)
+        ms = _timed(torch, lambda: (sp.fft(f, U), sp.ifft(U, f)), a.repeat)
+        print(f"spectral fft+ifft n={n}: {ms:.3f} ms")
+        return
+    po = P.padepoisson()
+    po.init(d, d, d, sp)
+    V = torch.randn_like(U)
+    W = torch.randn((n + 1, n, n // 2 + 1), dtype=torch.complex128, device="cuda", generator=g)
+    ms = _timed(torch, lambda: po.PressureProjection(U, V, W), a.repeat)
+    print(f"projection n={n}: {ms:.3f} ms")
 
 
 if __name__ == "__main__":

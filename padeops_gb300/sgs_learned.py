@@ -33,6 +33,15 @@ def _grads(ptrs):
     return ctypes.cast(arr, ctypes.POINTER(ctypes.c_void_p))
 
 
+def init_params(seed):
+    """Seeded initial parameters: weights uniform in +-1/sqrt(fan_in), biases 0, and b3 such
+    that the initial output is Cs^2 = 0.02."""
+    rng = np.random.default_rng(seed)
+    parts = [rng.uniform(-1, 1, (64, 10)) / np.sqrt(10), np.zeros(64), rng.uniform(-1, 1, (64, 64)) / 8.0,
+             np.zeros(64), rng.uniform(-1, 1, 64) / 8.0, np.array([np.log(np.expm1(0.02))])]
+    return np.concatenate([a.ravel() for a in parts]).astype(np.float32)
+
+
 def delta_les(dx, dy, dz):
     """Filter width of the periodic-z Smagorinsky model (smagorinsky.F90:13-16)."""
     return (1.5 * dx * 1.5 * dy * 1.5 * dz) ** (1.0 / 3.0)

@@ -10,7 +10,8 @@ import numpy as np
 import pytest
 
 import padeops_gb300 as P
-from oracle.les_oracle import LesOracle, hit_initial_field
+from oracle.les_oracle import LesOracle
+from padeops_gb300.synthetic import hit_initial_field
 from tests.fields import relerr
 
 pytestmark = pytest.mark.gpu

@@ -9,8 +9,8 @@ import pytest
 
 import padeops_gb300 as P
 from oracle import mlp_oracle as M
-from oracle.les_oracle import hit_initial_field
-from padeops_gb300.sgs_learned import LearnedClosure, delta_les, train, training_set
+from padeops_gb300.synthetic import hit_initial_field
+from padeops_gb300.sgs_learned import LearnedClosure, delta_les, init_params, train, training_set
 from tests.fields import relerr
 
 pytestmark = pytest.mark.gpu
@@ -26,7 +26,7 @@ def _data(B, seed):
 
 @pytest.mark.parametrize("B", [1, 128, 300, 4096])
 def test_loss_and_gradient_match_oracle(B):
-    p = M.init_params(5)
+    p = init_params(5)
     X, y = _data(B, B)
     c = LearnedClosure(p)
     loss, g = c.loss_grad(torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda())
@@ -36,7 +36,7 @@ def test_loss_and_gradient_match_oracle(B):
 
 
 def test_adamw_steps_match_oracle():
-    p = M.init_params(6)
+    p = init_params(6)
     X, y = _data(512, 7)
     c = LearnedClosure(p)
     Xd, yd = torch.from_numpy(X).cuda(), torch.from_numpy(y).cuda()
@@ -60,7 +60,7 @@ def test_features_and_inference_match_oracle():
     d = _grads(shape, 3)
     dd = [torch.from_numpy(np.ascontiguousarray(a.T)).cuda() for a in d]
     delta, nu = 0.3, 1e-3
-    p = M.init_params(8)
+    p = init_params(8)
     c = LearnedClosure(p)
     X = c.features(dd, delta, nu).cpu().numpy()
     rX, mag = M.features(d, delta, nu)
@@ -82,7 +82,7 @@ def test_learned_les_trains_and_runs():
     dyn = P.igrid()
     dyn.init(n, n, n)
     dyn.set_fields(dev(u), dev(v), dev(w))
-    c = LearnedClosure(M.init_params(0))
+    c = LearnedClosure(init_params(0))
     X, y = training_set(dyn, c, nsteps=4, every=1)
     hist = train(c, X, y, epochs=8, batch=2048, lr=3e-3)
     assert hist[-1] < hist[0]

@@ -2,7 +2,8 @@
 import numpy as np
 import pytest
 
-from oracle.les_oracle import LesOracle, hit_initial_field
+from oracle.les_oracle import LesOracle
+from padeops_gb300.synthetic import hit_initial_field
 
 
 @pytest.fixture(scope="module")

@@ -3,6 +3,7 @@ the BF16 rounding helper, and the feature definition."""
 import numpy as np
 
 from oracle import mlp_oracle as M
+from padeops_gb300.sgs_learned import init_params
 
 
 def test_parameter_count_matches_header():
@@ -13,7 +14,7 @@ def test_parameter_count_matches_header():
 
 def test_gradient_matches_finite_differences():
     rng = np.random.default_rng(1)
-    p = M.init_params(3).astype(np.float64)
+    p = init_params(3).astype(np.float64)
     X = rng.standard_normal((37, 10))
     y = 0.02 + 0.01 * rng.random(37)
     loss, g = M.loss_and_grad(p, X, y)
