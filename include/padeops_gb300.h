@@ -214,6 +214,16 @@ int pade_fft_c2c(int dir, int sign, const void* in, void* out, int n1, int n2, i
 int pade_fft_r2c_x(const double* in, void* out, int nx, int ny, int nz, void* stream);
 int pade_fft_c2r_x(const void* in, double* out, int nx, int ny, int nz, double scale, void* stream);
 
+/* Arithmetic of every transform above (process-wide): PADE_FFT_DF (default, double-float
+ * on the FP32 pipes, each line scaled by a power of two so its maximum is in [1, 2);
+ * ~48 significant bits, elements below 2^-74 of their line's maximum count as zero) or
+ * PADE_FFT_FP64 (native FP64, bound by GB300's FP64 rate).  A captured LES step graph
+ * keeps the arithmetic it was captured with. */
+#define PADE_FFT_DF 0
+#define PADE_FFT_FP64 1
+int pade_fft_set_arith(int arith);
+int pade_fft_get_arith(void);
+
 /* 2DECOMP transpose_x_to_y / y_to_z / z_to_y / y_to_x (pencil 1 = x, 2 = y, 3 = z) for
  * one rank: the pencils share the (i,j,k) layout, so this is a device copy of n1*n2*n3
  * elements of elem_bytes (8 real, 16 complex). */

@@ -49,6 +49,8 @@ class LesParams(ctypes.Structure):
 
 
 MLP_NPARAM = 4929
+FFT_DF = 0
+FFT_FP64 = 1
 
 LES_FIELDS = {"uhat": 0, "vhat": 1, "what": 2, "u": 3, "v": 4, "wC": 5, "w": 6, "uE": 7, "vE": 8,
               "nu_sgs_C": 30, "nu_sgs_E": 31}
@@ -131,6 +133,8 @@ def lib():
         "pade_fft_r2c_x": [vp, vp, i, i, i, vp],
         "pade_fft_c2r_x": [vp, vp, i, i, i, d, vp],
         "pade_transpose": [i, i, vp, vp, i, i, i, i, vp],
+        "pade_fft_set_arith": [i],
+        "pade_fft_get_arith": [],
         "pade_les_init": [pop, ctypes.POINTER(LesParams)],
         "pade_les_destroy": [vp],
         "pade_les_set_fields": [vp, vp, vp, vp, vp],

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -202,6 +203,8 @@ __global__ void __launch_bounds__(256) k_fft(const void* in, void* out, const Ff
     }
 }
 
+std::atomic<int> g_arith{FFT_ARITH_DF};
+
 std::mutex g_tw_mu;
 std::map<std::pair<int, int>, double2*> g_tw;  // (device, n) -> exp(-2 pi i t / n), t < n/2
 
@@ -273,11 +276,16 @@ FftLines fft_lines(int dir, long n1, long n2, long n3, long in_len, long out_len
     return s;
 }
 
+void fft_set_arith(int a) { g_arith.store(a == FFT_ARITH_FP64 ? FFT_ARITH_FP64 : FFT_ARITH_DF); }
+int fft_get_arith() { return g_arith.load(); }
+
 int fft_launch(int in_mode, int out_mode, int kind, int n, int sign, double scale, int oddball, const void* in,
                void* out, const FftLines& ls, const FftExtra& ex, cudaStream_t s) {
     const int logn = log2_exact(n);
     if (logn < 1 || logn > 13) return PS_ENOTSUP;
     if (ls.nlines <= 0) return PS_OK;
+    if (g_arith.load() == FFT_ARITH_DF)
+        return fft_launch_df(in_mode, out_mode, kind, logn, sign, scale, oddball, in, out, ls, ex, s);
     const double2* tw = nullptr;
     const int rc = twiddles(n, &tw);
     if (rc != PS_OK) return rc;

@@ -57,7 +57,13 @@ FftLines fft_lines(int dir, long n1, long n2, long n3, long in_len, long out_len
 int fft_launch(int in_mode, int out_mode, int kind, int n, int sign, double scale, int oddball, const void* in,
                void* out, const FftLines& ls, const FftExtra& ex, cudaStream_t s);
 
-// Number of kernels fft_launch starts per call (for launch accounting).
-constexpr int kFftKernelsPerLaunch = 1;
+// The same transform in double-float arithmetic (fft_df.cu); logn = log2(n)
+int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, double scale, int oddball, const void* in,
+                  void* out, const FftLines& ls, const FftExtra& ex, cudaStream_t s);
+
+// Arithmetic of every transform: FFT_ARITH_DF (default) or FFT_ARITH_FP64
+enum FftArith { FFT_ARITH_DF = 0, FFT_ARITH_FP64 = 1 };
+void fft_set_arith(int a);
+int fft_get_arith();
 
 }  // namespace pade

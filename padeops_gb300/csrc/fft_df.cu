@@ -1,0 +1,345 @@
+// Batched FFTs in double-float arithmetic (FP64 in and out, pairs of floats inside).
+//
+// The FP64 transform of fft.cu keeps GB300's FP64 pipe ~85 % busy at a few per cent of
+// the HBM bandwidth (4 n log2 n FP64 operations per line, FP64 issuing at 1/56 of the
+// FP32 rate).  This kernel does the same transforms on the FP32 pipes: every complex
+// value is (re_hi + re_lo, im_hi + im_lo), butterflies use the error-free TwoSum /
+// TwoProduct of dfmath.cuh with a renormalisation per stage, and twiddles are float pairs
+// of the correctly rounded values (~48 significant bits; transform error ~log2(n) 2^-47).
+//
+// Each line is scaled by a power of two before the split so that its largest element is
+// in [1, 2): the double-float range (|x| >= 2^-74 for full precision) then holds relative
+// to the line maximum and the scaling is exact, done on the exponent bits with integer
+// instructions (no FP64 multiply).  Elements below 2^-74 of their line's maximum are
+// treated as zero.  Loads are in natural order and the forward transform decimates in
+// frequency (bit-reversed result); the fused kinds multiply in that order and transform
+// back by decimation in time, so no reordering pass is needed.
+//
+// Same modes, kinds and conventions as k_fft (fft.cu).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "dfmath.cuh"
+#include "fft.h"
+#include "operators.h"
+
+namespace pade {
+
+namespace {
+
+struct cdf {
+    dfv r, i;
+};
+
+__device__ __forceinline__ cdf ldc(const float4* s, int idx) {
+    const float4 v = s[idx];
+    return cdf{dfv{v.x, v.y}, dfv{v.z, v.w}};
+}
+__device__ __forceinline__ void stc(float4* s, int idx, cdf c) { s[idx] = make_float4(c.r.h, c.r.l, c.i.h, c.i.l); }
+
+__device__ __forceinline__ cdf cadd(cdf a, cdf b) { return cdf{df_norm(df_add(a.r, b.r)), df_norm(df_add(a.i, b.i))}; }
+__device__ __forceinline__ cdf csub(cdf a, cdf b) { return cdf{df_norm(df_sub(a.r, b.r)), df_norm(df_sub(a.i, b.i))}; }
+
+// a * w (w a twiddle (c_hi, c_lo, s_hi, s_lo)); conj uses c - i s
+__device__ __forceinline__ cdf cmulw(cdf a, float4 w, bool conj) {
+    const dfv wr{w.x, w.y};
+    const dfv wi = conj ? dfv{-w.z, -w.w} : dfv{w.z, w.w};
+    const dfv rr = df_sub(df_mul(a.r, wr), df_mul(a.i, wi));
+    const dfv ii = df_add(df_mul(a.r, wi), df_mul(a.i, wr));
+    return cdf{df_norm(rr), df_norm(ii)};
+}
+
+__device__ __forceinline__ cdf cscale(cdf a, dfv m) { return cdf{df_norm(df_mul(a.r, m)), df_norm(df_mul(a.i, m))}; }
+
+__device__ __forceinline__ int brev(int p, int logn) { return (int)(__brev((unsigned)p) >> (32 - logn)); }
+
+__device__ __forceinline__ double ksq(double a, double b, double c) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+}
+
+__device__ __forceinline__ int bexp(double d) { return (__double2hiint(d) >> 20) & 0x7FF; }
+
+// d * 2^-k split into a df value; zero when below 2^-74 after the shift (or zero/subnormal)
+__device__ __forceinline__ dfv df_from_double_shift(double d, int k) {
+    const unsigned lo = (unsigned)__double2loint(d);
+    unsigned hi = (unsigned)__double2hiint(d);
+    const int ex = (int)((hi >> 20) & 0x7FFu);
+    const int e2 = ex - k;
+    if (ex == 0 || e2 < 949 || e2 > 1149) return dfv{0.0f, 0.0f};
+    hi = (hi & 0x800FFFFFu) | ((unsigned)e2 << 20);
+    unsigned bad = 0;
+    return df_from_double(__hiloint2double((int)hi, (int)lo), bad);
+}
+
+// r * 2^k on the exponent bits (flushes below the normal range)
+__device__ __forceinline__ double shift_up(double r, int k) {
+    const unsigned lo = (unsigned)__double2loint(r);
+    unsigned hi = (unsigned)__double2hiint(r);
+    const int ex = (int)((hi >> 20) & 0x7FFu);
+    if (ex == 0) return 0.0;
+    int e2 = ex + k;
+    if (e2 <= 0) return 0.0;
+    if (e2 >= 2047) return __hiloint2double((int)((hi & 0x80000000u) | 0x7FF00000u), 0);
+    hi = (hi & 0x800FFFFFu) | ((unsigned)e2 << 20);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// decimation in frequency: natural order -> bit-reversed
+__device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj) {
+    const int half = 1 << (logn - 1);
+    const int work = nl << (logn - 1);
+    for (int s = logn - 1; s >= 0; s--) {
+        for (int e = threadIdx.x; e < work; e += blockDim.x) {
+            const int l = e >> (logn - 1), j = e & (half - 1);
+            const int k = j & ((1 << s) - 1);
+            const int i0 = (l << logn) + ((j >> s) << (s + 1)) + k;
+            const int i1 = i0 + (1 << s);
+            const cdf a = ldc(x, i0), b = ldc(x, i1);
+            stc(x, i0, cadd(a, b));
+            const cdf d = csub(a, b);
+            stc(x, i1, s == 0 ? d : cmulw(d, __ldg(&tw[k << (logn - 1 - s)]), conj));
+        }
+        __syncthreads();
+    }
+}
+
+// decimation in time: bit-reversed -> natural order
+__device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj) {
+    const int half = 1 << (logn - 1);
+    const int work = nl << (logn - 1);
+    for (int s = 0; s < logn; s++) {
+        for (int e = threadIdx.x; e < work; e += blockDim.x) {
+            const int l = e >> (logn - 1), j = e & (half - 1);
+            const int k = j & ((1 << s) - 1);
+            const int i0 = (l << logn) + ((j >> s) << (s + 1)) + k;
+            const int i1 = i0 + (1 << s);
+            const cdf a = ldc(x, i0);
+            cdf b = ldc(x, i1);
+            if (s > 0) b = cmulw(b, __ldg(&tw[k << (logn - 1 - s)]), conj);
+            stc(x, i0, cadd(a, b));
+            stc(x, i1, csub(a, b));
+        }
+        __syncthreads();
+    }
+}
+
+template <int IN, int OUT, int KIND>
+__global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const FftLines ls,
+                                                const float4* __restrict__ tw, int logn, int lb, int sign,
+                                                int scale_exp, float2 scale_df, int use_scale_df, int oddball,
+                                                const FftExtra ex) {
+    extern __shared__ __align__(16) float4 smf[];
+    double2* smd = reinterpret_cast<double2*>(smf);
+    __shared__ int emax[64];
+    const int n = 1 << logn, half = n >> 1;
+    const long l0 = (long)blockIdx.x * lb;
+    const int nl = (int)min((long)lb, ls.nlines - l0);
+    const int total = nl << logn;
+    const bool pin = ls.fp == 1, pout = ls.op == 1;
+    for (int l = threadIdx.x; l < nl; l += blockDim.x) emax[l] = 0;
+    __syncthreads();
+
+    // ---- load (FP64, natural order) and the per-line maximum exponent
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int l = pin ? (e >> logn) : (e % nl);
+        const int p = pin ? (e & (n - 1)) : (e / nl);
+        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+        const long base = a * ls.fa + b * ls.fb;
+        double2 v;
+        if (IN == IN_COMPLEX) {
+            v = reinterpret_cast<const double2*>(in)[base + p * ls.fp];
+        } else if (IN == IN_REAL) {
+            v = make_double2(reinterpret_cast<const double*>(in)[base + p * ls.fp], 0.0);
+        } else {
+            const double2* src = reinterpret_cast<const double2*>(in);
+            if (p <= half) {
+                v = src[base + p * ls.fp];
+            } else {
+                const double2 c = src[base + (long)(n - p) * ls.fp];
+                v = make_double2(c.x, -c.y);
+            }
+            if (p == 0 || p == half) v.y = 0.0;
+            if (oddball && p == half) v.x = 0.0;
+        }
+        if (KIND == FK_PLAIN && ex.mul == MUL_MASK_AP) {
+            if (!(fabs(ex.ka[a]) < ex.cut_a && fabs(ex.kb[p]) < ex.cut_b)) v = make_double2(0.0, 0.0);
+        } else if (KIND == FK_PLAIN && ex.mul != MUL_NONE) {
+            const double k = ex.km[ex.mul == MUL_IK_A ? a : p];
+            v = make_double2(-k * v.y, k * v.x);
+        }
+        if (KIND == FK_PROJECT) {
+            const long idx = lg + p * ex.plane;
+            const double k1 = ex.k1[lg % ex.nxh], k2 = ex.k2[lg / ex.nxh];
+            const double2 uu = ex.u[idx], vv = ex.v[idx];
+            const double tx = __dadd_rn(__dmul_rn(k1, uu.x), __dmul_rn(k2, vv.x));
+            const double ty = __dadd_rn(__dmul_rn(k1, uu.y), __dmul_rn(k2, vv.y));
+            v = make_double2(v.x - ty, v.y + tx);
+        }
+        smd[(l << logn) + p] = v;
+        atomicMax(&emax[l], max(bexp(v.x), bexp(v.y)));
+    }
+    __syncthreads();
+    // ---- split in place, each line scaled by 2^-(emax - 1023)
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int k = emax[e >> logn] - 1023;
+        const double2 v = smd[e];
+        stc(smf, e, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
+    }
+    __syncthreads();
+
+    if (KIND == FK_PLAIN) {
+        dif_df(smf, nl, logn, tw, sign > 0);
+    } else {
+        dif_df(smf, nl, logn, tw, false);
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int l = e >> logn, q = e & (n - 1);
+            const int f = brev(q, logn);  // frequency held at position q
+            const long lg = l0 + l;
+            const long i = lg % ex.nxh, j = lg / ex.nxh;
+            if (KIND == FK_DEALIAS) {
+                const bool keep = fabs(ex.ka[i]) < ex.cut_a && fabs(ex.kb[j]) < ex.cut_b && fabs(ex.kc[f]) < ex.cut_c;
+                if (!keep) stc(smf, e, cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}});
+            } else {
+                const double kr = ksq(ex.ka[i], ex.kb[j], ex.kc[f]);
+                double m;
+                if (KIND == FK_PROJECT) {
+                    m = kr <= 1e-14 ? 0.0 : -(1.0 / kr);
+                } else {
+                    m = -1.0 / __dadd_rn(kr, 1e-20);
+                    if (lg == 0 && f == 0) m = 0.0;
+                }
+                unsigned bad = 0;
+                stc(smf, e, cscale(ldc(smf, e), df_from_double(m, bad)));
+            }
+        }
+        __syncthreads();
+        dit_df(smf, nl, logn, tw, true);
+    }
+
+    // ---- store (FP64)
+    const int nout = OUT == OUT_HALF ? half + 1 : n;
+    const dfv sdf{scale_df.x, scale_df.y};
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int l = pout ? (e >> logn) : (e % nl);
+        const int p = pout ? (e & (n - 1)) : (e / nl);
+        if (p >= nout) continue;
+        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+        const long o = a * ls.oa + b * ls.ob + p * ls.op;
+        cdf c = ldc(smf, (l << logn) + (KIND == FK_PLAIN ? brev(p, logn) : p));
+        if (use_scale_df) c = cscale(c, sdf);
+        const int k = emax[l] - 1023 + scale_exp;
+        const double2 v = make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
+        if (OUT == OUT_REAL) {
+            reinterpret_cast<double*>(out)[o] = v.x;
+        } else {
+            reinterpret_cast<double2*>(out)[o] = v;
+        }
+        if (KIND == FK_DEALIAS && ex.edge_copy && p == 0) reinterpret_cast<double2*>(out)[o + (long)n * ls.op] = v;
+        if (KIND == FK_PROJECT) {
+            const long idx = lg + p * ex.plane;
+            const double k1 = ex.k1[lg % ex.nxh], k2 = ex.k2[lg / ex.nxh];
+            double2 uu = ex.u[idx], vv = ex.v[idx];
+            uu = make_double2(uu.x + k1 * v.y, uu.y - k1 * v.x);
+            vv = make_double2(vv.x + k2 * v.y, vv.y - k2 * v.x);
+            ex.u[idx] = uu;
+            ex.v[idx] = vv;
+        }
+    }
+}
+
+std::mutex g_twdf_mu;
+std::map<std::pair<int, int>, float4*> g_twdf;  // (device, n) -> df exp(-2 pi i t / n), t < n/2
+
+void split_ld(long double x, float& h, float& l) {
+    h = (float)x;
+    l = (float)(x - (long double)h);
+}
+
+int twiddles_df(int n, const float4** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PS_ECUDA;
+    std::lock_guard<std::mutex> lock(g_twdf_mu);
+    auto it = g_twdf.find({dev, n});
+    if (it != g_twdf.end()) {
+        *out = it->second;
+        return PS_OK;
+    }
+    std::vector<float4> h(std::max(1, n / 2));
+    for (int t = 0; t < n / 2; t++) {
+        const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)t / (long double)n;
+        float ch, cl, sh, sl;
+        split_ld(cosl(ang), ch, cl);
+        split_ld(sinl(ang), sh, sl);
+        h[t] = make_float4(ch, cl, sh, sl);
+    }
+    float4* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float4) * h.size()) != cudaSuccess) {
+        cudaGetLastError();
+        return PS_ENOMEM;
+    }
+    if (cudaMemcpy(d, h.data(), sizeof(float4) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d);
+        return PS_ECUDA;
+    }
+    g_twdf[{dev, n}] = d;
+    *out = d;
+    return PS_OK;
+}
+
+template <int I, int O, int K>
+int launch_df_t(const void* in, void* out, const FftLines& ls, const float4* tw, int logn, int lb, int sign,
+                int sexp, float2 sdf, int use_sdf, int oddball, const FftExtra& ex, cudaStream_t s) {
+    const size_t smem = sizeof(float4) * ((size_t)lb << logn);
+    auto kern = k_fft_df<I, O, K>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return PS_ECUDA;
+    const long blocks = (ls.nlines + lb - 1) / lb;
+    if (blocks > 0x7fffffffL) return PS_ENOTSUP;
+    kern<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use_sdf, oddball, ex);
+    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+}
+
+}  // namespace
+
+int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, double scale, int oddball, const void* in,
+                  void* out, const FftLines& ls, const FftExtra& ex, cudaStream_t s) {
+    const int n = 1 << logn;
+    const float4* tw = nullptr;
+    const int rc = twiddles_df(n, &tw);
+    if (rc != PS_OK) return rc;
+    const int lb = std::max(1, std::min(64, 4096 >> logn));
+    // scale = 2^sexp exactly when its mantissa is 1/2; otherwise a df multiplier
+    int e2 = 0;
+    const double mant = std::frexp(scale, &e2);
+    int sexp = 0, use = 0;
+    float2 sdf = make_float2(1.0f, 0.0f);
+    if (mant == 0.5) {
+        sexp = e2 - 1;
+    } else {
+        use = 1;
+        sdf.x = (float)scale;
+        sdf.y = (float)(scale - (double)sdf.x);
+    }
+    if (kind == FK_PROJECT)
+        return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_PROJECT>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
+    if (kind == FK_POISSON3D)
+        return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_POISSON3D>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex,
+                                                                  s);
+    if (kind == FK_DEALIAS)
+        return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_DEALIAS>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
+    if (in_mode == IN_COMPLEX && out_mode == OUT_COMPLEX)
+        return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
+    if (in_mode == IN_REAL && out_mode == OUT_HALF)
+        return launch_df_t<IN_REAL, OUT_HALF, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
+    if (in_mode == IN_HALF && out_mode == OUT_REAL)
+        return launch_df_t<IN_HALF, OUT_REAL, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, oddball, ex, s);
+    return PS_EINVAL;
+}
+
+}  // namespace pade

@@ -493,6 +493,15 @@ int pade_fft_c2r_x(const void* in, double* out, int nx, int ny, int nz, double s
                       static_cast<cudaStream_t>(stream));
 }
 
+// ---------------------------------------------------------------- FFT arithmetic
+int pade_fft_set_arith(int arith) {
+    if (arith != PADE_FFT_DF && arith != PADE_FFT_FP64) return PS_EINVAL;
+    fft_set_arith(arith == PADE_FFT_FP64 ? FFT_ARITH_FP64 : FFT_ARITH_DF);
+    return PS_OK;
+}
+
+int pade_fft_get_arith(void) { return fft_get_arith() == FFT_ARITH_FP64 ? PADE_FFT_FP64 : PADE_FFT_DF; }
+
 // ---------------------------------------------------------------- pencil transposes
 int pade_transpose(int from_pencil, int to_pencil, const void* in, void* out, int n1, int n2, int n3,
                    int elem_bytes, void* stream) {

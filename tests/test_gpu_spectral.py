@@ -41,10 +41,23 @@ def crand(rng, shape):
     return np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
 
 
+# FFT arithmetic: double-float (default; ~48 bits, error ~log2(n) 2^-47) or native FP64
+FFT_TOL = {L.FFT_DF: 2e-13, L.FFT_FP64: 1e-13}
+
+
+@pytest.fixture(params=[L.FFT_DF, L.FFT_FP64], ids=["df", "fp64"])
+def arith(request, native_lib):
+    old = native_lib.pade_fft_get_arith()
+    L.check(native_lib.pade_fft_set_arith(request.param))
+    yield request.param
+    native_lib.pade_fft_set_arith(old)
+
+
 @pytest.mark.parametrize("dir", [1, 2, 3])
 @pytest.mark.parametrize("n", [2, 4, 32, 256, 1024])
 @pytest.mark.parametrize("sign", [-1, 1])
-def test_c2c_matches_numpy(native_lib, dir, n, sign):
+def test_c2c_matches_numpy(native_lib, arith, dir, n, sign):
+    tol = FFT_TOL[arith]
     rng = np.random.default_rng(n + dir)
     shape = [5, 3, 7]
     shape[dir - 1] = n
@@ -54,15 +67,16 @@ def test_c2c_matches_numpy(native_lib, dir, n, sign):
     L.check(native_lib.pade_fft_c2c(dir, sign, vp(x), vp(y), *shape, 0.5, stream()))
     torch.cuda.synchronize()
     ref = 0.5 * (np.fft.fft(a, axis=dir - 1) if sign < 0 else n * np.fft.ifft(a, axis=dir - 1))
-    assert relerr(host(y), ref) < 1e-13
+    assert relerr(host(y), ref) < tol
     # in place
     L.check(native_lib.pade_fft_c2c(dir, sign, vp(x), vp(x), *shape, 0.5, stream()))
     torch.cuda.synchronize()
-    assert relerr(host(x), ref) < 1e-13
+    assert relerr(host(x), ref) < tol
 
 
 @pytest.mark.parametrize("nx", [2, 8, 64, 512])
-def test_r2c_c2r_x(native_lib, nx):
+def test_r2c_c2r_x(native_lib, arith, nx):
+    tol = FFT_TOL[arith]
     rng = np.random.default_rng(nx)
     shape = (nx, 6, 5)
     f = np.asfortranarray(rng.standard_normal(shape))
@@ -71,11 +85,11 @@ def test_r2c_c2r_x(native_lib, nx):
     L.check(native_lib.pade_fft_r2c_x(vp(x), vp(h), *shape, stream()))
     torch.cuda.synchronize()
     ref = np.fft.rfft(f, axis=0)
-    assert relerr(host(h), ref) < 1e-13
+    assert relerr(host(h), ref) < tol
     back = torch.empty_like(x)
     L.check(native_lib.pade_fft_c2r_x(vp(h), vp(back), *shape, 1.0 / nx, stream()))
     torch.cuda.synchronize()
-    assert relerr(host(back), f) < 1e-13
+    assert relerr(host(back), f) < tol
     # c2r ignores the imaginary parts of the mean and Nyquist entries (like FFTW)
     hh = host(h).copy()
     hh[0] += 3j
@@ -83,11 +97,12 @@ def test_r2c_c2r_x(native_lib, nx):
     h2 = dev(hh)
     L.check(native_lib.pade_fft_c2r_x(vp(h2), vp(back), *shape, 1.0 / nx, stream()))
     torch.cuda.synchronize()
-    assert relerr(host(back), f) < 1e-13
+    assert relerr(host(back), f) < tol
 
 
 @pytest.mark.parametrize("fix", [True, False])
-def test_spectral_fft_ifft(native_lib, fix):
+def test_spectral_fft_ifft(native_lib, arith, fix):
+    tol = FFT_TOL[arith]
     nx, ny, nz = 64, 32, 6
     dx, dy = 2 * np.pi / nx, 2 * np.pi / ny
     sp = P.spectral()
@@ -101,14 +116,14 @@ def test_spectral_fft_ifft(native_lib, fix):
     sp.fft(fd, fh)
     torch.cuda.synchronize()
     ref = SO.fft2_x2y(f)
-    assert relerr(host(fh), ref) < 1e-13
+    assert relerr(host(fh), ref) < tol
     keep = fh.clone()
     out = torch.empty_like(fd)
     for odd in (False, True):
         sp.ifft(fh, out, setOddball=odd)
         torch.cuda.synchronize()
         assert torch.equal(fh, keep)  # the input is not modified
-        assert relerr(host(out), SO.ifft2_y2x(ref, nx, odd)) < 1e-13
+        assert relerr(host(out), SO.ifft2_y2x(ref, nx, odd)) < tol
     sp.destroy()
 
 
@@ -131,7 +146,7 @@ def _velocity(nx, ny, nz, seed, clean=False):
 
 
 @pytest.mark.parametrize("nx,ny,nz", [(32, 16, 16), (64, 32, 32), (16, 16, 64)])
-def test_pressure_projection_matches_oracle(native_lib, oracle, nx, ny, nz):
+def test_pressure_projection_matches_oracle(native_lib, oracle, arith, nx, ny, nz):
     dx, dy, dz = 2 * np.pi / nx, 2 * np.pi / ny, 2 * np.pi / nz
     sp = P.spectral()
     sp.init(nx, ny, nz, dx, dy)
@@ -162,7 +177,7 @@ def test_pressure_projection_matches_oracle(native_lib, oracle, nx, ny, nz):
     sp.destroy()
 
 
-def test_divergence_check_and_fixdiv(native_lib, oracle):
+def test_divergence_check_and_fixdiv(native_lib, oracle, arith):
     nx, ny, nz = 32, 32, 16
     dx, dy, dz = 2 * np.pi / nx, 2 * np.pi / ny, 2 * np.pi / nz
     sp = P.spectral()
@@ -192,7 +207,7 @@ def _cd06_modk(kd):
 
 
 @pytest.mark.parametrize("dir_id", [1, 3])
-def test_poisson_periodic_manufactured(native_lib, dir_id):
+def test_poisson_periodic_manufactured(native_lib, arith, dir_id):
     """tests/test_PoissonPeriodic.F90:42-111 (nx, ny, nz = 64, 32, 16; waves 6, 3, 1)."""
     nx, ny, nz = 64, 32, 16
     L_ = 2 * np.pi
@@ -244,3 +259,30 @@ def test_transposes_are_layout_preserving_copies(native_lib):
     D.transpose_y_to_z(c, d)
     torch.cuda.synchronize()
     assert torch.equal(c, d)
+
+
+@pytest.mark.parametrize("amp", [1e-200, 1e-30, 1.0, 1e30, 1e200])
+def test_df_fft_is_scale_invariant(native_lib, amp):
+    """The double-float transform scales each line by a power of two, so its relative
+    accuracy does not depend on the amplitude (FP64 range, not the float range)."""
+    old = native_lib.pade_fft_get_arith()
+    L.check(native_lib.pade_fft_set_arith(L.FFT_DF))
+    try:
+        rng = np.random.default_rng(11)
+        shape = [64, 8, 4]
+        a = crand(rng, shape) * amp
+        a[:, 0, 0] *= 1e-40  # one line far below the others: still accurate relative to itself
+        x = dev(a)
+        y = torch.empty_like(x)
+        for dir in (1, 2, 3):
+            sh = list(shape)
+            L.check(native_lib.pade_fft_c2c(dir, -1, vp(x), vp(y), *sh, 1.0, stream()))
+            torch.cuda.synchronize()
+            ref = np.fft.fft(a, axis=dir - 1)
+            assert relerr(host(y), ref) < 2e-13, dir
+        # the x line scaled by 1e-40 keeps its own relative accuracy
+        L.check(native_lib.pade_fft_c2c(1, -1, vp(x), vp(y), *shape, 1.0, stream()))
+        torch.cuda.synchronize()
+        assert relerr(host(y)[:, 0, 0], np.fft.fft(a[:, 0, 0])) < 2e-13
+    finally:
+        native_lib.pade_fft_set_arith(old)
