@@ -134,6 +134,8 @@ def lib():
         "pade_fft_c2r_x": [vp, vp, i, i, i, d, vp],
         "pade_transpose": [i, i, vp, vp, i, i, i, i, vp],
         "pade_fft_set_arith": [i],
+        "pade_dense_apply": [vp, i, i, vp, vp, i, i, i, i, vp],
+        "pade_dense_status": [pi],
         "pade_fft_get_arith": [],
         "pade_les_init": [pop, ctypes.POINTER(LesParams)],
         "pade_les_destroy": [vp],

@@ -20,6 +20,11 @@ inline int plan_key(int opcode, int bc1, int bcn) { return opcode * 16 + bcid(bc
 
 }  // namespace pade
 
+namespace pade {
+// frees the dense (tensor-core path) matrices cached for a handle (dense_tc.cu)
+void dense_release(const void* h);
+}  // namespace pade
+
 struct pade_op_s {
     int family = 0;
     int n = 0;
@@ -37,6 +42,7 @@ struct pade_op_s {
     void* stage_out = nullptr;
     size_t stage_in_bytes = 0, stage_out_bytes = 0;
     ~pade_op_s() {
+        pade::dense_release(this);
         if (status) cudaFree(status);
         if (stage_in) cudaFree(stage_in);
         if (stage_out) cudaFree(stage_out);

@@ -1,0 +1,85 @@
+"""The tensor-core dense operator path (3xTF32 on tcgen05) against the oracle (GPU).
+
+Tolerance: 3e-6 normwise relative (max|a-b| / max|b|).  The FP32 accumulation of
+256 products bounds the error by ~2^-24 sum|D||f| and the dropped lo*lo term by
+~2^-22 |D||f|; sum|D||f| / max|D f| is O(1-10) for these operators and fields.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import padeops_gb300 as P
+from padeops_gb300 import _lib as L
+from tests.fields import relerr
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def field(n, na, nb, seed):
+    rng = np.random.default_rng(seed)
+    x = np.arange(n) * 2 * np.pi / n
+    f = np.zeros((n, na, nb))
+    for _ in range(8):
+        k = rng.integers(1, n // 4)
+        f += rng.standard_normal() * np.cos(k * x + rng.uniform(0, 6.3))[:, None, None] * \
+            rng.standard_normal((1, na, nb))
+    return np.asfortranarray(f)
+
+
+def dense(obj, opcode, f, bc=(0, 0)):
+    n, na, nb = f.shape
+    fd = torch.from_numpy(np.ascontiguousarray(f.T)).cuda()
+    od = torch.full_like(fd, float("nan"))
+    lib = L.lib()
+    L.check(lib.pade_dense_apply(obj.handle, opcode, 1, ctypes.c_void_p(fd.data_ptr()),
+                                 ctypes.c_void_p(od.data_ptr()), na, nb, bc[0], bc[1],
+                                 ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    to = ctypes.c_int()
+    L.check(lib.pade_dense_status(ctypes.byref(to)))
+    assert to.value == 0
+    return np.asfortranarray(od.cpu().numpy().T)
+
+
+@pytest.mark.parametrize("n,na,nb", [(256, 10, 20), (256, 40, 33), (128, 7, 3), (512, 16, 9)])
+def test_dense_cd10_periodic(oracle, n, na, nb):
+    dx = 2 * np.pi / n
+    o = P.cd10()
+    assert o.init(n, dx, True) == 0
+    f = field(n, na, nb, n + na)
+    for order in (1, 2):
+        out = dense(o, order, f)
+        ref = oracle.cd10(f, dx, periodic=True, order=order, dir=1)
+        assert np.isfinite(out).all()
+        assert relerr(out, ref) < 3e-6, order
+
+
+def test_dense_cf90_and_nonperiodic(oracle):
+    n, na, nb = 256, 12, 11
+    f = field(n, na, nb, 5)
+    c = P.cf90()
+    assert c.init(n, True) == 0
+    assert relerr(dense(c, 0, f), oracle.cf90(f, periodic=True, dir=1)) < 3e-6
+    z = P.cd10()
+    dz = 1.0 / (n - 1)
+    assert z.init(n, dz, False) == 0
+    for bc in ((0, 0), (1, -1)):
+        out = dense(z, 1, f, bc)
+        ref = oracle.cd10(f, dz, periodic=False, bc1=bc[0], bcn=bc[1], order=1, dir=1)
+        assert relerr(out, ref) < 3e-6, bc
+
+
+def test_dense_rejects_unsupported():
+    o = P.cd10()
+    assert o.init(96, 0.1, True) == 0  # n_out 96 is not a TMEM-friendly size
+    f = torch.zeros(96 * 4, dtype=torch.float64, device="cuda")
+    g = torch.empty_like(f)
+    lib = L.lib()
+    rc = lib.pade_dense_apply(o.handle, 1, 1, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(g.data_ptr()), 4, 1,
+                              0, 0, None)
+    assert rc == L.PADE_ENOTSUP
+    rc = lib.pade_dense_apply(o.handle, 1, 2, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(g.data_ptr()), 4, 1,
+                              0, 0, None)
+    assert rc == L.PADE_ENOTSUP
