@@ -15,7 +15,8 @@ data.  Metric: operator throughput in Gpts/s (points x operator applications per
   cpu_baseline  the oracle port of the reference algorithm on the host cores (OpenMP over
             lines), on the same workload
 
-`extras` (same line): the FP32 and native-FP64 paths of the step, the 512^3 periodic
+`extras` (same line): the FP32 and native-FP64 paths of the step, the tensor-core dense
+(3xTF32) path along x with its error against the FP64 path, the 512^3 periodic
 pressure projection, and s/step of the 256^3 LES step with the dynamic procedure and with
 the learned closure.
 
@@ -281,6 +282,40 @@ def extras(args, P, torch, f_host):
         torch.cuda.empty_cache()
     except Exception as ex:  # pragma: no cover - reported in the JSON line
         out["paths_error"] = repr(ex)
+    try:
+        import ctypes
+
+        from padeops_gb300 import _lib as L
+
+        lib = L.lib()
+        base = torch.from_numpy(np.ascontiguousarray(f_host.T)).to(dev)
+        ref = torch.empty_like(base)
+        got = torch.empty_like(base)
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        xops = [(obj, opc, name) for (obj, opc, d, name) in plan if d == 1]
+        errs = {}
+        for obj, opc, name in xops:
+            obj.apply(opc, 1, base, ref, N, N, 0, 0)
+            L.check(lib.pade_dense_apply(obj.handle, opc, 1, ctypes.c_void_p(base.data_ptr()),
+                                         ctypes.c_void_p(got.data_ptr()), N, N, 0, 0, st))
+            torch.cuda.synchronize()
+            errs[name] = float((got - ref).abs().max() / ref.abs().max())
+
+        def dstep():
+            for obj, opc, _ in xops:
+                lib.pade_dense_apply(obj.handle, opc, 1, ctypes.c_void_p(base.data_ptr()),
+                                     ctypes.c_void_p(got.data_ptr()), N, N, 0, 0, st)
+
+        ms = _time(torch, dstep, reps)
+        out["dense_tf32_x"] = {"value": len(xops) * npts / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+                               "ms_per_op": ms / len(xops),
+                               "achieved_GBps": len(xops) * npts * 16 / (ms * 1e-3) / 1e9,
+                               "relerr_vs_fp64_path": errs,
+                               "note": "tcgen05 kind::tf32, 3 products (hi/lo splits), x lines; reduced precision"}
+        del base, ref, got
+        torch.cuda.empty_cache()
+    except Exception as ex:  # pragma: no cover
+        out["dense_error"] = repr(ex)
     try:
         n = 512
         d = 2 * np.pi / n

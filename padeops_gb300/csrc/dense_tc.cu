@@ -10,12 +10,13 @@
 // (~2^-22).  This is the reduced-precision variant of the operator (~1e-6), next to the
 // double-float banded path (1e-12).
 //
-// Per CTA (128 threads): 128 lines; TMEM holds n_out/128 accumulators of 128 x 128 FP32.
-// For each K chunk of 32: all threads stage D's rows (hi, lo) and the 128 lines' FP64
-// values converted to TF32 pairs (integer split, no FP64 instruction) in shared memory in
-// the 128-byte-swizzled K-major layout; one thread issues the tcgen05.mma instructions
-// (3 per K=8 step per 128-row half) and commits them to an mbarrier; every wait on it is
-// bounded (a timeout sets the error word, frees TMEM and returns).  The epilogue reads the
+// Per CTA (512 threads): 128 lines; TMEM holds n_out/128 accumulators of 128 x 128 FP32.
+// For each K chunk of 32: D's rows (hi, lo) arrive by cp.async and the 128 lines' FP64
+// values, converted to TF32 pairs (integer split, no FP64 instruction), are stored by the
+// threads, both in the 128-byte-swizzled K-major layout of shared memory; one thread
+// issues the tcgen05.mma instructions (3 per K=8 step per 128-row half) and commits them
+// to the stage's mbarrier; with two stages the next chunk loads while the tensor cores
+// work.  Every wait is bounded (a timeout sets the error word, frees TMEM and returns).  The epilogue reads the
 // accumulators with tcgen05.ld (a warp per 32 rows) and stores FP64, coalesced along x.
 #include <cuda_runtime.h>
 
@@ -128,24 +129,47 @@ __device__ __forceinline__ void split_tf32(double v, float& h, float& l, unsigne
 // byte offset of 16-byte chunk `ch` of row `r` in a 128-byte-swizzled K-major tile
 __device__ __forceinline__ uint32_t swz(int r, int ch) { return (uint32_t)(r * 128 + ((ch ^ (r & 7)) << 4)); }
 
-__global__ void __launch_bounds__(128) k_dense_x_tf32(const double* __restrict__ f, double* __restrict__ out,
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// bounded wait for an mbarrier phase; false (and the error word set) on timeout
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned phase) {
+    unsigned it = 0;
+    while (!mbar_try_wait(bar, phase)) {
+        if (++it > kWaitLimit) {
+            atomicOr(&g_dense_err, 1u);
+            return false;
+        }
+    }
+    return true;
+}
+
+constexpr int NTHR = 512;            // threads per CTA: 16 warps share the staging work
+constexpr int FPT = NT * 16 / NTHR;  // double2 of the line tile per thread and chunk
+
+// STAGES = 2: the loads of chunk c+1 (D by cp.async, the lines through registers) overlap
+// the tensor-core work of chunk c; STAGES = 1 when two stages do not fit in shared memory.
+template <int STAGES>
+__global__ void __launch_bounds__(NTHR) k_dense_x_tf32(const double* __restrict__ f, double* __restrict__ out,
                                                       const float* __restrict__ Dh, const float* __restrict__ Dl,
                                                       int nin, int nout, long nlines, unsigned* __restrict__ rangeflag) {
     extern __shared__ uint8_t dsm_raw[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[2];
     __shared__ uint32_t tslot;
     __shared__ int abort_flag;
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsm_raw) + 1023) & ~(uintptr_t)1023);
-    uint8_t* Ah = base;
-    uint8_t* Al = Ah + (size_t)nout * 128;
-    uint8_t* Bh = Al + (size_t)nout * 128;
-    uint8_t* Bl = Bh + (size_t)NT * 128;
+    const size_t a_bytes = (size_t)nout * 128, b_bytes = (size_t)NT * 128;
+    const size_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t ncols = (uint32_t)nout;  // nout/128 accumulators of NT = 128 columns
     const long l0 = (long)blockIdx.x * NT;
     if (warp == 0) tmem_alloc(&tslot, ncols);
     if (tid == 0) {
-        mbar_init(&mbar, 1);
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
         fence_barrier_init();
         abort_flag = 0;
     }
@@ -154,33 +178,64 @@ __global__ void __launch_bounds__(128) k_dense_x_tf32(const double* __restrict__
     tc_fence_after();
     const uint32_t tmem = tslot;
     unsigned bad = 0;
-    unsigned phase = 0;
+    unsigned ph[2] = {0u, 0u};
     const int nchunks = nin / KC;
-    for (int c = 0; c < nchunks; c++) {
-        // D rows, hi and lo: nout rows x 8 chunks of 16 B each
-        for (int idx = tid; idx < nout * 8 * 2; idx += blockDim.x) {
+
+    auto stage_ptr = [&](int s) { return base + (size_t)s * stage_bytes; };
+    // D rows of chunk c (hi then lo) into stage s, 16-byte asynchronous copies
+    auto issue_D = [&](int c, int s) {
+        uint8_t* Ah = stage_ptr(s);
+        uint8_t* Al = Ah + a_bytes;
+        for (int idx = tid; idx < nout * 16; idx += blockDim.x) {
             const int which = idx / (nout * 8), rem = idx % (nout * 8);
             const int r = rem >> 3, ch = rem & 7;
-            const float4 v = *reinterpret_cast<const float4*>((which ? Dl : Dh) + (size_t)r * nin + c * KC + ch * 4);
-            *reinterpret_cast<float4*>((which ? Al : Ah) + swz(r, ch)) = v;
+            const float* src = (which ? Dl : Dh) + (size_t)r * nin + c * KC + ch * 4;
+            cp_async16(su32((which ? Al : Ah) + swz(r, ch)), src);
         }
-        // 128 lines x 16 double2 of this chunk
-        for (int idx = tid; idx < NT * 16; idx += blockDim.x) {
+        cp_async_commit();
+    };
+    auto load_F = [&](int c, double2* R) {
+#pragma unroll
+        for (int i = 0; i < FPT; i++) {
+            const int idx = tid + i * NTHR;
             const int ln = idx >> 4, q = idx & 15;
             const long line = l0 + ln;
-            double2 v = make_double2(0.0, 0.0);
-            if (line < nlines) v = *reinterpret_cast<const double2*>(f + line * nin + c * KC + 2 * q);
-            float h0, l0f, h1, l1f;
-            split_tf32(v.x, h0, l0f, bad);
-            split_tf32(v.y, h1, l1f, bad);
+            R[i] = line < nlines ? __ldg(reinterpret_cast<const double2*>(f + line * nin + c * KC + 2 * q))
+                                 : make_double2(0.0, 0.0);
+        }
+    };
+    auto store_F = [&](int s, const double2* R) {
+        uint8_t* Bh = stage_ptr(s) + 2 * a_bytes;
+        uint8_t* Bl = Bh + b_bytes;
+#pragma unroll
+        for (int i = 0; i < FPT; i++) {
+            const int idx = tid + i * NTHR;
+            const int ln = idx >> 4, q = idx & 15;
+            float h0, lo0, h1, lo1;
+            split_tf32(R[i].x, h0, lo0, bad);
+            split_tf32(R[i].y, h1, lo1, bad);
             const uint32_t off = swz(ln, q >> 1) + ((q & 1) << 3);
             *reinterpret_cast<float2*>(Bh + off) = make_float2(h0, h1);
-            *reinterpret_cast<float2*>(Bl + off) = make_float2(l0f, l1f);
+            *reinterpret_cast<float2*>(Bl + off) = make_float2(lo0, lo1);
         }
+    };
+
+    double2 R[FPT];
+    issue_D(0, 0);
+    load_F(0, R);
+    store_F(0, R);
+    for (int c = 0; c < nchunks; c++) {
+        const int s = STAGES == 2 ? (c & 1) : 0;
+        cp_async_wait_all();
         fence_async_smem();
         __syncthreads();
+        if (abort_flag) break;
         if (tid == 0) {
             tc_fence_after();
+            uint8_t* Ah = stage_ptr(s);
+            uint8_t* Al = Ah + a_bytes;
+            uint8_t* Bh = Al + a_bytes;
+            uint8_t* Bl = Bh + b_bytes;
             for (int mh = 0; mh < nout / 128; mh++) {
                 const uint32_t d = tmem + (uint32_t)(mh * NT);
                 for (int kk = 0; kk < KC / 8; kk++) {
@@ -193,29 +248,44 @@ __global__ void __launch_bounds__(128) k_dense_x_tf32(const double* __restrict__
                     mma_tf32(d, al, bh, kIdesc, 1u);
                 }
             }
-            mma_commit(&mbar);
+            mma_commit(&mbar[s]);
         }
-        // the MMAs of this chunk finish before its shared memory is rewritten
-        unsigned it = 0;
-        while (!mbar_try_wait(&mbar, phase)) {
-            if (++it > kWaitLimit) {
-                atomicOr(&g_dense_err, 1u);
-                abort_flag = 1;
-                break;
+        if (c + 1 < nchunks) {
+            const int s2 = STAGES == 2 ? (s ^ 1) : 0;
+            load_F(c + 1, R);  // global loads in flight while the tensor cores work
+            // stage s2 was last read by chunk c-1 (two stages) or chunk c (one stage)
+            if (STAGES == 1 || c >= 1) {
+                if (!mbar_wait_bounded(&mbar[s2], ph[s2])) abort_flag = 1;
+                ph[s2] ^= 1u;
+            }
+            if (!abort_flag) {
+                issue_D(c + 1, s2);
+                store_F(s2, R);
             }
         }
-        phase ^= 1u;
-        __syncthreads();
-        if (abort_flag) break;
     }
+    // the last one or two commits
+    if (!abort_flag) {
+        if (STAGES == 2 && nchunks >= 2) {
+            const int sp = (nchunks - 2) & 1;
+            if (!mbar_wait_bounded(&mbar[sp], ph[sp])) abort_flag = 1;
+            ph[sp] ^= 1u;
+        }
+        const int sl = STAGES == 2 ? ((nchunks - 1) & 1) : 0;
+        if (!abort_flag && !mbar_wait_bounded(&mbar[sl], ph[sl])) abort_flag = 1;
+    }
+    __syncthreads();
     if (bad) atomicOr(rangeflag, 1u);
     tc_fence_after();
     if (!abort_flag) {
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (the lanes it may access) and the
+        // column blocks cb = w / 4, w / 4 + 4, ...
+        const int lq = warp & 3;
         for (int mh = 0; mh < nout / 128; mh++) {
-            const int row = mh * 128 + warp * 32 + lane;  // output point along x
-            for (int cb = 0; cb < NT / 16; cb++) {
+            const int row = mh * 128 + lq * 32 + lane;  // output point along x
+            for (int cb = warp >> 2; cb < NT / 16; cb += NTHR / 128) {
                 uint32_t r[16];
-                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mh * NT + cb * 16), r);
+                tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(mh * NT + cb * 16), r);
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     const long line = l0 + cb * 16 + j;
@@ -320,12 +390,15 @@ int pade_dense_apply(pade_op h, int opcode, int dir, const double* f, double* ou
         return PS_ENOTSUP;
     if ((reinterpret_cast<uintptr_t>(f) & 15) || (reinterpret_cast<uintptr_t>(out) & 7)) return PS_EINVAL;
     const long nlines = (long)na * nb;
-    const size_t smem = 1024 + (size_t)D->nout * 128 * 2 + (size_t)NT * 128 * 2;
-    if (cudaFuncSetAttribute(k_dense_x_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return PS_ECUDA;
+    const size_t stage = (size_t)D->nout * 128 * 2 + (size_t)NT * 128 * 2;
+    const int stages = 1024 + 2 * stage <= 220 * 1024 ? 2 : 1;
+    const size_t smem = 1024 + stages * stage;
     const long blocks = (nlines + NT - 1) / NT;
-    k_dense_x_tf32<<<(unsigned)blocks, 128, smem, static_cast<cudaStream_t>(stream)>>>(
-        f, out, D->Dh, D->Dl, D->nin, D->nout, nlines, h->status);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    auto kern = stages == 2 ? k_dense_x_tf32<2> : k_dense_x_tf32<1>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return PS_ECUDA;
+    kern<<<(unsigned)blocks, NTHR, smem, s>>>(f, out, D->Dh, D->Dl, D->nin, D->nout, nlines, h->status);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
