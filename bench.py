@@ -337,7 +337,7 @@ def extras(args, P, torch, f_host):
         out["projection_512"] = {"PressureProjection_ms": ms_p, "DivergenceCheck_ms": ms_d,
                                  "spectral_fft_ms": ms_f, "spectral_ifft_ms": ms_i,
                                  "projection_compulsory_GBps": 6 * cbytes / (ms_p * 1e-3) / 1e9,
-                                 "note": "FP64 radix-2 FFTs; FP64-pipe bound (4 n log2 n FP64 ops per line)"}
+                                 "note": "double-float radix-2 FFTs on the FP32 pipes (default arithmetic)"}
         del U, V, W, div, phys, sp, po
         torch.cuda.empty_cache()
     except Exception as ex:  # pragma: no cover

@@ -1,6 +1,7 @@
 // C ABI of the compact-operator library (see include/padeops_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -121,6 +122,90 @@ int grow(void** buf, size_t* cur, size_t need) {
     return PS_OK;
 }
 
+constexpr int kPipeChunks = 8;
+constexpr size_t kPipeMinBytes = 8u << 20;
+
+int ensure_pipe(pade_op h) {
+    if (h->pipe_ok) return PS_OK;
+    for (int i = 0; i < 3; i++)
+        if (cudaStreamCreateWithFlags(&h->pipe[i], cudaStreamNonBlocking) != cudaSuccess) return PS_ECUDA;
+    for (int k = 0; k < 2; k++)
+        for (int c = 0; c < 16; c++)
+            if (cudaEventCreateWithFlags(&h->pev[k][c], cudaEventDisableTiming) != cudaSuccess) return PS_ECUDA;
+    if (cudaEventCreateWithFlags(&h->pstart, cudaEventDisableTiming) != cudaSuccess) return PS_ECUDA;
+    h->pipe_ok = true;
+    return PS_OK;
+}
+
+// Host input and host output: the lines are split into chunks whose host->device copy,
+// operator launch and device->host copy run on three streams, so the copies of one chunk
+// overlap the computation of its neighbours.  Chunks follow the memory layout of the
+// LineSet: whole b-rows (contiguous slabs) when lines are grouped (fb != 0), runs of
+// contiguous lines for x lines, and pitched 2-D copies when lines are strided (z lines).
+int apply_host_pipelined(pade_op h, const DevicePlan& P, int path, const void* f, void* out, const LineSet& ls,
+                         size_t esz, int m, int nout, cudaStream_t s) {
+    int rc = ensure_pipe(h);
+    if (rc != PS_OK) return rc;
+    const long nl = ls.nlines;
+    const int mode = ls.fb != 0 ? 0 : (ls.fp == 1 ? 1 : 2);
+    const long units = mode == 0 ? nl / ls.na : nl;  // b-rows or lines
+    const long per = (units + kPipeChunks - 1) / kPipeChunks;
+    const unsigned char* fh = static_cast<const unsigned char*>(f);
+    unsigned char* oh = static_cast<unsigned char*>(out);
+    unsigned char* fd = static_cast<unsigned char*>(h->stage_in);
+    unsigned char* od = static_cast<unsigned char*>(h->stage_out);
+    if (cudaEventRecord(h->pstart, s) != cudaSuccess) return PS_ECUDA;
+    for (int i = 0; i < 3; i++)
+        if (cudaStreamWaitEvent(h->pipe[i], h->pstart, 0) != cudaSuccess) return PS_ECUDA;
+    int c = 0;
+    for (long u0 = 0; u0 < units; u0 += per, c++) {
+        const long u1 = std::min(units, u0 + per);
+        LineSet cs = ls;
+        size_t ioff = 0, ooff = 0;  // element offsets of the chunk
+        if (mode == 0) {
+            cs.nlines = ls.na * (u1 - u0);
+            ioff = (size_t)(u0 * ls.fb);
+            ooff = (size_t)(u0 * ls.ob);
+        } else {
+            cs.nlines = u1 - u0;
+            cs.na = cs.nlines;
+            ioff = (size_t)(u0 * ls.fa);
+            ooff = (size_t)(u0 * ls.oa);
+        }
+        // host -> device
+        if (mode == 2) {
+            if (cudaMemcpy2DAsync(fd + ioff * esz, ls.fp * esz, fh + ioff * esz, ls.fp * esz, (u1 - u0) * esz, m,
+                                  cudaMemcpyHostToDevice, h->pipe[0]) != cudaSuccess)
+                return PS_ECUDA;
+        } else {
+            const size_t bytes = (size_t)((mode == 0 ? (u1 - u0) * ls.fb : (u1 - u0) * ls.fa)) * esz;
+            if (cudaMemcpyAsync(fd + ioff * esz, fh + ioff * esz, bytes, cudaMemcpyHostToDevice, h->pipe[0]) !=
+                cudaSuccess)
+                return PS_ECUDA;
+        }
+        if (cudaEventRecord(h->pev[0][c], h->pipe[0]) != cudaSuccess) return PS_ECUDA;
+        if (cudaStreamWaitEvent(h->pipe[1], h->pev[0][c], 0) != cudaSuccess) return PS_ECUDA;
+        if ((rc = launch_lines(P, path, fd + ioff * esz, od + ooff * esz, cs, h->status, h->pipe[1])) != PS_OK)
+            return rc;
+        if (cudaEventRecord(h->pev[1][c], h->pipe[1]) != cudaSuccess) return PS_ECUDA;
+        if (cudaStreamWaitEvent(h->pipe[2], h->pev[1][c], 0) != cudaSuccess) return PS_ECUDA;
+        // device -> host
+        if (mode == 2) {
+            if (cudaMemcpy2DAsync(oh + ooff * esz, ls.op * esz, od + ooff * esz, ls.op * esz, (u1 - u0) * esz,
+                                  nout, cudaMemcpyDeviceToHost, h->pipe[2]) != cudaSuccess)
+                return PS_ECUDA;
+        } else {
+            const size_t bytes = (size_t)((mode == 0 ? (u1 - u0) * ls.ob : (u1 - u0) * ls.oa)) * esz;
+            if (cudaMemcpyAsync(oh + ooff * esz, od + ooff * esz, bytes, cudaMemcpyDeviceToHost, h->pipe[2]) !=
+                cudaSuccess)
+                return PS_ECUDA;
+        }
+    }
+    if (cudaStreamSynchronize(h->pipe[2]) != cudaSuccess) return PS_ECUDA;
+    if (cudaStreamSynchronize(h->pipe[1]) != cudaSuccess) return PS_ECUDA;
+    return PS_OK;
+}
+
 int apply(pade_op h, int opcode, int dir, int cplx, const void* f, void* out, int na, int nb, int bc1, int bcn,
           int path, void* stream) {
     if (!h || !f || !out) return PS_EINVAL;
@@ -150,6 +235,18 @@ int apply(pade_op h, int opcode, int dir, int cplx, const void* f, void* out, in
     const void* fd = f;
     void* od = out;
     int rc;
+    if (!din && !dout && in_bytes >= kPipeMinBytes) {
+        if ((rc = grow(&h->stage_in, &h->stage_in_bytes, in_bytes)) != PS_OK) return rc;
+        if ((rc = grow(&h->stage_out, &h->stage_out_bytes, out_bytes)) != PS_OK) return rc;
+        if ((rc = apply_host_pipelined(h, P, path, f, out, ls, esz, d.m, d.nout, s)) != PS_OK) return rc;
+        unsigned flag = 0;
+        if (cudaMemcpy(&flag, h->status, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return PS_ECUDA;
+        if (flag) {
+            cudaMemset(h->status, 0, sizeof(unsigned));
+            return PS_ERANGE;
+        }
+        return PS_OK;
+    }
     if (!din) {
         if ((rc = grow(&h->stage_in, &h->stage_in_bytes, in_bytes)) != PS_OK) return rc;
         if (cudaMemcpyAsync(h->stage_in, f, in_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PS_ECUDA;

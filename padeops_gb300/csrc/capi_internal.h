@@ -41,8 +41,19 @@ struct pade_op_s {
     void* stage_in = nullptr;
     void* stage_out = nullptr;
     size_t stage_in_bytes = 0, stage_out_bytes = 0;
+    // host-pointer pipeline: copy-in, compute and copy-out streams and per-chunk events
+    cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t pev[2][16] = {};
+    cudaEvent_t pstart = nullptr;
+    bool pipe_ok = false;
     ~pade_op_s() {
         pade::dense_release(this);
+        if (pipe_ok) {
+            for (int i = 0; i < 3; i++) cudaStreamDestroy(pipe[i]);
+            for (int k = 0; k < 2; k++)
+                for (int c = 0; c < 16; c++) cudaEventDestroy(pev[k][c]);
+            cudaEventDestroy(pstart);
+        }
         if (status) cudaFree(status);
         if (stage_in) cudaFree(stage_in);
         if (stage_out) cudaFree(stage_out);
