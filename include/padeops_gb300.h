@@ -155,9 +155,10 @@ const char* pade_strerror(int status);
 /* ==== dense operator on the tensor cores (reduced precision; no counterpart in the reference) ====
  * out = D f along x with D = A^-1 B of the object's operation (opcode, bc1, bcn) as a
  * dense matrix, on tcgen05 in "3xTF32" (D and f split into TF32 hi + lo, three products,
- * FP32 accumulation): relative error ~1e-6 of sum|D||f|, at the HBM rate.  Device
- * pointers, lines along x only (dir 1), n_out in {128, 256, 512}, n_in a multiple of 32;
- * otherwise PADE_ENOTSUP.  f must be 16-byte aligned. */
+ * FP32 accumulation): relative error ~1e-6 of sum|D||f|.  Device pointers; lines along
+ * dir 1, 2 or 3 of an (n, na, nb) / (na, n, nb) / (na, nb, n) array; n_out in
+ * {128, 256, 512} and n_in a multiple of 32, otherwise PADE_ENOTSUP.  f must be 16-byte
+ * aligned. */
 int pade_dense_apply(pade_op op, int opcode, int dir, const double* f, double* out, int na, int nb, int bc1, int bcn,
                      void* stream);
 /* *timed_out = 1 if a tensor-core wait gave up since the last call (then cleared) */

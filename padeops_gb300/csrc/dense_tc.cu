@@ -1,9 +1,11 @@
 // Dense operator path on the 5th-generation tensor cores (tcgen05, TF32 kind).
 //
-// A compact operator is a dense matrix D = A^-1 B (n_out x n_in).  Along x the lines are
-// contiguous, so applying it to a field is one GEMM per tile of lines:
+// A compact operator is a dense matrix D = A^-1 B (n_out x n_in).  Applying it to the lines
+// of a field is one GEMM per tile of 128 lines:
 //     out[line][m] = sum_k D[m][k] f[line][k]       (M = n_out, N = lines, K = n_in)
-// with D as the K-major A operand and the field as the K-major B operand.  "3xTF32":
+// with D as the K-major A operand and the lines as the K-major B operand, whichever the
+// direction: the staging writes the lines K-major into shared memory (x lines are read
+// along K, y and z lines across lines), so one tensor-core schedule serves all three.  "3xTF32":
 // D = Dh + Dl and f = fh + fl with every part exact in TF32 (11 significant bits), and
 // D f ~ Dh fh + Dh fl + Dl fh accumulates in one FP32 accumulator in tensor memory; the
 // error is set by the FP32 accumulation (~2^-24 of sum |D||f|) and the dropped Dl fl term
@@ -152,10 +154,17 @@ constexpr int FPT = NT * 16 / NTHR;  // double2 of the line tile per thread and 
 
 // STAGES = 2: the loads of chunk c+1 (D by cp.async, the lines through registers) overlap
 // the tensor-core work of chunk c; STAGES = 1 when two stages do not fit in shared memory.
-template <int STAGES>
-__global__ void __launch_bounds__(NTHR) k_dense_x_tf32(const double* __restrict__ f, double* __restrict__ out,
-                                                      const float* __restrict__ Dh, const float* __restrict__ Dl,
-                                                      int nin, int nout, long nlines, unsigned* __restrict__ rangeflag) {
+// XL: lines contiguous (x lines, fp == 1): a thread loads double2 along K of one line and
+// the epilogue stores rows of consecutive points.  Otherwise (y, z lines) consecutive
+// threads take consecutive lines for each K index and the epilogue stores each thread's
+// 16 lines at the lines' own addresses.  Line l = a + na*b sits at a*fa + b*fb (input)
+// and a*oa + b*ob (output), point p at p*fp / p*op.
+template <int STAGES, bool XL>
+__global__ void __launch_bounds__(NTHR) k_dense_tf32(const double* __restrict__ f, double* __restrict__ out,
+                                                    const float* __restrict__ Dh, const float* __restrict__ Dl,
+                                                    int nin, int nout, const LineSet ls,
+                                                    unsigned* __restrict__ rangeflag) {
+    const long nlines = ls.nlines;
     extern __shared__ uint8_t dsm_raw[];
     __shared__ uint64_t mbar[2];
     __shared__ uint32_t tslot;
@@ -198,10 +207,23 @@ __global__ void __launch_bounds__(NTHR) k_dense_x_tf32(const double* __restrict_
 #pragma unroll
         for (int i = 0; i < FPT; i++) {
             const int idx = tid + i * NTHR;
-            const int ln = idx >> 4, q = idx & 15;
-            const long line = l0 + ln;
-            R[i] = line < nlines ? __ldg(reinterpret_cast<const double2*>(f + line * nin + c * KC + 2 * q))
-                                 : make_double2(0.0, 0.0);
+            if (XL) {
+                const int ln = idx >> 4, q = idx & 15;
+                const long line = l0 + ln;
+                R[i] = line < nlines ? __ldg(reinterpret_cast<const double2*>(f + line * ls.fa + c * KC + 2 * q))
+                                     : make_double2(0.0, 0.0);
+            } else {
+                // two K indices per entry: k = 2*(idx / NT) + {0, 1}, line ln = idx % NT
+                const int ln = idx % NT, k = 2 * (idx / NT);
+                const long line = l0 + ln;
+                if (line < nlines) {
+                    const long a = line % ls.na, b = line / ls.na;
+                    const double* src = f + a * ls.fa + b * ls.fb + (long)(c * KC + k) * ls.fp;
+                    R[i] = make_double2(__ldg(src), __ldg(src + ls.fp));
+                } else {
+                    R[i] = make_double2(0.0, 0.0);
+                }
+            }
         }
     };
     auto store_F = [&](int s, const double2* R) {
@@ -210,13 +232,20 @@ __global__ void __launch_bounds__(NTHR) k_dense_x_tf32(const double* __restrict_
 #pragma unroll
         for (int i = 0; i < FPT; i++) {
             const int idx = tid + i * NTHR;
-            const int ln = idx >> 4, q = idx & 15;
             float h0, lo0, h1, lo1;
             split_tf32(R[i].x, h0, lo0, bad);
             split_tf32(R[i].y, h1, lo1, bad);
-            const uint32_t off = swz(ln, q >> 1) + ((q & 1) << 3);
-            *reinterpret_cast<float2*>(Bh + off) = make_float2(h0, h1);
-            *reinterpret_cast<float2*>(Bl + off) = make_float2(lo0, lo1);
+            if (XL) {
+                const int ln = idx >> 4, q = idx & 15;
+                const uint32_t off = swz(ln, q >> 1) + ((q & 1) << 3);
+                *reinterpret_cast<float2*>(Bh + off) = make_float2(h0, h1);
+                *reinterpret_cast<float2*>(Bl + off) = make_float2(lo0, lo1);
+            } else {
+                const int ln = idx % NT, k = 2 * (idx / NT);  // k even: both values in one 16-byte chunk
+                const uint32_t off = swz(ln, k >> 2) + ((k & 3) << 2);
+                *reinterpret_cast<float2*>(Bh + off) = make_float2(h0, h1);
+                *reinterpret_cast<float2*>(Bl + off) = make_float2(lo0, lo1);
+            }
         }
     };
 
@@ -289,7 +318,14 @@ __global__ void __launch_bounds__(NTHR) k_dense_x_tf32(const double* __restrict_
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     const long line = l0 + cb * 16 + j;
-                    if (line < nlines) out[line * nout + row] = float_bits_to_double(__uint_as_float(r[j]));
+                    if (line >= nlines) continue;
+                    const double v = float_bits_to_double(__uint_as_float(r[j]));
+                    if (XL) {
+                        out[line * ls.oa + row] = v;
+                    } else {
+                        const long a = line % ls.na, b = line / ls.na;
+                        out[a * ls.oa + b * ls.ob + (long)row * ls.op] = v;
+                    }
                 }
             }
         }
@@ -374,7 +410,7 @@ extern "C" {
 int pade_dense_apply(pade_op h, int opcode, int dir, const double* f, double* out, int na, int nb, int bc1, int bcn,
                      void* stream) {
     if (!h || na < 1 || nb < 1) return PS_EINVAL;
-    if (dir != 1) return PS_ENOTSUP;
+    if (dir < 1 || dir > 3) return PS_EINVAL;
     if (!device_ptr(f) || !device_ptr(out)) return PS_EINVAL;
     if (h->family == F_CD10 || h->family == F_CF90 || h->family == F_GAUSS) {
         if (!bc_valid(bc1) || !bc_valid(bcn)) return PS_EREF_BC;
@@ -389,16 +425,28 @@ int pade_dense_apply(pade_op h, int opcode, int dir, const double* f, double* ou
     if (D->nin % KC != 0 || (D->nout != 128 && D->nout != 256 && D->nout != 512) || D->nin > 4096)
         return PS_ENOTSUP;
     if ((reinterpret_cast<uintptr_t>(f) & 15) || (reinterpret_cast<uintptr_t>(out) & 7)) return PS_EINVAL;
+    // lines of a (m, na, nb) / (na, m, nb) / (na, nb, m) array, m = nin on input, nout on output
+    LineSet ls{};
     const long nlines = (long)na * nb;
+    ls.nlines = nlines;
+    if (dir == 1) {
+        ls.na = nlines; ls.fa = D->nin; ls.fb = 0; ls.fp = 1; ls.oa = D->nout; ls.ob = 0; ls.op = 1;
+    } else if (dir == 2) {
+        ls.na = na; ls.fa = 1; ls.fb = (long)na * D->nin; ls.fp = na;
+        ls.oa = 1; ls.ob = (long)na * D->nout; ls.op = na;
+    } else {
+        ls.na = nlines; ls.fa = 1; ls.fb = 0; ls.fp = nlines; ls.oa = 1; ls.ob = 0; ls.op = nlines;
+    }
     const size_t stage = (size_t)D->nout * 128 * 2 + (size_t)NT * 128 * 2;
     const int stages = 1024 + 2 * stage <= 220 * 1024 ? 2 : 1;
     const size_t smem = 1024 + stages * stage;
     const long blocks = (nlines + NT - 1) / NT;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    auto kern = stages == 2 ? k_dense_x_tf32<2> : k_dense_x_tf32<1>;
+    auto kern = dir == 1 ? (stages == 2 ? k_dense_tf32<2, true> : k_dense_tf32<1, true>)
+                         : (stages == 2 ? k_dense_tf32<2, false> : k_dense_tf32<1, false>);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return PS_ECUDA;
-    kern<<<(unsigned)blocks, NTHR, smem, s>>>(f, out, D->Dh, D->Dl, D->nin, D->nout, nlines, h->status);
+    kern<<<(unsigned)blocks, NTHR, smem, s>>>(f, out, D->Dh, D->Dl, D->nin, D->nout, ls, h->status);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 

@@ -1,4 +1,5 @@
-"""The tensor-core dense operator path (3xTF32 on tcgen05) against the oracle (GPU).
+"""The tensor-core dense operator path (3xTF32 on tcgen05) against the oracle (GPU),
+along x (contiguous lines) and y, z (strided lines).
 
 Tolerance: 3e-6 normwise relative (max|a-b| / max|b|).  The FP32 accumulation of
 256 products bounds the error by ~2^-24 sum|D||f| and the dropped lo*lo term by
@@ -28,12 +29,12 @@ def field(n, na, nb, seed):
     return np.asfortranarray(f)
 
 
-def dense(obj, opcode, f, bc=(0, 0)):
-    n, na, nb = f.shape
+def dense(obj, opcode, f, bc=(0, 0), dir=1):
+    na, nb = [s for k, s in enumerate(f.shape) if k != dir - 1]
     fd = torch.from_numpy(np.ascontiguousarray(f.T)).cuda()
     od = torch.full_like(fd, float("nan"))
     lib = L.lib()
-    L.check(lib.pade_dense_apply(obj.handle, opcode, 1, ctypes.c_void_p(fd.data_ptr()),
+    L.check(lib.pade_dense_apply(obj.handle, opcode, dir, ctypes.c_void_p(fd.data_ptr()),
                                  ctypes.c_void_p(od.data_ptr()), na, nb, bc[0], bc[1],
                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     torch.cuda.synchronize()
@@ -71,6 +72,25 @@ def test_dense_cf90_and_nonperiodic(oracle):
         assert relerr(out, ref) < 3e-6, bc
 
 
+@pytest.mark.parametrize("dir", [2, 3])
+@pytest.mark.parametrize("other", [(40, 9), (128, 3), (7, 130)])
+def test_dense_strided_directions(oracle, dir, other):
+    n = 256
+    dx = 2 * np.pi / n
+    o = P.cd10()
+    assert o.init(n, dx, True) == 0
+    shape = list(other)
+    shape.insert(dir - 1, n)
+    fx = field(n, other[0], other[1], 7)  # (n, a, b) -> move the operated axis into place
+    f = np.asfortranarray(np.moveaxis(fx, 0, dir - 1))
+    assert f.shape == tuple(shape)
+    for order in (1, 2):
+        out = dense(o, order, f, dir=dir)
+        ref = oracle.cd10(f, dx, periodic=True, order=order, dir=dir)
+        assert np.isfinite(out).all()
+        assert relerr(out, ref) < 3e-6, (dir, order)
+
+
 def test_dense_rejects_unsupported():
     o = P.cd10()
     assert o.init(96, 0.1, True) == 0  # n_out 96 is not a TMEM-friendly size
@@ -80,6 +100,6 @@ def test_dense_rejects_unsupported():
     rc = lib.pade_dense_apply(o.handle, 1, 1, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(g.data_ptr()), 4, 1,
                               0, 0, None)
     assert rc == L.PADE_ENOTSUP
-    rc = lib.pade_dense_apply(o.handle, 1, 2, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(g.data_ptr()), 4, 1,
+    rc = lib.pade_dense_apply(o.handle, 1, 4, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(g.data_ptr()), 4, 1,
                               0, 0, None)
-    assert rc == L.PADE_ENOTSUP
+    assert rc == L.PADE_EINVAL
