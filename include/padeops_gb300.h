@@ -37,7 +37,7 @@ extern "C" {
 #define PADE_ECUDA 1003
 #define PADE_ENOTSUP 1004
 #define PADE_ETIMEOUT 1005
-#define PADE_ERANGE 1006 /* an input left the double-float path's range (|f| in [2^-74, 2^127)) */
+#define PADE_ERANGE 1006 /* a line given to the double-float path holds an infinity or NaN */
 #define PADE_ESCRATCH 1007 /* pade_apply_noalloc: a host buffer exceeds its static staging capacity */
 
 /* ---- arithmetic paths (pade_set_path) ---- */

@@ -18,8 +18,15 @@ namespace pade {
 struct ArDF {
     using V = dfv;
     using IO = double;
+    // lines are scaled by a power of two so that their maximum is in [1, 2) (exact)
+    static constexpr bool kScaled = true;
     static __device__ __forceinline__ V load(double x, unsigned& bad) { return df_from_double(x, bad); }
     static __device__ __forceinline__ double store(V v) { return df_to_double(v); }
+    // shift each part on its bits unless the low part could leave the normal FP64 range
+    // (lines below ~1e-270), where the sum is formed first and then shifted
+    static __device__ __forceinline__ double store_scaled(V v, int k) {
+        return k >= -900 ? df_to_double_shift(v, k) : shift_up(df_to_double(v), k);
+    }
     static __device__ __forceinline__ V coef(F2 c) { return dfv{c.h, c.l}; }
     static __device__ __forceinline__ V zero() { return df_zero(); }
     static __device__ __forceinline__ V add(V a, V b) { return df_add(a, b); }
@@ -44,8 +51,10 @@ struct ArDF {
 struct ArF32 {
     using V = float;
     using IO = float;
+    static constexpr bool kScaled = false;
     static __device__ __forceinline__ V load(float x, unsigned&) { return x; }
     static __device__ __forceinline__ float store(V v) { return v; }
+    static __device__ __forceinline__ float store_scaled(V v, int) { return v; }
     static __device__ __forceinline__ V coef(F2 c) { return c.h; }
     static __device__ __forceinline__ V zero() { return 0.0f; }
     static __device__ __forceinline__ V add(V a, V b) { return a + b; }
@@ -75,6 +84,8 @@ __device__ __forceinline__ int spos(int p) {
 
 // Staging loads keep up to kLoadUnroll loads in flight per thread before converting.
 constexpr int kLoadUnroll = 8;
+// Largest per-thread share of a line staged in registers by the one-pass scaled load.
+constexpr int kStageRegs = 16;
 
 template <class AR, int Q, int M, bool CIRC>
 __global__ void __launch_bounds__(256, 3)
@@ -89,9 +100,11 @@ __global__ void __launch_bounds__(256, 3)
     V* work = tile + (size_t)cp.L * cp.LS;                  // per-row RHS / solution, L x LS
     IO* wio = reinterpret_cast<IO*>(work);                  // same storage, output values
 
+    __shared__ int lexp[256];  // per-line maximum FP64 exponent (scaled double-float path)
     const int tid = threadIdx.x, nth = blockDim.x;
     const long line0 = (long)blockIdx.x * cp.L;
     const int nl = (int)min((long)cp.L, ls.nlines - line0);
+    if (AR::kScaled && tid < nl) lexp[tid] = 0;
     if (tid < cp.L) {
         const long lg = line0 + tid;
         const long a = lg % ls.na, b = lg / ls.na;
@@ -101,44 +114,145 @@ __global__ void __launch_bounds__(256, 3)
     __syncthreads();
 
     // ---- A: stage the input lines in shared memory, converted once ----
+    // Double-float: each line is split as d * 2^-(e_max - 1023), e_max its largest FP64
+    // exponent, so the df range (2^-74 .. 2^127) holds relative to the line maximum
+    // whatever the input scale.  When a thread's share of a line fits in kStageRegs
+    // registers the values are loaded, reduced and split in one pass; longer lines are
+    // staged as FP64 first and split in place.
     unsigned bad = 0;
-    if (ls.fp == 1) {
-        // contiguous lines: one warp per line, kLoadUnroll loads in flight per lane
-        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
-        for (int l = warp; l < nl; l += nw) {
-            const IO* src = f + base_in[l];
-            V* dst = tile + l * cp.LS;
-            for (int p0 = lane; p0 < cp.m; p0 += 32 * kLoadUnroll) {
-                IO v[kLoadUnroll];
+    bool staged = false;
+    if constexpr (AR::kScaled) {
+        if (ls.fp == 1) {
+            const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+            const int U = (cp.m + 31) >> 5;
+            if (U <= kStageRegs) {
+                staged = true;
+                for (int l = warp; l < nl; l += nw) {
+                    const IO* src = f + base_in[l];
+                    V* dst = tile + l * cp.LS;
+                    double v[kStageRegs];
+                    int mx = 0;
 #pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int p = p0 + 32 * u;
-                    v[u] = p < cp.m ? __ldg(src + p) : (IO)0;
+                    for (int u = 0; u < kStageRegs; u++) {
+                        const int p = lane + 32 * u;
+                        v[u] = (u < U && p < cp.m) ? __ldg(src + p) : 0.0;
+                        mx = max(mx, bexp(v[u]));
+                    }
+                    mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
+                    bad |= (unsigned)(mx == 2047);  // infinity or NaN in the line
+                    if (lane == 0) lexp[l] = mx;
+#pragma unroll
+                    for (int u = 0; u < kStageRegs; u++) {
+                        const int p = lane + 32 * u;
+                        if (u < U && p < cp.m) dst[spos<M>(p)] = df_from_double_shift(v[u], mx - 1023);
+                    }
                 }
+            }
+        } else {
+            const int pstep = nth / cp.L;
+            const int U = (cp.m + pstep - 1) / pstep;
+            if (U <= kStageRegs) {
+                staged = true;
+                const int l = tid % cp.L, q0 = tid / cp.L;
+                double v[kStageRegs];
+                int mx = 0;
+                if (l < nl) {
+                    const IO* src = f + base_in[l];
 #pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int p = p0 + 32 * u;
-                    if (p < cp.m) dst[spos<M>(p)] = AR::load(v[u], bad);
+                    for (int u = 0; u < kStageRegs; u++) {
+                        const int p = q0 + pstep * u;
+                        v[u] = (u < U && p < cp.m) ? __ldg(src + (long)p * ls.fp) : 0.0;
+                        mx = max(mx, bexp(v[u]));
+                    }
+                    atomicMax(&lexp[l], mx);
+                }
+                __syncthreads();
+                if (l < nl) {
+                    const int k = lexp[l] - 1023;
+                    bad |= (unsigned)(lexp[l] == 2047);
+                    V* dst = tile + l * cp.LS;
+#pragma unroll
+                    for (int u = 0; u < kStageRegs; u++) {
+                        const int p = q0 + pstep * u;
+                        if (u < U && p < cp.m) dst[spos<M>(p)] = df_from_double_shift(v[u], k);
+                    }
                 }
             }
         }
-    } else {
-        // strided lines: consecutive threads take consecutive lines (coalesced rows)
-        const int l = tid % cp.L, pstep = nth / cp.L;
-        if (l < nl) {
-            const IO* src = f + base_in[l];
-            V* dst = tile + l * cp.LS;
-            for (int p0 = tid / cp.L; p0 < cp.m; p0 += pstep * kLoadUnroll) {
-                IO v[kLoadUnroll];
+    }
+    if (!staged) {
+        if (ls.fp == 1) {
+            // contiguous lines: one warp per line, kLoadUnroll loads in flight per lane
+            const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+            for (int l = warp; l < nl; l += nw) {
+                const IO* src = f + base_in[l];
+                V* dst = tile + l * cp.LS;
+                int mx = 0;
+                for (int p0 = lane; p0 < cp.m; p0 += 32 * kLoadUnroll) {
+                    IO v[kLoadUnroll];
 #pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int p = p0 + pstep * u;
-                    v[u] = p < cp.m ? __ldg(src + (long)p * ls.fp) : (IO)0;
+                    for (int u = 0; u < kLoadUnroll; u++) {
+                        const int p = p0 + 32 * u;
+                        v[u] = p < cp.m ? __ldg(src + p) : (IO)0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kLoadUnroll; u++) {
+                        const int p = p0 + 32 * u;
+                        if (p < cp.m) {
+                            if constexpr (AR::kScaled) {
+                                reinterpret_cast<double*>(dst)[spos<M>(p)] = v[u];
+                                mx = max(mx, bexp(v[u]));
+                            } else {
+                                dst[spos<M>(p)] = AR::load(v[u], bad);
+                            }
+                        }
+                    }
                 }
+                if constexpr (AR::kScaled) {
+                    mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
+                    if (lane == 0) lexp[l] = mx;
+                }
+            }
+        } else {
+            // strided lines: consecutive threads take consecutive lines (coalesced rows)
+            const int l = tid % cp.L, pstep = nth / cp.L;
+            if (l < nl) {
+                const IO* src = f + base_in[l];
+                V* dst = tile + l * cp.LS;
+                int mx = 0;
+                for (int p0 = tid / cp.L; p0 < cp.m; p0 += pstep * kLoadUnroll) {
+                    IO v[kLoadUnroll];
 #pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int p = p0 + pstep * u;
-                    if (p < cp.m) dst[spos<M>(p)] = AR::load(v[u], bad);
+                    for (int u = 0; u < kLoadUnroll; u++) {
+                        const int p = p0 + pstep * u;
+                        v[u] = p < cp.m ? __ldg(src + (long)p * ls.fp) : (IO)0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kLoadUnroll; u++) {
+                        const int p = p0 + pstep * u;
+                        if (p < cp.m) {
+                            if constexpr (AR::kScaled) {
+                                reinterpret_cast<double*>(dst)[spos<M>(p)] = v[u];
+                                mx = max(mx, bexp(v[u]));
+                            } else {
+                                dst[spos<M>(p)] = AR::load(v[u], bad);
+                            }
+                        }
+                    }
+                }
+                if constexpr (AR::kScaled) atomicMax(&lexp[l], mx);
+            }
+        }
+        __syncthreads();
+        if constexpr (AR::kScaled) {
+            const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+            for (int ll = warp; ll < nl; ll += nw) {
+                const int k = lexp[ll] - 1023;
+                bad |= (unsigned)(lexp[ll] == 2047);  // infinity or NaN in the line
+                V* row = tile + ll * cp.LS;
+                for (int p = lane; p < cp.m; p += 32) {
+                    const int ps = spos<M>(p);
+                    row[ps] = df_from_double_shift(reinterpret_cast<const double*>(row)[ps], k);
                 }
             }
         }
@@ -193,11 +307,12 @@ __global__ void __launch_bounds__(256, 3)
     if constexpr (Q == 0) {
         // explicit operator: the right-hand side is the result
         IO* wlio = reinterpret_cast<IO*>(wl);
+        const int kl = AR::kScaled && l < nl ? lexp[l] - 1023 : 0;
 #pragma unroll 1
         for (int i = r0; i < r1; i++) {
             V x = rhs_row(i);
             if (cp.resid) x = AR::norm(AR::sub(line[spos<M>(i)], x));
-            wlio[spos<M>(i)] = AR::store(x);
+            wlio[spos<M>(i)] = AR::store_scaled(x, kl);
         }
     } else {
         const int Pp = cp.Pp;
@@ -319,6 +434,7 @@ __global__ void __launch_bounds__(256, 3)
         }
         // ---- H+I: backward correction, residual form, FP64 conversion (in place) ----
         IO* wlio = reinterpret_cast<IO*>(wl);
+        const int kl = AR::kScaled && l < nl ? lexp[l] - 1023 : 0;
 #pragma unroll 2
         for (int i = r0; i < r1; i++) {
             const int ps = spos<M>(i);
@@ -333,7 +449,7 @@ __global__ void __launch_bounds__(256, 3)
             }
             V x = (Q == 2) ? AR::mac2(wl[ps], p1, j1, p2, j2) : AR::mac1(wl[ps], p1, j1);
             if (cp.resid) x = AR::norm(AR::sub(line[ps], x));
-            wlio[ps] = AR::store(x);
+            wlio[ps] = AR::store_scaled(x, kl);
         }
     }
     __syncthreads();

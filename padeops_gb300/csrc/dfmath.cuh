@@ -19,7 +19,8 @@ struct dfv {
 // Split an FP64 value into (hi, lo): hi keeps the leading 24 significant bits
 // (truncated), lo the remaining 29 bits rounded to float.  Exact to 2^-47 relative.
 // Full precision needs the biased FP64 exponent in [949, 1150] (|d| in [2^-74, 2^127));
-// other non-zero values set `bad` and are flushed (the host reports PADE_ERANGE).
+// other non-zero values set `bad` and are flushed.  The kernels scale each line into
+// range first (df_from_double_shift), so only infinities and NaNs reach that case.
 __device__ __forceinline__ dfv df_from_double(double d, unsigned& bad) {
     const unsigned lo32 = (unsigned)__double2loint(d);
     const unsigned hi32 = (unsigned)__double2hiint(d);
@@ -53,6 +54,61 @@ __device__ __forceinline__ double float_bits_to_double(float x) {
 // (h + l) rounded once to FP64: two exact conversions and one FP64 add.
 __device__ __forceinline__ double df_to_double(dfv a) {
     return __dadd_rn(float_bits_to_double(a.h), float_bits_to_double(a.l));
+}
+
+// Per-line power-of-two scaling keeps the df range relative to a line's maximum: values
+// are split as d * 2^-k and reassembled as r * 2^k, both on the exponent bits.
+// Biased FP64 exponent of d (0 for zero and subnormals, 2047 for inf/NaN).
+__device__ __forceinline__ int bexp(double d) { return (__double2hiint(d) >> 20) & 0x7FF; }
+
+// d * 2^-k split into a df value: df_from_double with the exponent lowered by k on the
+// bits; zero for zero/subnormal input and when the shifted value is below 2^-74.
+__device__ __forceinline__ dfv df_from_double_shift(double d, int k) {
+    const unsigned lo32 = (unsigned)__double2loint(d);
+    const unsigned h0 = (unsigned)__double2hiint(d);
+    const int e2 = (int)((h0 >> 20) & 0x7FFu) - k;
+    const bool ok = (h0 & 0x7FF00000u) != 0u && e2 >= 949 && e2 <= 1149;
+    const unsigned sign = h0 & 0x80000000u;
+    const unsigned hi32 = (h0 & 0x800FFFFFu) | ((unsigned)(e2 & 0x7FF) << 20);
+    const unsigned ex = hi32 & 0x7FF00000u;
+    const unsigned hb = (((hi32 - (896u << 20)) << 3) & 0x7FFFFFF8u) | (lo32 >> 29) | sign;
+    const float lf = __uint2float_rn(lo32 & 0x1FFFFFFFu);
+    const unsigned sb = (ex - (948u << 20)) << 3;
+    float lo = __fmul_rn(lf, __uint_as_float(sb));
+    lo = __uint_as_float(__float_as_uint(lo) ^ sign);
+    return dfv{ok ? __uint_as_float(hb) : 0.0f, ok ? lo : 0.0f};
+}
+
+// float x * 2^k as an exact double (x normal; zero, subnormal x and results below the
+// normal FP64 range give 0, results above it infinity)
+__device__ __forceinline__ double float_bits_to_double_shift(float x, int k) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned mag = b & 0x7FFFFFFFu;
+    const unsigned sg = b & 0x80000000u;
+    const int e2 = (int)(mag >> 23) + 896 + k;  // FP64 biased exponent of the result
+    const bool z = mag < 0x00800000u || e2 <= 0;
+    const bool inf = !z && e2 >= 2047;           // beyond the FP64 range: infinity
+    const unsigned hi = z ? sg : (inf ? (sg | 0x7FF00000u) : ((((mag >> 3) & 0x000FFFFFu) | ((unsigned)e2 << 20)) | sg));
+    const unsigned lo = (z || inf) ? 0u : (b << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// (h + l) * 2^k rounded once to FP64
+__device__ __forceinline__ double df_to_double_shift(dfv a, int k) {
+    return __dadd_rn(float_bits_to_double_shift(a.h, k), float_bits_to_double_shift(a.l, k));
+}
+
+// r * 2^k on the exponent bits (flushes below the normal range)
+__device__ __forceinline__ double shift_up(double r, int k) {
+    const unsigned lo = (unsigned)__double2loint(r);
+    unsigned hi = (unsigned)__double2hiint(r);
+    const int ex = (int)((hi >> 20) & 0x7FFu);
+    if (ex == 0) return 0.0;
+    int e2 = ex + k;
+    if (e2 <= 0) return 0.0;
+    if (e2 >= 2047) return __hiloint2double((int)((hi & 0x80000000u) | 0x7FF00000u), 0);
+    hi = (hi & 0x800FFFFFu) | ((unsigned)e2 << 20);
+    return __hiloint2double((int)hi, (int)lo);
 }
 
 __device__ __forceinline__ dfv df_zero() { return dfv{0.0f, 0.0f}; }

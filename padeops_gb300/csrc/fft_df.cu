@@ -62,33 +62,6 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
     return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
 }
 
-__device__ __forceinline__ int bexp(double d) { return (__double2hiint(d) >> 20) & 0x7FF; }
-
-// d * 2^-k split into a df value; zero when below 2^-74 after the shift (or zero/subnormal)
-__device__ __forceinline__ dfv df_from_double_shift(double d, int k) {
-    const unsigned lo = (unsigned)__double2loint(d);
-    unsigned hi = (unsigned)__double2hiint(d);
-    const int ex = (int)((hi >> 20) & 0x7FFu);
-    const int e2 = ex - k;
-    if (ex == 0 || e2 < 949 || e2 > 1149) return dfv{0.0f, 0.0f};
-    hi = (hi & 0x800FFFFFu) | ((unsigned)e2 << 20);
-    unsigned bad = 0;
-    return df_from_double(__hiloint2double((int)hi, (int)lo), bad);
-}
-
-// r * 2^k on the exponent bits (flushes below the normal range)
-__device__ __forceinline__ double shift_up(double r, int k) {
-    const unsigned lo = (unsigned)__double2loint(r);
-    unsigned hi = (unsigned)__double2hiint(r);
-    const int ex = (int)((hi >> 20) & 0x7FFu);
-    if (ex == 0) return 0.0;
-    int e2 = ex + k;
-    if (e2 <= 0) return 0.0;
-    if (e2 >= 2047) return __hiloint2double((int)((hi & 0x80000000u) | 0x7FF00000u), 0);
-    hi = (hi & 0x800FFFFFu) | ((unsigned)e2 << 20);
-    return __hiloint2double((int)hi, (int)lo);
-}
-
 // decimation in frequency: natural order -> bit-reversed
 __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj) {
     const int half = 1 << (logn - 1);

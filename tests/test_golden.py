@@ -128,7 +128,9 @@ def test_cuda_path_matches_golden(dir):
     assert o.init(32, 2 * np.pi / 31, False) == 0
     for d in (1, 2):
         out = _gpu_apply(o, d, G["cd10_np32_f"], dir).ravel()
-        assert relerr(out, G[f"cd10_np32_d{d}_oracle"]) < 1e-12
+        # one-sided second-derivative closures amplify the double-float 2^-48 representation
+        # error by their coefficient sums (~1e3): 1e-10 for d2, as for the seeded d2 lines
+        assert relerr(out, G[f"cd10_np32_d{d}_oracle"]) < (1e-12 if d == 1 else 1e-10)
     c = P.cd06()
     assert c.init(256, 2 * np.pi / 256, True) == 0
     assert relerr(_gpu_apply(c, 1, G["cd06_p256_f"], dir).ravel(), G["cd06_p256_oracle"]) < 1e-12

@@ -281,20 +281,39 @@ def test_bench_scale_fields(oracle):
         assert relerr(out, oracle.cf90(f, dir=dir)) < 1e-12
 
 
-def test_range_flag_reported(oracle):
-    """Inputs outside the double-float range raise PADE_ERANGE instead of silently losing digits."""
+@pytest.mark.parametrize("amp", [1e-300, 1e-200, 1e-30, 1e30, 1e200, 1e300])
+def test_double_float_path_is_range_free(oracle, amp):
+    """Each line is scaled by a power of two before the double-float split, so any FP64
+    magnitude keeps full relative accuracy, along every direction."""
+    n = 16
+    c = P.cd10()
+    assert c.init(n, 0.1, True) == 0
+    z = P.cf90()
+    assert z.init(n, False) == 0
+    f = field((n, n, n), 9) * amp
+    f[:, 2, 3] *= 1e-80  # a line far below the others keeps its own relative accuracy
+    for dir in (1, 2, 3):
+        out = run(c, 1, dir, f, f.shape)
+        ref = oracle.cd10(f, 0.1, order=1, dir=dir)
+        assert relerr(out, ref) < 1e-12, dir
+        out = run(z, 0, dir, f, f.shape)
+        assert relerr(out, oracle.cf90(f, periodic=False, dir=dir)) < CF90_DF_NOISE_TOL, dir
+    out = run(c, 1, 1, f, f.shape)
+    ref = oracle.cd10(f, 0.1, order=1, dir=1)
+    assert relerr(out[:, 2, 3], ref[:, 2, 3]) < 1e-12
+
+
+def test_range_flag_for_non_finite_input(oracle):
+    """A NaN or infinity in a line raises PADE_ERANGE on host-buffer calls."""
     n = 16
     c = P.cd10()
     assert c.init(n, 0.1, True) == 0
     f = np.zeros((n, 4, 4), order="F")
-    f[3, 1, 1] = 1e-300
+    f[3, 1, 1] = np.inf
     df = np.zeros_like(f, order="F")
     with pytest.raises(L.PadeError) as e:
         c.dd1(f, df, 4, 4)
     assert e.value.code == L.PADE_ERANGE
-    c.set_path(L.PATH_NATIVE)
-    c.dd1(f, df, 4, 4)  # the native FP64 path has no such range limit
-    assert relerr(df, oracle.cd10(f, 0.1)) < 1e-12
 
 
 def test_reference_error_codes():
