@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -62,8 +63,10 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
     return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
 }
 
-// decimation in frequency: natural order -> bit-reversed
-__device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj) {
+// decimation in frequency: natural order -> bit-reversed.  tw holds exp(-2 pi i t / (n 2^tws)),
+// so a table made for a longer transform serves with stride 2^tws.
+__device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj,
+                                       int tws = 0) {
     const int half = 1 << (logn - 1);
     const int work = nl << (logn - 1);
     for (int s = logn - 1; s >= 0; s--) {
@@ -75,14 +78,15 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4
             const cdf a = ldc(x, i0), b = ldc(x, i1);
             stc(x, i0, cadd(a, b));
             const cdf d = csub(a, b);
-            stc(x, i1, s == 0 ? d : cmulw(d, __ldg(&tw[k << (logn - 1 - s)]), conj));
+            stc(x, i1, s == 0 ? d : cmulw(d, __ldg(&tw[k << (logn - 1 - s + tws)]), conj));
         }
         __syncthreads();
     }
 }
 
 // decimation in time: bit-reversed -> natural order
-__device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj) {
+__device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj,
+                                       int tws = 0) {
     const int half = 1 << (logn - 1);
     const int work = nl << (logn - 1);
     for (int s = 0; s < logn; s++) {
@@ -93,7 +97,7 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4
             const int i1 = i0 + (1 << s);
             const cdf a = ldc(x, i0);
             cdf b = ldc(x, i1);
-            if (s > 0) b = cmulw(b, __ldg(&tw[k << (logn - 1 - s)]), conj);
+            if (s > 0) b = cmulw(b, __ldg(&tw[k << (logn - 1 - s + tws)]), conj);
             stc(x, i0, cadd(a, b));
             stc(x, i1, csub(a, b));
         }
@@ -225,6 +229,147 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     }
 }
 
+__device__ __forceinline__ cdf cconj(cdf a) { return cdf{a.r, df_neg(a.i)}; }
+__device__ __forceinline__ cdf chalf(cdf a) {
+    return cdf{dfv{0.5f * a.r.h, 0.5f * a.r.l}, dfv{0.5f * a.i.h, 0.5f * a.i.l}};
+}
+__device__ __forceinline__ double2 cstore(cdf c, int k) {
+    return make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
+}
+
+// Real transforms along x lines (fp == 1) of N = 2^logN points through one complex transform
+// of M = N/2 points (the classical even/odd packing):
+//   r2c: z[j] = x[2j] + i x[2j+1], Z = FFT_M(z), and for k = 0..M
+//        X[k] = ((Z[k] + conj Z[M-k]) - i W^k (Z[k] - conj Z[M-k])) / 2,   W = exp(-2 pi i / N)
+//   c2r: Z'[k] = (X[k] + conj X[M-k]) + i conj(W^k) (X[k] - conj X[M-k]), k = 0..M-1,
+//        w = unnormalised backward FFT_M(Z'), x[2j] = Re w[j], x[2j+1] = Im w[j]
+// (the imaginary parts of X[0] and X[M] are ignored, as FFTW's c2r does; oddball zeroes X[M]).
+template <bool R2C>
+__global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, const FftLines ls,
+                                                     const float4* __restrict__ tw, int logN, int lb, int scale_exp,
+                                                     float2 scale_df, int use_scale_df, int oddball) {
+    extern __shared__ __align__(16) float4 smf[];
+    double2* smd = reinterpret_cast<double2*>(smf);
+    __shared__ int emax[64];
+    __shared__ float4 xlast[64];  // c2r: X[M] of each line (split)
+    __shared__ double2 xlast_raw[64];
+    const int logM = logN - 1, M = 1 << logM;
+    const long l0 = (long)blockIdx.x * lb;
+    const int nl = (int)min((long)lb, ls.nlines - l0);
+    const int total = nl << logM;
+    for (int l = threadIdx.x; l < nl; l += blockDim.x) emax[l] = 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int l = e >> logM, j = e & (M - 1);
+        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+        const long base = a * ls.fa + b * ls.fb;
+        double2 v;
+        if (R2C) {
+            v = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(in) + base + 2 * j);
+        } else {
+            v = reinterpret_cast<const double2*>(in)[base + j];
+            if (j == 0) v.y = 0.0;
+        }
+        smd[e] = v;
+        atomicMax(&emax[l], max(bexp(v.x), bexp(v.y)));
+    }
+    if (!R2C) {
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+            const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+            double2 v = reinterpret_cast<const double2*>(in)[a * ls.fa + b * ls.fb + M];
+            v.y = 0.0;
+            if (oddball) v.x = 0.0;
+            xlast_raw[l] = v;
+            atomicMax(&emax[l], bexp(v.x));
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int k = emax[e >> logM] - 1023;
+        const double2 v = smd[e];
+        stc(smf, e, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
+    }
+    if (!R2C) {
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+            const int k = emax[l] - 1023;
+            const double2 v = xlast_raw[l];
+            stc(xlast, l, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
+        }
+    }
+    __syncthreads();
+    const dfv sdf{scale_df.x, scale_df.y};
+    if (R2C) {
+        dif_df(smf, nl, logM, tw, false, 1);  // Z in bit-reversed order
+        for (int e = threadIdx.x; e < total + nl; e += blockDim.x) {
+            int l, k;
+            if (e < total) {
+                l = e >> logM;
+                k = e & (M - 1);
+            } else {
+                l = e - total;
+                k = M;
+            }
+            const int ka = k & (M - 1), kb = (M - k) & (M - 1);
+            const cdf za = ldc(smf, (l << logM) + brev(ka, logM));
+            const cdf zb = cconj(ldc(smf, (l << logM) + brev(kb, logM)));
+            const cdf sm = cadd(za, zb), df = csub(za, zb);
+            cdf t;
+            if (k < M) {
+                t = cmulw(df, __ldg(&tw[k]), false);
+            } else {
+                t = cdf{df_neg(df.r), df_neg(df.i)};  // W^M = -1
+            }
+            // X = (sm - i t) / 2, -i t = (t.i, -t.r)
+            cdf X = chalf(cdf{df_norm(df_add(sm.r, t.i)), df_norm(df_sub(sm.i, t.r))});
+            if (use_scale_df) X = cscale(X, sdf);
+            const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+            reinterpret_cast<double2*>(out)[a * ls.oa + b * ls.ob + k] = cstore(X, emax[l] - 1023 + scale_exp);
+        }
+    } else {
+        // pairs (k, M-k) for k = 0 .. M/2 - 1, in place; X[M] of k = 0 comes from xlast
+        const int half = M >> 1;
+        for (int e = threadIdx.x; e < (nl << (logM - 1)); e += blockDim.x) {
+            const int l = e >> (logM - 1), k = e & (half - 1);
+            const int k2 = M - k;
+            const cdf xk = ldc(smf, (l << logM) + k);
+            const cdf xk2 = k == 0 ? ldc(xlast, l) : ldc(smf, (l << logM) + k2);
+            // Z'[k] = (xk + conj xk2) + i conj(W^k) (xk - conj xk2)
+            {
+                const cdf c2 = cconj(xk2);
+                const cdf sm = cadd(xk, c2);
+                cdf d = csub(xk, c2);
+                if (k > 0) d = cmulw(d, __ldg(&tw[k]), true);
+                stc(smf, (l << logM) + k, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+            }
+            if (k > 0) {  // Z'[k2], k2 = M - k in (M/2, M)
+                const cdf c1 = cconj(xk);
+                const cdf sm = cadd(xk2, c1);
+                const cdf d = cmulw(csub(xk2, c1), __ldg(&tw[k2]), true);
+                stc(smf, (l << logM) + k2, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+            }
+        }
+        // k = M/2 pairs with itself: conj(W^(M/2)) = i
+        for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+            const cdf x = ldc(smf, (l << logM) + half);
+            const cdf c = cconj(x);
+            const cdf sm = cadd(x, c);
+            cdf d = csub(x, c);
+            d = cdf{df_neg(d.i), d.r};  // i * d
+            stc(smf, (l << logM) + half, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+        }
+        __syncthreads();
+        dif_df(smf, nl, logM, tw, true, 1);  // backward, bit-reversed
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int l = e >> logM, j = e & (M - 1);
+            cdf w = ldc(smf, (l << logM) + brev(j, logM));
+            if (use_scale_df) w = cscale(w, sdf);
+            const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+            *reinterpret_cast<double2*>(reinterpret_cast<double*>(out) + a * ls.oa + b * ls.ob + 2 * j) =
+                cstore(w, emax[l] - 1023 + scale_exp);
+        }
+    }
+}
+
 std::mutex g_twdf_mu;
 std::map<std::pair<int, int>, float4*> g_twdf;  // (device, n) -> df exp(-2 pi i t / n), t < n/2
 
@@ -308,6 +453,24 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
         return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_DEALIAS>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
     if (in_mode == IN_COMPLEX && out_mode == OUT_COMPLEX)
         return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
+    // 16-byte pair loads (r2c input) / stores (c2r output) need aligned real lines
+    const bool aligned = in_mode == IN_REAL
+                             ? ((reinterpret_cast<uintptr_t>(in) & 15) == 0 && ls.fa % 2 == 0 && ls.fb % 2 == 0)
+                             : ((reinterpret_cast<uintptr_t>(out) & 15) == 0 && ls.oa % 2 == 0 && ls.ob % 2 == 0);
+    const bool xreal = ls.fp == 1 && ls.op == 1 && logn >= 3 && ex.mul == MUL_NONE && aligned;
+    if (xreal && ((in_mode == IN_REAL && out_mode == OUT_HALF) || (in_mode == IN_HALF && out_mode == OUT_REAL))) {
+        // half-length complex transform; lb lines of M = n/2 points per CTA
+        const int lbr = std::max(1, std::min(64, 4096 >> (logn - 1)));
+        const size_t smem = sizeof(float4) * ((size_t)lbr << (logn - 1));
+        const bool r2c = in_mode == IN_REAL;
+        auto kern = r2c ? k_fft_df_real<true> : k_fft_df_real<false>;
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return PS_ECUDA;
+        const long blocks = (ls.nlines + lbr - 1) / lbr;
+        kern<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, logn, lbr, sexp, sdf, use, oddball);
+        return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+    }
     if (in_mode == IN_REAL && out_mode == OUT_HALF)
         return launch_df_t<IN_REAL, OUT_HALF, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
     if (in_mode == IN_HALF && out_mode == OUT_REAL)
