@@ -137,7 +137,7 @@ def step_plan(objs):
 
 
 def run_device(args, P, torch):
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", torch.cuda.current_device())
     f_host = make_field()
     plan = step_plan(setup_objects(P))
     nops = len(plan)
@@ -164,14 +164,18 @@ def run_device(args, P, torch):
     evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nops)]
            for _ in range(args.steps)]
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clk = ClockSampler(0)
+    from padeops_gb300.replicas import barrier
+
+    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clk.start()
     torch.cuda.synchronize()
+    barrier()
     t0.record(stream)
     for s in range(args.steps):
         one_step(evs[s])
     t1.record(stream)
     torch.cuda.synchronize()
+    barrier()
     clocks = clk.stop()
     ms = t0.elapsed_time(t1)
     per_launch = np.zeros(nops)
@@ -259,7 +263,7 @@ def extras(args, P, torch, f_host):
     paths of the same step, the 512^3 periodic projection, and the 256^3 LES step with the
     dynamic procedure and with the learned closure.  Errors are reported, not raised."""
     out = {}
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", torch.cuda.current_device())
     plan = step_plan(setup_objects(P))
     npts = N ** 3
     reps = max(3, min(args.steps, 10))
@@ -444,10 +448,9 @@ def main():
         dist.init_process_group("nccl")
     ms_step, per_launch, clocks, plan, f_host = run_device(args, P, torch)
     if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-        dist.barrier()
+        from padeops_gb300.replicas import max_over_ranks
+
+        ms_step = max_over_ranks(ms_step, device="cuda")
     npts = N ** 3
     value = world * len(plan) * npts / (ms_step * 1e-3) / 1e9
     e2e = None
