@@ -98,6 +98,23 @@ __device__ __forceinline__ double df_to_double_shift(dfv a, int k) {
     return __dadd_rn(float_bits_to_double_shift(a.h, k), float_bits_to_double_shift(a.l, k));
 }
 
+// float x * 2^k as an exact double when -800 <= k <= 800 (every normal float then lands
+// in the normal FP64 range, so no range checks); zero and subnormal x give 0.
+// kadd = (896 + k) << 20, the FP32-to-FP64 exponent rebias plus the shift.
+__device__ __forceinline__ double float_bits_to_double_kadd(float x, unsigned kadd) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned mag = b & 0x7FFFFFFFu;
+    const unsigned sg = b & 0x80000000u;
+    const bool z = mag < 0x00800000u;
+    const unsigned hi = z ? sg : (((mag >> 3) + kadd) | sg);
+    return __hiloint2double((int)hi, z ? 0 : (int)(b << 29));
+}
+
+// (h + l) * 2^k rounded once to FP64, for -800 <= k <= 800
+__device__ __forceinline__ double df_to_double_kadd(dfv a, unsigned kadd) {
+    return __dadd_rn(float_bits_to_double_kadd(a.h, kadd), float_bits_to_double_kadd(a.l, kadd));
+}
+
 // r * 2^k on the exponent bits (flushes below the normal range)
 __device__ __forceinline__ double shift_up(double r, int k) {
     const unsigned lo = (unsigned)__double2loint(r);

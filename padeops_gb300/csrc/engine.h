@@ -40,6 +40,39 @@ struct ChunkParams {
     const F2* phb;
 };
 
+// Operators with an instantiated fixed-stencil kernel (stencil_kernel.cuh): chunk length,
+// threads per CTA (NT / Pp lines each), and the stencil shapes (Q = LHS half bandwidth,
+// NP pairs at offsets +-1..NP), each for circulant (periodic) and banded lines.
+constexpr int kLineM = 16;
+constexpr int kLineThreadsCirc = 128;
+constexpr int kLineThreadsBand = 256;
+enum LineShape : int {
+    SHAPE_NONE = -1,
+    SHAPE_T2A = 0,  // tridiagonal, 2 antisymmetric pairs (cd06 first derivative)
+    SHAPE_T2S = 1,  // tridiagonal, centre + 2 symmetric pairs (cd06 second derivative)
+    SHAPE_P3A = 2,  // pentadiagonal, 3 antisymmetric pairs (cd10 first derivative)
+    SHAPE_P3S = 3,  // pentadiagonal, centre + 3 symmetric pairs (cd10 second derivative)
+    SHAPE_P4S = 4,  // pentadiagonal, centre + 4 symmetric pairs (cf90, residual form)
+};
+
+struct StencilParams {
+    int ns, nout, P, Pp, nsteps, L, resid;
+    int circ;         // circulant line (ring wrap, constant coefficients)
+    int nlo, nhi, tw; // banded: edge rows at both ends, taps per edge row
+    F2 c0;            // centre coefficient (symmetric stencils; 0 when absent)
+    F2 c[kMaxPairs];  // pair coefficients: pair k (k = 1..NP) at offsets +-k, in c[k-1]
+    F2 ca1, ca2;      // circulant recurrence constants (forward and backward)
+    const int* tidx;  // banded edge rows: tap rows and coefficients (nlo + nhi rows x tw)
+    const F2* tc;
+    const F2* rc;     // banded: ns x 5 (g, a1, a2, b1, b2)
+    const F2* fscan;
+    const F2* bscan;
+    const F2* fwrap;
+    const F2* bwrap;
+    const F2* phf;    // circulant: kLineM x 2 per chunk position; banded: ns x 2 per row
+    const F2* phb;
+};
+
 class DevicePlan {
    public:
     DevicePlan() = default;
@@ -54,6 +87,8 @@ class DevicePlan {
     ChunkParams chunk_df() const { return cdf_; }
     ChunkParams chunk_f32() const { return cf32_; }
     int chunk_M() const { return ch_.M; }
+    int line_shape() const { return line_shape_; }
+    const StencilParams& line_params() const { return cline_; }
 
    private:
     HostPlan hp_;
@@ -62,7 +97,13 @@ class DevicePlan {
     void* dev_ = nullptr;
     PlanView<double> vd_{};
     ChunkParams cdf_{}, cf32_{};
+    int line_shape_ = SHAPE_NONE;
+    StencilParams cline_{};
 };
+
+// Fixed-stencil kernel (double-float) for a plan with line_shape() != SHAPE_NONE.
+int launch_line(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
+                cudaStream_t s);
 
 // Launch the operator on a set of lines.  f/out are device pointers to double (FP64 paths)
 // or float (PATH_FP32).  status (device word) collects out-of-range flags of the df path.

@@ -251,6 +251,64 @@ int DevicePlan::upload(const HostPlan& hp) {
             (v == 0 ? cdf_ : cf32_) = c;
         }
     }
+
+    // fixed-stencil kernel: whole chunks, pairs at +-1..NP, one sign; banded lines also need
+    // edge rows covering the stencil's reach at both ends
+    line_shape_ = SHAPE_NONE;
+    if (cok_ && ch_.M == kLineM && d.m == d.ns && d.ns % kLineM == 0 && d.ns <= 512 && ch_.P <= kMaxLanes &&
+        (ch_.Q == 1 || ch_.Q == 2) && (ch_.circ || d.nout == d.ns)) {
+        const int np = ch_.npair;
+        bool ok = np >= 1 && np <= kMaxPairs;
+        bool seen[kMaxPairs + 1] = {};
+        int sgn = 0;
+        StencilParams cc{};
+        for (int k = 0; k < np && ok; k++) {
+            const int o = ch_.pair_op[k];
+            if (o < 1 || o > np || ch_.pair_om[k] != -o || seen[o]) {
+                ok = false;
+                break;
+            }
+            seen[o] = true;
+            cc.c[o - 1] = cdf_.pair_c[k];
+            if (sgn == 0) sgn = ch_.pair_sign[k];
+            else if (sgn != ch_.pair_sign[k]) ok = false;
+        }
+        if (ch_.has_center && (ch_.center_off != 0 || sgn < 0)) ok = false;
+        if (!ch_.circ && (ch_.nlo < np || ch_.nhi < np || ch_.nlo + ch_.nhi > 32)) ok = false;
+        int shape = SHAPE_NONE;
+        if (ok) {
+            if (ch_.Q == 1 && np == 2) shape = sgn < 0 ? SHAPE_T2A : SHAPE_T2S;
+            else if (ch_.Q == 2 && np == 3) shape = sgn < 0 ? SHAPE_P3A : SHAPE_P3S;
+            else if (ch_.Q == 2 && np == 4 && sgn > 0) shape = SHAPE_P4S;
+        }
+        if (shape != SHAPE_NONE) {
+            cc.ns = ch_.ns;
+            cc.nout = ch_.nout;
+            cc.P = ch_.P;
+            cc.Pp = ch_.Pp;
+            cc.nsteps = ch_.nsteps;
+            cc.L = (ch_.circ ? kLineThreadsCirc : kLineThreadsBand) / ch_.Pp;
+            cc.resid = ch_.resid;
+            cc.circ = ch_.circ;
+            cc.nlo = ch_.circ ? 0 : ch_.nlo;
+            cc.nhi = ch_.circ ? 0 : ch_.nhi;
+            cc.tw = ch_.tw;
+            cc.c0 = ch_.has_center ? cdf_.center_c : F2{0.0f, 0.0f};
+            cc.ca1 = cdf_.ca1;
+            cc.ca2 = cdf_.ca2;
+            cc.tidx = cdf_.tidx;
+            cc.tc = cdf_.tc;
+            cc.rc = cdf_.rc;
+            cc.fscan = cdf_.fscan;
+            cc.bscan = cdf_.bscan;
+            cc.fwrap = cdf_.fwrap;
+            cc.bwrap = cdf_.bwrap;
+            cc.phf = cdf_.phf;
+            cc.phb = cdf_.phb;
+            cline_ = cc;
+            line_shape_ = shape;
+        }
+    }
     return PS_OK;
 }
 
@@ -279,6 +337,7 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
     if (!p.chunk_ok()) return PS_ENOTSUP;
     const auto& h = p.chunk_host();
     if (path == PATH_DF) {
+        if (p.line_shape() != SHAPE_NONE) return launch_line(p.line_shape(), p.line_params(), f, out, ls, status, s);
         return h.M == 16 ? launch_chunk_m<ArDF, 16>(h, p.chunk_df(), f, out, ls, status, s)
                          : launch_chunk_m<ArDF, 32>(h, p.chunk_df(), f, out, ls, status, s);
     }

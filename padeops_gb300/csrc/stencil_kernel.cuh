@@ -1,0 +1,399 @@
+// Chunked kernel with a compile-time stencil shape (double-float arithmetic).
+//
+// The compact derivatives and filters (cd06 / cd10 first and second derivatives, cf90 in
+// residual form) have an interior RHS stencil that is symmetric or antisymmetric about the
+// row, and a tridiagonal or pentadiagonal LHS.  k_line runs the algorithm of k_chunk
+// (forward recurrence from a zero state, log-step scan of the chunk transfers, corrected
+// backward recurrence, backward scan, correction) with
+//   * the stencil shape as a template (pair k at offsets +-k, optional centre), so the RHS
+//     is straight-line code with its coefficients in registers;
+//   * each lane's chunk staged with its own halo: periodic lines copy the neighbouring
+//     rows around the ring, so every row uses the interior stencil; non-periodic lines
+//     take their edge rows (one-sided closures) from a small pre-pass instead;
+//   * circulant lines: the recurrence constants in registers and the chunk fundamental
+//     solutions per chunk position; banded lines: per-row tables in shared memory, laid
+//     out chunk by chunk with an odd stride (conflict-free, like the work rows);
+//   * a shift-and-assemble FP64 store without range checks for line scales within
+//     2^+-800 (the checked path otherwise).
+// Lines hold a whole number of chunks (ns = P * M), at most 512 rows.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "chunk_kernel.cuh"
+
+namespace pade {
+
+// Odd lane strides keep the lanes of a line on distinct shared-memory banks.
+template <int M, int H>
+struct LineLayout {
+    static constexpr int S0 = M + 2 * H;
+    static constexpr int S = (S0 % 2 == 0) ? S0 + 1 : S0;  // input window: H + M + H rows
+    static constexpr int W = M + 1;                          // work rows / row tables
+};
+
+template <int NP, bool SYM>
+__device__ __forceinline__ dfv line_stencil(const dfv* __restrict__ p, const dfv (&c)[NP], dfv c0) {
+    dfv acc;
+    if constexpr (SYM) {
+        acc = df_mul(p[0], c0);
+#pragma unroll
+        for (int k = 1; k <= NP; k++) acc = df_add(acc, df_mul(df_add(p[k], p[-k]), c[k - 1]));
+    } else {
+        acc = df_mul(df_sub(p[1], p[-1]), c[0]);
+#pragma unroll
+        for (int k = 2; k <= NP; k++) acc = df_add(acc, df_mul(df_sub(p[k], p[-k]), c[k - 1]));
+    }
+    return df_norm(acc);
+}
+
+// Line stride in 8-byte words, made odd.
+__host__ __device__ constexpr int line_stride(int n) { return n % 2 == 0 ? n + 1 : n; }
+
+// Number of per-row tables of a banded line: g a1 a2 b1 b2 pf1 pf2 pb1 pb2.
+constexpr int kRowTables = 9;
+
+template <int Q, int NP, bool SYM, bool CIRC, int M, int NT>
+__global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
+    k_line(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
+           unsigned* __restrict__ status) {
+    using AR = ArDF;
+    using V = dfv;
+    constexpr int H = NP;
+    constexpr int S = LineLayout<M, H>::S, W = LineLayout<M, H>::W;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ns = cp.ns, P = cp.P, L = cp.L;
+    const int PW = P * W;                      // one row table (banded)
+    // odd line strides: strided staging and stores put consecutive lines on distinct banks
+    const int LT = line_stride(P * S), LW = line_stride(PW);
+    const int ne = cp.nlo + cp.nhi;            // edge rows (banded)
+    V* tab = reinterpret_cast<V*>(smem_raw);   // circulant: phf, phb (M x 2 each); banded: 9 x PW
+    V* tile = tab + (CIRC ? 4 * M : kRowTables * PW);  // L lines x (P windows x S), stride LT
+    V* work = tile + (size_t)L * LT;                    // L lines x (P chunks x W), stride LW
+    V* edge = work + (size_t)L * LW;                    // banded: L x ne edge-row RHS values
+    __shared__ int lexp[NT];
+    __shared__ long base_in[NT], base_out[NT];
+
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const long line0 = (long)blockIdx.x * L;
+    const int nl = (int)min((long)L, ls.nlines - line0);
+    if (tid < L) {
+        lexp[tid] = 0;
+        const long lg = line0 + tid;
+        const long a = lg % ls.na, b = lg / ls.na;
+        base_in[tid] = a * ls.fa + b * ls.fb;
+        base_out[tid] = a * ls.oa + b * ls.ob;
+    }
+    if constexpr (CIRC) {
+        for (int i = tid; i < 2 * M; i += nth) {
+            tab[i] = AR::coef(cp.phf[i]);
+            tab[2 * M + i] = AR::coef(cp.phb[i]);
+        }
+    } else {
+        for (int i = tid; i < ns; i += nth) {
+            const int ps = (i / M) * W + (i % M);
+#pragma unroll
+            for (int k = 0; k < 5; k++) tab[k * PW + ps] = AR::coef(cp.rc[i * 5 + k]);
+            tab[5 * PW + ps] = AR::coef(cp.phf[i * 2]);
+            tab[6 * PW + ps] = AR::coef(cp.phf[i * 2 + 1]);
+            tab[7 * PW + ps] = AR::coef(cp.phb[i * 2]);
+            tab[8 * PW + ps] = AR::coef(cp.phb[i * 2 + 1]);
+        }
+    }
+    __syncthreads();
+
+    // ---- A: stage each line scaled by 2^-(e_max - 1023) into the main rows of the windows ----
+    auto main_pos = [&](int l, int p) -> int { return l * LT + (p / M) * S + H + (p % M); };
+    unsigned bad = 0;
+    if (ls.fp == 1) {
+        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+        const int U = (ns + 31) >> 5;
+        for (int l = warp; l < nl; l += nw) {
+            const double* src = f + base_in[l];
+            double v[kStageRegs];
+            int mx = 0;
+#pragma unroll
+            for (int u = 0; u < kStageRegs; u++) {
+                const int p = lane + 32 * u;
+                v[u] = (u < U && p < ns) ? __ldg(src + p) : 0.0;
+                mx = max(mx, bexp(v[u]));
+            }
+            mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
+            bad |= (unsigned)(mx == 2047);
+            if (lane == 0) lexp[l] = mx;
+#pragma unroll
+            for (int u = 0; u < kStageRegs; u++) {
+                const int p = lane + 32 * u;
+                if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], mx - 1023);
+            }
+        }
+    } else {
+        const int pstep = nth / L;
+        const int U = (ns + pstep - 1) / pstep;
+        const int l = tid % L, q0 = tid / L;
+        double v[kStageRegs];
+        int mx = 0;
+        if (l < nl) {
+            const double* src = f + base_in[l];
+#pragma unroll
+            for (int u = 0; u < kStageRegs; u++) {
+                const int p = q0 + pstep * u;
+                v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
+                mx = max(mx, bexp(v[u]));
+            }
+            atomicMax(&lexp[l], mx);
+        }
+        __syncthreads();
+        if (l < nl) {
+            const int k = lexp[l] - 1023;
+            bad |= (unsigned)(lexp[l] == 2047);
+#pragma unroll
+            for (int u = 0; u < kStageRegs; u++) {
+                const int p = q0 + pstep * u;
+                if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], k);
+            }
+        }
+    }
+    __syncthreads();
+
+    const int t = tid % cp.Pp, l = tid / cp.Pp;
+    const bool active = (l < nl) && (t < P);
+    V* win = tile + (size_t)l * LT + t * S + H;  // row j of the chunk at win[j], -H <= j < M + H
+    V* wk = work + (size_t)l * LW + t * W;
+    const V* rt = tab + t * W;                    // banded: row tables of this chunk, rt[k * PW + j]
+
+    // ---- halo of the window: ring neighbours (periodic) or zeros (non-periodic) ----
+    if (active) {
+#pragma unroll
+        for (int h = 1; h <= H; h++) {
+            const int p = t * M - h, q = t * M + M - 1 + h;
+            if constexpr (CIRC) {
+                win[-h] = tile[main_pos(l, p < 0 ? p + ns : p)];
+                win[M - 1 + h] = tile[main_pos(l, q >= ns ? q - ns : q)];
+            } else {
+                win[-h] = p < 0 ? AR::zero() : tile[main_pos(l, p)];
+                win[M - 1 + h] = q >= ns ? AR::zero() : tile[main_pos(l, q)];
+            }
+        }
+    }
+    // ---- banded: RHS of the edge rows (explicit one-sided closures) ----
+    if constexpr (!CIRC) {
+        for (int it = tid; it < nl * ne; it += nth) {
+            const int ll = it / ne, e = it - ll * ne;
+            V acc = AR::zero();
+#pragma unroll 1
+            for (int k = 0; k < cp.tw; k++) {
+                const int idx = __ldg(cp.tidx + e * cp.tw + k);
+                acc = AR::add(acc, AR::mul(tile[main_pos(ll, idx)], AR::coef(cp.tc[e * cp.tw + k])));
+            }
+            edge[it] = AR::norm(acc);
+        }
+        __syncthreads();
+    }
+
+    V cc[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) cc[k] = AR::coef(cp.c[k]);
+    const V c0 = AR::coef(cp.c0);
+    const V a1 = AR::coef(cp.ca1), a2 = AR::coef(cp.ca2);
+    const int Pp = cp.Pp;
+
+    // ---- B: right-hand side and forward recurrence from a zero state ----
+    V s1 = AR::zero(), s2 = AR::zero();
+    if (active) {
+        const int nlo = cp.nlo, ehi = ns - cp.nhi;
+#pragma unroll 4
+        for (int j = 0; j < M; j++) {
+            V y;
+            if constexpr (CIRC) {
+                const V r = line_stencil<NP, SYM>(win + j, cc, c0);
+                y = (Q == 2) ? AR::fms2(r, a1, s1, a2, s2) : AR::fms1(r, a1, s1);
+            } else {
+                const int i = t * M + j;
+                V r;
+                if (i < nlo) r = edge[l * ne + i];
+                else if (i >= ehi) r = edge[l * ne + nlo + (i - ehi)];
+                else r = line_stencil<NP, SYM>(win + j, cc, c0);
+                r = df_mul(r, rt[j]);
+                y = (Q == 2) ? AR::fms2(r, rt[PW + j], s1, rt[2 * PW + j], s2) : AR::fms1(r, rt[PW + j], s1);
+            }
+            wk[j] = y;
+            s2 = s1;
+            s1 = y;
+        }
+    }
+    // ---- D: log-step scan of the chunk transfers (then the ring wrap, periodic) ----
+    for (int k = 0; k < cp.nsteps; k++) {
+        const unsigned dlt = 1u << k;
+        const V o1 = AR::shfl_up(s1, dlt, Pp);
+        const V o2 = (Q == 2) ? AR::shfl_up(s2, dlt, Pp) : AR::zero();
+        if (t >= (int)dlt) {
+            const F2* Fm = cp.fscan + ((size_t)t * kMaxSteps + k) * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(s1, AR::coef(Fm[0]), o1, AR::coef(Fm[1]), o2);
+                const V n2 = AR::mac2(s2, AR::coef(Fm[2]), o1, AR::coef(Fm[3]), o2);
+                s1 = n1;
+                s2 = n2;
+            } else {
+                s1 = AR::mac1(s1, AR::coef(Fm[0]), o1);
+            }
+        }
+    }
+    V i1 = AR::shfl_up(s1, 1, Pp);
+    V i2 = (Q == 2) ? AR::shfl_up(s2, 1, Pp) : AR::zero();
+    if (t == 0) {
+        i1 = AR::zero();
+        i2 = AR::zero();
+    }
+    if constexpr (CIRC) {
+        const V E1 = AR::shfl_idx(s1, P - 1, Pp);
+        const V E2 = (Q == 2) ? AR::shfl_idx(s2, P - 1, Pp) : AR::zero();
+        if (t < P) {
+            const F2* Wm = cp.fwrap + (size_t)t * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(i1, AR::coef(Wm[0]), E1, AR::coef(Wm[1]), E2);
+                const V n2 = AR::mac2(i2, AR::coef(Wm[2]), E1, AR::coef(Wm[3]), E2);
+                i1 = n1;
+                i2 = n2;
+            } else {
+                i1 = AR::mac1(i1, AR::coef(Wm[0]), E1);
+            }
+        }
+    }
+    // ---- E+F: forward correction and backward recurrence from a zero state ----
+    V u1 = AR::zero(), u2 = AR::zero();
+    if (active) {
+#pragma unroll 4
+        for (int j = M - 1; j >= 0; j--) {
+            V p1, p2, b1 = a1, b2 = a2;
+            if constexpr (CIRC) {
+                p1 = tab[2 * j];
+                p2 = tab[2 * j + 1];
+            } else {
+                p1 = rt[5 * PW + j];
+                p2 = rt[6 * PW + j];
+                b1 = rt[3 * PW + j];
+                b2 = rt[4 * PW + j];
+            }
+            const V y = (Q == 2) ? AR::mac2(wk[j], p1, i1, p2, i2) : AR::mac1(wk[j], p1, i1);
+            const V x = (Q == 2) ? AR::fms2(y, b1, u1, b2, u2) : AR::fms1(y, b1, u1);
+            wk[j] = x;
+            u2 = u1;
+            u1 = x;
+        }
+    }
+    // ---- G: reverse scan (then the ring wrap, periodic) ----
+    for (int k = 0; k < cp.nsteps; k++) {
+        const unsigned dlt = 1u << k;
+        const V o1 = AR::shfl_down(u1, dlt, Pp);
+        const V o2 = (Q == 2) ? AR::shfl_down(u2, dlt, Pp) : AR::zero();
+        if (t + (int)dlt < Pp) {
+            const F2* Bm = cp.bscan + ((size_t)t * kMaxSteps + k) * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(u1, AR::coef(Bm[0]), o1, AR::coef(Bm[1]), o2);
+                const V n2 = AR::mac2(u2, AR::coef(Bm[2]), o1, AR::coef(Bm[3]), o2);
+                u1 = n1;
+                u2 = n2;
+            } else {
+                u1 = AR::mac1(u1, AR::coef(Bm[0]), o1);
+            }
+        }
+    }
+    V j1 = AR::shfl_down(u1, 1, Pp);
+    V j2 = (Q == 2) ? AR::shfl_down(u2, 1, Pp) : AR::zero();
+    if (t >= P - 1) {
+        j1 = AR::zero();
+        j2 = AR::zero();
+    }
+    if constexpr (CIRC) {
+        const V F1 = AR::shfl_idx(u1, 0, Pp);
+        const V F2v = (Q == 2) ? AR::shfl_idx(u2, 0, Pp) : AR::zero();
+        if (t < P) {
+            const F2* Wm = cp.bwrap + (size_t)t * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(j1, AR::coef(Wm[0]), F1, AR::coef(Wm[1]), F2v);
+                const V n2 = AR::mac2(j2, AR::coef(Wm[2]), F1, AR::coef(Wm[3]), F2v);
+                j1 = n1;
+                j2 = n2;
+            } else {
+                j1 = AR::mac1(j1, AR::coef(Wm[0]), F1);
+            }
+        }
+    }
+    // ---- H+I: backward correction, residual form, FP64 assembly (in place) ----
+    auto corrected = [&](int j) -> V {
+        V q1, q2;
+        if constexpr (CIRC) {
+            q1 = tab[2 * M + 2 * (M - 1 - j)];
+            q2 = tab[2 * M + 2 * (M - 1 - j) + 1];
+        } else {
+            q1 = rt[7 * PW + j];
+            q2 = rt[8 * PW + j];
+        }
+        return (Q == 2) ? AR::mac2(wk[j], q1, j1, q2, j2) : AR::mac1(wk[j], q1, j1);
+    };
+    if (active) {
+        double* wio = reinterpret_cast<double*>(wk);
+        const int kl = lexp[l] - 1023;
+        if (kl >= -800 && kl <= 800) {
+            const unsigned kadd = (unsigned)(896 + kl) << 20;
+#pragma unroll 4
+            for (int j = 0; j < M; j++) {
+                V x = corrected(j);
+                if (cp.resid) x = df_sub(win[j], x);
+                wio[j] = df_to_double_kadd(x, kadd);
+            }
+        } else {
+#pragma unroll 1
+            for (int j = 0; j < M; j++) {
+                V x = corrected(j);
+                if (cp.resid) x = AR::norm(df_sub(win[j], x));
+                wio[j] = AR::store_scaled(x, kl);
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- J: coalesced stores ----
+    const double* wd = reinterpret_cast<const double*>(work);
+    auto out_pos = [&](int ll, int p) -> int { return ll * LW + (p / M) * W + (p % M); };
+    if (ls.op == 1) {
+        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+        for (int ll = warp; ll < nl; ll += nw) {
+            double* o = out + base_out[ll];
+            for (int p = lane; p < cp.nout; p += 32) o[p] = wd[out_pos(ll, p < ns ? p : p - ns)];
+        }
+    } else {
+        const int ll = tid % L, pstep = nth / L;
+        if (ll < nl) {
+            double* o = out + base_out[ll];
+            for (int p = tid / L; p < cp.nout; p += pstep) o[(long)p * ls.op] = wd[out_pos(ll, p < ns ? p : p - ns)];
+        }
+    }
+    if (bad) atomicOr(status, 1u);
+}
+
+template <bool CIRC, int NP>
+size_t line_smem(const StencilParams& c) {
+    using Lay = LineLayout<kLineM, NP>;
+    const int PW = c.P * Lay::W;
+    const size_t tabs = CIRC ? 4 * (size_t)kLineM : kRowTables * (size_t)PW;
+    const size_t edges = CIRC ? 0 : (size_t)c.L * (c.nlo + c.nhi);
+    return sizeof(dfv) * (tabs + (size_t)c.L * line_stride(c.P * Lay::S) + (size_t)c.L * line_stride(PW) + edges);
+}
+
+template <int Q, int NP, bool SYM, bool CIRC>
+int launch_line_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
+                  cudaStream_t s) {
+    constexpr int NT = CIRC ? kLineThreadsCirc : kLineThreadsBand;
+    const long blocks = (ls.nlines + c.L - 1) / c.L;
+    const size_t smem = line_smem<CIRC, NP>(c);
+    auto kern = k_line<Q, NP, SYM, CIRC, kLineM, NT>;
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return PS_ECUDA;
+    }
+    kern<<<(unsigned)blocks, NT, smem, s>>>(c, (const double*)f, (double*)out, ls, status);
+    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+}
+
+}  // namespace pade
