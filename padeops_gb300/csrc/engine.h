@@ -56,6 +56,8 @@ enum LineShape : int {
 };
 
 struct StencilParams {
+    int M;            // chunk length (16 or 32)
+    int alias;        // work rows overwrite the input window (operators without residual form)
     int ns, nout, P, Pp, nsteps, L, resid;
     int circ;         // circulant line (ring wrap, constant coefficients)
     int nlo, nhi, tw; // banded: edge rows at both ends, taps per edge row

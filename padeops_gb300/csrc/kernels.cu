@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "chunk_kernel.cuh"
@@ -172,6 +173,88 @@ int DevicePlan::upload(const HostPlan& hp) {
             o_pb[v] = A.put(pb.data(), pb.size() * sizeof(F2));
         }
     }
+    // fixed-stencil kernel: whole chunks, pairs at +-1..NP, one sign; banded lines also need
+    // edge rows covering the stencil's reach at both ends
+    line_shape_ = SHAPE_NONE;
+    size_t o_lk[6] = {0, 0, 0, 0, 0, 0};
+    if (cok_ && ch_.M == kLineM && d.m == d.ns && d.ns % kLineM == 0 && d.ns <= 512 && ch_.P <= kMaxLanes &&
+        (ch_.Q == 1 || ch_.Q == 2) && (ch_.circ || d.nout == d.ns)) {
+        const int np = ch_.npair;
+        bool ok = np >= 1 && np <= kMaxPairs;
+        bool seen[kMaxPairs + 1] = {};
+        int sgn = 0;
+        StencilParams cc{};
+        for (int k = 0; k < np && ok; k++) {
+            const int o = ch_.pair_op[k];
+            if (o < 1 || o > np || ch_.pair_om[k] != -o || seen[o]) {
+                ok = false;
+                break;
+            }
+            seen[o] = true;
+            cc.c[o - 1] = split(ch_.pair_c[k] * cg);
+            if (sgn == 0) sgn = ch_.pair_sign[k];
+            else if (sgn != ch_.pair_sign[k]) ok = false;
+        }
+        if (ch_.has_center && (ch_.center_off != 0 || sgn < 0)) ok = false;
+        if (!ch_.circ && (ch_.nlo < np || ch_.nhi < np || ch_.nlo + ch_.nhi > 32)) ok = false;
+        int shape = SHAPE_NONE;
+        if (ok) {
+            if (ch_.Q == 1 && np == 2) shape = sgn < 0 ? SHAPE_T2A : SHAPE_T2S;
+            else if (ch_.Q == 2 && np == 3) shape = sgn < 0 ? SHAPE_P3A : SHAPE_P3S;
+            else if (ch_.Q == 2 && np == 4 && sgn > 0) shape = SHAPE_P4S;
+        }
+        // residual-form operators keep the input beside the work rows (chunks of 16); the
+        // others overwrite their input window and take chunks of 32 rows where they fit
+        const bool alias = !ch_.resid;
+        if (alias == (shape == SHAPE_P4S)) shape = SHAPE_NONE;  // instantiated pairings only
+        int Ml = kLineM;
+        if (alias && ch_.circ && d.ns % 32 == 0) Ml = 32;
+        if (const char* e = std::getenv("PADE_LINE_CHUNK")) {  // tuning override: 16, 32 or 64
+            const int v = std::atoi(e);
+            if (v == 16 || (v == 32 && alias && d.ns % 32 == 0) || (v == 64 && alias && ch_.circ && d.ns % 64 == 0))
+                Ml = v;
+        }
+        ChunkPlanHost c32;
+        const ChunkPlanHost* cl = &ch_;
+        if (shape != SHAPE_NONE && Ml != ch_.M) {
+            if (build_chunk_plan(hp, Ml, c32) == PS_OK && c32.ok) {
+                cl = &c32;
+                auto put = [&](const std::vector<double>& src) {
+                    std::vector<F2> o(src.size());
+                    for (size_t k = 0; k < src.size(); k++) o[k] = split(src[k]);
+                    return A.put(o.data(), o.size() * sizeof(F2));
+                };
+                o_lk[0] = put(c32.fscan);
+                o_lk[1] = put(c32.bscan);
+                o_lk[2] = put(c32.fwrap);
+                o_lk[3] = put(c32.bwrap);
+                o_lk[4] = put(c32.phf);
+                o_lk[5] = put(c32.phb);
+            } else {
+                Ml = ch_.M;
+            }
+        }
+        if (shape != SHAPE_NONE) {
+            cc.M = Ml;
+            cc.alias = alias ? 1 : 0;
+            cc.ns = cl->ns;
+            cc.nout = cl->nout;
+            cc.P = cl->P;
+            cc.Pp = cl->Pp;
+            cc.nsteps = cl->nsteps;
+            cc.L = (ch_.circ ? kLineThreadsCirc : kLineThreadsBand) / cl->Pp;
+            cc.resid = ch_.resid;
+            cc.circ = ch_.circ;
+            cc.nlo = ch_.circ ? 0 : ch_.nlo;
+            cc.nhi = ch_.circ ? 0 : ch_.nhi;
+            cc.tw = ch_.tw;
+            cc.c0 = ch_.has_center ? split(ch_.center_c * cg) : F2{0.0f, 0.0f};
+            cc.ca1 = split(ch_.circ ? ch_.rc[1] : 0.0);
+            cc.ca2 = split(ch_.circ ? ch_.rc[2] : 0.0);
+            cline_ = cc;
+            line_shape_ = shape;
+        }
+    }
     const cudaError_t me = cudaMalloc(&dev_, A.host.size());
     if (me != cudaSuccess) {
         dev_ = nullptr;
@@ -252,62 +335,18 @@ int DevicePlan::upload(const HostPlan& hp) {
         }
     }
 
-    // fixed-stencil kernel: whole chunks, pairs at +-1..NP, one sign; banded lines also need
-    // edge rows covering the stencil's reach at both ends
-    line_shape_ = SHAPE_NONE;
-    if (cok_ && ch_.M == kLineM && d.m == d.ns && d.ns % kLineM == 0 && d.ns <= 512 && ch_.P <= kMaxLanes &&
-        (ch_.Q == 1 || ch_.Q == 2) && (ch_.circ || d.nout == d.ns)) {
-        const int np = ch_.npair;
-        bool ok = np >= 1 && np <= kMaxPairs;
-        bool seen[kMaxPairs + 1] = {};
-        int sgn = 0;
-        StencilParams cc{};
-        for (int k = 0; k < np && ok; k++) {
-            const int o = ch_.pair_op[k];
-            if (o < 1 || o > np || ch_.pair_om[k] != -o || seen[o]) {
-                ok = false;
-                break;
-            }
-            seen[o] = true;
-            cc.c[o - 1] = cdf_.pair_c[k];
-            if (sgn == 0) sgn = ch_.pair_sign[k];
-            else if (sgn != ch_.pair_sign[k]) ok = false;
-        }
-        if (ch_.has_center && (ch_.center_off != 0 || sgn < 0)) ok = false;
-        if (!ch_.circ && (ch_.nlo < np || ch_.nhi < np || ch_.nlo + ch_.nhi > 32)) ok = false;
-        int shape = SHAPE_NONE;
-        if (ok) {
-            if (ch_.Q == 1 && np == 2) shape = sgn < 0 ? SHAPE_T2A : SHAPE_T2S;
-            else if (ch_.Q == 2 && np == 3) shape = sgn < 0 ? SHAPE_P3A : SHAPE_P3S;
-            else if (ch_.Q == 2 && np == 4 && sgn > 0) shape = SHAPE_P4S;
-        }
-        if (shape != SHAPE_NONE) {
-            cc.ns = ch_.ns;
-            cc.nout = ch_.nout;
-            cc.P = ch_.P;
-            cc.Pp = ch_.Pp;
-            cc.nsteps = ch_.nsteps;
-            cc.L = (ch_.circ ? kLineThreadsCirc : kLineThreadsBand) / ch_.Pp;
-            cc.resid = ch_.resid;
-            cc.circ = ch_.circ;
-            cc.nlo = ch_.circ ? 0 : ch_.nlo;
-            cc.nhi = ch_.circ ? 0 : ch_.nhi;
-            cc.tw = ch_.tw;
-            cc.c0 = ch_.has_center ? cdf_.center_c : F2{0.0f, 0.0f};
-            cc.ca1 = cdf_.ca1;
-            cc.ca2 = cdf_.ca2;
-            cc.tidx = cdf_.tidx;
-            cc.tc = cdf_.tc;
-            cc.rc = cdf_.rc;
-            cc.fscan = cdf_.fscan;
-            cc.bscan = cdf_.bscan;
-            cc.fwrap = cdf_.fwrap;
-            cc.bwrap = cdf_.bwrap;
-            cc.phf = cdf_.phf;
-            cc.phb = cdf_.phb;
-            cline_ = cc;
-            line_shape_ = shape;
-        }
+    if (line_shape_ != SHAPE_NONE) {
+        unsigned char* lb = base;
+        const bool own = cline_.M != ch_.M;  // separate chunk tables for the line kernel
+        cline_.tidx = cdf_.tidx;
+        cline_.tc = cdf_.tc;
+        cline_.rc = cdf_.rc;
+        cline_.fscan = own ? (const F2*)(lb + o_lk[0]) : cdf_.fscan;
+        cline_.bscan = own ? (const F2*)(lb + o_lk[1]) : cdf_.bscan;
+        cline_.fwrap = own ? (const F2*)(lb + o_lk[2]) : cdf_.fwrap;
+        cline_.bwrap = own ? (const F2*)(lb + o_lk[3]) : cdf_.bwrap;
+        cline_.phf = own ? (const F2*)(lb + o_lk[4]) : cdf_.phf;
+        cline_.phb = own ? (const F2*)(lb + o_lk[5]) : cdf_.phb;
     }
     return PS_OK;
 }

@@ -15,7 +15,10 @@
 //     out chunk by chunk with an odd stride (conflict-free, like the work rows);
 //   * a shift-and-assemble FP64 store without range checks for line scales within
 //     2^+-800 (the checked path otherwise).
-// Lines hold a whole number of chunks (ns = P * M), at most 512 rows.
+// Operators without residual form write their work rows over the input window (row j's
+// value at window row j - H, which later rows no longer read), halving the shared memory
+// per line.  Lines hold a whole number of chunks (ns = P * M, M = 16 or 32), at most 512
+// rows.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -49,11 +52,17 @@ __device__ __forceinline__ dfv line_stencil(const dfv* __restrict__ p, const dfv
 // Line stride in 8-byte words, made odd.
 __host__ __device__ constexpr int line_stride(int n) { return n % 2 == 0 ? n + 1 : n; }
 
+// Resident CTAs per SM the register allocation is sized for (what shared memory allows):
+// lines with the input window reused and chunks of 16 hold about 3 KB per line.
+__host__ __device__ constexpr int line_min_blocks(bool circ, int m, bool alias) {
+    return circ ? ((alias && m == 16) ? 7 : (alias && m == 64) ? 3 : 5) : ((alias && m == 16) ? 3 : 2);
+}
+
 // Number of per-row tables of a banded line: g a1 a2 b1 b2 pf1 pf2 pb1 pb2.
 constexpr int kRowTables = 9;
 
-template <int Q, int NP, bool SYM, bool CIRC, int M, int NT>
-__global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
+template <int Q, int NP, bool SYM, bool CIRC, int M, int NT, bool ALIAS>
+__global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
     k_line(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
            unsigned* __restrict__ status) {
     using AR = ArDF;
@@ -68,8 +77,10 @@ __global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
     const int ne = cp.nlo + cp.nhi;            // edge rows (banded)
     V* tab = reinterpret_cast<V*>(smem_raw);   // circulant: phf, phb (M x 2 each); banded: 9 x PW
     V* tile = tab + (CIRC ? 4 * M : kRowTables * PW);  // L lines x (P windows x S), stride LT
+    // separate work rows (residual form); otherwise chunk row j's work value overwrites
+    // window row j - H, which no later row of the chunk reads
     V* work = tile + (size_t)L * LT;                    // L lines x (P chunks x W), stride LW
-    V* edge = work + (size_t)L * LW;                    // banded: L x ne edge-row RHS values
+    V* edge = work + (ALIAS ? 0 : (size_t)L * LW);      // banded: L x ne edge-row RHS values
     __shared__ int lexp[NT];
     __shared__ long base_in[NT], base_out[NT];
 
@@ -126,6 +137,41 @@ __global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
                 if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], mx - 1023);
             }
         }
+    } else if ((ns + nth / L - 1) / (nth / L) > kStageRegs) {
+        // more rows per thread than staging registers: raw FP64 first, split in place
+        const int pstep = nth / L;
+        const int l = tid % L, q0 = tid / L;
+        double* raw = reinterpret_cast<double*>(tile);
+        int mx = 0;
+        if (l < nl) {
+            const double* src = f + base_in[l];
+            for (int p0 = q0; p0 < ns; p0 += pstep * kLoadUnroll) {
+                double v[kLoadUnroll];
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int p = p0 + pstep * u;
+                    v[u] = p < ns ? __ldg(src + (long)p * ls.fp) : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int p = p0 + pstep * u;
+                    if (p < ns) {
+                        raw[main_pos(l, p)] = v[u];
+                        mx = max(mx, bexp(v[u]));
+                    }
+                }
+            }
+            atomicMax(&lexp[l], mx);
+        }
+        __syncthreads();
+        if (l < nl) {
+            const int k = lexp[l] - 1023;
+            bad |= (unsigned)(lexp[l] == 2047);
+            for (int p = q0; p < ns; p += pstep) {
+                const int ps = main_pos(l, p);
+                tile[ps] = df_from_double_shift(raw[ps], k);
+            }
+        }
     } else {
         const int pstep = nth / L;
         const int U = (ns + pstep - 1) / pstep;
@@ -158,7 +204,7 @@ __global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
     const int t = tid % cp.Pp, l = tid / cp.Pp;
     const bool active = (l < nl) && (t < P);
     V* win = tile + (size_t)l * LT + t * S + H;  // row j of the chunk at win[j], -H <= j < M + H
-    V* wk = work + (size_t)l * LW + t * W;
+    V* wk = ALIAS ? win - H : work + (size_t)l * LW + t * W;
     const V* rt = tab + t * W;                    // banded: row tables of this chunk, rt[k * PW + j]
 
     // ---- halo of the window: ring neighbours (periodic) or zeros (non-periodic) ----
@@ -339,14 +385,14 @@ __global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
 #pragma unroll 4
             for (int j = 0; j < M; j++) {
                 V x = corrected(j);
-                if (cp.resid) x = df_sub(win[j], x);
+                if (!ALIAS && cp.resid) x = df_sub(win[j], x);
                 wio[j] = df_to_double_kadd(x, kadd);
             }
         } else {
 #pragma unroll 1
             for (int j = 0; j < M; j++) {
                 V x = corrected(j);
-                if (cp.resid) x = AR::norm(df_sub(win[j], x));
+                if (!ALIAS && cp.resid) x = AR::norm(df_sub(win[j], x));
                 wio[j] = AR::store_scaled(x, kl);
             }
         }
@@ -354,8 +400,10 @@ __global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
     __syncthreads();
 
     // ---- J: coalesced stores ----
-    const double* wd = reinterpret_cast<const double*>(work);
-    auto out_pos = [&](int ll, int p) -> int { return ll * LW + (p / M) * W + (p % M); };
+    const double* wd = reinterpret_cast<const double*>(ALIAS ? tile : work);
+    auto out_pos = [&](int ll, int p) -> int {
+        return ALIAS ? ll * LT + (p / M) * S + (p % M) : ll * LW + (p / M) * W + (p % M);
+    };
     if (ls.op == 1) {
         const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
         for (int ll = warp; ll < nl; ll += nw) {
@@ -372,22 +420,23 @@ __global__ void __launch_bounds__(NT, CIRC ? 5 : 2)
     if (bad) atomicOr(status, 1u);
 }
 
-template <bool CIRC, int NP>
+template <bool CIRC, int NP, int M, bool ALIAS>
 size_t line_smem(const StencilParams& c) {
-    using Lay = LineLayout<kLineM, NP>;
+    using Lay = LineLayout<M, NP>;
     const int PW = c.P * Lay::W;
-    const size_t tabs = CIRC ? 4 * (size_t)kLineM : kRowTables * (size_t)PW;
+    const size_t tabs = CIRC ? 4 * (size_t)M : kRowTables * (size_t)PW;
     const size_t edges = CIRC ? 0 : (size_t)c.L * (c.nlo + c.nhi);
-    return sizeof(dfv) * (tabs + (size_t)c.L * line_stride(c.P * Lay::S) + (size_t)c.L * line_stride(PW) + edges);
+    const size_t work = ALIAS ? 0 : (size_t)c.L * line_stride(PW);
+    return sizeof(dfv) * (tabs + (size_t)c.L * line_stride(c.P * Lay::S) + work + edges);
 }
 
-template <int Q, int NP, bool SYM, bool CIRC>
+template <int Q, int NP, bool SYM, bool CIRC, int M, bool ALIAS>
 int launch_line_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                   cudaStream_t s) {
     constexpr int NT = CIRC ? kLineThreadsCirc : kLineThreadsBand;
     const long blocks = (ls.nlines + c.L - 1) / c.L;
-    const size_t smem = line_smem<CIRC, NP>(c);
-    auto kern = k_line<Q, NP, SYM, CIRC, kLineM, NT>;
+    const size_t smem = line_smem<CIRC, NP, M, ALIAS>(c);
+    auto kern = k_line<Q, NP, SYM, CIRC, M, NT, ALIAS>;
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return PS_ECUDA;
@@ -395,5 +444,45 @@ int launch_line_t(const StencilParams& c, const void* f, void* out, const LineSe
     kern<<<(unsigned)blocks, NT, smem, s>>>(c, (const double*)f, (double*)out, ls, status);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
+
+// Dispatch over the instantiated shapes: residual-form cf90 (P4S) with chunks of 16 and
+// separate work rows; the others with the input window reused and chunks of 16 or 32.
+template <bool CIRC>
+int launch_line_shapes(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                       unsigned* status, cudaStream_t s) {
+    const bool m32 = c.M == 32;
+    if constexpr (CIRC) {
+        if (c.M == 64) {
+            switch (shape) {
+                case SHAPE_T2A: return launch_line_t<1, 2, false, true, 64, true>(c, f, out, ls, status, s);
+                case SHAPE_T2S: return launch_line_t<1, 2, true, true, 64, true>(c, f, out, ls, status, s);
+                case SHAPE_P3A: return launch_line_t<2, 3, false, true, 64, true>(c, f, out, ls, status, s);
+                case SHAPE_P3S: return launch_line_t<2, 3, true, true, 64, true>(c, f, out, ls, status, s);
+                default: return PS_ENOTSUP;
+            }
+        }
+    }
+    switch (shape) {
+        case SHAPE_T2A:
+            return m32 ? launch_line_t<1, 2, false, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<1, 2, false, CIRC, 16, true>(c, f, out, ls, status, s);
+        case SHAPE_T2S:
+            return m32 ? launch_line_t<1, 2, true, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<1, 2, true, CIRC, 16, true>(c, f, out, ls, status, s);
+        case SHAPE_P3A:
+            return m32 ? launch_line_t<2, 3, false, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<2, 3, false, CIRC, 16, true>(c, f, out, ls, status, s);
+        case SHAPE_P3S:
+            return m32 ? launch_line_t<2, 3, true, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<2, 3, true, CIRC, 16, true>(c, f, out, ls, status, s);
+        case SHAPE_P4S: return launch_line_t<2, 4, true, CIRC, 16, false>(c, f, out, ls, status, s);
+        default: return PS_ENOTSUP;
+    }
+}
+
+int launch_line_circ(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                     unsigned* status, cudaStream_t s);
+int launch_line_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                     unsigned* status, cudaStream_t s);
 
 }  // namespace pade
