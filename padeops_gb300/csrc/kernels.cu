@@ -204,15 +204,15 @@ int DevicePlan::upload(const HostPlan& hp) {
             else if (ch_.Q == 2 && np == 4 && sgn > 0) shape = SHAPE_P4S;
         }
         // residual-form operators keep the input beside the work rows (chunks of 16); the
-        // others overwrite their input window and take chunks of 32 rows where they fit
+        // others overwrite their input window and take chunks of 32 rows on periodic lines
+        // (16 on banded lines: measured faster there)
         const bool alias = !ch_.resid;
         if (alias == (shape == SHAPE_P4S)) shape = SHAPE_NONE;  // instantiated pairings only
         int Ml = kLineM;
         if (alias && ch_.circ && d.ns % 32 == 0) Ml = 32;
-        if (const char* e = std::getenv("PADE_LINE_CHUNK")) {  // tuning override: 16, 32 or 64
+        if (const char* e = std::getenv("PADE_LINE_CHUNK")) {  // tuning override: 16 or 32
             const int v = std::atoi(e);
-            if (v == 16 || (v == 32 && alias && d.ns % 32 == 0) || (v == 64 && alias && ch_.circ && d.ns % 64 == 0))
-                Ml = v;
+            if (v == 16 || (v == 32 && alias && d.ns % 32 == 0)) Ml = v;
         }
         ChunkPlanHost c32;
         const ChunkPlanHost* cl = &ch_;

@@ -55,7 +55,7 @@ __host__ __device__ constexpr int line_stride(int n) { return n % 2 == 0 ? n + 1
 // Resident CTAs per SM the register allocation is sized for (what shared memory allows):
 // lines with the input window reused and chunks of 16 hold about 3 KB per line.
 __host__ __device__ constexpr int line_min_blocks(bool circ, int m, bool alias) {
-    return circ ? ((alias && m == 16) ? 7 : (alias && m == 64) ? 3 : 5) : ((alias && m == 16) ? 3 : 2);
+    return circ ? ((alias && m == 16) ? 7 : 5) : ((alias && m == 16) ? 3 : 2);
 }
 
 // Number of per-row tables of a banded line: g a1 a2 b1 b2 pf1 pf2 pb1 pb2.
@@ -451,17 +451,6 @@ template <bool CIRC>
 int launch_line_shapes(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                        unsigned* status, cudaStream_t s) {
     const bool m32 = c.M == 32;
-    if constexpr (CIRC) {
-        if (c.M == 64) {
-            switch (shape) {
-                case SHAPE_T2A: return launch_line_t<1, 2, false, true, 64, true>(c, f, out, ls, status, s);
-                case SHAPE_T2S: return launch_line_t<1, 2, true, true, 64, true>(c, f, out, ls, status, s);
-                case SHAPE_P3A: return launch_line_t<2, 3, false, true, 64, true>(c, f, out, ls, status, s);
-                case SHAPE_P3S: return launch_line_t<2, 3, true, true, 64, true>(c, f, out, ls, status, s);
-                default: return PS_ENOTSUP;
-            }
-        }
-    }
     switch (shape) {
         case SHAPE_T2A:
             return m32 ? launch_line_t<1, 2, false, CIRC, 32, true>(c, f, out, ls, status, s)
