@@ -22,6 +22,7 @@
 // accumulators with tcgen05.ld (a warp per 32 rows) and stores FP64, coalesced along x.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -335,9 +336,302 @@ __global__ void __launch_bounds__(NTHR) k_dense_tf32(const double* __restrict__ 
     if (warp == 0) tmem_dealloc(tmem, ncols);
 }
 
+// ------------------------------------------------------------------------------------
+// k_dense_ws: persistent, warp-specialised pipeline (n_out <= 256, two stages)
+// ------------------------------------------------------------------------------------
+// Each CTA walks one stream of (tile, K chunk) items over its 128-line tiles.
+//  * Warps 0..15 produce: they keep the lines of the next two items in flight in
+//    registers while they split the current one into TF32 pairs and store it into the
+//    stage's B tile, then arrive on the stage's "full" barrier.
+//  * Warp 16 (one lane) issues the MMAs: it waits for "full", issues the chunk's MMAs and
+//    commits them to the stage's "empty" barrier; after a tile's last chunk it commits to
+//    the accumulator's "acc full" barrier.
+//  * Warp 17 (one lane) loads D: as soon as "empty" releases a stage it fills the stage's
+//    A tiles with the item's D chunk, one bulk copy of D's pre-swizzled image completing
+//    on the stage's "full" barrier by transaction bytes.  (Issuing MMAs can block the
+//    issuing thread, so the copies have a thread of their own.)
+//  * Warps 18..21 (one per TMEM lane quadrant) read the accumulators (tcgen05.ld), store
+//    FP64 and arrive on "acc empty"; two TMEM accumulators let a tile's epilogue run while
+//    the next tile computes.
+// Waits are bounded: a timeout sets the error word and the abort flag, every role runs out
+// its loops without waiting, the loader waits (bounded) for the copies it issued, and
+// TMEM is freed.
+constexpr int WS_PROD_WARPS = 16;
+constexpr int WS_EPI_WARPS = 4;  // one per TMEM lane quadrant
+constexpr int WS_STAGES = 2;
+constexpr int WS_FPT = NT * 16 / (WS_PROD_WARPS * 32);  // double2 per producer thread and item
+constexpr uint32_t kBulkPiece = 16384;                  // bytes per bulk copy
+// warps: producers 0..15, MMA issuer 16, D loader 17, epilogue 18..21
+constexpr int WS_THREADS = (WS_PROD_WARPS + 2 + WS_EPI_WARPS) * 32;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(su32(bar))
+                 : "memory");
+}
+
+template <bool XL>
+__global__ void __launch_bounds__(WS_THREADS, 1)
+    k_dense_ws(const double* __restrict__ f, double* __restrict__ out, const float* __restrict__ Dimg, int nin,
+               int nout, const LineSet ls, long ntiles, unsigned* __restrict__ rangeflag) {
+    constexpr int NACC = 2;  // accumulator buffers: the epilogue of a tile overlaps the next
+    const long nlines = ls.nlines;
+    extern __shared__ uint8_t dsm_raw[];
+    __shared__ uint64_t full[WS_STAGES], empty[WS_STAGES], accf[NACC], acce[NACC];
+    __shared__ uint32_t tslot;
+    __shared__ volatile int abort_flag;
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(dsm_raw) + 1023) & ~(uintptr_t)1023);
+    const uint32_t a_bytes = (uint32_t)nout * 128, b_bytes = (uint32_t)NT * 128;
+    const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const bool producer = warp < WS_PROD_WARPS;
+    const bool control = warp == WS_PROD_WARPS && lane == 0;     // MMA issuer
+    const bool loader = warp == WS_PROD_WARPS + 1 && lane == 0;  // D copies
+    const bool epi_warp = warp > WS_PROD_WARPS + 1;
+    const uint32_t ncols = (uint32_t)(nout * NACC);
+    const int nchunks = nin / KC;
+    if (warp == 0) tmem_alloc(&tslot, ncols);
+    if (tid == 0) {
+        for (int s = 0; s < WS_STAGES; s++) {
+            mbar_init(&full[s], WS_PROD_WARPS + 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < NACC; b++) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], WS_EPI_WARPS);
+        }
+        fence_barrier_init();
+        abort_flag = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tslot;
+    unsigned bad = 0;
+    auto stage_ptr = [&](int s) { return base + (size_t)s * stage_bytes; };
+    auto wait = [&](uint64_t* bar, unsigned parity) {
+        if (abort_flag) return;
+        if (!mbar_wait_bounded(bar, parity)) abort_flag = 1;
+    };
+    const long my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const long nitems = my_tiles * nchunks;
+    auto tile_of = [&](long it) { return blockIdx.x + it * gridDim.x; };
+    long issued[WS_STAGES] = {-1, -1};  // loader: last item whose D copy went to each stage
+
+    // x lines: R[i] holds two consecutive K values of one line (16-byte loads).  y, z lines:
+    // thread t takes line t / 4 and K = 4 kq + t % 4 for kq = 2i, 2i + 1, so that a warp's
+    // stores cover 8 lines x 4 K values of one 16-byte chunk: all 32 banks of the swizzled
+    // tile (consecutive lines on a K index would share 8 banks); its loads read 64-byte row
+    // segments of 8 consecutive lines.
+    auto load_F = [&](long l0, int c, double2* R) {
+#pragma unroll
+        for (int i = 0; i < WS_FPT; i++) {
+            if (XL) {
+                const int idx = tid + i * WS_PROD_WARPS * 32;
+                const int ln = idx >> 4, q = idx & 15;
+                const long line = l0 + ln;
+                R[i] = line < nlines ? __ldg(reinterpret_cast<const double2*>(f + line * ls.fa + c * KC + 2 * q))
+                                     : make_double2(0.0, 0.0);
+            } else {
+                const int ln = tid >> 2, k0 = 8 * i + (tid & 3);
+                const long line = l0 + ln;
+                if (line < nlines) {
+                    const long a = line % ls.na, b = line / ls.na;
+                    const double* src = f + a * ls.fa + b * ls.fb + (long)(c * KC + k0) * ls.fp;
+                    R[i] = make_double2(__ldg(src), __ldg(src + 4 * ls.fp));
+                } else {
+                    R[i] = make_double2(0.0, 0.0);
+                }
+            }
+        }
+    };
+    auto load_item = [&](long q, double2* R) {
+        if (q < nitems) load_F(tile_of(q / nchunks) * NT, (int)(q % nchunks), R);
+    };
+    auto store_F = [&](int s, const double2* R) {
+        uint8_t* Bh = stage_ptr(s) + 2 * a_bytes;
+        uint8_t* Bl = Bh + b_bytes;
+#pragma unroll
+        for (int i = 0; i < WS_FPT; i++) {
+            float h0, lo0, h1, lo1;
+            split_tf32(R[i].x, h0, lo0, bad);
+            split_tf32(R[i].y, h1, lo1, bad);
+            if (XL) {
+                const int idx = tid + i * WS_PROD_WARPS * 32;
+                const int ln = idx >> 4, q = idx & 15;
+                const uint32_t off = swz(ln, q >> 1) + ((q & 1) << 3);
+                *reinterpret_cast<float2*>(Bh + off) = make_float2(h0, h1);
+                *reinterpret_cast<float2*>(Bl + off) = make_float2(lo0, lo1);
+            } else {
+                const int ln = tid >> 2, k0 = 8 * i + (tid & 3), k1 = k0 + 4;
+                const uint32_t o0 = swz(ln, k0 >> 2) + ((k0 & 3) << 2), o1 = swz(ln, k1 >> 2) + ((k1 & 3) << 2);
+                *reinterpret_cast<float*>(Bh + o0) = h0;
+                *reinterpret_cast<float*>(Bl + o0) = lo0;
+                *reinterpret_cast<float*>(Bh + o1) = h1;
+                *reinterpret_cast<float*>(Bl + o1) = lo1;
+            }
+        }
+    };
+    // control: D chunk c of the image into the A tiles of stage s (hi then lo, contiguous)
+    auto issue_D = [&](int c, int s) {
+        const uint8_t* src = reinterpret_cast<const uint8_t*>(Dimg) + (size_t)c * 2 * a_bytes;
+        const uint32_t dst = su32(stage_ptr(s));
+        mbar_arrive_expect_tx(&full[s], 2 * a_bytes);
+        for (uint32_t o = 0; o < 2 * a_bytes; o += kBulkPiece) {
+            const uint32_t n = min(kBulkPiece, 2 * a_bytes - o);
+            bulk_g2s(dst + o, src + o, n, &full[s]);
+        }
+    };
+    // epilogue of tile `it` from accumulator b by an epilogue warp: TMEM lane quadrant
+    // warp % 4 (rows), 16 columns (lines) per tcgen05.ld.  x lines: lanes hold consecutive
+    // rows of a line (contiguous).  y, z lines: a thread holds 16 consecutive lines of one
+    // row, contiguous when the lines do not wrap in a (na % 16 == 0): 16-byte stores.
+    const bool vec16 = !XL && ls.oa == 1 && ls.na % 16 == 0 && ls.op % 2 == 0 && ls.ob % 2 == 0 &&
+                       (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    auto epilogue = [&](long it, int b) {
+        const long l0 = tile_of(it) * NT;
+        const int lq = warp & 3;
+        for (int mh = 0; mh < nout / 128; mh++) {
+            const int row = mh * 128 + lq * 32 + lane;
+            for (int cb = 0; cb < NT / 16; cb++) {
+                uint32_t r[16];
+                tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(b * nout + mh * NT + cb * 16), r);
+                const long line0 = l0 + cb * 16;
+                if (XL) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const long line = line0 + j;
+                        if (line < nlines) out[line * ls.oa + row] = float_bits_to_double(__uint_as_float(r[j]));
+                    }
+                } else if (vec16 && line0 + 16 <= nlines) {
+                    const long a = line0 % ls.na, bb = line0 / ls.na;
+                    double* o = out + a + bb * ls.ob + (long)row * ls.op;
+#pragma unroll
+                    for (int j = 0; j < 16; j += 2)
+                        *reinterpret_cast<double2*>(o + j) = make_double2(float_bits_to_double(__uint_as_float(r[j])),
+                                                                          float_bits_to_double(__uint_as_float(r[j + 1])));
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const long line = line0 + j;
+                        if (line >= nlines) continue;
+                        const long a = line % ls.na, bb = line / ls.na;
+                        out[a * ls.oa + bb * ls.ob + (long)row * ls.op] = float_bits_to_double(__uint_as_float(r[j]));
+                    }
+                }
+            }
+        }
+    };
+
+    if (producer) {
+        double2 R0[WS_FPT], R1[WS_FPT];
+        load_item(0, R0);
+        load_item(1, R1);
+        for (long it = 0; it < my_tiles; it++) {
+            for (int c = 0; c < nchunks; c++) {
+                const long gg = it * nchunks + c;
+                const int s = (int)(gg % WS_STAGES);
+                double2 R2[WS_FPT];
+                load_item(gg + 2, R2);
+                if (gg >= WS_STAGES) wait(&empty[s], (unsigned)((gg / WS_STAGES - 1) & 1));
+                if (!abort_flag) store_F(s, R0);
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
+#pragma unroll
+                for (int i = 0; i < WS_FPT; i++) {
+                    R0[i] = R1[i];
+                    R1[i] = R2[i];
+                }
+            }
+        }
+    } else if (control) {
+        for (long it = 0; it < my_tiles; it++) {
+            const int b = (int)(it % NACC);
+            // the accumulator's previous tile has been read out
+            if (it >= NACC) wait(&acce[b], (unsigned)((it / NACC - 1) & 1));
+            tc_fence_after();
+            for (int c = 0; c < nchunks; c++) {
+                const long gg = it * nchunks + c;
+                const int s = (int)(gg % WS_STAGES);
+                wait(&full[s], (unsigned)((gg / WS_STAGES) & 1));
+                if (!abort_flag) {
+                    tc_fence_after();
+                    uint8_t* Ah = stage_ptr(s);
+                    uint8_t* Al = Ah + a_bytes;
+                    uint8_t* Bh = Al + a_bytes;
+                    uint8_t* Bl = Bh + b_bytes;
+                    for (int mh = 0; mh < nout / 128; mh++) {
+                        const uint32_t d = tmem + (uint32_t)(b * nout + mh * NT);
+#pragma unroll
+                        for (int kk = 0; kk < KC / 8; kk++) {
+                            const uint64_t ah = desc_sw128(su32(Ah + mh * 128 * 128 + kk * 32));
+                            const uint64_t al = desc_sw128(su32(Al + mh * 128 * 128 + kk * 32));
+                            const uint64_t bh = desc_sw128(su32(Bh + kk * 32));
+                            const uint64_t bl = desc_sw128(su32(Bl + kk * 32));
+                            mma_tf32(d, ah, bh, kIdesc, (c > 0 || kk > 0) ? 1u : 0u);
+                            mma_tf32(d, ah, bl, kIdesc, 1u);
+                            mma_tf32(d, al, bh, kIdesc, 1u);
+                        }
+                    }
+                    mma_commit(&empty[s]);
+                } else {
+                    mbar_arrive(&empty[s]);
+                }
+            }
+            if (!abort_flag) mma_commit(&accf[b]);
+            else mbar_arrive(&accf[b]);
+        }
+    } else if (loader) {
+        // each item's D chunk as soon as the MMAs two items back release its stage
+        for (long gn = 0; gn < nitems; gn++) {
+            const int sn = (int)(gn % WS_STAGES);
+            if (gn >= WS_STAGES) wait(&empty[sn], (unsigned)((gn / WS_STAGES - 1) & 1));
+            if (!abort_flag) {
+                issue_D((int)(gn % nchunks), sn);
+                issued[sn] = gn;
+            } else {
+                mbar_arrive(&full[sn]);  // keep the arrival count; no bytes expected
+            }
+        }
+    } else if (epi_warp) {
+        for (long it = 0; it < my_tiles; it++) {
+            const int b = (int)(it % NACC);
+            wait(&accf[b], (unsigned)((it / NACC) & 1));
+            tc_fence_after();
+            if (!abort_flag) epilogue(it, b);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[b]);
+        }
+    }
+    if (abort_flag && loader) {
+        // the copies issued: a phase cannot complete before its copy's bytes land, so wait
+        // (bounded) for the last phase of each stage that received one
+        for (int s = 0; s < WS_STAGES; s++) {
+            if (issued[s] < 0) continue;
+            unsigned k = 0;
+            while (!mbar_try_wait(&full[s], (unsigned)((issued[s] / WS_STAGES) & 1)) && ++k < kWaitLimit) {
+            }
+        }
+    }
+    if (abort_flag) atomicOr(&g_dense_err, 1u);
+    if (bad) atomicOr(rangeflag, 1u);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
 struct DenseMat {
     float* Dh = nullptr;
     float* Dl = nullptr;
+    float* Dimg = nullptr;  // per K chunk: hi then lo, nout rows of 128 bytes, swizzled as in shared memory
     int nin = 0, nout = 0;
 };
 
@@ -377,9 +671,29 @@ int dense_for(pade_op h, int opcode, int bc1, int bcn, DenseMat** out) {
         hi[i] = tf32_host(M[i]);
         lo[i] = tf32_host(M[i] - (double)hi[i]);
     }
+    // the shared-memory image of every K chunk, for one bulk copy per chunk
+    std::vector<float> img;
+    if (dm.nin % KC == 0) {
+        const int nch = dm.nin / KC;
+        img.assign((size_t)nch * 2 * dm.nout * 32, 0.0f);
+        for (int c = 0; c < nch; c++)
+            for (int hl = 0; hl < 2; hl++)
+                for (int r = 0; r < dm.nout; r++)
+                    for (int k = 0; k < KC; k++) {
+                        const size_t byte = ((size_t)c * 2 + hl) * dm.nout * 128 + (size_t)r * 128 +
+                                            (size_t)(((k >> 2) ^ (r & 7)) << 4) + (size_t)(k & 3) * 4;
+                        const size_t src = (size_t)r * dm.nin + (size_t)c * KC + k;
+                        img[byte / 4] = hl ? lo[src] : hi[src];
+                    }
+    }
     if ((rc = upload(&dm.Dh, hi)) != PS_OK) return rc;
     if ((rc = upload(&dm.Dl, lo)) != PS_OK) {
         cudaFree(dm.Dh);
+        return rc;
+    }
+    if (!img.empty() && (rc = upload(&dm.Dimg, img)) != PS_OK) {
+        cudaFree(dm.Dh);
+        cudaFree(dm.Dl);
         return rc;
     }
     auto ins = g_dense.emplace(std::make_pair((const void*)h, key), dm);
@@ -397,6 +711,7 @@ void dense_release(const void* h) {
         if (it->first.first == h) {
             cudaFree(it->second.Dh);
             cudaFree(it->second.Dl);
+            cudaFree(it->second.Dimg);
             it = g_dense.erase(it);
         } else {
             ++it;
@@ -442,6 +757,21 @@ int pade_dense_apply(pade_op h, int opcode, int dir, const double* f, double* ou
     const size_t smem = 1024 + stages * stage;
     const long blocks = (nlines + NT - 1) / NT;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (stages == 2 && D->Dimg) {
+        // persistent warp-specialised pipeline: one CTA per SM over the 128-line tiles
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+            return PS_ECUDA;
+        auto kw = dir == 1 ? k_dense_ws<true> : k_dense_ws<false>;
+        const size_t smem_ws = smem;
+        if (cudaFuncSetAttribute(kw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ws) != cudaSuccess)
+            return PS_ECUDA;
+        const long grid = std::min<long>(blocks, nsm);
+        kw<<<(unsigned)grid, WS_THREADS, smem_ws, s>>>(f, out, D->Dimg, D->nin, D->nout, ls, blocks,
+                                                                 h->status);
+        return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+    }
     auto kern = dir == 1 ? (stages == 2 ? k_dense_tf32<2, true> : k_dense_tf32<1, true>)
                          : (stages == 2 ? k_dense_tf32<2, false> : k_dense_tf32<1, false>);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

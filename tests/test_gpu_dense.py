@@ -103,3 +103,33 @@ def test_dense_rejects_unsupported():
     rc = lib.pade_dense_apply(o.handle, 1, 4, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(g.data_ptr()), 4, 1,
                               0, 0, None)
     assert rc == L.PADE_EINVAL
+
+
+@pytest.mark.parametrize("dir", [1, 2, 3])
+@pytest.mark.parametrize("n,other", [(128, (256, 160)), (256, (128, 200))])
+def test_dense_many_tiles_per_cta(dir, n, other):
+    # more 128-line tiles than SMs: each CTA of the persistent kernel runs several tiles,
+    # so the stage and accumulator hand-offs between tiles are exercised; checked against
+    # the double-float line path (itself pinned to the oracle)
+    o = P.cd10()
+    assert o.init(n, 2 * np.pi / n, True) == 0
+    shape = list(other)
+    shape.insert(dir - 1, n)
+    g = torch.Generator(device="cuda").manual_seed(11 + dir)
+    fd = torch.randn(tuple(reversed(shape)), generator=g, dtype=torch.float64, device="cuda")
+    na, nb = other
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lib = L.lib()
+    for order in (1, 2):
+        od = torch.full_like(fd, float("nan"))
+        ref = torch.empty_like(fd)
+        L.check(lib.pade_dense_apply(o.handle, order, dir, ctypes.c_void_p(fd.data_ptr()),
+                                     ctypes.c_void_p(od.data_ptr()), na, nb, 0, 0, st))
+        o.apply(order, dir, fd, ref, na, nb)
+        torch.cuda.synchronize()
+        to = ctypes.c_int()
+        L.check(lib.pade_dense_status(ctypes.byref(to)))
+        assert to.value == 0
+        assert bool(torch.isfinite(od).all())
+        err = float((od - ref).abs().max() / ref.abs().max())
+        assert err < 3e-6, (dir, order, err)
