@@ -258,6 +258,72 @@ def _time(torch, fn, reps, stream=None):
     return s.elapsed_time(e) / reps
 
 
+def band_errors(P, torch, lib, L, st):
+    """Errors of the reduced-precision variants per wavenumber band, x lines of 256 points:
+    line j carries one Fourier mode k_j = 1 + j mod 127 with a random phase; per line the
+    max error is normalised by the line's max |double-float result|, then the max over the
+    lines of each band k in [1, 32), [32, 64), [64, 96), [96, 128) is reported.  For the
+    derivatives the double-float path's own error against the analytic derivative (the
+    scheme's truncation error) is listed beside them."""
+    import ctypes
+
+    nl = 2048
+    rng = np.random.default_rng(8)
+    ks = 1 + (np.arange(nl) % (N // 2 - 1))
+    ph = rng.uniform(0, 2 * np.pi, nl)
+    x = np.arange(N) * 2 * np.pi / N
+    arg = ks[:, None] * x[None, :] + ph[:, None]  # (line, point): x fastest in memory
+    dev = torch.device("cuda", torch.cuda.current_device())
+    f = torch.from_numpy(np.cos(arg)).to(dev)
+    exact = {1: torch.from_numpy(-ks[:, None] * np.sin(arg)).to(dev),
+             2: torch.from_numpy(-(ks[:, None] ** 2) * np.cos(arg)).to(dev)}
+    bands = [(1, 32), (32, 64), (64, 96), (96, 128)]
+    kt = torch.from_numpy(ks).to(dev)
+
+    def per_band(err_line):
+        return {f"k{lo}-{hi - 1}": float(err_line[(kt >= lo) & (kt < hi)].max()) for lo, hi in bands}
+
+    res = {}
+    h = 2 * np.pi / N
+    for fam, opc, name in (("cd10", 1, "cd10 d1"), ("cd10", 2, "cd10 d2"), ("cf90", 0, "cf90")):
+        o = P.cd10() if fam == "cd10" else P.cf90()
+        assert (o.init(N, h, True) if fam == "cd10" else o.init(N, True)) == 0
+        ref = torch.empty_like(f)
+        o.apply(opc, 1, f, ref, nl, 1, 0, 0)
+        got = torch.empty_like(f)
+        L.check(lib.pade_dense_apply(o.handle, opc, 1, ctypes.c_void_p(f.data_ptr()),
+                                     ctypes.c_void_p(got.data_ptr()), nl, 1, 0, 0, st))
+        f32 = f.float().contiguous()
+        o32 = torch.empty_like(f32)
+        o.apply(opc, 1, f32, o32, nl, 1, 0, 0, P.PATH_FP32)
+        torch.cuda.synchronize()
+        scale = ref.abs().amax(dim=1)
+        row = {"dense_tf32": per_band((got - ref).abs().amax(dim=1) / scale),
+               "fp32_path": per_band((o32.double() - ref).abs().amax(dim=1) / scale)}
+        if fam == "cd10":
+            ex = exact[opc]
+            row["fp64_path_vs_analytic"] = per_band((ref - ex).abs().amax(dim=1) / ex.abs().amax(dim=1))
+        res[name] = row
+    return res
+
+
+def les_stats(stats, n):
+    """Learned against dynamic after the same number of steps: spectrum deviation per shell
+    (1 .. n/3), kinetic energy, resolved and SGS dissipation."""
+    from padeops_gb300 import diagnostics as D
+
+    d, lr = stats["dynamic"], stats["learned"]
+    c = D.compare_spectra(lr["spectrum"], d["spectrum"], n, floor=1e-10)
+    return {"steps": d["step"], "tsim": {"dynamic": d["tsim"], "learned": lr["tsim"]},
+            "spectrum_max_rel_dev": c["max"], "spectrum_mean_rel_dev": c["mean"],
+            "shells": f"1..{c['kmax']} (shells holding at least 1e-10 of the peak energy)",
+            "spectrum_rel_dev_k1_4_8_16_32": [float(c["per_shell"][k - 1]) for k in (1, 4, 8, 16, 32)
+                                              if k <= c["kmax"]],
+            "ke": {"dynamic": d["ke"], "learned": lr["ke"]},
+            "eps_resolved": {"dynamic": d["eps"][0], "learned": lr["eps"][0]},
+            "eps_sgs": {"dynamic": d["eps"][1], "learned": lr["eps"][1]}}
+
+
 def extras(args, P, torch, f_host):
     """Secondary measurements of the other hot-path rows (rank 0): the FP32 and native-FP64
     paths of the same step, the 512^3 periodic projection, and the 256^3 LES step with the
@@ -297,27 +363,37 @@ def extras(args, P, torch, f_host):
         got = torch.empty_like(base)
         st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         xops = [(obj, opc, name) for (obj, opc, d, name) in plan if d == 1]
-        errs = {}
-        for obj, opc, name in xops:
-            obj.apply(opc, 1, base, ref, N, N, 0, 0)
-            L.check(lib.pade_dense_apply(obj.handle, opc, 1, ctypes.c_void_p(base.data_ptr()),
+        # every operator of the step along its own direction (z non-periodic: bc 0, 0)
+        per_op = {}
+        for obj, opc, d, name in plan:
+            obj.apply(opc, d, base, ref, N, N, 0, 0)
+            L.check(lib.pade_dense_apply(obj.handle, opc, d, ctypes.c_void_p(base.data_ptr()),
                                          ctypes.c_void_p(got.data_ptr()), N, N, 0, 0, st))
             torch.cuda.synchronize()
-            errs[name] = float((got - ref).abs().max() / ref.abs().max())
+            err = float((got - ref).abs().max() / ref.abs().max())
 
-        def dstep():
-            for obj, opc, _ in xops:
-                lib.pade_dense_apply(obj.handle, opc, 1, ctypes.c_void_p(base.data_ptr()),
+            def one_dense(obj=obj, opc=opc, d=d):
+                lib.pade_dense_apply(obj.handle, opc, d, ctypes.c_void_p(base.data_ptr()),
                                      ctypes.c_void_p(got.data_ptr()), N, N, 0, 0, st)
 
-        ms = _time(torch, dstep, reps)
-        out["dense_tf32_x"] = {"value": len(xops) * npts / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
-                               "ms_per_op": ms / len(xops),
-                               "achieved_GBps": len(xops) * npts * 16 / (ms * 1e-3) / 1e9,
-                               "relerr_vs_fp64_path": errs,
-                               "note": "tcgen05 kind::tf32, 3 products (hi/lo splits), x lines; reduced precision"}
+            def one_line(obj=obj, opc=opc, d=d):
+                obj.apply(opc, d, base, ref, N, N, 0, 0)
+
+            md, ml = _time(torch, one_dense, reps), _time(torch, one_line, reps)
+            per_op[name] = {"ms": md, "relerr_vs_fp64_path": err, "fp64_path_ms": ml, "speedup_vs_fp64_path": ml / md}
+        ms = sum(v["ms"] for v in per_op.values())
+        ms_line = sum(v["fp64_path_ms"] for v in per_op.values())
+        xy = [v for k, v in per_op.items() if not k.endswith("dir3")]
+        out["dense_tf32"] = {"value": len(plan) * npts / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+                             "ms_per_step": ms, "speedup_vs_fp64_path_step": ms_line / ms,
+                             "speedup_vs_fp64_path_xy": sum(v["fp64_path_ms"] for v in xy) / sum(v["ms"] for v in xy),
+                             "achieved_GBps": len(plan) * npts * 16 / (ms * 1e-3) / 1e9,
+                             "per_op": per_op,
+                             "note": "tcgen05 kind::tf32, 3 products (hi/lo splits) of the dense A^-1 B; reduced "
+                                     "precision; per-op CUDA-event times of the same 9 applications"}
         del base, ref, got
         torch.cuda.empty_cache()
+        out["band_relerr"] = band_errors(P, torch, lib, L, st)
     except Exception as ex:  # pragma: no cover
         out["dense_error"] = repr(ex)
     try:
@@ -353,22 +429,51 @@ def extras(args, P, torch, f_host):
         def tdev(a):
             return torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
 
-        n0 = 64
+        from padeops_gb300 import diagnostics as D
+
+        # training: a 64^3 dynamic run from seed 4, 300 steps, a snapshot every 15 (5.2 M samples)
+        n0, nrun = 64, 300
         u, v, w = hit_initial_field(n0, seed=4)
         g0 = P.igrid()
         g0.init(n0, n0, n0)
         g0.set_fields(tdev(u), tdev(v), tdev(w))
         clo = LearnedClosure(init_params(0))
-        X, y = training_set(g0, clo, nsteps=8, every=2)
+        X, y = training_set(g0, clo, nsteps=nrun, every=15)
+        nsamp = int(X.shape[0])
         hist = train(clo, X, y, epochs=10, batch=4096, lr=3e-3)
         del g0, X, y
-        n = 256
-        u, v, w = hit_initial_field(n, seed=4)
-        res = {}
-        for mode in ("dynamic", "learned"):
+        # developed flow: dynamic and learned from seed 5 (not trained on), 300 steps at 64^3
+        u, v, w = hit_initial_field(n0, seed=5)
+        st64 = {}
+        for mode in ("dynamic", "learned", "learned_planeavg"):
             g1 = P.igrid()
-            if mode == "learned":
-                g1.init(n, n, n, learnedSGS=True, JudgeFreq=0)
+            if mode != "dynamic":
+                g1.init(n0, n0, n0, learnedSGS=True, JudgeFreq=0, learnedPlaneAvg=mode == "learned_planeavg")
+                g1.set_mlp(clo)
+            else:
+                g1.init(n0, n0, n0)
+            g1.set_fields(tdev(u), tdev(v), tdev(w))
+            g1.timeAdvance(use_graph=False)
+            while g1.info()["step"] < nrun:
+                g1.timeAdvance(use_graph=True)
+            inf = g1.info()
+            st64[mode] = {"step": inf["step"], "tsim": inf["tsim"], "spectrum": D.energy_spectrum(g1),
+                          "ke": D.kinetic_energy(g1), "eps": D.dissipation(g1, 1.0 / 1000.0)}
+            del g1
+        out["les_64_developed"] = {
+            "pointwise": les_stats(st64, n0),
+            "plane_averaged": les_stats({"dynamic": st64["dynamic"], "learned": st64["learned_planeavg"]}, n0),
+            "training_samples": nsamp,
+            "note": "closure trained on a 64^3 dynamic run from seed 4; compared from seed 5 after 300 steps; "
+                    "pointwise: nu = Cs^2(x) Delta^2 |S|; plane_averaged: nu = <Cs^2 Delta^2>_xy |S|"}
+        n = 256
+        nstat = 30  # steps from the same initial field before the statistics are compared
+        u, v, w = hit_initial_field(n, seed=4)
+        res, stats = {}, {}
+        for mode in ("dynamic", "learned", "learned_planeavg"):
+            g1 = P.igrid()
+            if mode != "dynamic":
+                g1.init(n, n, n, learnedSGS=True, JudgeFreq=0, learnedPlaneAvg=mode == "learned_planeavg")
                 g1.set_mlp(clo)
             else:
                 g1.init(n, n, n)
@@ -377,14 +482,25 @@ def extras(args, P, torch, f_host):
             with torch.cuda.stream(side):
                 g1.timeAdvance(use_graph=False)  # step 0 carries the divergence check
                 ms = _time(torch, lambda g1=g1: g1.timeAdvance(use_graph=True), 3, stream=side)
+                while g1.info()["step"] < nstat:
+                    g1.timeAdvance(use_graph=True)
+            side.synchronize()
             res[mode] = ms
+            inf = g1.info()
+            stats[mode] = {"step": inf["step"], "tsim": inf["tsim"], "spectrum": D.energy_spectrum(g1),
+                           "ke": D.kinetic_energy(g1), "eps": D.dissipation(g1, 1.0 / 1000.0)}
             del g1
             torch.cuda.empty_cache()
         out["les_256"] = {"s_per_step_dynamic": res["dynamic"] / 1e3, "s_per_step_learned": res["learned"] / 1e3,
                           "learned_speedup": res["dynamic"] / res["learned"],
+                          "s_per_step_learned_planeavg": res["learned_planeavg"] / 1e3,
+                          "learned_planeavg_speedup": res["dynamic"] / res["learned_planeavg"],
                           "config": "256^3 periodic, Re 1000, CFL 0.5, TVD-RK3, Smagorinsky (dynamic, deltaRatio 2)"
-                                    " vs learned closure trained on a 64^3 dynamic run; CUDA-graph steps",
-                          "training_loss": [hist[0], hist[-1]]}
+                                    " vs learned closure trained on a 64^3 dynamic run (300 steps); CUDA-graph steps",
+                          "training_loss": [hist[0], hist[-1]],
+                          "statistics": les_stats(stats, n),
+                          "statistics_planeavg": les_stats({"dynamic": stats["dynamic"],
+                                                            "learned": stats["learned_planeavg"]}, n)}
     except Exception as ex:  # pragma: no cover
         out["les_error"] = repr(ex)
     return out

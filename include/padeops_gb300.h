@@ -265,6 +265,9 @@ typedef struct {
     int learnedSGS;        /* 1: nu from the learned closure (pade_les_set_mlp) */
     int JudgeFreq;         /* learnedSGS: run the dynamic procedure every JudgeFreq steps as a
                               reference for the closure (lambda1d of pade_les_info); 0: never */
+    int learnedPlaneAvg;   /* learnedSGS: 1 = the closure's coefficient averaged over each x-y plane
+                              (nu = <Cs^2 Delta^2>_xy |S|, the dynamic procedure's form);
+                              0 = pointwise (nu = Cs^2(x) Delta^2 |S|) */
 } pade_les_params;
 #define PADE_LES_UHAT 0
 #define PADE_LES_VHAT 1

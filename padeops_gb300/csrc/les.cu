@@ -178,7 +178,8 @@ __global__ void k_num_den(Ptr6 L, Ptr6 M, double* __restrict__ num, double* __re
     }
 }
 
-// per-plane sums of two arrays: grid (chunks, nz); partials [nz][chunks][2]
+// per-plane sums of two arrays (b == nullptr: of a and of ones): grid (chunks, nz);
+// partials [nz][chunks][2]
 constexpr int kPlaneChunks = 16;
 __global__ void k_plane_sums(const double* __restrict__ a, const double* __restrict__ b, long plane,
                              double* __restrict__ part) {
@@ -189,7 +190,7 @@ __global__ void k_plane_sums(const double* __restrict__ a, const double* __restr
     double x = 0.0, y = 0.0;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < plane; e += (long)gridDim.x * blockDim.x) {
         x += pa[e];
-        y += pb[e];
+        y += b ? pb[e] : 1.0;
     }
     for (int o = 16; o > 0; o >>= 1) {
         x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -229,6 +230,11 @@ __global__ void k_lambda(const double* __restrict__ part, int chunks, double mea
 __global__ void k_scale_nu(double* __restrict__ nu, const double* __restrict__ lambda, double c, long plane,
                            long n) {
     GRID_STRIDE(e, n) { nu[e] = lambda ? mul(lambda[e / plane], nu[e]) : mul(c, nu[e]); }
+}
+
+// learned closure, plane-averaged form: a = Cs^2 Delta^2 from the closure's FP32 output
+__global__ void k_cs2_delta2(const float* __restrict__ cs2, double d2, double* __restrict__ a, long n) {
+    GRID_STRIDE(e, n) { a[e] = mul((double)cs2[e], d2); }
 }
 
 __global__ void k_clip_neg(double* __restrict__ x, long n) {
@@ -364,7 +370,7 @@ struct pade_les_s {
     double *nuC = nullptr, *nuE = nullptr, *div = nullptr;
     // dynamic procedure
     double *Sf[6] = {nullptr}, *M[6] = {nullptr}, *Lm[6] = {nullptr}, *uf[3] = {nullptr};
-    double *Df = nullptr, *Dsgs = nullptr, *lambda = nullptr, *part = nullptr;
+    double *Df = nullptr, *Dsgs = nullptr, *lambda = nullptr, *part = nullptr, *lamL = nullptr;
     double *d_dt = nullptr, *d_tsim = nullptr, *cflpart = nullptr;
     std::vector<void*> allocs;
     int step = 0, mstep = 0;
@@ -543,7 +549,25 @@ int sgs_rhs(pade_les h, cudaStream_t s) {
         }
         const double* grads[9];
         for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
-        CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, s));
+        if (h->prm.learnedPlaneAvg) {
+            // nu = <Cs^2 Delta^2>_xy |S|: the closure's coefficient through the dynamic
+            // procedure's plane average (Cs^2 as FP32 in the rC1 scratch)
+            float* cs2 = reinterpret_cast<float*>(h->rC1);
+            CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, cs2, s));
+            k_cs2_delta2<<<g, 256, 0, s>>>(cs2, h->deltaLES * h->deltaLES, h->rC2, n);
+            KCHECK();
+            dim3 grid(kPlaneChunks, h->nz);
+            k_plane_sums<<<grid, 256, 0, s>>>(h->rC2, nullptr, h->plane, h->part);
+            KCHECK();
+            k_lambda<<<(h->nz + 127) / 128, 128, 0, s>>>(h->part, kPlaneChunks, h->meanfact, h->nz, h->lamL);
+            KCHECK();
+            k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, nullptr, n);
+            KCHECK();
+            k_scale_nu<<<g, 256, 0, s>>>(h->nuC, h->lamL, 0.0, h->plane, n);
+            KCHECK();
+        } else {
+            CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, s));
+        }
     } else {
         k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
         KCHECK();
@@ -768,6 +792,10 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
         if (rc == PS_OK) rc = al(h, &h->Df, r8 * h->NC);
         if (rc == PS_OK) rc = al(h, &h->Dsgs, r8 * h->NC);
         if (rc == PS_OK) rc = al(h, &h->part, r8 * 2 * kPlaneChunks * h->nz);
+    }
+    if (p->useSGS && p->learnedSGS && p->learnedPlaneAvg) {
+        if (!h->part && rc == PS_OK) rc = al(h, &h->part, r8 * 2 * kPlaneChunks * h->nz);
+        if (rc == PS_OK) rc = al(h, &h->lamL, r8 * h->nz);
     }
     if (rc == PS_OK) rc = al(h, &h->lambda, r8 * h->nz);
     if (rc == PS_OK) rc = al(h, &h->d_dt, r8);
