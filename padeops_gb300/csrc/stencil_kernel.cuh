@@ -26,13 +26,21 @@
 
 namespace pade {
 
-// Odd lane strides keep the lanes of a line on distinct shared-memory banks.
+// Lane strides (8-byte words) that keep a half-warp's accesses on distinct banks.  Chunks
+// of 16: the 16 lanes of a line fill a half-warp, odd S gives 16 distinct bank pairs.
+// Chunks of 32 (8 lanes per line on 256-row lines): two lines share a half-warp; S = 2 mod
+// 4 puts one line's 8 lanes on 8 distinct even words and, with the odd line stride, the
+// other line's on odd words.
 template <int M, int H>
 struct LineLayout {
     static constexpr int S0 = M + 2 * H;
-    static constexpr int S = (S0 % 2 == 0) ? S0 + 1 : S0;  // input window: H + M + H rows
-    static constexpr int W = M + 1;                          // work rows / row tables
+    static constexpr int S = M == 32 ? (S0 % 4 == 2 ? S0 : S0 + (4 + 2 - S0 % 4) % 4)
+                                     : ((S0 % 2 == 0) ? S0 + 1 : S0);  // input window: H + M + H rows
+    static constexpr int W = M + 1;  // work rows / row tables
 };
+static_assert(LineLayout<32, 3>::S % 4 == 2 && LineLayout<32, 4>::S % 4 == 2 && LineLayout<32, 2>::S % 4 == 2,
+              "32-row chunk stride");
+static_assert(LineLayout<16, 3>::S % 2 == 1 && LineLayout<16, 4>::S % 2 == 1, "16-row chunk stride");
 
 template <int NP, bool SYM>
 __device__ __forceinline__ dfv line_stencil(const dfv* __restrict__ p, const dfv (&c)[NP], dfv c0) {
