@@ -9,16 +9,18 @@ data.  Metric: operator throughput in Gpts/s (points x operator applications per
   value     device throughput: inputs resident in HBM, CUDA events around K steps
   e2e       the same step through the reference-named C-ABI entry points with pinned
             HOST buffers (host->device copy, kernel, device->host copy per call)
-  roofline  the chunked double-float kernel (every launch of the step), algorithmic
-            16 B/point (read f once, write the result once) against the measured HBM copy
-            bandwidth in MEASURED_PEAKS.json
+  roofline  the fixed-stencil double-float line kernel (every launch of the step),
+            algorithmic 16 B/point (read f once, write the result once) against the
+            measured HBM copy bandwidth in MEASURED_PEAKS.json
   cpu_baseline  the oracle port of the reference algorithm on the host cores (OpenMP over
             lines), on the same workload
 
 `extras` (same line): the FP32 and native-FP64 paths of the step, the tensor-core dense
-(3xTF32) path along x with its error against the FP64 path, the 512^3 periodic
-pressure projection, and s/step of the 256^3 LES step with the dynamic procedure and with
-the learned closure.
+(3xTF32) path for every operator of the step with its error against the FP64 path and its
+speed-up, errors of the reduced-precision variants per wavenumber band, the 512^3 periodic
+pressure projection, and the LES: s/step at 256^3 with the dynamic procedure and with the
+learned closure, and the flow statistics (shell spectrum, kinetic energy, resolved and
+SGS dissipation) of learned against dynamic runs at 256^3 (30 steps) and 64^3 (300 steps).
 
 `--impl reference` times the oracle port alone (the Fortran reference cannot be built on
 this hardware: no Fortran compiler or MPI) and prints its line.
@@ -507,7 +509,7 @@ def extras(args, P, torch, f_host):
 
 
 def traffic_per_launch():
-    p = os.path.join(ROOT, "profiles", "chunk_kernel_traffic.json")
+    p = os.path.join(ROOT, "profiles", "line_kernel_traffic.json")
     if os.path.exists(p):
         try:
             d = json.load(open(p))
@@ -580,7 +582,7 @@ def main():
     tr = traffic_per_launch()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": tr, "peak_source": src,
-            "kernel": "k_chunk<ArDF> (double-float chunked scan), mean over the 9 launches",
+            "kernel": "k_line (fixed-stencil double-float chunked scan), mean over the 9 launches",
             "algorithmic_bytes_per_launch": npts * BYTES_PER_POINT,
             "per_launch_ms": {p[3]: round(float(v), 4) for p, v in zip(plan, per_launch)}}
     cb = None
