@@ -122,7 +122,6 @@ int grow(void** buf, size_t* cur, size_t need) {
     return PS_OK;
 }
 
-constexpr int kPipeChunks = 8;
 constexpr size_t kPipeMinBytes = 8u << 20;
 
 int ensure_pipe(pade_op h) {
@@ -130,7 +129,7 @@ int ensure_pipe(pade_op h) {
     for (int i = 0; i < 3; i++)
         if (cudaStreamCreateWithFlags(&h->pipe[i], cudaStreamNonBlocking) != cudaSuccess) return PS_ECUDA;
     for (int k = 0; k < 2; k++)
-        for (int c = 0; c < 16; c++)
+        for (int c = 0; c < kPipeChunks; c++)
             if (cudaEventCreateWithFlags(&h->pev[k][c], cudaEventDisableTiming) != cudaSuccess) return PS_ECUDA;
     if (cudaEventCreateWithFlags(&h->pstart, cudaEventDisableTiming) != cudaSuccess) return PS_ECUDA;
     h->pipe_ok = true;

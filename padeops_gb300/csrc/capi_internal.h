@@ -18,6 +18,9 @@ inline bool bc_valid(int bc) { return bc == 0 || bc == 1 || bc == -1; }
 // plans are keyed by opcode * 16 + bc index (bcid(bc1) * 3 + bcid(bcn))
 inline int plan_key(int opcode, int bc1, int bcn) { return opcode * 16 + bcid(bc1) * 3 + bcid(bcn); }
 
+// chunks of the host-buffer copy-in / compute / copy-out pipeline (capi.cpp)
+constexpr int kPipeChunks = 8;
+
 }  // namespace pade
 
 namespace pade {
@@ -43,7 +46,7 @@ struct pade_op_s {
     size_t stage_in_bytes = 0, stage_out_bytes = 0;
     // host-pointer pipeline: copy-in, compute and copy-out streams and per-chunk events
     cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t pev[2][16] = {};
+    cudaEvent_t pev[2][pade::kPipeChunks] = {};
     cudaEvent_t pstart = nullptr;
     bool pipe_ok = false;
     ~pade_op_s() {
@@ -51,7 +54,7 @@ struct pade_op_s {
         if (pipe_ok) {
             for (int i = 0; i < 3; i++) cudaStreamDestroy(pipe[i]);
             for (int k = 0; k < 2; k++)
-                for (int c = 0; c < 16; c++) cudaEventDestroy(pev[k][c]);
+                for (int c = 0; c < pade::kPipeChunks; c++) cudaEventDestroy(pev[k][c]);
             cudaEventDestroy(pstart);
         }
         if (status) cudaFree(status);
