@@ -103,9 +103,12 @@ class DevicePlan {
     StencilParams cline_{};
 };
 
-// Fixed-stencil kernel (double-float) for a plan with line_shape() != SHAPE_NONE.
+// Fixed-stencil kernel for a plan with line_shape() != SHAPE_NONE: double-float (FP64 in
+// and out) or FP32.
 int launch_line(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                 cudaStream_t s);
+int launch_line_f32(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                    unsigned* status, cudaStream_t s);
 
 // Launch the operator on a set of lines.  f/out are device pointers to double (FP64 paths)
 // or float (PATH_FP32).  status (device word) collects out-of-range flags of the df path.

@@ -381,6 +381,8 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
                          : launch_chunk_m<ArDF, 32>(h, p.chunk_df(), f, out, ls, status, s);
     }
     if (path == PATH_FP32) {
+        if (p.line_shape() != SHAPE_NONE)
+            return launch_line_f32(p.line_shape(), p.line_params(), f, out, ls, status, s);
         return h.M == 16 ? launch_chunk_m<ArF32, 16>(h, p.chunk_f32(), f, out, ls, status, s)
                          : launch_chunk_m<ArF32, 32>(h, p.chunk_f32(), f, out, ls, status, s);
     }

@@ -5,7 +5,7 @@ namespace pade {
 
 int launch_line_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                      unsigned* status, cudaStream_t s) {
-    return launch_line_shapes<false>(shape, c, f, out, ls, status, s);
+    return launch_line_shapes<ArDF, false>(shape, c, f, out, ls, status, s);
 }
 
 }  // namespace pade

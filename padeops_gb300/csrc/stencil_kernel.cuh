@@ -1,4 +1,5 @@
-// Chunked kernel with a compile-time stencil shape (double-float arithmetic).
+// Chunked kernel with a compile-time stencil shape (double-float arithmetic with FP64 in
+// and out, or FP32 throughout).
 //
 // The compact derivatives and filters (cd06 / cd10 first and second derivatives, cf90 in
 // residual form) have an interior RHS stencil that is symmetric or antisymmetric about the
@@ -42,19 +43,20 @@ static_assert(LineLayout<32, 3>::S % 4 == 2 && LineLayout<32, 4>::S % 4 == 2 && 
               "32-row chunk stride");
 static_assert(LineLayout<16, 3>::S % 2 == 1 && LineLayout<16, 4>::S % 2 == 1, "16-row chunk stride");
 
-template <int NP, bool SYM>
-__device__ __forceinline__ dfv line_stencil(const dfv* __restrict__ p, const dfv (&c)[NP], dfv c0) {
-    dfv acc;
+template <class AR, int NP, bool SYM>
+__device__ __forceinline__ typename AR::V line_stencil(const typename AR::V* __restrict__ p,
+                                                      const typename AR::V (&c)[NP], typename AR::V c0) {
+    typename AR::V acc;
     if constexpr (SYM) {
-        acc = df_mul(p[0], c0);
+        acc = AR::mul(p[0], c0);
 #pragma unroll
-        for (int k = 1; k <= NP; k++) acc = df_add(acc, df_mul(df_add(p[k], p[-k]), c[k - 1]));
+        for (int k = 1; k <= NP; k++) acc = AR::add(acc, AR::mul(AR::add(p[k], p[-k]), c[k - 1]));
     } else {
-        acc = df_mul(df_sub(p[1], p[-1]), c[0]);
+        acc = AR::mul(AR::sub(p[1], p[-1]), c[0]);
 #pragma unroll
-        for (int k = 2; k <= NP; k++) acc = df_add(acc, df_mul(df_sub(p[k], p[-k]), c[k - 1]));
+        for (int k = 2; k <= NP; k++) acc = AR::add(acc, AR::mul(AR::sub(p[k], p[-k]), c[k - 1]));
     }
-    return df_norm(acc);
+    return AR::norm(acc);
 }
 
 // Line stride in 8-byte words, made odd.
@@ -69,12 +71,12 @@ __host__ __device__ constexpr int line_min_blocks(bool circ, int m, bool alias) 
 // Number of per-row tables of a banded line: g a1 a2 b1 b2 pf1 pf2 pb1 pb2.
 constexpr int kRowTables = 9;
 
-template <int Q, int NP, bool SYM, bool CIRC, int M, int NT, bool ALIAS>
+template <class AR, int Q, int NP, bool SYM, bool CIRC, int M, int NT, bool ALIAS>
 __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
-    k_line(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
-           unsigned* __restrict__ status) {
-    using AR = ArDF;
-    using V = dfv;
+    k_line(const StencilParams cp, const typename AR::IO* __restrict__ f, typename AR::IO* __restrict__ out,
+           const LineSet ls, unsigned* __restrict__ status) {
+    using V = typename AR::V;
+    using IO = typename AR::IO;
     constexpr int H = NP;
     constexpr int S = LineLayout<M, H>::S, W = LineLayout<M, H>::W;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -123,87 +125,107 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
     // ---- A: stage each line scaled by 2^-(e_max - 1023) into the main rows of the windows ----
     auto main_pos = [&](int l, int p) -> int { return l * LT + (p / M) * S + H + (p % M); };
     unsigned bad = 0;
-    if (ls.fp == 1) {
-        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
-        const int U = (ns + 31) >> 5;
-        for (int l = warp; l < nl; l += nw) {
-            const double* src = f + base_in[l];
-            double v[kStageRegs];
-            int mx = 0;
-#pragma unroll
-            for (int u = 0; u < kStageRegs; u++) {
-                const int p = lane + 32 * u;
-                v[u] = (u < U && p < ns) ? __ldg(src + p) : 0.0;
-                mx = max(mx, bexp(v[u]));
-            }
-            mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
-            bad |= (unsigned)(mx == 2047);
-            if (lane == 0) lexp[l] = mx;
-#pragma unroll
-            for (int u = 0; u < kStageRegs; u++) {
-                const int p = lane + 32 * u;
-                if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], mx - 1023);
-            }
-        }
-    } else if ((ns + nth / L - 1) / (nth / L) > kStageRegs) {
-        // more rows per thread than staging registers: raw FP64 first, split in place
-        const int pstep = nth / L;
-        const int l = tid % L, q0 = tid / L;
-        double* raw = reinterpret_cast<double*>(tile);
-        int mx = 0;
-        if (l < nl) {
-            const double* src = f + base_in[l];
-            for (int p0 = q0; p0 < ns; p0 += pstep * kLoadUnroll) {
-                double v[kLoadUnroll];
-#pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int p = p0 + pstep * u;
-                    v[u] = p < ns ? __ldg(src + (long)p * ls.fp) : 0.0;
+    if constexpr (AR::kScaled) {
+        if (ls.fp == 1) {
+            const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+            const int U = (ns + 31) >> 5;
+            for (int l = warp; l < nl; l += nw) {
+                const double* src = f + base_in[l];
+                double v[kStageRegs];
+                int mx = 0;
+    #pragma unroll
+                for (int u = 0; u < kStageRegs; u++) {
+                    const int p = lane + 32 * u;
+                    v[u] = (u < U && p < ns) ? __ldg(src + p) : 0.0;
+                    mx = max(mx, bexp(v[u]));
                 }
-#pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int p = p0 + pstep * u;
-                    if (p < ns) {
-                        raw[main_pos(l, p)] = v[u];
-                        mx = max(mx, bexp(v[u]));
+                mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
+                bad |= (unsigned)(mx == 2047);
+                if (lane == 0) lexp[l] = mx;
+    #pragma unroll
+                for (int u = 0; u < kStageRegs; u++) {
+                    const int p = lane + 32 * u;
+                    if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], mx - 1023);
+                }
+            }
+        } else if ((ns + nth / L - 1) / (nth / L) > kStageRegs) {
+            // more rows per thread than staging registers: raw FP64 first, split in place
+            const int pstep = nth / L;
+            const int l = tid % L, q0 = tid / L;
+            double* raw = reinterpret_cast<double*>(tile);
+            int mx = 0;
+            if (l < nl) {
+                const double* src = f + base_in[l];
+                for (int p0 = q0; p0 < ns; p0 += pstep * kLoadUnroll) {
+                    double v[kLoadUnroll];
+    #pragma unroll
+                    for (int u = 0; u < kLoadUnroll; u++) {
+                        const int p = p0 + pstep * u;
+                        v[u] = p < ns ? __ldg(src + (long)p * ls.fp) : 0.0;
+                    }
+    #pragma unroll
+                    for (int u = 0; u < kLoadUnroll; u++) {
+                        const int p = p0 + pstep * u;
+                        if (p < ns) {
+                            raw[main_pos(l, p)] = v[u];
+                            mx = max(mx, bexp(v[u]));
+                        }
                     }
                 }
+                atomicMax(&lexp[l], mx);
             }
-            atomicMax(&lexp[l], mx);
-        }
-        __syncthreads();
-        if (l < nl) {
-            const int k = lexp[l] - 1023;
-            bad |= (unsigned)(lexp[l] == 2047);
-            for (int p = q0; p < ns; p += pstep) {
-                const int ps = main_pos(l, p);
-                tile[ps] = df_from_double_shift(raw[ps], k);
+            __syncthreads();
+            if (l < nl) {
+                const int k = lexp[l] - 1023;
+                bad |= (unsigned)(lexp[l] == 2047);
+                for (int p = q0; p < ns; p += pstep) {
+                    const int ps = main_pos(l, p);
+                    tile[ps] = df_from_double_shift(raw[ps], k);
+                }
+            }
+        } else {
+            const int pstep = nth / L;
+            const int U = (ns + pstep - 1) / pstep;
+            const int l = tid % L, q0 = tid / L;
+            double v[kStageRegs];
+            int mx = 0;
+            if (l < nl) {
+                const double* src = f + base_in[l];
+    #pragma unroll
+                for (int u = 0; u < kStageRegs; u++) {
+                    const int p = q0 + pstep * u;
+                    v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
+                    mx = max(mx, bexp(v[u]));
+                }
+                atomicMax(&lexp[l], mx);
+            }
+            __syncthreads();
+            if (l < nl) {
+                const int k = lexp[l] - 1023;
+                bad |= (unsigned)(lexp[l] == 2047);
+    #pragma unroll
+                for (int u = 0; u < kStageRegs; u++) {
+                    const int p = q0 + pstep * u;
+                    if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], k);
+                }
             }
         }
     } else {
-        const int pstep = nth / L;
-        const int U = (ns + pstep - 1) / pstep;
-        const int l = tid % L, q0 = tid / L;
-        double v[kStageRegs];
-        int mx = 0;
-        if (l < nl) {
-            const double* src = f + base_in[l];
-#pragma unroll
-            for (int u = 0; u < kStageRegs; u++) {
-                const int p = q0 + pstep * u;
-                v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
-                mx = max(mx, bexp(v[u]));
+        // FP32 in and out: no line scaling, values stored as loaded
+        if (ls.fp == 1) {
+            const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+            for (int l = warp; l < nl; l += nw) {
+                const IO* src = f + base_in[l];
+#pragma unroll 4
+                for (int p = lane; p < ns; p += 32) tile[main_pos(l, p)] = AR::load(__ldg(src + p), bad);
             }
-            atomicMax(&lexp[l], mx);
-        }
-        __syncthreads();
-        if (l < nl) {
-            const int k = lexp[l] - 1023;
-            bad |= (unsigned)(lexp[l] == 2047);
-#pragma unroll
-            for (int u = 0; u < kStageRegs; u++) {
-                const int p = q0 + pstep * u;
-                if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], k);
+        } else {
+            const int pstep = nth / L;
+            const int l = tid % L, q0 = tid / L;
+            if (l < nl) {
+                const IO* src = f + base_in[l];
+#pragma unroll 4
+                for (int p = q0; p < ns; p += pstep) tile[main_pos(l, p)] = AR::load(__ldg(src + (long)p * ls.fp), bad);
             }
         }
     }
@@ -259,15 +281,15 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
         for (int j = 0; j < M; j++) {
             V y;
             if constexpr (CIRC) {
-                const V r = line_stencil<NP, SYM>(win + j, cc, c0);
+                const V r = line_stencil<AR, NP, SYM>(win + j, cc, c0);
                 y = (Q == 2) ? AR::fms2(r, a1, s1, a2, s2) : AR::fms1(r, a1, s1);
             } else {
                 const int i = t * M + j;
                 V r;
                 if (i < nlo) r = edge[l * ne + i];
                 else if (i >= ehi) r = edge[l * ne + nlo + (i - ehi)];
-                else r = line_stencil<NP, SYM>(win + j, cc, c0);
-                r = df_mul(r, rt[j]);
+                else r = line_stencil<AR, NP, SYM>(win + j, cc, c0);
+                r = AR::mul(r, rt[j]);
                 y = (Q == 2) ? AR::fms2(r, rt[PW + j], s1, rt[2 * PW + j], s2) : AR::fms1(r, rt[PW + j], s1);
             }
             wk[j] = y;
@@ -386,93 +408,103 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
         return (Q == 2) ? AR::mac2(wk[j], q1, j1, q2, j2) : AR::mac1(wk[j], q1, j1);
     };
     if (active) {
-        double* wio = reinterpret_cast<double*>(wk);
-        const int kl = lexp[l] - 1023;
-        if (kl >= -800 && kl <= 800) {
-            const unsigned kadd = (unsigned)(896 + kl) << 20;
+        IO* wio = reinterpret_cast<IO*>(wk);
+        if constexpr (AR::kScaled) {
+            const int kl = lexp[l] - 1023;
+            if (kl >= -800 && kl <= 800) {
+                const unsigned kadd = (unsigned)(896 + kl) << 20;
+#pragma unroll 4
+                for (int j = 0; j < M; j++) {
+                    V x = corrected(j);
+                    if (!ALIAS && cp.resid) x = df_sub(win[j], x);
+                    wio[j] = df_to_double_kadd(x, kadd);
+                }
+            } else {
+#pragma unroll 1
+                for (int j = 0; j < M; j++) {
+                    V x = corrected(j);
+                    if (!ALIAS && cp.resid) x = AR::norm(df_sub(win[j], x));
+                    wio[j] = AR::store_scaled(x, kl);
+                }
+            }
+        } else {
 #pragma unroll 4
             for (int j = 0; j < M; j++) {
                 V x = corrected(j);
-                if (!ALIAS && cp.resid) x = df_sub(win[j], x);
-                wio[j] = df_to_double_kadd(x, kadd);
-            }
-        } else {
-#pragma unroll 1
-            for (int j = 0; j < M; j++) {
-                V x = corrected(j);
-                if (!ALIAS && cp.resid) x = AR::norm(df_sub(win[j], x));
-                wio[j] = AR::store_scaled(x, kl);
+                if (!ALIAS && cp.resid) x = AR::sub(win[j], x);
+                wio[j] = AR::store(x);
             }
         }
     }
     __syncthreads();
 
     // ---- J: coalesced stores ----
-    const double* wd = reinterpret_cast<const double*>(ALIAS ? tile : work);
+    const IO* wd = reinterpret_cast<const IO*>(ALIAS ? tile : work);
     auto out_pos = [&](int ll, int p) -> int {
         return ALIAS ? ll * LT + (p / M) * S + (p % M) : ll * LW + (p / M) * W + (p % M);
     };
     if (ls.op == 1) {
         const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
         for (int ll = warp; ll < nl; ll += nw) {
-            double* o = out + base_out[ll];
+            IO* o = out + base_out[ll];
             for (int p = lane; p < cp.nout; p += 32) o[p] = wd[out_pos(ll, p < ns ? p : p - ns)];
         }
     } else {
         const int ll = tid % L, pstep = nth / L;
         if (ll < nl) {
-            double* o = out + base_out[ll];
+            IO* o = out + base_out[ll];
             for (int p = tid / L; p < cp.nout; p += pstep) o[(long)p * ls.op] = wd[out_pos(ll, p < ns ? p : p - ns)];
         }
     }
     if (bad) atomicOr(status, 1u);
 }
 
-template <bool CIRC, int NP, int M, bool ALIAS>
+template <class AR, bool CIRC, int NP, int M, bool ALIAS>
 size_t line_smem(const StencilParams& c) {
     using Lay = LineLayout<M, NP>;
     const int PW = c.P * Lay::W;
     const size_t tabs = CIRC ? 4 * (size_t)M : kRowTables * (size_t)PW;
     const size_t edges = CIRC ? 0 : (size_t)c.L * (c.nlo + c.nhi);
     const size_t work = ALIAS ? 0 : (size_t)c.L * line_stride(PW);
-    return sizeof(dfv) * (tabs + (size_t)c.L * line_stride(c.P * Lay::S) + work + edges);
+    return sizeof(typename AR::V) * (tabs + (size_t)c.L * line_stride(c.P * Lay::S) + work + edges);
 }
 
-template <int Q, int NP, bool SYM, bool CIRC, int M, bool ALIAS>
+template <class AR, int Q, int NP, bool SYM, bool CIRC, int M, bool ALIAS>
 int launch_line_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                   cudaStream_t s) {
+    using IO = typename AR::IO;
     constexpr int NT = CIRC ? kLineThreadsCirc : kLineThreadsBand;
     const long blocks = (ls.nlines + c.L - 1) / c.L;
-    const size_t smem = line_smem<CIRC, NP, M, ALIAS>(c);
-    auto kern = k_line<Q, NP, SYM, CIRC, M, NT, ALIAS>;
+    const size_t smem = line_smem<AR, CIRC, NP, M, ALIAS>(c);
+    auto kern = k_line<AR, Q, NP, SYM, CIRC, M, NT, ALIAS>;
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return PS_ECUDA;
     }
-    kern<<<(unsigned)blocks, NT, smem, s>>>(c, (const double*)f, (double*)out, ls, status);
+    kern<<<(unsigned)blocks, NT, smem, s>>>(c, (const IO*)f, (IO*)out, ls, status);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
 // Dispatch over the instantiated shapes: residual-form cf90 (P4S) with chunks of 16 and
 // separate work rows; the others with the input window reused and chunks of 16 or 32.
-template <bool CIRC>
+template <class AR, bool CIRC>
 int launch_line_shapes(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                        unsigned* status, cudaStream_t s) {
     const bool m32 = c.M == 32;
     switch (shape) {
         case SHAPE_T2A:
-            return m32 ? launch_line_t<1, 2, false, CIRC, 32, true>(c, f, out, ls, status, s)
-                       : launch_line_t<1, 2, false, CIRC, 16, true>(c, f, out, ls, status, s);
+            return m32 ? launch_line_t<AR, 1, 2, false, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<AR, 1, 2, false, CIRC, 16, true>(c, f, out, ls, status, s);
         case SHAPE_T2S:
-            return m32 ? launch_line_t<1, 2, true, CIRC, 32, true>(c, f, out, ls, status, s)
-                       : launch_line_t<1, 2, true, CIRC, 16, true>(c, f, out, ls, status, s);
+            return m32 ? launch_line_t<AR, 1, 2, true, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<AR, 1, 2, true, CIRC, 16, true>(c, f, out, ls, status, s);
         case SHAPE_P3A:
-            return m32 ? launch_line_t<2, 3, false, CIRC, 32, true>(c, f, out, ls, status, s)
-                       : launch_line_t<2, 3, false, CIRC, 16, true>(c, f, out, ls, status, s);
+            return m32 ? launch_line_t<AR, 2, 3, false, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<AR, 2, 3, false, CIRC, 16, true>(c, f, out, ls, status, s);
         case SHAPE_P3S:
-            return m32 ? launch_line_t<2, 3, true, CIRC, 32, true>(c, f, out, ls, status, s)
-                       : launch_line_t<2, 3, true, CIRC, 16, true>(c, f, out, ls, status, s);
-        case SHAPE_P4S: return launch_line_t<2, 4, true, CIRC, 16, false>(c, f, out, ls, status, s);
+            return m32 ? launch_line_t<AR, 2, 3, true, CIRC, 32, true>(c, f, out, ls, status, s)
+                       : launch_line_t<AR, 2, 3, true, CIRC, 16, true>(c, f, out, ls, status, s);
+        case SHAPE_P4S: return launch_line_t<AR, 2, 4, true, CIRC, 16, false>(c, f, out, ls, status, s);
         default: return PS_ENOTSUP;
     }
 }
@@ -481,5 +513,9 @@ int launch_line_circ(int shape, const StencilParams& c, const void* f, void* out
                      unsigned* status, cudaStream_t s);
 int launch_line_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                      unsigned* status, cudaStream_t s);
+int launch_line_f32_circ(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                         unsigned* status, cudaStream_t s);
+int launch_line_f32_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                         unsigned* status, cudaStream_t s);
 
 }  // namespace pade
