@@ -197,10 +197,17 @@ int pade_spectral_ifft(pade_spectral sp, const void* in, double* out, int set_od
 /* padepoisson with PeriodicInZ (src/incompressible/PadePoisson.F90:130-200, 76-128): the
  * periodic staggered-CD06 projection.  Keeps a pointer to `sp` (which must outlive it). */
 int pade_poisson_periodic_init(pade_poisson* p, pade_spectral sp, double dx, double dy, double dz);
+/* padepoisson with walls (PeriodicInZ false; PadePoisson.F90:130-318 init, 434-624
+ * PressureProjection, 320-384 ProjectStokesPressure): the projection solves on the even /
+ * odd extension of the fields to 2 nz points in z; compute_stokes_pressure adds the wall
+ * correction with the lambda-profiles of a domain of height Lz.  DivergenceCheck then uses
+ * the odd-odd staggered ddz_E2C (Pade6stagg bot = top = -1).  Keeps `sp`. */
+int pade_poisson_wall_init(pade_poisson* p, pade_spectral sp, double dx, double dy, double dz, double Lz,
+                           int compute_stokes_pressure);
 int pade_poisson_destroy(pade_poisson p);
-/* k3 modified wavenumbers used in |k|^2 (nz entries) */
+/* k3 modified wavenumbers used in |k|^2 (nz entries; PADE_ENOTSUP for a walled solver) */
 int pade_poisson_get_modified_k3(pade_poisson p, double* k3mod);
-/* PressureProjection -> PeriodicProjection (PadePoisson.F90:386-441): uhat, vhat complex
+/* PressureProjection (PadePoisson.F90:386-441 periodic, 434-624 walls): uhat, vhat complex
  * (nx/2+1,ny,nz), what complex (nx/2+1,ny,nz+1), all updated in place. */
 int pade_poisson_projection(pade_poisson p, void* uhat, void* vhat, void* what, void* stream);
 /* DivergenceCheck (PadePoisson.F90:1165-1246): divergence real (nx,ny,nz).  fix_div

@@ -103,6 +103,97 @@ class PeriodicPoisson:
         return ifft2_y2x(f, self.nx)
 
 
+def _stagg_oo(f, nz, dz, op):
+    """Pade6stagg ddz with bot = top = -1 on a non-periodic grid: the odd-odd cd06stagg
+    (PadeDerOps.F90:92-95, 592-595), real and imaginary parts separately."""
+    kw = dict(periodic=False, topEven=False, botEven=False, topSided=False, botSided=False)
+    return C.stagg(f.real, nz, dz, op, **kw) + 1j * C.stagg(f.imag, nz, dz, op, **kw)
+
+
+class WallPoisson:
+    """padepoisson with PeriodicInZ false: walls at z = 0 and Lz (PadePoisson.F90:130-318
+    init, 434-624 PressureProjection, 320-384 ProjectStokesPressure, 1165-1246
+    DivergenceCheck with derivZ%ddz_E2C(.., -1, -1)).  The projection works on the even
+    extension of the divergence and the odd extension of w to 2 nz points along z, with the
+    CD06-stagg modified wavenumbers phase-shifted by -+ dz/2 (edge <-> centre)."""
+
+    def __init__(self, nx, ny, nz, dx, dy, dz, Lz, stokes=False, fixOddball=True):
+        self.nx, self.ny, self.nz, self.dz, self.stokes = nx, ny, nz, dz, stokes
+        self.k1, self.k2 = spectral_wavenumbers(nx, ny, dx, dy, fixOddball)  # sp%k1, sp%k2
+        self.k1r = GetWaveNums(nx, dx)[: nx // 2 + 1]                       # k1inZ
+        self.k2r = GetWaveNums(ny, dy)
+        nze = 2 * nz
+        k3 = GetWaveNums(nze, dz)
+        k3mod = getmodCD06stagg(k3, dz)
+        self.k3mc = k3mod * np.exp(1j * (-dz / 2.0) * k3)  # init 194-199
+        self.k3mp = k3mod * np.exp(1j * (dz / 2.0) * k3)
+        kr = (self.k1r[:, None, None] ** 2 + self.k2r[None, :, None] ** 2) + k3mod[None, None, :] ** 2
+        with np.errstate(divide="ignore"):
+            self.kinv = np.where(kr <= 1e-14, 0.0, 1.0 / kr)
+        if stokes:  # init 235-306
+            lam = np.sqrt(self.k1r[:, None] ** 2 + self.k2r[None, :] ** 2)
+            temp = lam * Lz
+            with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+                den = np.where(temp < 500.0, 1.0 / (lam * np.sinh(np.minimum(temp, 500.0)) + 1e-13), 0.0)
+            den[den < 1e-16] = 0.0
+            den[0, 0] = 0.0
+            self.denFact = den
+            zE = np.linspace(0.0, Lz, nz + 1)
+            zC = 0.5 * (zE[:-1] + zE[1:])
+            L3 = lam[:, :, None]
+            t = L3 * (Lz - zC)[None, None, :]
+            self.cosh_bot = np.where(t < 32.0, np.cosh(np.minimum(t, 32.0)), 4e13)
+            t = L3 * zC[None, None, :]
+            self.cosh_top = np.where(t < 32.0, np.cosh(np.minimum(t, 32.0)), 1e13)
+            t = L3 * (Lz - zE)[None, None, :]
+            self.sinh_bot = np.where(t < 32.0, -L3 * np.sinh(np.minimum(t, 32.0)), -4e13)
+            t = L3 * zE[None, None, :]
+            self.sinh_top = np.where(t < 32.0, L3 * np.sinh(np.minimum(t, 32.0)), 4e13)
+
+    def projection(self, uhat, vhat, what):
+        """PressureProjection: returns new (uhat, vhat, what) and the pressure."""
+        nz = self.nz
+        u, v, w = uhat.copy(), vhat.copy(), what.copy()
+        if self.stokes:
+            K1, K2 = self.k1r[:, None, None], self.k2r[None, :, None]
+            chat = -w[:, :, 0] * self.denFact  # bottom (ProjectStokesPressure 331-357)
+            ph = 1j * chat[:, :, None] * self.cosh_bot
+            u -= K1 * ph
+            v -= K2 * ph
+            w[:, :, 0] = 0.0
+            w[:, :, 1:] -= chat[:, :, None] * self.sinh_bot[:, :, 1:]
+            chat = w[:, :, nz] * self.denFact  # top (361-381)
+            ph = 1j * chat[:, :, None] * self.cosh_top
+            u -= K1 * ph
+            v -= K2 * ph
+            w[:, :, :nz] -= chat[:, :, None] * self.sinh_top[:, :, :nz]
+            w[:, :, nz] = 0.0
+        else:
+            K1, K2 = self.k1[:, None, None], self.k2[None, :, None]
+        f2d = 1j * (K1 * u + K2 * v)
+        fext = np.concatenate([f2d[:, :, ::-1], f2d], axis=2)           # step 3 (476-492)
+        wext = np.concatenate([-w[:, :, nz - 1:0:-1], w], axis=2)        # (494-510)
+        F = np.fft.fft(fext, axis=2)
+        W = np.fft.fft(wext, axis=2)
+        F = F + 1j * self.k3mc[None, None, :] * W                        # step 5 (518-526)
+        F = -F * self.kinv
+        W = W - 1j * self.k3mp[None, None, :] * F                        # step 6 (529-536)
+        F = np.fft.ifft(F, axis=2)                                       # step 7, times 1/(2 nz)
+        W = np.fft.ifft(W, axis=2)
+        p = F[:, :, nz:]
+        wn = W[:, :, nz - 1:].copy()
+        wn[:, :, 0] = 0.0
+        wn[:, :, nz] = 0.0
+        return u - 1j * K1 * p, v - 1j * K2 * p, wn, p
+
+    def divergence(self, uhat, vhat, what):
+        """DivergenceCheck steps 1-3 (no fixDiv): odd-odd staggered dw/dz + i k1 u + i k2 v."""
+        K1 = self.k1[:, None, None]
+        K2 = self.k2[None, :, None]
+        f = _stagg_oo(what, self.nz, self.dz, "ddz_E2C") + 1j * K1 * uhat + 1j * K2 * vhat
+        return ifft2_y2x(f, self.nx)
+
+
 def poisson_periodic(rhs, dx, dy, dz, modk=(None, None, None)):
     """PoissonPeriodic.F90:37-111: fft3, times -1/(|k|^2 + 1e-20), zero mode 0, ifft3."""
     nx, ny, nz = rhs.shape

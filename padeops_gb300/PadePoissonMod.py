@@ -1,9 +1,10 @@
 """Mirror of module PadePoissonMod (src/incompressible/PadePoisson.F90): type padepoisson.
 
-The periodic-in-z configuration (``PeriodicInZ = .true.``): the pressure projection that
-is consistent with the staggered CD06 z derivative, and the divergence check.  uhat and
-vhat are complex (nx/2+1, ny, nz) CUDA tensors, what is complex (nx/2+1, ny, nz+1); all
-are updated in place.  The wall-bounded (non-periodic z) solver is not provided.
+Periodic in z (``PeriodicInZ = .true.``) or with walls at z = 0 and Lz (``PeriodicInZ =
+.false.``, with the optional Stokes-pressure wall correction): the pressure projection
+that is consistent with the staggered CD06 z derivative, and the divergence check.  uhat
+and vhat are complex (nx/2+1, ny, nz) CUDA tensors, what is complex (nx/2+1, ny, nz+1);
+all are updated in place.  getPressure / getPressureAndUpdateRHS are not provided.
 """
 import ctypes
 
@@ -17,19 +18,25 @@ class padepoisson:
     def __init__(self):
         self._h = ctypes.c_void_p(None)
 
-    def init(self, dx, dy, dz, sp, PeriodicInZ=True):
-        """PadePoisson.F90:130-200 + InitPeriodicPoissonSolver 76-128."""
-        if not PeriodicInZ:
-            raise L.PadeError(L.PADE_ENOTSUP, "padepoisson.init: only PeriodicInZ is provided")
+    def init(self, dx, dy, dz, sp, PeriodicInZ=True, computeStokesPressure=False, Lz=None):
+        """PadePoisson.F90:130-318 (+ InitPeriodicPoissonSolver 76-128 when PeriodicInZ)."""
         self.destroy()
         h = ctypes.c_void_p(None)
-        L.check(L.lib().pade_poisson_periodic_init(ctypes.byref(h), sp.handle, float(dx), float(dy), float(dz)),
-                "padepoisson.init")
+        if PeriodicInZ:
+            L.check(L.lib().pade_poisson_periodic_init(ctypes.byref(h), sp.handle, float(dx), float(dy), float(dz)),
+                    "padepoisson.init")
+        else:
+            lz = float(Lz) if Lz is not None else float(dz) * sp.nz_g
+            L.check(L.lib().pade_poisson_wall_init(ctypes.byref(h), sp.handle, float(dx), float(dy), float(dz), lz,
+                                                   int(bool(computeStokesPressure))), "padepoisson.init")
         self._h = h
         self._sp = sp  # the handle keeps a pointer to it
-        k3 = np.empty(sp.nz_g)
-        L.check(L.lib().pade_poisson_get_modified_k3(h, k3.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
-        self.k3mod = k3
+        self.PeriodicInZ = bool(PeriodicInZ)
+        self.k3mod = None
+        if PeriodicInZ:
+            k3 = np.empty(sp.nz_g)
+            L.check(L.lib().pade_poisson_get_modified_k3(h, k3.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+            self.k3mod = k3
 
     @property
     def handle(self):

@@ -178,6 +178,7 @@ using namespace pade;
 namespace {
 
 int projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStream_t s) {
+    if (!h->periodic) return wall_projection(h, uhat, vhat, what, s);
     const int nxh = h->nxh, ny = h->ny, nz = h->nz;
     // dwdz at cell centres (PadePoisson.F90:405)
     int rc = pade_apply(h->stagg, 0, 3, 1, what, h->f2d, nxh, ny, 0, 0, PADE_PATH_DF, s);
@@ -343,21 +344,49 @@ int pade_poisson_periodic_init(pade_poisson* out, pade_spectral sp, double dx, d
     return PS_OK;
 }
 
+int pade_poisson_wall_init(pade_poisson* out, pade_spectral sp, double dx, double dy, double dz, double Lz,
+                           int compute_stokes_pressure) {
+    if (!out) return PS_EINVAL;
+    *out = nullptr;
+    if (!sp || !(dx > 0) || !(dy > 0) || !(dz > 0)) return PS_EINVAL;
+    if (compute_stokes_pressure && !(Lz > 0)) return PS_EINVAL;
+    if (!pow2_len(sp->nz) || !pow2_len(2 * sp->nz)) return PS_ENOTSUP;
+    auto* h = new pade_poisson_s();
+    h->sp = sp;
+    h->nx = sp->nx;
+    h->ny = sp->ny;
+    h->nz = sp->nz;
+    h->nxh = sp->nxh;
+    h->dz = dz;
+    h->periodic = 0;
+    h->stokes = compute_stokes_pressure ? 1 : 0;
+    // DivergenceCheck's derivZ%ddz_E2C(.., -1, -1): the odd-odd staggered operator
+    int rc = pade_cd06stagg_init_nonperiodic(&h->stagg, h->nz, dz, 0, 0, 0, 0);
+    if (rc == PS_OK) rc = wall_setup(h, dx, dy, dz, Lz);
+    const size_t plane = (size_t)h->nxh * h->ny;
+    if (rc == PS_OK) rc = dalloc((void**)&h->f2d, sizeof(double2) * plane * h->nz);
+    if (rc == PS_OK) rc = dalloc((void**)&h->part, sizeof(double) * kMaxPartials);
+    if (rc != PS_OK) {
+        pade_poisson_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return PS_OK;
+}
+
 int pade_poisson_destroy(pade_poisson h) {
     if (!h) return PS_OK;
     if (h->stagg) pade_destroy(h->stagg);
-    cudaFree(h->d_k1r);
-    cudaFree(h->d_k2r);
-    cudaFree(h->d_k3m);
-    cudaFree(h->f2d);
-    cudaFree(h->dwE);
-    cudaFree(h->part);
+    void* bufs[] = {h->d_k1r, h->d_k2r, h->d_k3m, h->f2d, h->dwE, h->part, h->d_k3e, h->d_k3mc, h->d_k3mp,
+                    h->fext, h->wext, h->d_den, h->d_coshb, h->d_cosht, h->d_sinhb, h->d_sinht};
+    for (void* b : bufs) cudaFree(b);
     delete h;
     return PS_OK;
 }
 
 int pade_poisson_get_modified_k3(pade_poisson h, double* k3mod) {
     if (!h || !k3mod) return PS_EINVAL;
+    if (!h->periodic) return PS_ENOTSUP;
     for (int k = 0; k < h->nz; k++) k3mod[k] = h->k3mod[k];
     return PS_OK;
 }

@@ -28,6 +28,18 @@ struct pade_poisson_s {
     double2* f2d = nullptr;    // (nxh, ny, nz): dwdz, then the pressure
     double2* dwE = nullptr;    // (nxh, ny, nz+1)
     double* part = nullptr;    // kMaxPartials
+    // walls at z = 0 and Lz (PeriodicInZ false): stagg is then the odd-odd operator
+    int periodic = 1, stokes = 0;
+    double* d_k3e = nullptr;    // CD06-stagg modified wavenumbers of the 2 nz extension
+    double2* d_k3mc = nullptr;  // k3mod exp(-i dz k3 / 2)
+    double2* d_k3mp = nullptr;  // k3mod exp(+i dz k3 / 2)
+    double2* fext = nullptr;    // (nxh, ny, 2 nz)
+    double2* wext = nullptr;    // (nxh, ny, 2 nz)
+    double* d_den = nullptr;    // Stokes pressure: 1 / (lambda sinh(lambda Lz)) (nxh, ny)
+    double* d_coshb = nullptr;  // (nxh, ny, nz)
+    double* d_cosht = nullptr;  // (nxh, ny, nz)
+    double* d_sinhb = nullptr;  // (nxh, ny, nz + 1)
+    double* d_sinht = nullptr;  // (nxh, ny, nz + 1)
 };
 
 struct pade_poisson3d_s {
@@ -65,6 +77,9 @@ int upload(T** d, const std::vector<T>& h) {
 // (FftMul) of the spectral input, oddball, c2r x, 1/(nx ny))
 int spectral_fft(pade_spectral h, const double* in, void* out, cudaStream_t s);
 int spectral_ifft(pade_spectral h, const void* in, double* out, int oddball, cudaStream_t s, int mul = 0);
+// walled padepoisson (poisson_wall.cu): tables of init, and PressureProjection
+int wall_setup(pade_poisson h, double dx, double dy, double dz, double Lz);
+int wall_projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStream_t s);
 // ifft of fhat * G, G = 1 where |k1| < cut1 and |k2| < cut2 (the test filter's TestFilter_oop)
 int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s);
 

@@ -59,3 +59,46 @@ def test_oracle_poisson_manufactured_solution():
     rhs = -(l * l + m * m + n * n) * ftrue
     f = SO.poisson_periodic(rhs, dx, dy, dz)
     assert np.max(np.abs(f - ftrue)) < 1e-13
+
+
+def _wall_velocity(nx, ny, nz, seed, clean=True, wall_w=False):
+    from oracle import spectral_oracle as SO
+
+    rng = np.random.default_rng(seed)
+    u = rng.standard_normal((nx, ny, nz))
+    v = rng.standard_normal((nx, ny, nz))
+    w = rng.standard_normal((nx, ny, nz + 1))
+    if not wall_w:  # no penetration: w = 0 on both walls
+        w[:, :, 0] = 0.0
+        w[:, :, nz] = 0.0
+    hats = [SO.fft2_x2y(a) for a in (u, v, w)]
+    if clean:
+        for a in hats:
+            a[nx // 2, :, :] = 0.0
+            a[:, ny // 2, :] = 0.0
+    return hats
+
+
+@pytest.mark.parametrize("stokes", [False, True])
+def test_wall_projection_oracle_properties(oracle, stokes):
+    """The restated walled projection (PadePoisson.F90:434-624) leaves the field
+    divergence free under the reference's own DivergenceCheck operator (the odd-odd
+    staggered ddz_E2C), with w zero on both walls, and is idempotent.  The plain projection
+    assumes no penetration on input (its odd extension of w is odd only then); with the
+    Stokes-pressure correction a wall-normal velocity on input is removed as well."""
+    from oracle import spectral_oracle as SO
+
+    nx, ny, nz = 16, 8, 16
+    Lz = 1.0
+    wp = SO.WallPoisson(nx, ny, nz, 2 * np.pi / nx, 2 * np.pi / ny, Lz / nz, Lz, stokes=stokes)
+    uh, vh, wh = _wall_velocity(nx, ny, nz, 3, wall_w=stokes)
+    d0 = np.abs(wp.divergence(uh, vh, wh)).max()
+    u2, v2, w2, p = wp.projection(uh, vh, wh)
+    assert np.abs(wp.divergence(u2, v2, w2)).max() < 1e-14 * d0
+    if not stokes:  # without the correction a wall-normal input velocity leaves divergence
+        uw, vw, ww = _wall_velocity(nx, ny, nz, 3, wall_w=True)
+        u4, v4, w4, _ = wp.projection(uw, vw, ww)
+        assert np.abs(wp.divergence(u4, v4, w4)).max() > 1e-3 * np.abs(wp.divergence(uw, vw, ww)).max()
+    assert np.abs(w2[:, :, 0]).max() == 0.0 and np.abs(w2[:, :, nz]).max() == 0.0
+    u3, v3, w3, p3 = wp.projection(u2, v2, w2)
+    assert max(np.abs(u3 - u2).max(), np.abs(w3 - w2).max()) < 1e-13 * np.abs(uh).max()
