@@ -18,9 +18,10 @@ data.  Metric: operator throughput in Gpts/s (points x operator applications per
 `extras` (same line): the FP32 and native-FP64 paths of the step, the tensor-core dense
 (3xTF32) path for every operator of the step with its error against the FP64 path and its
 speed-up, errors of the reduced-precision variants per wavenumber band, the 512^3 periodic
-pressure projection, and the LES: s/step at 256^3 with the dynamic procedure and with the
-learned closure, and the flow statistics (shell spectrum, kinetic energy, resolved and
-SGS dissipation) of learned against dynamic runs at 256^3 (30 steps) and 64^3 (300 steps).
+pressure projection, the 256^3 walled projection (with and without the Stokes pressure),
+and the LES: s/step at 256^3 with the dynamic procedure and with the learned closure, and
+the flow statistics (shell spectrum, kinetic energy, resolved and SGS dissipation) of
+learned against dynamic runs at 256^3 (30 steps) and 64^3 (300 steps).
 
 `--impl reference` times the oracle port alone (the Fortran reference cannot be built on
 this hardware: no Fortran compiler or MPI) and prints its line.
@@ -421,6 +422,25 @@ def extras(args, P, torch, f_host):
                                  "projection_compulsory_GBps": 6 * cbytes / (ms_p * 1e-3) / 1e9,
                                  "note": "double-float radix-2 FFTs on the FP32 pipes (default arithmetic)"}
         del U, V, W, div, phys, sp, po
+        torch.cuda.empty_cache()
+        # walls at z = 0 and Lz (PeriodicInZ false), with and without the Stokes pressure, 256^3
+        n = 256
+        d = 2 * np.pi / n
+        sp = P.spectral()
+        sp.init(n, n, n, d, d)
+        U = torch.randn((n, n, n // 2 + 1), dtype=torch.complex128, device=dev, generator=g)
+        V = torch.randn_like(U)
+        W = torch.randn((n + 1, n, n // 2 + 1), dtype=torch.complex128, device=dev, generator=g)
+        wall = {}
+        for stokes in (False, True):
+            po = P.padepoisson()
+            po.init(d, d, 1.0 / n, sp, PeriodicInZ=False, computeStokesPressure=stokes, Lz=1.0)
+            wall["stokes" if stokes else "plain"] = _time(torch, lambda po=po: po.PressureProjection(U, V, W), 3)
+            del po
+        out["projection_wall_256"] = {"PressureProjection_ms": wall["plain"],
+                                      "PressureProjection_stokes_ms": wall["stokes"],
+                                      "note": "even/odd extension to 2 nz, library FFTs (double-float)"}
+        del U, V, W, sp
         torch.cuda.empty_cache()
     except Exception as ex:  # pragma: no cover
         out["projection_error"] = repr(ex)
