@@ -210,6 +210,17 @@ int pade_poisson_get_modified_k3(pade_poisson p, double* k3mod);
 /* PressureProjection (PadePoisson.F90:386-441 periodic, 434-624 walls): uhat, vhat complex
  * (nx/2+1,ny,nz), what complex (nx/2+1,ny,nz+1), all updated in place. */
 int pade_poisson_projection(pade_poisson p, void* uhat, void* vhat, void* what, void* stream);
+/* getPressure (PadePoisson.F90:716-750 periodic, 752-898 walls): the pressure that the
+ * projection of (uhat, vhat, what) -- right-hand sides in the solver -- would remove, as a
+ * real (nx,ny,nz) field, including the Stokes pressure with walls; the inputs are not
+ * modified.  getPressureAndUpdateRHS (900-1163): the same pressure, and the inputs are
+ * projected in place.  (With walls and the Stokes pressure the reference's
+ * getPressureAndUpdateRHS adds the Stokes-pressure arrays that only getPressure fills; here
+ * the Stokes pressure of the current call is added.) */
+int pade_poisson_get_pressure(pade_poisson p, const void* uhat, const void* vhat, const void* what, double* pressure,
+                              void* stream);
+int pade_poisson_get_pressure_and_update_rhs(pade_poisson p, void* uhat, void* vhat, void* what, double* pressure,
+                                             void* stream);
 /* DivergenceCheck (PadePoisson.F90:1165-1246): divergence real (nx,ny,nz).  fix_div
  * re-projects when max(divergence) > 1e-13 (and again above 1e-10).  maxdiv (host, may be
  * NULL when fix_div is 0) receives the signed maximum of the last divergence computed;

@@ -102,6 +102,10 @@ class PeriodicPoisson:
         f = _stagg_c(what, self.nz, self.dz, "ddz_E2C") + 1j * K1 * uhat + 1j * K2 * vhat
         return ifft2_y2x(f, self.nx)
 
+    def get_pressure(self, uhat, vhat, what):
+        """Periodic_getPressure (PadePoisson.F90:716-750): the projection's pressure, physical."""
+        return ifft2_y2x(self.projection(uhat, vhat, what)[3], self.nx)
+
 
 def _stagg_oo(f, nz, dz, op):
     """Pade6stagg ddz with bot = top = -1 on a non-periodic grid: the odd-odd cd06stagg
@@ -154,16 +158,19 @@ class WallPoisson:
         """PressureProjection: returns new (uhat, vhat, what) and the pressure."""
         nz = self.nz
         u, v, w = uhat.copy(), vhat.copy(), what.copy()
+        self.phat_stokes = None
         if self.stokes:
             K1, K2 = self.k1r[:, None, None], self.k2r[None, :, None]
             chat = -w[:, :, 0] * self.denFact  # bottom (ProjectStokesPressure 331-357)
             ph = 1j * chat[:, :, None] * self.cosh_bot
+            self.phat_stokes = ph
             u -= K1 * ph
             v -= K2 * ph
             w[:, :, 0] = 0.0
             w[:, :, 1:] -= chat[:, :, None] * self.sinh_bot[:, :, 1:]
             chat = w[:, :, nz] * self.denFact  # top (361-381)
             ph = 1j * chat[:, :, None] * self.cosh_top
+            self.phat_stokes = (self.phat_stokes, ph)
             u -= K1 * ph
             v -= K2 * ph
             w[:, :, :nz] -= chat[:, :, None] * self.sinh_top[:, :, :nz]
@@ -185,6 +192,14 @@ class WallPoisson:
         wn[:, :, 0] = 0.0
         wn[:, :, nz] = 0.0
         return u - 1j * K1 * p, v - 1j * K2 * p, wn, p
+
+    def get_pressure(self, uhat, vhat, what):
+        """getPressure (PadePoisson.F90:752-898): the projection's pressure plus, with the
+        Stokes pressure, phat_z1 + phat_z2 of the same fields; physical."""
+        p = self.projection(uhat, vhat, what)[3]
+        if self.stokes:
+            p = (p + self.phat_stokes[0]) + self.phat_stokes[1]
+        return ifft2_y2x(p, self.nx)
 
     def divergence(self, uhat, vhat, what):
         """DivergenceCheck steps 1-3 (no fixDiv): odd-odd staggered dw/dz + i k1 u + i k2 v."""

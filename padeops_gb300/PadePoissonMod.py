@@ -4,7 +4,8 @@ Periodic in z (``PeriodicInZ = .true.``) or with walls at z = 0 and Lz (``Period
 .false.``, with the optional Stokes-pressure wall correction): the pressure projection
 that is consistent with the staggered CD06 z derivative, and the divergence check.  uhat
 and vhat are complex (nx/2+1, ny, nz) CUDA tensors, what is complex (nx/2+1, ny, nz+1);
-all are updated in place.  getPressure / getPressureAndUpdateRHS are not provided.
+all are updated in place; getPressure / getPressureAndUpdateRHS return the pressure in
+physical space.
 """
 import ctypes
 
@@ -49,6 +50,24 @@ class padepoisson:
         pv, _, _ = _dev(vhat, "vhat")
         pw, _, _ = _dev(what, "what")
         L.check(L.lib().pade_poisson_projection(self.handle, pu, pv, pw, s), "PressureProjection")
+
+    def getPressure(self, uhat, vhat, what, pressure):
+        """PadePoisson.F90:716-898: pressure (real (nx, ny, nz) CUDA tensor, physical space)
+        of the right-hand sides uhat, vhat, what, which are left unchanged."""
+        pu, _, s = _dev(uhat, "uhat")
+        pv, _, _ = _dev(vhat, "vhat")
+        pw, _, _ = _dev(what, "what")
+        pp, _, _ = _dev(pressure, "pressure")
+        L.check(L.lib().pade_poisson_get_pressure(self.handle, pu, pv, pw, pp, s), "getPressure")
+
+    def getPressureAndUpdateRHS(self, uhat, vhat, what, pressure):
+        """PadePoisson.F90:900-1163: the pressure, and uhat, vhat, what projected in place."""
+        pu, _, s = _dev(uhat, "uhat")
+        pv, _, _ = _dev(vhat, "vhat")
+        pw, _, _ = _dev(what, "what")
+        pp, _, _ = _dev(pressure, "pressure")
+        L.check(L.lib().pade_poisson_get_pressure_and_update_rhs(self.handle, pu, pv, pw, pp, s),
+                "getPressureAndUpdateRHS")
 
     def DivergenceCheck(self, uhat, vhat, what, divergence, fixDiv=False):
         """Fills divergence; returns max(divergence) (the reference keeps it internal)."""

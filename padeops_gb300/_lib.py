@@ -123,6 +123,8 @@ def lib():
         "pade_spectral_ifft": [vp, vp, vp, i, vp],
         "pade_poisson_periodic_init": [pop, vp, d, d, d],
         "pade_poisson_wall_init": [pop, vp, d, d, d, d, i],
+        "pade_poisson_get_pressure": [vp, vp, vp, vp, vp, vp],
+        "pade_poisson_get_pressure_and_update_rhs": [vp, vp, vp, vp, vp, vp],
         "pade_poisson_destroy": [vp],
         "pade_poisson_get_modified_k3": [vp, dp],
         "pade_poisson_projection": [vp, vp, vp, vp, vp],

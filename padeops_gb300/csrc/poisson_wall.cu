@@ -28,11 +28,13 @@ __global__ void k_wall_stokes(double2* __restrict__ u, double2* __restrict__ v, 
                               const double* __restrict__ k1, const double* __restrict__ k2,
                               const double* __restrict__ den, const double* __restrict__ coshb,
                               const double* __restrict__ cosht, const double* __restrict__ sinhb,
-                              const double* __restrict__ sinht, int nxh, long plane, int nz) {
+                              const double* __restrict__ sinht, double2* __restrict__ chats, int nxh, long plane,
+                              int nz) {
     const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= plane) return;
     const double a = k1[q % nxh], b = k2[q / nxh], d = den[q];
     double2 c = make_double2(-w[q].x * d, -w[q].y * d);
+    chats[q] = c;
     for (int k = 0; k < nz; k++) {
         const long e = q + k * plane;
         const double cb = coshb[e];
@@ -51,6 +53,7 @@ __global__ void k_wall_stokes(double2* __restrict__ u, double2* __restrict__ v, 
     }
     const long top = q + nz * plane;
     c = make_double2(w[top].x * d, w[top].y * d);
+    chats[plane + q] = c;
     for (int k = 0; k < nz; k++) {
         const long e = q + k * plane;
         const double ct = cosht[e], st = sinht[e];
@@ -133,7 +136,34 @@ __global__ void k_wall_restrict(const double2* __restrict__ F, const double2* __
     }
 }
 
+// the pressure of the projection, p(k) = F(nz + k) (times 1/(2 nz) already), plus the
+// Stokes pressure i chat_bot cosh_bot + i chat_top cosh_top (getPressure 862-871)
+__global__ void k_wall_pressure(const double2* __restrict__ F, const double2* __restrict__ chats,
+                                const double* __restrict__ coshb, const double* __restrict__ cosht,
+                                double2* __restrict__ p, long plane, int nz) {
+    const long n = plane * nz;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const long q = e % plane;
+        const int k = (int)(e / plane);
+        double2 v = F[q + (long)(nz + k) * plane];
+        if (chats) {
+            const double2 cb = chats[q], ct = chats[plane + q];
+            const double hb = coshb[e], ht = cosht[e];
+            v.x = (v.x + (-cb.y * hb)) + (-ct.y * ht);
+            v.y = (v.y + cb.x * hb) + ct.x * ht;
+        }
+        p[e] = v;
+    }
+}
+
 }  // namespace
+
+int wall_pressure(pade_poisson h, cudaStream_t s) {
+    const long plane = (long)h->nxh * h->ny;
+    k_wall_pressure<<<grid_for(plane * h->nz), 256, 0, s>>>(h->fext, h->stokes ? h->d_chats : nullptr, h->d_coshb,
+                                                            h->d_cosht, h->f2d, plane, h->nz);
+    return cudaGetLastError() == cudaSuccess ? PS_OK_ : PADE_ECUDA;
+}
 
 int wall_setup(pade_poisson h, double dx, double dy, double dz, double Lz) {
     const int nxh = h->nxh, ny = h->ny, nz = h->nz, nze = 2 * nz;
@@ -157,6 +187,8 @@ int wall_setup(pade_poisson h, double dx, double dy, double dz, double Lz) {
     if (rc == PS_OK_) rc = dalloc((void**)&h->fext, sizeof(double2) * plane * nze);
     if (rc == PS_OK_) rc = dalloc((void**)&h->wext, sizeof(double2) * plane * nze);
     if (rc != PS_OK_ || !h->stokes) return rc;
+    rc = dalloc((void**)&h->d_chats, sizeof(double2) * plane * 2);
+    if (rc != PS_OK_) return rc;
     // Stokes-pressure tables (init 235-306), with the reference's overflow guards
     std::vector<double> den(plane), cb(plane * nz), ct(plane * nz), sb(plane * (nz + 1)), st(plane * (nz + 1));
     std::vector<double> zE(nz + 1), zC(nz);
@@ -203,7 +235,8 @@ int wall_projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStre
     const double* k2 = h->stokes ? h->d_k2r : h->sp->d_k2;
     if (h->stokes) {
         k_wall_stokes<<<(unsigned)((plane + 127) / 128), 128, 0, s>>>(u, v, w, h->d_k1r, h->d_k2r, h->d_den, h->d_coshb,
-                                                                     h->d_cosht, h->d_sinhb, h->d_sinht, nxh, plane, nz);
+                                                                     h->d_cosht, h->d_sinhb, h->d_sinht, h->d_chats,
+                                                                     nxh, plane, nz);
         if (cudaGetLastError() != cudaSuccess) return PADE_ECUDA;
     }
     k_wall_extend<<<grid_for(plane * nze), 256, 0, s>>>(u, v, w, k1, k2, h->fext, h->wext, nxh, plane, nz);

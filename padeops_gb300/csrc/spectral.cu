@@ -204,6 +204,33 @@ int projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStream_t 
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
+// getPressure / getPressureAndUpdateRHS (PadePoisson.F90:716-1163): the projection's
+// pressure (plus the Stokes pressure with walls), as a real (nx, ny, nz) field; `update`
+// also projects uhat, vhat, what, otherwise they are left unchanged (the projection runs
+// on copies).
+int get_pressure(pade_poisson h, void* uhat, void* vhat, void* what, double* pressure, int update, cudaStream_t s) {
+    const size_t plane = (size_t)h->nxh * h->ny;
+    const size_t bc = sizeof(double2) * plane * h->nz, be = sizeof(double2) * plane * (h->nz + 1);
+    void *u = uhat, *v = vhat, *w = what;
+    int rc = PS_OK;
+    if (!update) {
+        if (!h->su) rc = dalloc((void**)&h->su, bc);
+        if (rc == PS_OK && !h->sv) rc = dalloc((void**)&h->sv, bc);
+        if (rc == PS_OK && !h->sw) rc = dalloc((void**)&h->sw, be);
+        if (rc != PS_OK) return rc;
+        if (cudaMemcpyAsync(h->su, uhat, bc, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(h->sv, vhat, bc, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(h->sw, what, be, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return PS_ECUDA;
+        u = h->su;
+        v = h->sv;
+        w = h->sw;
+    }
+    if ((rc = projection(h, u, v, w, s)) != PS_OK) return rc;  // leaves the pressure in f2d (periodic)
+    if (!h->periodic && (rc = wall_pressure(h, s)) != PS_OK) return rc;
+    return spectral_ifft(h->sp, h->f2d, pressure, 0, s);
+}
+
 int divergence(pade_poisson h, const void* uhat, const void* vhat, const void* what, double* div, cudaStream_t s) {
     const int nxh = h->nxh, ny = h->ny, nz = h->nz;
     int rc = pade_apply(h->stagg, 0, 3, 1, what, h->f2d, nxh, ny, 0, 0, PADE_PATH_DF, s);
@@ -378,7 +405,8 @@ int pade_poisson_destroy(pade_poisson h) {
     if (!h) return PS_OK;
     if (h->stagg) pade_destroy(h->stagg);
     void* bufs[] = {h->d_k1r, h->d_k2r, h->d_k3m, h->f2d, h->dwE, h->part, h->d_k3e, h->d_k3mc, h->d_k3mp,
-                    h->fext, h->wext, h->d_den, h->d_coshb, h->d_cosht, h->d_sinhb, h->d_sinht};
+                    h->fext, h->wext, h->d_den, h->d_coshb, h->d_cosht, h->d_sinhb, h->d_sinht, h->d_chats,
+                    h->su, h->sv, h->sw};
     for (void* b : bufs) cudaFree(b);
     delete h;
     return PS_OK;
@@ -417,6 +445,19 @@ int pade_poisson_divergence_check(pade_poisson h, void* uhat, void* vhat, void* 
     }
     if (maxdiv) *maxdiv = m;
     return PS_OK;
+}
+
+int pade_poisson_get_pressure(pade_poisson h, const void* uhat, const void* vhat, const void* what, double* pressure,
+                              void* stream) {
+    if (!h || !device_ptr(uhat) || !device_ptr(vhat) || !device_ptr(what) || !device_ptr(pressure)) return PS_EINVAL;
+    return get_pressure(h, const_cast<void*>(uhat), const_cast<void*>(vhat), const_cast<void*>(what), pressure, 0,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int pade_poisson_get_pressure_and_update_rhs(pade_poisson h, void* uhat, void* vhat, void* what, double* pressure,
+                                             void* stream) {
+    if (!h || !device_ptr(uhat) || !device_ptr(vhat) || !device_ptr(what) || !device_ptr(pressure)) return PS_EINVAL;
+    return get_pressure(h, uhat, vhat, what, pressure, 1, static_cast<cudaStream_t>(stream));
 }
 
 // ---------------------------------------------------------------- PoissonPeriodic

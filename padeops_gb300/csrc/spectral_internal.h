@@ -40,6 +40,10 @@ struct pade_poisson_s {
     double* d_cosht = nullptr;  // (nxh, ny, nz)
     double* d_sinhb = nullptr;  // (nxh, ny, nz + 1)
     double* d_sinht = nullptr;  // (nxh, ny, nz + 1)
+    double2* d_chats = nullptr; // Stokes pressure coefficients of the last projection (2 x nxh x ny)
+    double2* su = nullptr;      // getPressure: copies of its inputs (allocated on first use)
+    double2* sv = nullptr;
+    double2* sw = nullptr;
 };
 
 struct pade_poisson3d_s {
@@ -80,6 +84,8 @@ int spectral_ifft(pade_spectral h, const void* in, double* out, int oddball, cud
 // walled padepoisson (poisson_wall.cu): tables of init, and PressureProjection
 int wall_setup(pade_poisson h, double dx, double dy, double dz, double Lz);
 int wall_projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStream_t s);
+// the pressure of the last walled projection (plus its Stokes pressure) into f2d
+int wall_pressure(pade_poisson h, cudaStream_t s);
 // ifft of fhat * G, G = 1 where |k1| < cut1 and |k2| < cut2 (the test filter's TestFilter_oop)
 int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s);
 

@@ -91,3 +91,36 @@ def test_wall_rejects(native_lib):
     assert po.k3mod is None
     po.destroy()
     sp.destroy()
+
+
+@pytest.mark.parametrize("walls,stokes", [(False, False), (True, False), (True, True)])
+def test_get_pressure_matches_oracle(native_lib, oracle, walls, stokes):
+    nx, ny, nz = 16, 8, 16
+    Lz = 1.3 if walls else 2 * np.pi
+    dx, dy, dz = 2 * np.pi / nx, 2 * np.pi / ny, Lz / nz
+    sp = P.spectral()
+    sp.init(nx, ny, nz, dx, dy)
+    po = P.padepoisson()
+    if walls:
+        po.init(dx, dy, dz, sp, PeriodicInZ=False, computeStokesPressure=stokes, Lz=Lz)
+        ref = SO.WallPoisson(nx, ny, nz, dx, dy, dz, Lz, stokes=stokes)
+        uh, vh, wh = _wall_velocity(nx, ny, nz, 11, clean=False)
+    else:
+        po.init(dx, dy, dz, sp)
+        ref = SO.PeriodicPoisson(nx, ny, nz, dx, dy, dz)
+        uh, vh, wh = _wall_velocity(nx, ny, nz, 11, clean=False)
+        wh = np.asfortranarray(np.concatenate([wh[:, :, :nz], wh[:, :, :1]], axis=2))  # periodic edge plane
+    U, V, W = dev(uh), dev(vh), dev(wh)
+    pr = torch.empty((nz, ny, nx), dtype=torch.float64, device="cuda")
+    po.getPressure(U, V, W, pr)
+    torch.cuda.synchronize()
+    assert relerr(host(pr), ref.get_pressure(uh, vh, wh)) < 1e-12
+    assert relerr(host(U), uh) == 0.0 and relerr(host(W), wh) == 0.0  # inputs unchanged
+    pr2 = torch.empty_like(pr)
+    po.getPressureAndUpdateRHS(U, V, W, pr2)
+    torch.cuda.synchronize()
+    assert relerr(host(pr2), host(pr)) < 1e-14
+    ru, rv, rw, _ = ref.projection(uh, vh, wh)
+    assert relerr(host(U), ru) < 1e-12 and relerr(host(W), rw) < 1e-12
+    po.destroy()
+    sp.destroy()
