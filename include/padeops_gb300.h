@@ -310,6 +310,9 @@ int pade_les_step(pade_les les, int use_graph, void* stream);
 /* last dt, simulated time, completed steps and the dynamic coefficient per z plane (nz
  * entries, may be NULL); synchronises */
 int pade_les_info(pade_les les, double* dt, double* tsim, int* step, double* lambda1d);
+/* simulated time and step counter, as a restart sets them (igrid.F90:2719-2765 reads tsim;
+ * the step continues from the restart's time index) */
+int pade_les_set_time(pade_les les, double tsim, int step);
 /* device pointer of an internal field (PADE_LES_*), valid until pade_les_destroy */
 int pade_les_field(pade_les les, int which, void** ptr);
 /* attach the learned closure used when learnedSGS is set (the object must outlive the

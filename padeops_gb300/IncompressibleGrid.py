@@ -19,6 +19,31 @@ except ImportError:  # pragma: no cover
     torch = None
 
 
+def restart_name(rid, var, tid):
+    """RESTART file name (igrid.F90:2729, 2775): format (A7,A4,I2.2,A3,I6.6), and
+    (A7,A4,I2.2,A6,I6.6) for the info file."""
+    return f"RESTART_Run{rid:02d}_{var}.{tid:06d}"
+
+
+def fortran_g15_5(x):
+    """Fortran list item of format (100g15.5) for one real (the restart info file): F editing
+    with 5 significant digits and 4 trailing blanks when 0.1 <= |x| < 1e5 after rounding,
+    E15.5 otherwise."""
+    x = float(x)
+    if x == 0.0:
+        return f"{'0.0000':>11}    "
+    r = float(f"{abs(x):.5g}") if np.isfinite(x) else abs(x)
+    if np.isfinite(x) and 0.1 <= r < 1e5:
+        k = int(np.floor(np.log10(r))) + 1  # digits before the decimal point
+        if k == 5:  # F11.0 keeps the decimal point
+            return f"{f'{x:.0f}.':>11}    "
+        return f"{x:11.{5 - k}f}    "
+    m, e = f"{abs(x):.4e}".split("e")  # d.dddd e+XX -> 0.ddddd E+(XX+1)
+    mant = "0." + m.replace(".", "")
+    ex = int(e) + 1
+    return f"{('-' if x < 0 else '') + mant + ('E+' if ex >= 0 else 'E-') + f'{abs(ex):02d}':>15}"
+
+
 class igrid:
     def __init__(self):
         self._h = ctypes.c_void_p(None)
@@ -96,6 +121,43 @@ class igrid:
         L.check(L.lib().pade_transpose(1, 2, p, ctypes.c_void_p(t.data_ptr()), n, 1, 1, 8,
                                        torch.cuda.current_stream().cuda_stream))
         return (t.view(torch.complex128) if cplx else t).view(shape)
+
+    def set_time(self, tsim, step):
+        L.check(L.lib().pade_les_set_time(self.handle, float(tsim), int(step)), "igrid.set_time")
+
+    def dumpRestartFile(self, OutputDir, runID=0):
+        """igrid.F90:2767-2802: u, v (nx, ny, nz) and w (nx, ny, nz+1) as raw FP64 in the
+        global x-pencil order of decomp_2d_write_one (column-major, x fastest), and tsim in
+        the _info file; named by runID and the current step.  Returns the step."""
+        import os
+
+        inf = self.info()
+        step = inf["step"]
+        for var in ("u", "v", "w"):
+            self.field(var).cpu().numpy().tofile(os.path.join(OutputDir, restart_name(runID, var, step)))
+        with open(os.path.join(OutputDir, restart_name(runID, "info", step)), "w") as fh:
+            fh.write(fortran_g15_5(inf["tsim"]) + "\n")
+        return step
+
+    def readRestartFile(self, InputDir, tid, rid):
+        """igrid.F90:2719-2765 (u, v, w and tsim), with the step continuing from tid as
+        the reference's init does after reading a restart.  The fields pass through
+        set_fields (transform, dealias, projection: a no-op for a projected field)."""
+        import os
+
+        nx, ny, nz = self.nx, self.ny, self.nz
+        arrs = {}
+        for var, nzz in (("u", nz), ("v", nz), ("w", nz + 1)):
+            a = np.fromfile(os.path.join(InputDir, restart_name(rid, var, tid)), dtype=np.float64)
+            if a.size != nx * ny * nzz:
+                raise L.PadeError(L.PADE_EINVAL, f"readRestartFile: {var} has {a.size} values, expected "
+                                                 f"{nx * ny * nzz}")
+            arrs[var] = torch.from_numpy(a.reshape(nzz, ny, nx)).cuda()
+        with open(os.path.join(InputDir, restart_name(rid, "info", tid))) as fh:
+            tsim = float(fh.readline()[:15].replace("D", "E").replace("d", "e"))
+        self.set_fields(arrs["u"], arrs["v"], arrs["w"])
+        self.set_time(tsim, tid)
+        return tsim
 
     def destroy(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -145,6 +145,7 @@ def lib():
         "pade_les_set_fields": [vp, vp, vp, vp, vp],
         "pade_les_step": [vp, i, vp],
         "pade_les_info": [vp, dp, dp, pi, dp],
+        "pade_les_set_time": [vp, d, i],
         "pade_les_field": [vp, i, pop],
         "pade_les_set_mlp": [vp, vp],
         "pade_mlp_create": [pop],

@@ -845,6 +845,14 @@ int pade_les_set_fields(pade_les h, const double* u, const double* v, const doub
     return cudaStreamSynchronize(s) == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
+int pade_les_set_time(pade_les h, double tsim, int step) {
+    if (!h || step < 0 || !std::isfinite(tsim)) return PS_EINVAL;
+    if (cudaMemcpy(h->d_tsim, &tsim, sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) return PS_ECUDA;
+    h->step = step;
+    h->mstep = step;
+    return PS_OK;
+}
+
 int pade_les_step(pade_les h, int use_graph, void* stream) {
     if (!h) return PS_EINVAL;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
