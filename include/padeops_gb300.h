@@ -286,6 +286,9 @@ typedef struct {
     int learnedPlaneAvg;   /* learnedSGS: 1 = the closure's coefficient averaged over each x-y plane
                               (nu = <Cs^2 Delta^2>_xy |S|, the dynamic procedure's form);
                               0 = pointwise (nu = Cs^2(x) Delta^2 |S|) */
+    int SGSModelID;        /* eddy-viscosity kernel (init_destroy_sgs_igrid.F90:158-165): 0 Smagorinsky,
+                              1 sigma (sigma.F90), 2 AMD (AMD.F90); 1 and 2 with constant coefficients
+                              (DynamicProcedureType 0) */
 } pade_les_params;
 #define PADE_LES_UHAT 0
 #define PADE_LES_VHAT 1

@@ -39,7 +39,8 @@ def _sz(f, nz, dz, op):
 
 class LesOracle:
     def __init__(self, nx, ny, nz, Lx, Ly, Lz, Re=1000.0, CFL=0.5, dynamic=True, Csgs=0.17, deltaRatio=2.0,
-                 DynProcFreq=1, dealiasFact=2.0 / 3.0, t_DivergenceCheck=10, useSGS=True, isInviscid=False):
+                 DynProcFreq=1, dealiasFact=2.0 / 3.0, t_DivergenceCheck=10, useSGS=True, isInviscid=False,
+                 SGSModelID=0):
         self.nx, self.ny, self.nz = nx, ny, nz
         self.dx, self.dy, self.dz = Lx / nx, Ly / ny, Lz / nz
         self.Re, self.CFL = Re, CFL
@@ -68,6 +69,12 @@ class LesOracle:
         self.deltaRat = deltaRatio
         deltaLES = (1.5 * self.dx * 1.5 * self.dy * 1.5 * self.dz) ** (1.0 / 3.0)
         self.cmodel_global = (Csgs * deltaLES) ** 2
+        self.SGSModelID = SGSModelID
+        assert SGSModelID == 0 or not dynamic, "sigma / AMD with constant coefficients only"
+        if SGSModelID == 2:  # AMD.F90:1-14
+            self.camd = (Csgs * self.dx * np.sqrt(1.0 / 12.0), Csgs * self.dy * np.sqrt(1.0 / 12.0),
+                         Csgs * self.dz * (1.0 / np.sqrt(10.0)))
+            self.cmodel_global = 1.0
         self.meanfact = 1.0 / (float(nx) * float(ny))
         # Poisson (PadePoisson.F90:76-128): raw wavenumbers, CD06-stagg modified k3
         k1r = GetWaveNums(nx, self.dx)[:nxh]
@@ -195,6 +202,58 @@ class LesOracle:
         s = s + S[5] * S[5]
         return np.sqrt(2.0 * s)
 
+    @staticmethod
+    def sigma_kernel(d):
+        """sigma.F90:30-95, in the reference's operation order."""
+        G11 = d[0] * d[0] + d[3] * d[3] + d[6] * d[6]
+        G12 = d[0] * d[1] + d[3] * d[4] + d[6] * d[7]
+        G13 = d[0] * d[2] + d[3] * d[5] + d[6] * d[8]
+        G22 = d[1] * d[1] + d[4] * d[4] + d[7] * d[7]
+        G23 = d[1] * d[2] + d[4] * d[5] + d[7] * d[8]
+        G33 = d[2] * d[2] + d[5] * d[5] + d[8] * d[8]
+        I1 = G11 + G22 + G33
+        I1sq = I1 * I1
+        I1cu = I1sq * I1
+        I2 = -(G11 * G11) - G22 * G22 - G33 * G33
+        I2 = I2 - 2.0 * G12 * G12 - 2.0 * G13 * G13
+        I2 = I2 - 2.0 * G23 * G23
+        I2 = I2 + I1sq
+        I2 = 0.5 * I2
+        I3 = G11 * (G22 * G33 - G23 * G23)
+        I3 = I3 + G12 * (G13 * G23 - G12 * G33)
+        I3 = I3 + G13 * (G12 * G23 - G22 * G13)
+        a1 = np.maximum(I1sq / 9.0 - I2 / 3.0, 0.0)
+        a2 = I1cu / 27.0 - I1 * I2 / 6.0 + I3 / 2.0
+        a1s = np.sqrt(a1)
+        t = a2 / (a1 * a1s + 1e-13)
+        t = np.maximum(np.minimum(t, 1.0), -1.0)
+        a3 = (1.0 / 3.0) * np.arccos(t)
+        s1sq = np.maximum(I1 / 3.0 + 2.0 * a1s * np.cos(a3), 0.0)
+        s1 = np.sqrt(s1sq)
+        s2 = np.sqrt(np.maximum((-2.0) * a1s * np.cos(np.pi / 3.0 + a3) + I1 / 3.0, 0.0))
+        s3 = np.sqrt(np.maximum((-2.0) * a1s * np.cos(np.pi / 3.0 - a3) + I1 / 3.0, 0.0))
+        return s3 * (s1 - s2) * (s2 - s3) / (s1sq + 1e-15)
+
+    @staticmethod
+    def amd_kernel(d, S, camd):
+        """AMD.F90:23-72, in the reference's operation order."""
+        cx, cy, cz = camd
+
+        def dot(r, q):
+            return ((d[3 * r] * cx) * (d[3 * q] * cx) + (d[3 * r + 1] * cy) * (d[3 * q + 1] * cy)
+                    + (d[3 * r + 2] * cz) * (d[3 * q + 2] * cz))
+
+        num = dot(0, 0) * S[0]
+        num = num + dot(1, 1) * S[3]
+        num = num + dot(2, 2) * S[5]
+        num = num + 2.0 * dot(0, 1) * S[1]
+        num = num + 2.0 * dot(0, 2) * S[2]
+        num = num + 2.0 * dot(1, 2) * S[4]
+        den = d[0] * d[0]
+        for i in range(1, 9):
+            den = den + d[i] * d[i]
+        return np.maximum(-num / (den + 1e-32), 0.0)
+
     def dynamic_procedure(self, SC, Dsgs):
         """DoStandardDynamicProcedure (standardDynamicProcedure.F90:74-165) -> lambda(z)."""
         Sf = [self.test_filter_r2r(s) for s in SC]
@@ -221,7 +280,12 @@ class LesOracle:
     def sgs_rhs(self, urhs, vrhs, wrhs):
         SC = self.sij(self.duidxjC)
         SE = self.sij(self.duidxjE)
-        nuC = self.smag_kernel(SC)
+        if self.SGSModelID == 1:
+            nuC = self.sigma_kernel(self.duidxjC)
+        elif self.SGSModelID == 2:
+            nuC = self.amd_kernel(self.duidxjC, SC, self.camd)
+        else:
+            nuC = self.smag_kernel(SC)
         if self.dynamic:
             if self.newTimeStep:
                 Dsgs = nuC.copy()

@@ -50,19 +50,22 @@ class igrid:
 
     def init(self, nx, ny, nz, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, Re=1000.0, isInviscid=False, CFL=0.5,
              dt=-1.0, useSGS=True, DynamicProcedureType=1, Csgs=0.17, deltaRatio=2.0, DynProcFreq=1,
-             dealiasFact=2.0 / 3.0, t_DivergenceCheck=10, learnedSGS=False, JudgeFreq=0, learnedPlaneAvg=False):
+             dealiasFact=2.0 / 3.0, t_DivergenceCheck=10, learnedSGS=False, JudgeFreq=0, learnedPlaneAvg=False,
+             SGSModelID=0):
         """igrid init (igrid.F90:330-660) for PeriodicInZ with SGSModelID 0 (Smagorinsky).
 
         learnedSGS replaces the model coefficient by the learned closure (set_mlp), with the
         dynamic procedure run every JudgeFreq steps as its reference (0: never);
         learnedPlaneAvg applies the closure's coefficient averaged over each x-y plane, the
-        form of the dynamic procedure's lambda(z), instead of pointwise."""
+        form of the dynamic procedure's lambda(z), instead of pointwise.  SGSModelID: 0
+        Smagorinsky, 1 sigma, 2 AMD (the last two with DynamicProcedureType 0)."""
         if DynamicProcedureType not in (0, 1):
             raise L.PadeError(L.PADE_ENOTSUP, "only DynamicProcedureType 0 or 1")
         self.destroy()
         p = L.LesParams(nx, ny, nz, Lx, Ly, Lz, Re, int(bool(isInviscid)), CFL, dt, int(bool(useSGS)),
                         int(DynamicProcedureType == 1), Csgs, deltaRatio, DynProcFreq, dealiasFact,
-                        t_DivergenceCheck, int(bool(learnedSGS)), int(JudgeFreq), int(bool(learnedPlaneAvg)))
+                        t_DivergenceCheck, int(bool(learnedSGS)), int(JudgeFreq), int(bool(learnedPlaneAvg)),
+                        int(SGSModelID))
         self.Lx, self.Ly, self.Lz, self.Re = Lx, Ly, Lz, Re
         h = ctypes.c_void_p(None)
         L.check(L.lib().pade_les_init(ctypes.byref(h), ctypes.byref(p)), "igrid.init")

@@ -45,7 +45,8 @@ class LesParams(ctypes.Structure):
                 ("dt", ctypes.c_double), ("useSGS", ctypes.c_int), ("dynamic", ctypes.c_int),
                 ("Csgs", ctypes.c_double), ("deltaRatio", ctypes.c_double), ("DynProcFreq", ctypes.c_int),
                 ("dealiasFact", ctypes.c_double), ("t_DivergenceCheck", ctypes.c_int),
-                ("learnedSGS", ctypes.c_int), ("JudgeFreq", ctypes.c_int), ("learnedPlaneAvg", ctypes.c_int)]
+                ("learnedSGS", ctypes.c_int), ("JudgeFreq", ctypes.c_int), ("learnedPlaneAvg", ctypes.c_int),
+                ("SGSModelID", ctypes.c_int)]
 
 
 MLP_NPARAM = 4929

@@ -126,6 +126,77 @@ __global__ void k_nu_kernel(Ptr9 dC, double* __restrict__ nu, double* __restrict
     }
 }
 
+// sigma model kernel (sigma.F90:30-95): singular values of the velocity gradient from the
+// invariants of G = g^T g; FP64 in the reference's operation order
+__global__ void k_sigma_kernel(Ptr9 d, double* __restrict__ nu, long n) {
+    GRID_STRIDE(e, n) {
+        const double d1 = d.p[0][e], d2 = d.p[1][e], d3 = d.p[2][e], d4 = d.p[3][e], d5 = d.p[4][e],
+                     d6 = d.p[5][e], d7 = d.p[6][e], d8 = d.p[7][e], d9 = d.p[8][e];
+        const double G11 = add(add(mul(d1, d1), mul(d4, d4)), mul(d7, d7));
+        const double G12 = add(add(mul(d1, d2), mul(d4, d5)), mul(d7, d8));
+        const double G13 = add(add(mul(d1, d3), mul(d4, d6)), mul(d7, d9));
+        const double G22 = add(add(mul(d2, d2), mul(d5, d5)), mul(d8, d8));
+        const double G23 = add(add(mul(d2, d3), mul(d5, d6)), mul(d8, d9));
+        const double G33 = add(add(mul(d3, d3), mul(d6, d6)), mul(d9, d9));
+        const double I1 = add(add(G11, G22), G33);
+        const double I1sq = mul(I1, I1), I1cu = mul(I1sq, I1);
+        double I2 = sub(sub(-mul(G11, G11), mul(G22, G22)), mul(G33, G33));
+        I2 = sub(sub(I2, mul(mul(2.0, G12), G12)), mul(mul(2.0, G13), G13));
+        I2 = sub(I2, mul(mul(2.0, G23), G23));
+        I2 = add(I2, I1sq);
+        I2 = mul(0.5, I2);
+        double I3 = mul(G11, sub(mul(G22, G33), mul(G23, G23)));
+        I3 = add(I3, mul(G12, sub(mul(G13, G23), mul(G12, G33))));
+        I3 = add(I3, mul(G13, sub(mul(G12, G23), mul(G22, G13))));
+        double a1 = sub(I1sq / 9.0, I2 / 3.0);
+        a1 = fmax(a1, 0.0);
+        const double a2 = add(sub(I1cu / 27.0, mul(I1, I2) / 6.0), I3 / 2.0);
+        const double a1s = sqrt(a1);
+        double t = mul(a1, a1s);
+        t = a2 / add(t, 1e-13);
+        t = fmin(t, 1.0);
+        t = fmax(t, -1.0);
+        t = acos(t);
+        const double a3 = mul(1.0 / 3.0, t);
+        const double third = I1 / 3.0;
+        double s1sq = add(third, mul(mul(2.0, a1s), cos(a3)));
+        s1sq = fmax(s1sq, 0.0);
+        const double s1 = sqrt(s1sq);
+        const double pi3 = 3.14159265358979323846 / 3.0;
+        double s2 = mul(mul(-2.0, a1s), cos(add(pi3, a3)));
+        s2 = sqrt(fmax(add(s2, third), 0.0));
+        double s3 = mul(mul(-2.0, a1s), cos(sub(pi3, a3)));
+        s3 = sqrt(fmax(add(s3, third), 0.0));
+        nu[e] = mul(mul(s3, sub(s1, s2)), sub(s2, s3)) / add(s1sq, 1e-15);
+    }
+}
+
+// AMD model kernel (AMD.F90:23-72), with S_ij from the same gradients
+__global__ void k_amd_kernel(Ptr9 d, double cx, double cy, double cz, double* __restrict__ nu, long n) {
+    GRID_STRIDE(e, n) {
+        double g[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) g[i] = d.p[i][e];
+        const double S[6] = {sij(d.p, 0, e), sij(d.p, 1, e), sij(d.p, 2, e),
+                             sij(d.p, 3, e), sij(d.p, 4, e), sij(d.p, 5, e)};
+        // row r of the scaled gradient: (g[3r] cx, g[3r+1] cy, g[3r+2] cz)
+        auto dot = [&](int r, int q) {
+            return add(add(mul(mul(g[3 * r], cx), mul(g[3 * q], cx)), mul(mul(g[3 * r + 1], cy), mul(g[3 * q + 1], cy))),
+                       mul(mul(g[3 * r + 2], cz), mul(g[3 * q + 2], cz)));
+        };
+        double num = mul(dot(0, 0), S[0]);
+        num = add(num, mul(dot(1, 1), S[3]));
+        num = add(num, mul(dot(2, 2), S[5]));
+        num = add(num, mul(mul(2.0, dot(0, 1)), S[1]));
+        num = add(num, mul(mul(2.0, dot(0, 2)), S[2]));
+        num = add(num, mul(mul(2.0, dot(1, 2)), S[4]));
+        double den = mul(g[0], g[0]);
+#pragma unroll
+        for (int i = 1; i < 9; i++) den = add(den, mul(g[i], g[i]));
+        nu[e] = fmax(-num / add(den, 1e-32), 0.0);
+    }
+}
+
 // |S| of six arrays
 __global__ void k_smag6(const double* s0, const double* s1, const double* s2, const double* s3, const double* s4,
                         const double* s5, double* __restrict__ out, long n) {
@@ -354,6 +425,7 @@ struct pade_les_s {
     double* d_k3 = nullptr;  // spectral k3 (oddball sign flipped) for the dealias mask
     double cut_x = 0, cut_y = 0, cut_z = 0, tf_x = 0, tf_y = 0;
     double cmodel_global = 0, meanfact = 0, tvisc = 0;
+    double camd_x = 0, camd_y = 0, camd_z = 0;
     // spectral state and stage copies
     double2 *uhat = nullptr, *vhat = nullptr, *what = nullptr;
     double2 *uhat1 = nullptr, *vhat1 = nullptr, *what1 = nullptr;
@@ -569,7 +641,13 @@ int sgs_rhs(pade_les h, cudaStream_t s) {
             CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, s));
         }
     } else {
-        k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
+        if (h->prm.SGSModelID == 1) {
+            k_sigma_kernel<<<g, 256, 0, s>>>(dC, h->nuC, n);
+        } else if (h->prm.SGSModelID == 2) {
+            k_amd_kernel<<<g, 256, 0, s>>>(dC, h->camd_x, h->camd_y, h->camd_z, h->nuC, n);
+        } else {
+            k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
+        }
         KCHECK();
         if (dyn && h->newTimeStep && h->mstep % std::max(1, h->prm.DynProcFreq) == 0) CK(dynamic_procedure(h, s));
         k_scale_nu<<<g, 256, 0, s>>>(h->nuC, dyn ? h->lambda : nullptr, h->cmodel_global, h->plane, n);
@@ -727,6 +805,8 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
     if (!(p->isInviscid) && !(p->Re > 0)) return PS_EINVAL;
     if (!(p->CFL > 0) && !(p->dt > 0)) return PS_EINVAL;
     if (p->useSGS && (p->dynamic || p->learnedSGS) && !(p->deltaRatio > 0)) return PS_EINVAL;
+    if (p->SGSModelID < 0 || p->SGSModelID > 2) return PS_EINVAL;
+    if (p->useSGS && p->SGSModelID != 0 && (p->dynamic || p->learnedSGS)) return PS_ENOTSUP;
     if (p->useSGS && p->learnedSGS && !(p->Re > 0)) return PS_EINVAL;  // features use the molecular 1/Re
     for (int n : {p->nx, p->ny, p->nz})
         if (n > 8192 || (n & (n - 1)) != 0) return PS_ENOTSUP;
@@ -755,6 +835,12 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
     const double deltaLES = std::pow(1.5 * h->dx * 1.5 * h->dy * 1.5 * h->dz, 1.0 / 3.0);
     h->deltaLES = deltaLES;
     h->cmodel_global = (p->Csgs * deltaLES) * (p->Csgs * deltaLES);
+    if (p->SGSModelID == 2) {  // AMD.F90:1-14: anisotropic constants, cd06 Poincare constant in z
+        h->camd_x = p->Csgs * h->dx * std::sqrt(1.0 / 12.0);
+        h->camd_y = p->Csgs * h->dy * std::sqrt(1.0 / 12.0);
+        h->camd_z = p->Csgs * h->dz * (1.0 / std::sqrt(10.0));
+        h->cmodel_global = 1.0;
+    }
     h->meanfact = 1.0 / ((double)h->nx * (double)h->ny);
     const double mn = std::min(h->dx, std::min(h->dy, h->dz));
     h->tvisc = p->CFL * p->Re * (mn * mn);

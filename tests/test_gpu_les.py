@@ -59,7 +59,8 @@ def test_init_sequence_matches_oracle(oracle):
 
 
 @pytest.mark.parametrize("kw", [dict(dynamic=True), dict(dynamic=False), dict(useSGS=False),
-                                dict(useSGS=False, isInviscid=True)])
+                                dict(useSGS=False, isInviscid=True), dict(dynamic=False, SGSModelID=1),
+                                dict(dynamic=False, SGSModelID=2)])
 def test_two_steps_match_oracle(oracle, kw):
     g, ref = _pair(16, oracle, **kw)
     for step in range(2):

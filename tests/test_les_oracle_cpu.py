@@ -82,3 +82,48 @@ def test_dynamic_coefficient_nonnegative_and_planar(built):
     assert les.lambda1d.shape == (16,)
     assert np.all(les.lambda1d >= 0)
     assert les.lambda1d.max() > 0
+
+
+def _grad_list(g):
+    """(3, 3, ...) gradient g[i, j] = d u_i / d x_j -> the 9-array list duidxj(1..9)."""
+    return [g[i, j] for i in range(3) for j in range(3)]
+
+
+def test_sigma_kernel_against_singular_values():
+    """sigma.F90: nu / (C Delta)^2 = s3 (s1 - s2)(s2 - s3) / s1^2 from the singular values
+    of the velocity gradient: zero for pure shear, solid rotation and axisymmetric strain
+    (the model's defining properties), and the SVD value for general gradients."""
+    from oracle.les_oracle import LesOracle as LO
+
+    special = [np.array([[0, 1, 0], [0, 0, 0], [0, 0, 0]], float),
+               np.array([[0, 1, 0], [-1, 0, 0], [0, 0, 0]], float),
+               np.diag([1.0, -0.5, -0.5])]
+    for g in special:
+        nu = LO.sigma_kernel(_grad_list(g[:, :, None]))
+        # acos at exactly +-1 (equal singular values) turns the reference's 1e-13
+        # regularisation and last-bit rounding into ~sqrt(eps) of the gradient scale
+        assert abs(float(nu[0])) < 1e-6
+    rng = np.random.default_rng(3)
+    G = rng.standard_normal((3, 3, 200))
+    nu = LO.sigma_kernel(_grad_list(G))
+    s = np.linalg.svd(np.moveaxis(G, 2, 0), compute_uv=False)  # descending
+    ref = s[:, 2] * (s[:, 0] - s[:, 1]) * (s[:, 1] - s[:, 2]) / (s[:, 0] ** 2)
+    assert np.max(np.abs(nu - ref)) < 1e-9 * np.max(np.abs(ref))
+    assert np.all(nu >= 0)
+
+
+def test_amd_kernel_against_contraction():
+    """AMD.F90: nu = max(-(C_k g_ik)(C_k g_jk) S_ij / (g_lm g_lm), 0)."""
+    from oracle.les_oracle import LesOracle as LO
+
+    rng = np.random.default_rng(4)
+    G = rng.standard_normal((3, 3, 100))
+    c = (0.3, 0.2, 0.1)
+    S = 0.5 * (G + np.swapaxes(G, 0, 1))
+    Gs = G * np.array(c)[None, :, None]
+    num = np.einsum("ikn,jkn,ijn->n", Gs, Gs, S)
+    ref = np.maximum(-num / np.einsum("ijn,ijn->n", G, G), 0.0)
+    Sl = [S[0, 0], S[0, 1], S[0, 2], S[1, 1], S[1, 2], S[2, 2]]
+    nu = LO.amd_kernel(_grad_list(G), Sl, c)
+    assert np.max(np.abs(nu - ref)) < 1e-14 * np.max(np.abs(ref))
+    assert np.count_nonzero(nu) > 10 and np.count_nonzero(nu == 0) > 10  # both signs of num occur
