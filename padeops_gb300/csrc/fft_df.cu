@@ -113,20 +113,47 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     extern __shared__ __align__(16) float4 smf[];
     double2* smd = reinterpret_cast<double2*>(smf);
     __shared__ int emax[64];
+    // per line: input / output offsets, its index a in the first extent, and for the fused
+    // kinds its (x, y) wavenumber indices (one division per line, none per element)
+    __shared__ long lbin[64], lbout[64];
+    __shared__ int la[64], lxi[64], lyj[64];
     const int n = 1 << logn, half = n >> 1;
     const long l0 = (long)blockIdx.x * lb;
     const int nl = (int)min((long)lb, ls.nlines - l0);
     const int total = nl << logn;
     const bool pin = ls.fp == 1, pout = ls.op == 1;
-    for (int l = threadIdx.x; l < nl; l += blockDim.x) emax[l] = 0;
+    for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+        emax[l] = 0;
+        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+        lbin[l] = a * ls.fa + b * ls.fb;
+        lbout[l] = a * ls.oa + b * ls.ob;
+        la[l] = (int)a;
+        if (KIND != FK_PLAIN) {
+            lxi[l] = (int)(lg % ex.nxh);
+            lyj[l] = (int)(lg / ex.nxh);
+        }
+    }
     __syncthreads();
+    // element e = (l, p): e = l n + p on contiguous lines, e = p nl + l on strided lines
+    // (consecutive threads on consecutive lines); strided positions advance by (sl, sp)
+    const int sl = blockDim.x % nl, sp = blockDim.x / nl;
 
     // ---- load (FP64, natural order) and the per-line maximum exponent
+    int ls_l = threadIdx.x % nl, ls_p = threadIdx.x / nl;
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int l = pin ? (e >> logn) : (e % nl);
-        const int p = pin ? (e & (n - 1)) : (e / nl);
-        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
-        const long base = a * ls.fa + b * ls.fb;
+        const int l = pin ? (e >> logn) : ls_l;
+        const int p = pin ? (e & (n - 1)) : ls_p;
+        if (!pin) {
+            ls_l += sl;
+            ls_p += sp;
+            if (ls_l >= nl) {
+                ls_l -= nl;
+                ls_p++;
+            }
+        }
+        const long lg = l0 + l;
+        const int a = la[l];
+        const long base = lbin[l];
         double2 v;
         if (IN == IN_COMPLEX) {
             v = reinterpret_cast<const double2*>(in)[base + p * ls.fp];
@@ -151,7 +178,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
         }
         if (KIND == FK_PROJECT) {
             const long idx = lg + p * ex.plane;
-            const double k1 = ex.k1[lg % ex.nxh], k2 = ex.k2[lg / ex.nxh];
+            const double k1 = ex.k1[lxi[l]], k2 = ex.k2[lyj[l]];
             const double2 uu = ex.u[idx], vv = ex.v[idx];
             const double tx = __dadd_rn(__dmul_rn(k1, uu.x), __dmul_rn(k2, vv.x));
             const double ty = __dadd_rn(__dmul_rn(k1, uu.y), __dmul_rn(k2, vv.y));
@@ -177,7 +204,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             const int l = e >> logn, q = e & (n - 1);
             const int f = brev(q, logn);  // frequency held at position q
             const long lg = l0 + l;
-            const long i = lg % ex.nxh, j = lg / ex.nxh;
+            const int i = lxi[l], j = lyj[l];
             if (KIND == FK_DEALIAS) {
                 const bool keep = fabs(ex.ka[i]) < ex.cut_a && fabs(ex.kb[j]) < ex.cut_b && fabs(ex.kc[f]) < ex.cut_c;
                 if (!keep) stc(smf, e, cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}});
@@ -201,12 +228,21 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     // ---- store (FP64)
     const int nout = OUT == OUT_HALF ? half + 1 : n;
     const dfv sdf{scale_df.x, scale_df.y};
+    int ss_l = threadIdx.x % nl, ss_p = threadIdx.x / nl;
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int l = pout ? (e >> logn) : (e % nl);
-        const int p = pout ? (e & (n - 1)) : (e / nl);
+        const int l = pout ? (e >> logn) : ss_l;
+        const int p = pout ? (e & (n - 1)) : ss_p;
+        if (!pout) {
+            ss_l += sl;
+            ss_p += sp;
+            if (ss_l >= nl) {
+                ss_l -= nl;
+                ss_p++;
+            }
+        }
         if (p >= nout) continue;
-        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
-        const long o = a * ls.oa + b * ls.ob + p * ls.op;
+        const long lg = l0 + l;
+        const long o = lbout[l] + p * ls.op;
         cdf c = ldc(smf, (l << logn) + (KIND == FK_PLAIN ? brev(p, logn) : p));
         if (use_scale_df) c = cscale(c, sdf);
         const int k = emax[l] - 1023 + scale_exp;
@@ -219,7 +255,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
         if (KIND == FK_DEALIAS && ex.edge_copy && p == 0) reinterpret_cast<double2*>(out)[o + (long)n * ls.op] = v;
         if (KIND == FK_PROJECT) {
             const long idx = lg + p * ex.plane;
-            const double k1 = ex.k1[lg % ex.nxh], k2 = ex.k2[lg / ex.nxh];
+            const double k1 = ex.k1[lxi[l]], k2 = ex.k2[lyj[l]];
             double2 uu = ex.u[idx], vv = ex.v[idx];
             uu = make_double2(uu.x + k1 * v.y, uu.y - k1 * v.x);
             vv = make_double2(vv.x + k2 * v.y, vv.y - k2 * v.x);
@@ -253,16 +289,21 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     __shared__ int emax[64];
     __shared__ float4 xlast[64];  // c2r: X[M] of each line (split)
     __shared__ double2 xlast_raw[64];
+    __shared__ long lbin[64], lbout[64];  // per-line input / output offsets
     const int logM = logN - 1, M = 1 << logM;
     const long l0 = (long)blockIdx.x * lb;
     const int nl = (int)min((long)lb, ls.nlines - l0);
     const int total = nl << logM;
-    for (int l = threadIdx.x; l < nl; l += blockDim.x) emax[l] = 0;
+    for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+        emax[l] = 0;
+        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
+        lbin[l] = a * ls.fa + b * ls.fb;
+        lbout[l] = a * ls.oa + b * ls.ob;
+    }
     __syncthreads();
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
         const int l = e >> logM, j = e & (M - 1);
-        const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
-        const long base = a * ls.fa + b * ls.fb;
+        const long base = lbin[l];
         double2 v;
         if (R2C) {
             v = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(in) + base + 2 * j);
@@ -275,8 +316,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     }
     if (!R2C) {
         for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-            const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
-            double2 v = reinterpret_cast<const double2*>(in)[a * ls.fa + b * ls.fb + M];
+            double2 v = reinterpret_cast<const double2*>(in)[lbin[l] + M];
             v.y = 0.0;
             if (oddball) v.x = 0.0;
             xlast_raw[l] = v;
@@ -322,8 +362,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             // X = (sm - i t) / 2, -i t = (t.i, -t.r)
             cdf X = chalf(cdf{df_norm(df_add(sm.r, t.i)), df_norm(df_sub(sm.i, t.r))});
             if (use_scale_df) X = cscale(X, sdf);
-            const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
-            reinterpret_cast<double2*>(out)[a * ls.oa + b * ls.ob + k] = cstore(X, emax[l] - 1023 + scale_exp);
+            reinterpret_cast<double2*>(out)[lbout[l] + k] = cstore(X, emax[l] - 1023 + scale_exp);
         }
     } else {
         // pairs (k, M-k) for k = 0 .. M/2 - 1, in place; X[M] of k = 0 comes from xlast
@@ -363,8 +402,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             const int l = e >> logM, j = e & (M - 1);
             cdf w = ldc(smf, (l << logM) + brev(j, logM));
             if (use_scale_df) w = cscale(w, sdf);
-            const long lg = l0 + l, a = lg % ls.na, b = lg / ls.na;
-            *reinterpret_cast<double2*>(reinterpret_cast<double*>(out) + a * ls.oa + b * ls.ob + 2 * j) =
+            *reinterpret_cast<double2*>(reinterpret_cast<double*>(out) + lbout[l] + 2 * j) =
                 cstore(w, emax[l] - 1023 + scale_exp);
         }
     }
