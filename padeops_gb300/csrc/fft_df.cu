@@ -57,6 +57,17 @@ __device__ __forceinline__ cdf cmulw(cdf a, float4 w, bool conj) {
 
 __device__ __forceinline__ cdf cscale(cdf a, dfv m) { return cdf{df_norm(df_mul(a.r, m)), df_norm(df_mul(a.i, m))}; }
 
+// raises the line maximum emax[l] to m; `warp_line` (uniform over the block) says that the
+// 32 lanes of each warp hold points of one line, so one lane updates it for the warp
+__device__ __forceinline__ void emax_update(int* emax, int l, int m, bool warp_line) {
+    if (warp_line) {
+        m = __reduce_max_sync(0xffffffffu, m);
+        if ((threadIdx.x & 31) == 0) atomicMax(&emax[l], m);
+    } else {
+        atomicMax(&emax[l], m);
+    }
+}
+
 __device__ __forceinline__ int brev(int p, int logn) { return (int)(__brev((unsigned)p) >> (32 - logn)); }
 
 __device__ __forceinline__ double ksq(double a, double b, double c) {
@@ -64,42 +75,94 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
 }
 
 // decimation in frequency: natural order -> bit-reversed.  tw holds exp(-2 pi i t / (n 2^tws)),
-// so a table made for a longer transform serves with stride 2^tws.
+// so a table made for a longer transform serves with stride 2^tws.  Stages s and s - 1 run
+// fused (one pass over shared memory per two stages, four points per thread); the
+// arithmetic is that of the radix-2 stages, operation for operation.
 __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj,
                                        int tws = 0) {
-    const int half = 1 << (logn - 1);
-    const int work = nl << (logn - 1);
-    for (int s = logn - 1; s >= 0; s--) {
+    int s = logn - 1;
+    for (; s >= 1; s -= 2) {
+        const int work4 = nl << (logn - 2);
+        const int h = 1 << (s - 1);  // quarter of a block of 2^(s+1)
+        const int t1 = logn - 1 - s + tws, t2 = logn - s + tws;
+        for (int e = threadIdx.x; e < work4; e += blockDim.x) {
+            const int l = e >> (logn - 2), j = e & ((1 << (logn - 2)) - 1);
+            const int k = j & (h - 1);
+            const int i0 = (l << logn) + ((j >> (s - 1)) << (s + 1)) + k;
+            const cdf x0 = ldc(x, i0), x1 = ldc(x, i0 + h), x2 = ldc(x, i0 + 2 * h), x3 = ldc(x, i0 + 3 * h);
+            // stage s: (x0, x2) at offset k, (x1, x3) at offset k + h
+            const cdf a0 = cadd(x0, x2), a1 = cadd(x1, x3);
+            const cdf a2 = cmulw(csub(x0, x2), __ldg(&tw[k << t1]), conj);
+            const cdf a3 = cmulw(csub(x1, x3), __ldg(&tw[(k + h) << t1]), conj);
+            // stage s - 1: (a0, a1) and (a2, a3), both at offset k
+            stc(x, i0, cadd(a0, a1));
+            stc(x, i0 + 2 * h, cadd(a2, a3));
+            if (s == 1) {
+                stc(x, i0 + h, csub(a0, a1));
+                stc(x, i0 + 3 * h, csub(a2, a3));
+            } else {
+                const float4 w = __ldg(&tw[k << t2]);
+                stc(x, i0 + h, cmulw(csub(a0, a1), w, conj));
+                stc(x, i0 + 3 * h, cmulw(csub(a2, a3), w, conj));
+            }
+        }
+        __syncthreads();
+    }
+    if (s == 0) {  // odd logn: the last stage alone
+        const int work = nl << (logn - 1);
         for (int e = threadIdx.x; e < work; e += blockDim.x) {
-            const int l = e >> (logn - 1), j = e & (half - 1);
-            const int k = j & ((1 << s) - 1);
-            const int i0 = (l << logn) + ((j >> s) << (s + 1)) + k;
-            const int i1 = i0 + (1 << s);
-            const cdf a = ldc(x, i0), b = ldc(x, i1);
+            const int i0 = e << 1;
+            const cdf a = ldc(x, i0), b = ldc(x, i0 + 1);
             stc(x, i0, cadd(a, b));
-            const cdf d = csub(a, b);
-            stc(x, i1, s == 0 ? d : cmulw(d, __ldg(&tw[k << (logn - 1 - s + tws)]), conj));
+            stc(x, i0 + 1, csub(a, b));
         }
         __syncthreads();
     }
 }
 
-// decimation in time: bit-reversed -> natural order
+// decimation in time: bit-reversed -> natural order; stages s and s + 1 fused as in dif_df
 __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj,
                                        int tws = 0) {
-    const int half = 1 << (logn - 1);
-    const int work = nl << (logn - 1);
-    for (int s = 0; s < logn; s++) {
+    int s = 0;
+    for (; s + 1 < logn; s += 2) {
+        const int work4 = nl << (logn - 2);
+        const int h = 1 << s;  // quarter of a block of 2^(s+2)
+        const int t1 = logn - 1 - s + tws, t2 = logn - 2 - s + tws;
+        for (int e = threadIdx.x; e < work4; e += blockDim.x) {
+            const int l = e >> (logn - 2), j = e & ((1 << (logn - 2)) - 1);
+            const int k = j & (h - 1);
+            const int i0 = (l << logn) + ((j >> s) << (s + 2)) + k;
+            const cdf x0 = ldc(x, i0), x2 = ldc(x, i0 + 2 * h);
+            cdf x1 = ldc(x, i0 + h), x3 = ldc(x, i0 + 3 * h);
+            // stage s: (x0, x1) and (x2, x3), both at offset k
+            if (s > 0) {
+                const float4 w = __ldg(&tw[k << t1]);
+                x1 = cmulw(x1, w, conj);
+                x3 = cmulw(x3, w, conj);
+            }
+            const cdf a0 = cadd(x0, x1), a1 = csub(x0, x1);
+            cdf a2 = cadd(x2, x3), a3 = csub(x2, x3);
+            // stage s + 1: (a0, a2) at offset k, (a1, a3) at offset k + h
+            a2 = cmulw(a2, __ldg(&tw[k << t2]), conj);
+            a3 = cmulw(a3, __ldg(&tw[(k + h) << t2]), conj);
+            stc(x, i0, cadd(a0, a2));
+            stc(x, i0 + 2 * h, csub(a0, a2));
+            stc(x, i0 + h, cadd(a1, a3));
+            stc(x, i0 + 3 * h, csub(a1, a3));
+        }
+        __syncthreads();
+    }
+    if (s == logn - 1) {  // odd logn: the last stage alone
+        const int half = 1 << s;
+        const int work = nl << (logn - 1);
         for (int e = threadIdx.x; e < work; e += blockDim.x) {
-            const int l = e >> (logn - 1), j = e & (half - 1);
-            const int k = j & ((1 << s) - 1);
-            const int i0 = (l << logn) + ((j >> s) << (s + 1)) + k;
-            const int i1 = i0 + (1 << s);
+            const int l = e >> (logn - 1), k = e & (half - 1);
+            const int i0 = (l << logn) + k;
             const cdf a = ldc(x, i0);
-            cdf b = ldc(x, i1);
-            if (s > 0) b = cmulw(b, __ldg(&tw[k << (logn - 1 - s + tws)]), conj);
+            cdf b = ldc(x, i0 + half);
+            if (s > 0) b = cmulw(b, __ldg(&tw[k << tws]), conj);
             stc(x, i0, cadd(a, b));
-            stc(x, i1, csub(a, b));
+            stc(x, i0 + half, csub(a, b));
         }
         __syncthreads();
     }
@@ -185,7 +248,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             v = make_double2(v.x - ty, v.y + tx);
         }
         smd[(l << logn) + p] = v;
-        atomicMax(&emax[l], max(bexp(v.x), bexp(v.y)));
+        emax_update(emax, l, max(bexp(v.x), bexp(v.y)), pin && logn >= 5);
     }
     __syncthreads();
     // ---- split in place, each line scaled by 2^-(emax - 1023)
@@ -312,7 +375,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             if (j == 0) v.y = 0.0;
         }
         smd[e] = v;
-        atomicMax(&emax[l], max(bexp(v.x), bexp(v.y)));
+        emax_update(emax, l, max(bexp(v.x), bexp(v.y)), logM >= 5);
     }
     if (!R2C) {
         for (int l = threadIdx.x; l < nl; l += blockDim.x) {
