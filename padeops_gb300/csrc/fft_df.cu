@@ -75,11 +75,12 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
 }
 
 // decimation in frequency: natural order -> bit-reversed.  tw holds exp(-2 pi i t / (n 2^tws)),
-// so a table made for a longer transform serves with stride 2^tws.  Stages s and s - 1 run
+// so a table made for a longer transform serves with stride 2^tws; line l starts at l * lsd
+// (lsd >= 2^logn, padded to spread lines over the banks).  Stages s and s - 1 run
 // fused (one pass over shared memory per two stages, four points per thread); the
 // arithmetic is that of the radix-2 stages, operation for operation.
-__device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj,
-                                       int tws = 0) {
+__device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, const float4* __restrict__ tw,
+                                       bool conj, int tws = 0) {
     int s = logn - 1;
     for (; s >= 1; s -= 2) {
         const int work4 = nl << (logn - 2);
@@ -88,7 +89,7 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4
         for (int e = threadIdx.x; e < work4; e += blockDim.x) {
             const int l = e >> (logn - 2), j = e & ((1 << (logn - 2)) - 1);
             const int k = j & (h - 1);
-            const int i0 = (l << logn) + ((j >> (s - 1)) << (s + 1)) + k;
+            const int i0 = l * lsd + ((j >> (s - 1)) << (s + 1)) + k;
             const cdf x0 = ldc(x, i0), x1 = ldc(x, i0 + h), x2 = ldc(x, i0 + 2 * h), x3 = ldc(x, i0 + 3 * h);
             // stage s: (x0, x2) at offset k, (x1, x3) at offset k + h
             const cdf a0 = cadd(x0, x2), a1 = cadd(x1, x3);
@@ -111,7 +112,7 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4
     if (s == 0) {  // odd logn: the last stage alone
         const int work = nl << (logn - 1);
         for (int e = threadIdx.x; e < work; e += blockDim.x) {
-            const int i0 = e << 1;
+            const int i0 = (e >> (logn - 1)) * lsd + ((e & ((1 << (logn - 1)) - 1)) << 1);
             const cdf a = ldc(x, i0), b = ldc(x, i0 + 1);
             stc(x, i0, cadd(a, b));
             stc(x, i0 + 1, csub(a, b));
@@ -121,8 +122,8 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, const float4
 }
 
 // decimation in time: bit-reversed -> natural order; stages s and s + 1 fused as in dif_df
-__device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4* __restrict__ tw, bool conj,
-                                       int tws = 0) {
+__device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, const float4* __restrict__ tw,
+                                       bool conj, int tws = 0) {
     int s = 0;
     for (; s + 1 < logn; s += 2) {
         const int work4 = nl << (logn - 2);
@@ -131,7 +132,7 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4
         for (int e = threadIdx.x; e < work4; e += blockDim.x) {
             const int l = e >> (logn - 2), j = e & ((1 << (logn - 2)) - 1);
             const int k = j & (h - 1);
-            const int i0 = (l << logn) + ((j >> s) << (s + 2)) + k;
+            const int i0 = l * lsd + ((j >> s) << (s + 2)) + k;
             const cdf x0 = ldc(x, i0), x2 = ldc(x, i0 + 2 * h);
             cdf x1 = ldc(x, i0 + h), x3 = ldc(x, i0 + 3 * h);
             // stage s: (x0, x1) and (x2, x3), both at offset k
@@ -157,7 +158,7 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, const float4
         const int work = nl << (logn - 1);
         for (int e = threadIdx.x; e < work; e += blockDim.x) {
             const int l = e >> (logn - 1), k = e & (half - 1);
-            const int i0 = (l << logn) + k;
+            const int i0 = l * lsd + k;
             const cdf a = ldc(x, i0);
             cdf b = ldc(x, i0 + half);
             if (s > 0) b = cmulw(b, __ldg(&tw[k << tws]), conj);
@@ -181,6 +182,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     __shared__ long lbin[64], lbout[64];
     __shared__ int la[64], lxi[64], lyj[64];
     const int n = 1 << logn, half = n >> 1;
+    const int lsd = n + 1;  // shared-memory line stride: lines at one point apart start on distinct banks
     const long l0 = (long)blockIdx.x * lb;
     const int nl = (int)min((long)lb, ls.nlines - l0);
     const int total = nl << logn;
@@ -247,30 +249,32 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             const double ty = __dadd_rn(__dmul_rn(k1, uu.y), __dmul_rn(k2, vv.y));
             v = make_double2(v.x - ty, v.y + tx);
         }
-        smd[(l << logn) + p] = v;
+        smd[l * lsd + p] = v;
         emax_update(emax, l, max(bexp(v.x), bexp(v.y)), pin && logn >= 5);
     }
     __syncthreads();
     // ---- split in place, each line scaled by 2^-(emax - 1023)
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
         const int k = emax[e >> logn] - 1023;
-        const double2 v = smd[e];
-        stc(smf, e, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
+        const int i = e + (e >> logn);
+        const double2 v = smd[i];
+        stc(smf, i, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
     }
     __syncthreads();
 
     if (KIND == FK_PLAIN) {
-        dif_df(smf, nl, logn, tw, sign > 0);
+        dif_df(smf, nl, logn, lsd, tw, sign > 0);
     } else {
-        dif_df(smf, nl, logn, tw, false);
+        dif_df(smf, nl, logn, lsd, tw, false);
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int l = e >> logn, q = e & (n - 1);
             const int f = brev(q, logn);  // frequency held at position q
+            const int se = l * lsd + q;
             const long lg = l0 + l;
             const int i = lxi[l], j = lyj[l];
             if (KIND == FK_DEALIAS) {
                 const bool keep = fabs(ex.ka[i]) < ex.cut_a && fabs(ex.kb[j]) < ex.cut_b && fabs(ex.kc[f]) < ex.cut_c;
-                if (!keep) stc(smf, e, cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}});
+                if (!keep) stc(smf, se, cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}});
             } else {
                 const double kr = ksq(ex.ka[i], ex.kb[j], ex.kc[f]);
                 double m;
@@ -281,11 +285,11 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
                     if (lg == 0 && f == 0) m = 0.0;
                 }
                 unsigned bad = 0;
-                stc(smf, e, cscale(ldc(smf, e), df_from_double(m, bad)));
+                stc(smf, se, cscale(ldc(smf, se), df_from_double(m, bad)));
             }
         }
         __syncthreads();
-        dit_df(smf, nl, logn, tw, true);
+        dit_df(smf, nl, logn, lsd, tw, true);
     }
 
     // ---- store (FP64)
@@ -306,7 +310,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
         if (p >= nout) continue;
         const long lg = l0 + l;
         const long o = lbout[l] + p * ls.op;
-        cdf c = ldc(smf, (l << logn) + (KIND == FK_PLAIN ? brev(p, logn) : p));
+        cdf c = ldc(smf, l * lsd + (KIND == FK_PLAIN ? brev(p, logn) : p));
         if (use_scale_df) c = cscale(c, sdf);
         const int k = emax[l] - 1023 + scale_exp;
         const double2 v = make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
@@ -402,7 +406,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     __syncthreads();
     const dfv sdf{scale_df.x, scale_df.y};
     if (R2C) {
-        dif_df(smf, nl, logM, tw, false, 1);  // Z in bit-reversed order
+        dif_df(smf, nl, logM, M, tw, false, 1);  // Z in bit-reversed order
         for (int e = threadIdx.x; e < total + nl; e += blockDim.x) {
             int l, k;
             if (e < total) {
@@ -460,7 +464,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             stc(smf, (l << logM) + half, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
         }
         __syncthreads();
-        dif_df(smf, nl, logM, tw, true, 1);  // backward, bit-reversed
+        dif_df(smf, nl, logM, M, tw, true, 1);  // backward, bit-reversed
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int l = e >> logM, j = e & (M - 1);
             cdf w = ldc(smf, (l << logM) + brev(j, logM));
@@ -513,7 +517,7 @@ int twiddles_df(int n, const float4** out) {
 template <int I, int O, int K>
 int launch_df_t(const void* in, void* out, const FftLines& ls, const float4* tw, int logn, int lb, int sign,
                 int sexp, float2 sdf, int use_sdf, int oddball, const FftExtra& ex, cudaStream_t s) {
-    const size_t smem = sizeof(float4) * ((size_t)lb << logn);
+    const size_t smem = sizeof(float4) * (size_t)lb * (size_t)((1 << logn) + 1);  // lines padded by one point
     auto kern = k_fft_df<I, O, K>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
