@@ -57,6 +57,9 @@ __device__ __forceinline__ cdf cmulw(cdf a, float4 w, bool conj) {
 
 __device__ __forceinline__ cdf cscale(cdf a, dfv m) { return cdf{df_norm(df_mul(a.r, m)), df_norm(df_mul(a.i, m))}; }
 
+// global elements each thread reads before storing them to shared memory
+constexpr int kLoadBatch = 4;
+
 // raises the line maximum emax[l] to m; `warp_line` (uniform over the block) says that the
 // 32 lanes of each warp hold points of one line, so one lane updates it for the warp
 __device__ __forceinline__ void emax_update(int* emax, int l, int m, bool warp_line) {
@@ -79,7 +82,7 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
 // (lsd >= 2^logn, padded to spread lines over the banks).  Stages s and s - 1 run
 // fused (one pass over shared memory per two stages, four points per thread); the
 // arithmetic is that of the radix-2 stages, operation for operation.
-__device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, const float4* __restrict__ tw,
+__device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, const float4* tw,
                                        bool conj, int tws = 0) {
     int s = logn - 1;
     for (; s >= 1; s -= 2) {
@@ -93,8 +96,8 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, con
             const cdf x0 = ldc(x, i0), x1 = ldc(x, i0 + h), x2 = ldc(x, i0 + 2 * h), x3 = ldc(x, i0 + 3 * h);
             // stage s: (x0, x2) at offset k, (x1, x3) at offset k + h
             const cdf a0 = cadd(x0, x2), a1 = cadd(x1, x3);
-            const cdf a2 = cmulw(csub(x0, x2), __ldg(&tw[k << t1]), conj);
-            const cdf a3 = cmulw(csub(x1, x3), __ldg(&tw[(k + h) << t1]), conj);
+            const cdf a2 = cmulw(csub(x0, x2), tw[k << t1], conj);
+            const cdf a3 = cmulw(csub(x1, x3), tw[(k + h) << t1], conj);
             // stage s - 1: (a0, a1) and (a2, a3), both at offset k
             stc(x, i0, cadd(a0, a1));
             stc(x, i0 + 2 * h, cadd(a2, a3));
@@ -102,7 +105,7 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, con
                 stc(x, i0 + h, csub(a0, a1));
                 stc(x, i0 + 3 * h, csub(a2, a3));
             } else {
-                const float4 w = __ldg(&tw[k << t2]);
+                const float4 w = tw[k << t2];
                 stc(x, i0 + h, cmulw(csub(a0, a1), w, conj));
                 stc(x, i0 + 3 * h, cmulw(csub(a2, a3), w, conj));
             }
@@ -122,7 +125,7 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, con
 }
 
 // decimation in time: bit-reversed -> natural order; stages s and s + 1 fused as in dif_df
-__device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, const float4* __restrict__ tw,
+__device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, const float4* tw,
                                        bool conj, int tws = 0) {
     int s = 0;
     for (; s + 1 < logn; s += 2) {
@@ -137,15 +140,15 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
             cdf x1 = ldc(x, i0 + h), x3 = ldc(x, i0 + 3 * h);
             // stage s: (x0, x1) and (x2, x3), both at offset k
             if (s > 0) {
-                const float4 w = __ldg(&tw[k << t1]);
+                const float4 w = tw[k << t1];
                 x1 = cmulw(x1, w, conj);
                 x3 = cmulw(x3, w, conj);
             }
             const cdf a0 = cadd(x0, x1), a1 = csub(x0, x1);
             cdf a2 = cadd(x2, x3), a3 = csub(x2, x3);
             // stage s + 1: (a0, a2) at offset k, (a1, a3) at offset k + h
-            a2 = cmulw(a2, __ldg(&tw[k << t2]), conj);
-            a3 = cmulw(a3, __ldg(&tw[(k + h) << t2]), conj);
+            a2 = cmulw(a2, tw[k << t2], conj);
+            a3 = cmulw(a3, tw[(k + h) << t2], conj);
             stc(x, i0, cadd(a0, a2));
             stc(x, i0 + 2 * h, csub(a0, a2));
             stc(x, i0 + h, cadd(a1, a3));
@@ -161,7 +164,7 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
             const int i0 = l * lsd + k;
             const cdf a = ldc(x, i0);
             cdf b = ldc(x, i0 + half);
-            if (s > 0) b = cmulw(b, __ldg(&tw[k << tws]), conj);
+            if (s > 0) b = cmulw(b, tw[k << tws], conj);
             stc(x, i0, cadd(a, b));
             stc(x, i0 + half, csub(a, b));
         }
@@ -171,7 +174,7 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
 
 template <int IN, int OUT, int KIND>
 __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const FftLines ls,
-                                                const float4* __restrict__ tw, int logn, int lb, int sign,
+                                                const float4* __restrict__ twg, int logn, int lb, int sign,
                                                 int scale_exp, float2 scale_df, int use_scale_df, int oddball,
                                                 const FftExtra ex) {
     extern __shared__ __align__(16) float4 smf[];
@@ -183,6 +186,8 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     __shared__ int la[64], lxi[64], lyj[64];
     const int n = 1 << logn, half = n >> 1;
     const int lsd = n + 1;  // shared-memory line stride: lines at one point apart start on distinct banks
+    float4* tw = smf + (size_t)lb * lsd;  // the n/2 twiddles, staged behind the lines
+    for (int t = threadIdx.x; t < half; t += blockDim.x) tw[t] = __ldg(&twg[t]);
     const long l0 = (long)blockIdx.x * lb;
     const int nl = (int)min((long)lb, ls.nlines - l0);
     const int total = nl << logn;
@@ -203,21 +208,8 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     // (consecutive threads on consecutive lines); strided positions advance by (sl, sp)
     const int sl = blockDim.x % nl, sp = blockDim.x / nl;
 
-    // ---- load (FP64, natural order) and the per-line maximum exponent
-    int ls_l = threadIdx.x % nl, ls_p = threadIdx.x / nl;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int l = pin ? (e >> logn) : ls_l;
-        const int p = pin ? (e & (n - 1)) : ls_p;
-        if (!pin) {
-            ls_l += sl;
-            ls_p += sp;
-            if (ls_l >= nl) {
-                ls_l -= nl;
-                ls_p++;
-            }
-        }
-        const long lg = l0 + l;
-        const int a = la[l];
+    // one element (l, p) of the input, with the pre-transform multiplier of its kind applied
+    auto fetch = [&](int l, int p) -> double2 {
         const long base = lbin[l];
         double2 v;
         if (IN == IN_COMPLEX) {
@@ -236,21 +228,51 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             if (oddball && p == half) v.x = 0.0;
         }
         if (KIND == FK_PLAIN && ex.mul == MUL_MASK_AP) {
+            const int a = la[l];
             if (!(fabs(ex.ka[a]) < ex.cut_a && fabs(ex.kb[p]) < ex.cut_b)) v = make_double2(0.0, 0.0);
         } else if (KIND == FK_PLAIN && ex.mul != MUL_NONE) {
-            const double k = ex.km[ex.mul == MUL_IK_A ? a : p];
+            const double k = ex.km[ex.mul == MUL_IK_A ? la[l] : p];
             v = make_double2(-k * v.y, k * v.x);
         }
         if (KIND == FK_PROJECT) {
-            const long idx = lg + p * ex.plane;
+            const long idx = l0 + l + p * ex.plane;
             const double k1 = ex.k1[lxi[l]], k2 = ex.k2[lyj[l]];
             const double2 uu = ex.u[idx], vv = ex.v[idx];
             const double tx = __dadd_rn(__dmul_rn(k1, uu.x), __dmul_rn(k2, vv.x));
             const double ty = __dadd_rn(__dmul_rn(k1, uu.y), __dmul_rn(k2, vv.y));
             v = make_double2(v.x - ty, v.y + tx);
         }
-        smd[l * lsd + p] = v;
-        emax_update(emax, l, max(bexp(v.x), bexp(v.y)), pin && logn >= 5);
+        return v;
+    };
+
+    // ---- load (FP64, natural order) and the per-line maximum exponent; kLoadBatch elements
+    // per thread are read before any is stored, so their global loads overlap
+    int ls_l = threadIdx.x % nl, ls_p = threadIdx.x / nl;
+    for (int e0 = threadIdx.x; e0 < total; e0 += kLoadBatch * blockDim.x) {
+        double2 vb[kLoadBatch];
+        int lidx[kLoadBatch], pidx[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; u++) {
+            const int e = e0 + u * blockDim.x;
+            lidx[u] = pin ? (e >> logn) : ls_l;
+            pidx[u] = pin ? (e & (n - 1)) : ls_p;
+            if (!pin) {
+                ls_l += sl;
+                ls_p += sp;
+                if (ls_l >= nl) {
+                    ls_l -= nl;
+                    ls_p++;
+                }
+            }
+            if (e < total) vb[u] = fetch(lidx[u], pidx[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; u++) {
+            if (e0 + u * blockDim.x >= total) continue;
+            const double2 v = vb[u];
+            smd[lidx[u] * lsd + pidx[u]] = v;
+            emax_update(emax, lidx[u], max(bexp(v.x), bexp(v.y)), pin && logn >= 5);
+        }
     }
     __syncthreads();
     // ---- split in place, each line scaled by 2^-(emax - 1023)
@@ -349,7 +371,7 @@ __device__ __forceinline__ double2 cstore(cdf c, int k) {
 // (the imaginary parts of X[0] and X[M] are ignored, as FFTW's c2r does; oddball zeroes X[M]).
 template <bool R2C>
 __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, const FftLines ls,
-                                                     const float4* __restrict__ tw, int logN, int lb, int scale_exp,
+                                                     const float4* __restrict__ twg, int logN, int lb, int scale_exp,
                                                      float2 scale_df, int use_scale_df, int oddball) {
     extern __shared__ __align__(16) float4 smf[];
     double2* smd = reinterpret_cast<double2*>(smf);
@@ -358,6 +380,8 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     __shared__ double2 xlast_raw[64];
     __shared__ long lbin[64], lbout[64];  // per-line input / output offsets
     const int logM = logN - 1, M = 1 << logM;
+    float4* tw = smf + ((size_t)lb << logM);  // the M = N/2 twiddles of length N, staged behind the lines
+    for (int t = threadIdx.x; t < M; t += blockDim.x) tw[t] = __ldg(&twg[t]);
     const long l0 = (long)blockIdx.x * lb;
     const int nl = (int)min((long)lb, ls.nlines - l0);
     const int total = nl << logM;
@@ -368,18 +392,28 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
         lbout[l] = a * ls.oa + b * ls.ob;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int l = e >> logM, j = e & (M - 1);
-        const long base = lbin[l];
-        double2 v;
-        if (R2C) {
-            v = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(in) + base + 2 * j);
-        } else {
-            v = reinterpret_cast<const double2*>(in)[base + j];
-            if (j == 0) v.y = 0.0;
+    for (int e0 = threadIdx.x; e0 < total; e0 += kLoadBatch * blockDim.x) {
+        double2 vb[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; u++) {
+            const int e = e0 + u * blockDim.x;
+            if (e >= total) continue;
+            const int l = e >> logM, j = e & (M - 1);
+            const long base = lbin[l];
+            if (R2C) {
+                vb[u] = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(in) + base + 2 * j);
+            } else {
+                vb[u] = reinterpret_cast<const double2*>(in)[base + j];
+                if (j == 0) vb[u].y = 0.0;
+            }
         }
-        smd[e] = v;
-        emax_update(emax, l, max(bexp(v.x), bexp(v.y)), logM >= 5);
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; u++) {
+            const int e = e0 + u * blockDim.x;
+            if (e >= total) continue;
+            smd[e] = vb[u];
+            emax_update(emax, e >> logM, max(bexp(vb[u].x), bexp(vb[u].y)), logM >= 5);
+        }
     }
     if (!R2C) {
         for (int l = threadIdx.x; l < nl; l += blockDim.x) {
@@ -422,7 +456,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             const cdf sm = cadd(za, zb), df = csub(za, zb);
             cdf t;
             if (k < M) {
-                t = cmulw(df, __ldg(&tw[k]), false);
+                t = cmulw(df, tw[k], false);
             } else {
                 t = cdf{df_neg(df.r), df_neg(df.i)};  // W^M = -1
             }
@@ -444,13 +478,13 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
                 const cdf c2 = cconj(xk2);
                 const cdf sm = cadd(xk, c2);
                 cdf d = csub(xk, c2);
-                if (k > 0) d = cmulw(d, __ldg(&tw[k]), true);
+                if (k > 0) d = cmulw(d, tw[k], true);
                 stc(smf, (l << logM) + k, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
             }
             if (k > 0) {  // Z'[k2], k2 = M - k in (M/2, M)
                 const cdf c1 = cconj(xk);
                 const cdf sm = cadd(xk2, c1);
-                const cdf d = cmulw(csub(xk2, c1), __ldg(&tw[k2]), true);
+                const cdf d = cmulw(csub(xk2, c1), tw[k2], true);
                 stc(smf, (l << logM) + k2, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
             }
         }
@@ -517,7 +551,8 @@ int twiddles_df(int n, const float4** out) {
 template <int I, int O, int K>
 int launch_df_t(const void* in, void* out, const FftLines& ls, const float4* tw, int logn, int lb, int sign,
                 int sexp, float2 sdf, int use_sdf, int oddball, const FftExtra& ex, cudaStream_t s) {
-    const size_t smem = sizeof(float4) * (size_t)lb * (size_t)((1 << logn) + 1);  // lines padded by one point
+    // lines padded by one point, then the n/2 twiddles
+    const size_t smem = sizeof(float4) * ((size_t)lb * (size_t)((1 << logn) + 1) + (size_t)(1 << (logn - 1)));
     auto kern = k_fft_df<I, O, K>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
@@ -566,7 +601,7 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
     if (xreal && ((in_mode == IN_REAL && out_mode == OUT_HALF) || (in_mode == IN_HALF && out_mode == OUT_REAL))) {
         // half-length complex transform; lb lines of M = n/2 points per CTA
         const int lbr = std::max(1, std::min(64, 4096 >> (logn - 1)));
-        const size_t smem = sizeof(float4) * ((size_t)lbr << (logn - 1));
+        const size_t smem = sizeof(float4) * (((size_t)lbr << (logn - 1)) + (size_t)(1 << (logn - 1)));
         const bool r2c = in_mode == IN_REAL;
         auto kern = r2c ? k_fft_df_real<true> : k_fft_df_real<false>;
         if (smem > 48 * 1024 &&
