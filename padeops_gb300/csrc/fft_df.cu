@@ -73,6 +73,16 @@ __device__ __forceinline__ void emax_update(int* emax, int l, int m, bool warp_l
 
 __device__ __forceinline__ int brev(int p, int logn) { return (int)(__brev((unsigned)p) >> (32 - logn)); }
 
+// Bank swizzle of the points of a shared-memory line: q -> q ^ (bits 3..5 of q) ^ (for
+// lines of >= 256 points, the two top bits of q).  It is linear over XOR, its own inverse,
+// and permutes each aligned group of 8 points, so the butterfly passes (four points h apart),
+// bit-reversed reads and contiguous reads each meet few bank conflicts.
+struct Swz {
+    int sh, m2;
+};
+__device__ __forceinline__ Swz make_swz(int logn) { return logn >= 8 ? Swz{logn - 2, 3} : Swz{3, 0}; }
+__device__ __forceinline__ int swz(int q, Swz z) { return q ^ ((q >> 3) & 7) ^ ((q >> z.sh) & z.m2); }
+
 __device__ __forceinline__ double ksq(double a, double b, double c) {
     return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
 }
@@ -84,30 +94,34 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
 // arithmetic is that of the radix-2 stages, operation for operation.
 __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, const float4* tw,
                                        bool conj, int tws = 0) {
+    const Swz z = make_swz(logn);
     int s = logn - 1;
     for (; s >= 1; s -= 2) {
         const int work4 = nl << (logn - 2);
         const int h = 1 << (s - 1);  // quarter of a block of 2^(s+1)
         const int t1 = logn - 1 - s + tws, t2 = logn - s + tws;
+        const int c1 = swz(h, z), c2 = swz(2 * h, z), c3 = swz(3 * h, z);
         for (int e = threadIdx.x; e < work4; e += blockDim.x) {
             const int l = e >> (logn - 2), j = e & ((1 << (logn - 2)) - 1);
             const int k = j & (h - 1);
-            const int i0 = l * lsd + ((j >> (s - 1)) << (s + 1)) + k;
-            const cdf x0 = ldc(x, i0), x1 = ldc(x, i0 + h), x2 = ldc(x, i0 + 2 * h), x3 = ldc(x, i0 + 3 * h);
+            // points q0 + r h = q0 ^ (r h) (bits s-1 and s of q0 are clear), swizzled
+            const int lb = l * lsd, q0 = swz(((j >> (s - 1)) << (s + 1)) + k, z);
+            const int i0 = lb + q0, i1 = lb + (q0 ^ c1), i2 = lb + (q0 ^ c2), i3 = lb + (q0 ^ c3);
+            const cdf x0 = ldc(x, i0), x1 = ldc(x, i1), x2 = ldc(x, i2), x3 = ldc(x, i3);
             // stage s: (x0, x2) at offset k, (x1, x3) at offset k + h
             const cdf a0 = cadd(x0, x2), a1 = cadd(x1, x3);
             const cdf a2 = cmulw(csub(x0, x2), tw[k << t1], conj);
             const cdf a3 = cmulw(csub(x1, x3), tw[(k + h) << t1], conj);
             // stage s - 1: (a0, a1) and (a2, a3), both at offset k
             stc(x, i0, cadd(a0, a1));
-            stc(x, i0 + 2 * h, cadd(a2, a3));
+            stc(x, i2, cadd(a2, a3));
             if (s == 1) {
-                stc(x, i0 + h, csub(a0, a1));
-                stc(x, i0 + 3 * h, csub(a2, a3));
+                stc(x, i1, csub(a0, a1));
+                stc(x, i3, csub(a2, a3));
             } else {
                 const float4 w = tw[k << t2];
-                stc(x, i0 + h, cmulw(csub(a0, a1), w, conj));
-                stc(x, i0 + 3 * h, cmulw(csub(a2, a3), w, conj));
+                stc(x, i1, cmulw(csub(a0, a1), w, conj));
+                stc(x, i3, cmulw(csub(a2, a3), w, conj));
             }
         }
         __syncthreads();
@@ -115,10 +129,11 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, con
     if (s == 0) {  // odd logn: the last stage alone
         const int work = nl << (logn - 1);
         for (int e = threadIdx.x; e < work; e += blockDim.x) {
-            const int i0 = (e >> (logn - 1)) * lsd + ((e & ((1 << (logn - 1)) - 1)) << 1);
-            const cdf a = ldc(x, i0), b = ldc(x, i0 + 1);
+            const int lb = (e >> (logn - 1)) * lsd, q0 = swz((e & ((1 << (logn - 1)) - 1)) << 1, z);
+            const int i0 = lb + q0, i1 = lb + (q0 ^ 1);  // swz(1) = 1
+            const cdf a = ldc(x, i0), b = ldc(x, i1);
             stc(x, i0, cadd(a, b));
-            stc(x, i0 + 1, csub(a, b));
+            stc(x, i1, csub(a, b));
         }
         __syncthreads();
     }
@@ -127,17 +142,20 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, con
 // decimation in time: bit-reversed -> natural order; stages s and s + 1 fused as in dif_df
 __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, const float4* tw,
                                        bool conj, int tws = 0) {
+    const Swz z = make_swz(logn);
     int s = 0;
     for (; s + 1 < logn; s += 2) {
         const int work4 = nl << (logn - 2);
         const int h = 1 << s;  // quarter of a block of 2^(s+2)
         const int t1 = logn - 1 - s + tws, t2 = logn - 2 - s + tws;
+        const int c1 = swz(h, z), c2 = swz(2 * h, z), c3 = swz(3 * h, z);
         for (int e = threadIdx.x; e < work4; e += blockDim.x) {
             const int l = e >> (logn - 2), j = e & ((1 << (logn - 2)) - 1);
             const int k = j & (h - 1);
-            const int i0 = l * lsd + ((j >> s) << (s + 2)) + k;
-            const cdf x0 = ldc(x, i0), x2 = ldc(x, i0 + 2 * h);
-            cdf x1 = ldc(x, i0 + h), x3 = ldc(x, i0 + 3 * h);
+            const int lb = l * lsd, q0 = swz(((j >> s) << (s + 2)) + k, z);
+            const int i0 = lb + q0, i1 = lb + (q0 ^ c1), i2 = lb + (q0 ^ c2), i3 = lb + (q0 ^ c3);
+            const cdf x0 = ldc(x, i0), x2 = ldc(x, i2);
+            cdf x1 = ldc(x, i1), x3 = ldc(x, i3);
             // stage s: (x0, x1) and (x2, x3), both at offset k
             if (s > 0) {
                 const float4 w = tw[k << t1];
@@ -150,9 +168,9 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
             a2 = cmulw(a2, tw[k << t2], conj);
             a3 = cmulw(a3, tw[(k + h) << t2], conj);
             stc(x, i0, cadd(a0, a2));
-            stc(x, i0 + 2 * h, csub(a0, a2));
-            stc(x, i0 + h, cadd(a1, a3));
-            stc(x, i0 + 3 * h, csub(a1, a3));
+            stc(x, i2, csub(a0, a2));
+            stc(x, i1, cadd(a1, a3));
+            stc(x, i3, csub(a1, a3));
         }
         __syncthreads();
     }
@@ -161,12 +179,12 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
         const int work = nl << (logn - 1);
         for (int e = threadIdx.x; e < work; e += blockDim.x) {
             const int l = e >> (logn - 1), k = e & (half - 1);
-            const int i0 = l * lsd + k;
+            const int q0 = swz(k, z), i0 = l * lsd + q0, i1 = l * lsd + (q0 ^ swz(half, z));
             const cdf a = ldc(x, i0);
-            cdf b = ldc(x, i0 + half);
+            cdf b = ldc(x, i1);
             if (s > 0) b = cmulw(b, tw[k << tws], conj);
             stc(x, i0, cadd(a, b));
-            stc(x, i0 + half, csub(a, b));
+            stc(x, i1, csub(a, b));
         }
         __syncthreads();
     }
@@ -186,6 +204,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     __shared__ int la[64], lxi[64], lyj[64];
     const int n = 1 << logn, half = n >> 1;
     const int lsd = n + 1;  // shared-memory line stride: lines at one point apart start on distinct banks
+    const Swz z = make_swz(logn);  // point p of line l sits at l * lsd + swz(p)
     float4* tw = smf + (size_t)lb * lsd;  // the n/2 twiddles, staged behind the lines
     for (int t = threadIdx.x; t < half; t += blockDim.x) tw[t] = __ldg(&twg[t]);
     const long l0 = (long)blockIdx.x * lb;
@@ -270,7 +289,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
         for (int u = 0; u < kLoadBatch; u++) {
             if (e0 + u * blockDim.x >= total) continue;
             const double2 v = vb[u];
-            smd[lidx[u] * lsd + pidx[u]] = v;
+            smd[lidx[u] * lsd + swz(pidx[u], z)] = v;
             emax_update(emax, lidx[u], max(bexp(v.x), bexp(v.y)), pin && logn >= 5);
         }
     }
@@ -289,9 +308,9 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     } else {
         dif_df(smf, nl, logn, lsd, tw, false);
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
-            const int l = e >> logn, q = e & (n - 1);
-            const int f = brev(q, logn);  // frequency held at position q
-            const int se = l * lsd + q;
+            const int l = e >> logn, qs = e & (n - 1);
+            const int f = brev(swz(qs, z), logn);  // frequency held at (swizzled) position qs
+            const int se = l * lsd + qs;
             const long lg = l0 + l;
             const int i = lxi[l], j = lyj[l];
             if (KIND == FK_DEALIAS) {
@@ -332,7 +351,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
         if (p >= nout) continue;
         const long lg = l0 + l;
         const long o = lbout[l] + p * ls.op;
-        cdf c = ldc(smf, l * lsd + (KIND == FK_PLAIN ? brev(p, logn) : p));
+        cdf c = ldc(smf, l * lsd + swz(KIND == FK_PLAIN ? brev(p, logn) : p, z));
         if (use_scale_df) c = cscale(c, sdf);
         const int k = emax[l] - 1023 + scale_exp;
         const double2 v = make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
@@ -380,6 +399,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     __shared__ double2 xlast_raw[64];
     __shared__ long lbin[64], lbout[64];  // per-line input / output offsets
     const int logM = logN - 1, M = 1 << logM;
+    const Swz z = make_swz(logM);  // point j of line l sits at (l << logM) + swz(j)
     float4* tw = smf + ((size_t)lb << logM);  // the M = N/2 twiddles of length N, staged behind the lines
     for (int t = threadIdx.x; t < M; t += blockDim.x) tw[t] = __ldg(&twg[t]);
     const long l0 = (long)blockIdx.x * lb;
@@ -411,7 +431,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
         for (int u = 0; u < kLoadBatch; u++) {
             const int e = e0 + u * blockDim.x;
             if (e >= total) continue;
-            smd[e] = vb[u];
+            smd[(e & ~(M - 1)) + swz(e & (M - 1), z)] = vb[u];
             emax_update(emax, e >> logM, max(bexp(vb[u].x), bexp(vb[u].y)), logM >= 5);
         }
     }
@@ -451,8 +471,8 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
                 k = M;
             }
             const int ka = k & (M - 1), kb = (M - k) & (M - 1);
-            const cdf za = ldc(smf, (l << logM) + brev(ka, logM));
-            const cdf zb = cconj(ldc(smf, (l << logM) + brev(kb, logM)));
+            const cdf za = ldc(smf, (l << logM) + swz(brev(ka, logM), z));
+            const cdf zb = cconj(ldc(smf, (l << logM) + swz(brev(kb, logM), z)));
             const cdf sm = cadd(za, zb), df = csub(za, zb);
             cdf t;
             if (k < M) {
@@ -471,37 +491,39 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
         for (int e = threadIdx.x; e < (nl << (logM - 1)); e += blockDim.x) {
             const int l = e >> (logM - 1), k = e & (half - 1);
             const int k2 = M - k;
-            const cdf xk = ldc(smf, (l << logM) + k);
-            const cdf xk2 = k == 0 ? ldc(xlast, l) : ldc(smf, (l << logM) + k2);
+            const int ik = (l << logM) + swz(k, z), ik2 = (l << logM) + swz(k2 & (M - 1), z);
+            const cdf xk = ldc(smf, ik);
+            const cdf xk2 = k == 0 ? ldc(xlast, l) : ldc(smf, ik2);
             // Z'[k] = (xk + conj xk2) + i conj(W^k) (xk - conj xk2)
             {
                 const cdf c2 = cconj(xk2);
                 const cdf sm = cadd(xk, c2);
                 cdf d = csub(xk, c2);
                 if (k > 0) d = cmulw(d, tw[k], true);
-                stc(smf, (l << logM) + k, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+                stc(smf, ik, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
             }
             if (k > 0) {  // Z'[k2], k2 = M - k in (M/2, M)
                 const cdf c1 = cconj(xk);
                 const cdf sm = cadd(xk2, c1);
                 const cdf d = cmulw(csub(xk2, c1), tw[k2], true);
-                stc(smf, (l << logM) + k2, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+                stc(smf, ik2, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
             }
         }
         // k = M/2 pairs with itself: conj(W^(M/2)) = i
         for (int l = threadIdx.x; l < nl; l += blockDim.x) {
-            const cdf x = ldc(smf, (l << logM) + half);
+            const int ih = (l << logM) + swz(half, z);
+            const cdf x = ldc(smf, ih);
             const cdf c = cconj(x);
             const cdf sm = cadd(x, c);
             cdf d = csub(x, c);
             d = cdf{df_neg(d.i), d.r};  // i * d
-            stc(smf, (l << logM) + half, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+            stc(smf, ih, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
         }
         __syncthreads();
         dif_df(smf, nl, logM, M, tw, true, 1);  // backward, bit-reversed
         for (int e = threadIdx.x; e < total; e += blockDim.x) {
             const int l = e >> logM, j = e & (M - 1);
-            cdf w = ldc(smf, (l << logM) + brev(j, logM));
+            cdf w = ldc(smf, (l << logM) + swz(brev(j, logM), z));
             if (use_scale_df) w = cscale(w, sdf);
             *reinterpret_cast<double2*>(reinterpret_cast<double*>(out) + lbout[l] + 2 * j) =
                 cstore(w, emax[l] - 1023 + scale_exp);
