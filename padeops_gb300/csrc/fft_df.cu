@@ -55,7 +55,19 @@ __device__ __forceinline__ cdf cmulw(cdf a, float4 w, bool conj) {
     return cdf{df_norm(rr), df_norm(ii)};
 }
 
+// -i a (forward), +i a (backward): exact
+__device__ __forceinline__ cdf mul_mi(cdf a, bool conj) {
+    return conj ? cdf{df_neg(a.i), a.r} : cdf{a.i, df_neg(a.r)};
+}
+
 __device__ __forceinline__ cdf cscale(cdf a, dfv m) { return cdf{df_norm(df_mul(a.r, m)), df_norm(df_mul(a.i, m))}; }
+
+// W^t for t < 3N/4 from the table of t < N/2 (= nh): W^(t + N/2) = -W^t
+__device__ __forceinline__ float4 twiddle_ext(const float4* __restrict__ twg, int t, int nh) {
+    if (t < nh) return __ldg(&twg[t]);
+    const float4 w = __ldg(&twg[t - nh]);
+    return make_float4(-w.x, -w.y, -w.z, -w.w);
+}
 
 // global elements each thread reads before storing them to shared memory
 constexpr int kLoadBatch = 4;
@@ -88,10 +100,11 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
 }
 
 // decimation in frequency: natural order -> bit-reversed.  tw holds exp(-2 pi i t / (n 2^tws)),
-// so a table made for a longer transform serves with stride 2^tws; line l starts at l * lsd
-// (lsd >= 2^logn, padded to spread lines over the banks).  Stages s and s - 1 run
-// fused (one pass over shared memory per two stages, four points per thread); the
-// arithmetic is that of the radix-2 stages, operation for operation.
+// so a table made for a longer transform serves with stride 2^tws; it extends to 3/4 of that
+// transform's length (W^(t + N/2) = -W^t) for the radix-4 twiddle W^3k.  Line l starts at
+// l * lsd (lsd >= 2^logn, padded to spread lines over the banks).  Stages s and s - 1 run as
+// one radix-4 pass (four points h = 2^(s-1) apart per thread, twiddles W^k, W^2k, W^3k of the
+// block of 4h and the trivial W^h = -i), with a final radix-2 stage when logn is odd.
 __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, const float4* tw,
                                        bool conj, int tws = 0) {
     const Swz z = make_swz(logn);
@@ -108,21 +121,18 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, con
             const int lb = l * lsd, q0 = swz(((j >> (s - 1)) << (s + 1)) + k, z);
             const int i0 = lb + q0, i1 = lb + (q0 ^ c1), i2 = lb + (q0 ^ c2), i3 = lb + (q0 ^ c3);
             const cdf x0 = ldc(x, i0), x1 = ldc(x, i1), x2 = ldc(x, i2), x3 = ldc(x, i3);
-            // stage s: (x0, x2) at offset k, (x1, x3) at offset k + h
-            const cdf a0 = cadd(x0, x2), a1 = cadd(x1, x3);
-            const cdf a2 = cmulw(csub(x0, x2), tw[k << t1], conj);
-            const cdf a3 = cmulw(csub(x1, x3), tw[(k + h) << t1], conj);
-            // stage s - 1: (a0, a1) and (a2, a3), both at offset k
-            stc(x, i0, cadd(a0, a1));
-            stc(x, i2, cadd(a2, a3));
-            if (s == 1) {
-                stc(x, i1, csub(a0, a1));
-                stc(x, i3, csub(a2, a3));
-            } else {
-                const float4 w = tw[k << t2];
-                stc(x, i1, cmulw(csub(a0, a1), w, conj));
-                stc(x, i3, cmulw(csub(a2, a3), w, conj));
+            const cdf s02 = cadd(x0, x2), d02 = csub(x0, x2), s13 = cadd(x1, x3), d13 = csub(x1, x3);
+            const cdf c = mul_mi(d13, conj);  // W^h d13, W^h = -i (+i backward)
+            cdf y1 = csub(s02, s13), y2 = cadd(d02, c), y3 = csub(d02, c);
+            if (s > 1) {  // at s = 1 every k is 0
+                y1 = cmulw(y1, tw[k << t2], conj);
+                y2 = cmulw(y2, tw[k << t1], conj);
+                y3 = cmulw(y3, tw[(3 * k) << t1], conj);
             }
+            stc(x, i0, cadd(s02, s13));
+            stc(x, i1, y1);
+            stc(x, i2, y2);
+            stc(x, i3, y3);
         }
         __syncthreads();
     }
@@ -139,7 +149,7 @@ __device__ __forceinline__ void dif_df(float4* x, int nl, int logn, int lsd, con
     }
 }
 
-// decimation in time: bit-reversed -> natural order; stages s and s + 1 fused as in dif_df
+// decimation in time: bit-reversed -> natural order; stages s and s + 1 as one radix-4 pass
 __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, const float4* tw,
                                        bool conj, int tws = 0) {
     const Swz z = make_swz(logn);
@@ -154,23 +164,19 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
             const int k = j & (h - 1);
             const int lb = l * lsd, q0 = swz(((j >> s) << (s + 2)) + k, z);
             const int i0 = lb + q0, i1 = lb + (q0 ^ c1), i2 = lb + (q0 ^ c2), i3 = lb + (q0 ^ c3);
-            const cdf x0 = ldc(x, i0), x2 = ldc(x, i2);
-            cdf x1 = ldc(x, i1), x3 = ldc(x, i3);
-            // stage s: (x0, x1) and (x2, x3), both at offset k
-            if (s > 0) {
-                const float4 w = tw[k << t1];
-                x1 = cmulw(x1, w, conj);
-                x3 = cmulw(x3, w, conj);
+            const cdf x0 = ldc(x, i0);
+            cdf x1 = ldc(x, i1), x2 = ldc(x, i2), x3 = ldc(x, i3);
+            if (s > 0) {  // at s = 0 every k is 0
+                x1 = cmulw(x1, tw[k << t1], conj);
+                x2 = cmulw(x2, tw[k << t2], conj);
+                x3 = cmulw(x3, tw[(3 * k) << t2], conj);
             }
-            const cdf a0 = cadd(x0, x1), a1 = csub(x0, x1);
-            cdf a2 = cadd(x2, x3), a3 = csub(x2, x3);
-            // stage s + 1: (a0, a2) at offset k, (a1, a3) at offset k + h
-            a2 = cmulw(a2, tw[k << t2], conj);
-            a3 = cmulw(a3, tw[(k + h) << t2], conj);
-            stc(x, i0, cadd(a0, a2));
-            stc(x, i2, csub(a0, a2));
-            stc(x, i1, cadd(a1, a3));
-            stc(x, i3, csub(a1, a3));
+            const cdf s01 = cadd(x0, x1), d01 = csub(x0, x1), s23 = cadd(x2, x3);
+            const cdf c = mul_mi(csub(x2, x3), conj);  // W^h (x2 - x3), W^h = -i (+i backward)
+            stc(x, i0, cadd(s01, s23));
+            stc(x, i2, csub(s01, s23));
+            stc(x, i1, cadd(d01, c));
+            stc(x, i3, csub(d01, c));
         }
         __syncthreads();
     }
@@ -205,8 +211,8 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     const int n = 1 << logn, half = n >> 1;
     const int lsd = n + 1;  // shared-memory line stride: lines at one point apart start on distinct banks
     const Swz z = make_swz(logn);  // point p of line l sits at l * lsd + swz(p)
-    float4* tw = smf + (size_t)lb * lsd;  // the n/2 twiddles, staged behind the lines
-    for (int t = threadIdx.x; t < half; t += blockDim.x) tw[t] = __ldg(&twg[t]);
+    float4* tw = smf + (size_t)lb * lsd;  // the twiddles W^t, t < 3n/4, staged behind the lines
+    for (int t = threadIdx.x; t < half + (half >> 1); t += blockDim.x) tw[t] = twiddle_ext(twg, t, half);
     const long l0 = (long)blockIdx.x * lb;
     const int nl = (int)min((long)lb, ls.nlines - l0);
     const int total = nl << logn;
@@ -400,8 +406,8 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     __shared__ long lbin[64], lbout[64];  // per-line input / output offsets
     const int logM = logN - 1, M = 1 << logM;
     const Swz z = make_swz(logM);  // point j of line l sits at (l << logM) + swz(j)
-    float4* tw = smf + ((size_t)lb << logM);  // the M = N/2 twiddles of length N, staged behind the lines
-    for (int t = threadIdx.x; t < M; t += blockDim.x) tw[t] = __ldg(&twg[t]);
+    float4* tw = smf + ((size_t)lb << logM);  // the twiddles W_N^t, t < 3N/4, staged behind the lines
+    for (int t = threadIdx.x; t < M + (M >> 1); t += blockDim.x) tw[t] = twiddle_ext(twg, t, M);
     const long l0 = (long)blockIdx.x * lb;
     const int nl = (int)min((long)lb, ls.nlines - l0);
     const int total = nl << logM;
@@ -573,8 +579,8 @@ int twiddles_df(int n, const float4** out) {
 template <int I, int O, int K>
 int launch_df_t(const void* in, void* out, const FftLines& ls, const float4* tw, int logn, int lb, int sign,
                 int sexp, float2 sdf, int use_sdf, int oddball, const FftExtra& ex, cudaStream_t s) {
-    // lines padded by one point, then the n/2 twiddles
-    const size_t smem = sizeof(float4) * ((size_t)lb * (size_t)((1 << logn) + 1) + (size_t)(1 << (logn - 1)));
+    // lines padded by one point, then the 3n/4 twiddles
+    const size_t smem = sizeof(float4) * ((size_t)lb * (size_t)((1 << logn) + 1) + (size_t)(3 << logn) / 4);
     auto kern = k_fft_df<I, O, K>;
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
@@ -623,7 +629,7 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
     if (xreal && ((in_mode == IN_REAL && out_mode == OUT_HALF) || (in_mode == IN_HALF && out_mode == OUT_REAL))) {
         // half-length complex transform; lb lines of M = n/2 points per CTA
         const int lbr = std::max(1, std::min(64, 4096 >> (logn - 1)));
-        const size_t smem = sizeof(float4) * (((size_t)lbr << (logn - 1)) + (size_t)(1 << (logn - 1)));
+        const size_t smem = sizeof(float4) * (((size_t)lbr << (logn - 1)) + (size_t)(3 << logn) / 4);
         const bool r2c = in_mode == IN_REAL;
         auto kern = r2c ? k_fft_df_real<true> : k_fft_df_real<false>;
         if (smem > 48 * 1024 &&
