@@ -53,12 +53,20 @@ enum LineShape : int {
     SHAPE_P3A = 2,  // pentadiagonal, 3 antisymmetric pairs (cd10 first derivative)
     SHAPE_P3S = 3,  // pentadiagonal, centre + 3 symmetric pairs (cd10 second derivative)
     SHAPE_P4S = 4,  // pentadiagonal, centre + 4 symmetric pairs (cf90, residual form)
+    // staggered (cd06stagg, periodic, chunks of 32): tridiagonal, 2 pairs about the half point
+    // i + 1/2 (edges to cells: offsets (m, 1 - m)) or i - 1/2 (cells to edges: (m - 1, -m))
+    SHAPE_T2A_E2C = 5,  // derivative, edges to cells
+    SHAPE_T2S_E2C = 6,  // interpolation, edges to cells
+    SHAPE_T2A_C2E = 7,  // derivative, cells to edges
+    SHAPE_T2S_C2E = 8,  // interpolation, cells to edges
 };
 
 struct StencilParams {
     int M;            // chunk length (16 or 32)
     int alias;        // work rows overwrite the input window (operators without residual form)
     int ns, nout, P, Pp, nsteps, L, resid;
+    int xdup;         // edges to cells, periodic: the line's stored row ns (edge n + 1) is the
+                      // first row above the top, as the reference reads it (not row 0)
     int circ;         // circulant line (ring wrap, constant coefficients)
     int nlo, nhi, tw; // banded: edge rows at both ends, taps per edge row
     F2 c0;            // centre coefficient (symmetric stencils; 0 when absent)
@@ -104,7 +112,7 @@ class DevicePlan {
 };
 
 // Fixed-stencil kernel for a plan with line_shape() != SHAPE_NONE: double-float (FP64 in
-// and out) or FP32.
+// and out) or FP32 (the centred shapes, SHAPE_T2A .. SHAPE_P4S).
 int launch_line(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                 cudaStream_t s);
 int launch_line_f32(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,

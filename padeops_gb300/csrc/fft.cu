@@ -284,6 +284,11 @@ int fft_launch(int in_mode, int out_mode, int kind, int n, int sign, double scal
     const int logn = log2_exact(n);
     if (logn < 1 || logn > 13) return PS_ENOTSUP;
     if (ls.nlines <= 0) return PS_OK;
+    // a multiplier on load is defined for complex lines; on half-spectrum lines only i k(p)
+    // (MUL_IK_P, applied to the stored half and extended Hermitian), in the double-float path
+    if (ex.mul != MUL_NONE && in_mode != IN_COMPLEX &&
+        !(in_mode == IN_HALF && ex.mul == MUL_IK_P && g_arith.load() == FFT_ARITH_DF))
+        return PS_ENOTSUP;
     if (g_arith.load() == FFT_ARITH_DF)
         return fft_launch_df(in_mode, out_mode, kind, logn, sign, scale, oddball, in, out, ls, ex, s);
     const double2* tw = nullptr;

@@ -394,10 +394,13 @@ __device__ __forceinline__ double2 cstore(cdf c, int k) {
 //   c2r: Z'[k] = (X[k] + conj X[M-k]) + i conj(W^k) (X[k] - conj X[M-k]), k = 0..M-1,
 //        w = unnormalised backward FFT_M(Z'), x[2j] = Re w[j], x[2j+1] = Im w[j]
 // (the imaginary parts of X[0] and X[M] are ignored, as FFTW's c2r does; oddball zeroes X[M]).
+// km (c2r only, may be null): X[k] is first multiplied by i km[k], k = 0..M (the x derivative
+// of the spectrum, ahead of the dropped imaginary parts as when the product is stored).
 template <bool R2C>
 __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, const FftLines ls,
                                                      const float4* __restrict__ twg, int logN, int lb, int scale_exp,
-                                                     float2 scale_df, int use_scale_df, int oddball) {
+                                                     float2 scale_df, int use_scale_df, int oddball,
+                                                     const double* __restrict__ km) {
     extern __shared__ __align__(16) float4 smf[];
     double2* smd = reinterpret_cast<double2*>(smf);
     __shared__ int emax[64];
@@ -429,8 +432,10 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             if (R2C) {
                 vb[u] = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(in) + base + 2 * j);
             } else {
-                vb[u] = reinterpret_cast<const double2*>(in)[base + j];
-                if (j == 0) vb[u].y = 0.0;
+                double2 v = reinterpret_cast<const double2*>(in)[base + j];
+                if (km) v = make_double2(-km[j] * v.y, km[j] * v.x);  // i k(j) X[j]
+                if (j == 0) v.y = 0.0;
+                vb[u] = v;
             }
         }
 #pragma unroll
@@ -444,6 +449,7 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     if (!R2C) {
         for (int l = threadIdx.x; l < nl; l += blockDim.x) {
             double2 v = reinterpret_cast<const double2*>(in)[lbin[l] + M];
+            if (km) v = make_double2(-km[M] * v.y, km[M] * v.x);
             v.y = 0.0;
             if (oddball) v.x = 0.0;
             xlast_raw[l] = v;
@@ -625,7 +631,8 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
     const bool aligned = in_mode == IN_REAL
                              ? ((reinterpret_cast<uintptr_t>(in) & 15) == 0 && ls.fa % 2 == 0 && ls.fb % 2 == 0)
                              : ((reinterpret_cast<uintptr_t>(out) & 15) == 0 && ls.oa % 2 == 0 && ls.ob % 2 == 0);
-    const bool xreal = ls.fp == 1 && ls.op == 1 && logn >= 3 && ex.mul == MUL_NONE && aligned;
+    const bool xreal = ls.fp == 1 && ls.op == 1 && logn >= 3 && aligned &&
+                       (ex.mul == MUL_NONE || (in_mode == IN_HALF && ex.mul == MUL_IK_P));
     if (xreal && ((in_mode == IN_REAL && out_mode == OUT_HALF) || (in_mode == IN_HALF && out_mode == OUT_REAL))) {
         // half-length complex transform; lb lines of M = n/2 points per CTA
         const int lbr = std::max(1, std::min(64, 4096 >> (logn - 1)));
@@ -636,9 +643,11 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return PS_ECUDA;
         const long blocks = (ls.nlines + lbr - 1) / lbr;
-        kern<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, logn, lbr, sexp, sdf, use, oddball);
+        kern<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, logn, lbr, sexp, sdf, use, oddball,
+                                                 ex.mul == MUL_IK_P ? ex.km : nullptr);
         return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
     }
+    if (ex.mul != MUL_NONE) return PS_ENOTSUP;  // on real / half lines only the real kernel has one
     if (in_mode == IN_REAL && out_mode == OUT_HALF)
         return launch_df_t<IN_REAL, OUT_HALF, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
     if (in_mode == IN_HALF && out_mode == OUT_REAL)

@@ -173,20 +173,27 @@ int DevicePlan::upload(const HostPlan& hp) {
             o_pb[v] = A.put(pb.data(), pb.size() * sizeof(F2));
         }
     }
-    // fixed-stencil kernel: whole chunks, pairs at +-1..NP, one sign; banded lines also need
+    // fixed-stencil kernel: whole chunks, pairs k = 1..NP about the row or (staggered,
+    // periodic tridiagonal lines only) about a half point, one sign; banded lines also need
     // edge rows covering the stencil's reach at both ends
     line_shape_ = SHAPE_NONE;
     size_t o_lk[6] = {0, 0, 0, 0, 0, 0};
-    if (cok_ && ch_.M == kLineM && d.m == d.ns && d.ns % kLineM == 0 && d.ns <= 512 && ch_.P <= kMaxLanes &&
+    // (periodic lines may carry the duplicated point n + 1 of the edge grid: m = ns + 1 is read
+    // as ns rows, and an output of ns + 1 rows repeats row 0)
+    if (cok_ && ch_.M == kLineM && (d.m == d.ns || (ch_.circ && d.m == d.ns + 1)) && d.ns % kLineM == 0 &&
+        d.ns <= 512 && ch_.P <= kMaxLanes &&
         (ch_.Q == 1 || ch_.Q == 2) && (ch_.circ || d.nout == d.ns)) {
         const int np = ch_.npair;
         bool ok = np >= 1 && np <= kMaxPairs;
         bool seen[kMaxPairs + 1] = {};
         int sgn = 0;
         StencilParams cc{};
+        // twice the stencil centre: 0 (centred), +1 (edges to cells), -1 (cells to edges)
+        const int d2 = ok ? ch_.pair_op[0] + ch_.pair_om[0] : 0;
+        if (d2 < -1 || d2 > 1) ok = false;
         for (int k = 0; k < np && ok; k++) {
-            const int o = ch_.pair_op[k];
-            if (o < 1 || o > np || ch_.pair_om[k] != -o || seen[o]) {
+            const int o = d2 < 0 ? -ch_.pair_om[k] : ch_.pair_op[k];  // the pair's index 1..np
+            if (o < 1 || o > np || ch_.pair_op[k] + ch_.pair_om[k] != d2 || seen[o]) {
                 ok = false;
                 break;
             }
@@ -195,10 +202,13 @@ int DevicePlan::upload(const HostPlan& hp) {
             if (sgn == 0) sgn = ch_.pair_sign[k];
             else if (sgn != ch_.pair_sign[k]) ok = false;
         }
-        if (ch_.has_center && (ch_.center_off != 0 || sgn < 0)) ok = false;
+        if (ch_.has_center && (ch_.center_off != 0 || sgn < 0 || d2 != 0)) ok = false;
+        if (d2 != 0 && !(ch_.circ && ch_.Q == 1 && np == 2 && !ch_.resid && d.ns % 32 == 0)) ok = false;
         if (!ch_.circ && (ch_.nlo < np || ch_.nhi < np || ch_.nlo + ch_.nhi > 32)) ok = false;
         int shape = SHAPE_NONE;
-        if (ok) {
+        if (ok && d2 != 0) {
+            shape = d2 > 0 ? (sgn < 0 ? SHAPE_T2A_E2C : SHAPE_T2S_E2C) : (sgn < 0 ? SHAPE_T2A_C2E : SHAPE_T2S_C2E);
+        } else if (ok) {
             if (ch_.Q == 1 && np == 2) shape = sgn < 0 ? SHAPE_T2A : SHAPE_T2S;
             else if (ch_.Q == 2 && np == 3) shape = sgn < 0 ? SHAPE_P3A : SHAPE_P3S;
             else if (ch_.Q == 2 && np == 4 && sgn > 0) shape = SHAPE_P4S;
@@ -214,6 +224,7 @@ int DevicePlan::upload(const HostPlan& hp) {
             const int v = std::atoi(e);
             if (v == 16 || (v == 32 && alias && d.ns % 32 == 0)) Ml = v;
         }
+        if (shape >= SHAPE_T2A_E2C) Ml = 32;  // the staggered shapes run in chunks of 32 only
         ChunkPlanHost c32;
         const ChunkPlanHost* cl = &ch_;
         if (shape != SHAPE_NONE && Ml != ch_.M) {
@@ -234,6 +245,7 @@ int DevicePlan::upload(const HostPlan& hp) {
                 Ml = ch_.M;
             }
         }
+        if (shape >= SHAPE_T2A_E2C && Ml != 32) shape = SHAPE_NONE;
         if (shape != SHAPE_NONE) {
             cc.M = Ml;
             cc.alias = alias ? 1 : 0;
@@ -244,6 +256,7 @@ int DevicePlan::upload(const HostPlan& hp) {
             cc.nsteps = cl->nsteps;
             cc.L = (ch_.circ ? kLineThreadsCirc : kLineThreadsBand) / cl->Pp;
             cc.resid = ch_.resid;
+            cc.xdup = (shape == SHAPE_T2A_E2C || shape == SHAPE_T2S_E2C) && d.m == d.ns + 1;
             cc.circ = ch_.circ;
             cc.nlo = ch_.circ ? 0 : ch_.nlo;
             cc.nhi = ch_.circ ? 0 : ch_.nhi;
@@ -381,7 +394,7 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
                          : launch_chunk_m<ArDF, 32>(h, p.chunk_df(), f, out, ls, status, s);
     }
     if (path == PATH_FP32) {
-        if (p.line_shape() != SHAPE_NONE)
+        if (p.line_shape() != SHAPE_NONE && p.line_shape() < SHAPE_T2A_E2C)
             return launch_line_f32(p.line_shape(), p.line_params(), f, out, ls, status, s);
         return h.M == 16 ? launch_chunk_m<ArF32, 16>(h, p.chunk_f32(), f, out, ls, status, s)
                          : launch_chunk_m<ArF32, 32>(h, p.chunk_f32(), f, out, ls, status, s);

@@ -6,6 +6,7 @@ namespace pade {
 
 int launch_line_circ(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                      unsigned* status, cudaStream_t s) {
+    if (shape >= SHAPE_T2A_E2C) return launch_line_stagg(shape, c, f, out, ls, status, s);
     return launch_line_shapes<ArDF, true>(shape, c, f, out, ls, status, s);
 }
 

@@ -501,18 +501,13 @@ int dealias(pade_les h, double2* f, int edge, cudaStream_t s) {
     return fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_DEALIAS, h->nz, -1, 1.0 / (double)h->nz, 0, f, f, lz, ex, s);
 }
 
+// the y and z gradients; the x gradients come with the fields from prep_physical
 int compute_duidxj(pade_les h, cudaStream_t s) {
     pade_spectral C = h->spC, E = h->spE;
-    CK(spectral_ifft(C, h->uhat_cur, h->dC[0], 0, s, MUL_IK_A));
-    CK(spectral_ifft(E, h->uEhat, h->dE[0], 0, s, MUL_IK_A));
     CK(spectral_ifft(C, h->uhat_cur, h->dC[1], 0, s, MUL_IK_P));
     CK(spectral_ifft(E, h->uEhat, h->dE[1], 0, s, MUL_IK_P));
-    CK(spectral_ifft(C, h->vhat_cur, h->dC[3], 0, s, MUL_IK_A));
-    CK(spectral_ifft(E, h->vEhat, h->dE[3], 0, s, MUL_IK_A));
     CK(spectral_ifft(C, h->vhat_cur, h->dC[4], 0, s, MUL_IK_P));
     CK(spectral_ifft(E, h->vEhat, h->dE[4], 0, s, MUL_IK_P));
-    CK(spectral_ifft(C, h->whatC, h->dC[6], 0, s, MUL_IK_A));
-    CK(spectral_ifft(E, h->what_cur, h->dE[6], 0, s, MUL_IK_A));
     CK(spectral_ifft(C, h->whatC, h->dC[7], 0, s, MUL_IK_P));
     CK(spectral_ifft(E, h->what_cur, h->dE[7], 0, s, MUL_IK_P));
     // dwdz at C and E, d2wdz2 at E
@@ -534,16 +529,17 @@ int compute_duidxj(pade_les h, cudaStream_t s) {
     return spectral_ifft(C, h->tC1, h->dC[5], 0, s);
 }
 
+// physical fields and their x gradients (one y transform per pair), then the other gradients
 int prep_physical(pade_les h, cudaStream_t s) {
-    CK(spectral_ifft(h->spC, h->uhat_cur, h->u, 0, s));
-    CK(spectral_ifft(h->spC, h->vhat_cur, h->v, 0, s));
-    CK(spectral_ifft(h->spE, h->what_cur, h->w, 0, s));
+    CK(spectral_ifft_pair(h->spC, h->uhat_cur, h->u, h->dC[0], s));
+    CK(spectral_ifft_pair(h->spC, h->vhat_cur, h->v, h->dC[3], s));
+    CK(spectral_ifft_pair(h->spE, h->what_cur, h->w, h->dE[6], s));
     CK(zop(h, OP_I_E2C, 1, h->what_cur, h->whatC, s));
-    CK(spectral_ifft(h->spC, h->whatC, h->wC, 0, s));
+    CK(spectral_ifft_pair(h->spC, h->whatC, h->wC, h->dC[6], s));
     CK(zop(h, OP_I_C2E, 1, h->uhat_cur, h->uEhat, s));
-    CK(spectral_ifft(h->spE, h->uEhat, h->uE, 0, s));
+    CK(spectral_ifft_pair(h->spE, h->uEhat, h->uE, h->dE[0], s));
     CK(zop(h, OP_I_C2E, 1, h->vhat_cur, h->vEhat, s));
-    CK(spectral_ifft(h->spE, h->vEhat, h->vE, 0, s));
+    CK(spectral_ifft_pair(h->spE, h->vEhat, h->vE, h->dE[3], s));
     return compute_duidxj(h, s);
 }
 

@@ -155,6 +155,24 @@ int spectral_ifft(pade_spectral h, const void* in, double* out, int oddball, cud
     return fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, oddball, h->work, out, lx, ex, s);
 }
 
+int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out_dx, cudaStream_t s) {
+    FftExtra ex{};
+    FftLines ly = fft_lines(2, h->nxh, h->ny, h->nz, h->ny, h->ny);
+    int rc = fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PLAIN, h->ny, 1, 1.0, 0, in, h->work, ly, ex, s);
+    if (rc != PS_OK) return rc;
+    FftLines lx = fft_lines(1, h->nx, h->ny, h->nz, h->nxh, h->nx);
+    const double norm = 1.0 / ((double)h->nx * (double)h->ny);
+    rc = fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, h->work, out, lx, ex, s);
+    if (rc != PS_OK) return rc;
+    // i k1 on the y-transformed half spectrum: k1 depends on the x index alone, so it
+    // commutes with the y transform
+    ex.mul = MUL_IK_P;
+    ex.km = h->d_k1;
+    rc = fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, h->work, out_dx, lx, ex, s);
+    if (rc != PS_ENOTSUP) return rc;
+    return spectral_ifft(h, in, out_dx, 0, s, MUL_IK_A);  // transforms without that multiplier
+}
+
 int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s) {
     FftExtra ex{};
     ex.mul = MUL_MASK_AP;

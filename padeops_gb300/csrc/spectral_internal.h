@@ -86,6 +86,8 @@ int wall_setup(pade_poisson h, double dx, double dy, double dz, double Lz);
 int wall_projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStream_t s);
 // the pressure of the last walled projection (plus its Stokes pressure) into f2d
 int wall_pressure(pade_poisson h, cudaStream_t s);
+// out = ifft2(in) and out_dx = ifft2(i k1 in) from one y transform (oddball 0)
+int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out_dx, cudaStream_t s);
 // ifft of fhat * G, G = 1 where |k1| < cut1 and |k2| < cut2 (the test filter's TestFilter_oop)
 int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s);
 

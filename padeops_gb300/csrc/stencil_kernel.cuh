@@ -43,11 +43,21 @@ static_assert(LineLayout<32, 3>::S % 4 == 2 && LineLayout<32, 4>::S % 4 == 2 && 
               "32-row chunk stride");
 static_assert(LineLayout<16, 3>::S % 2 == 1 && LineLayout<16, 4>::S % 2 == 1, "16-row chunk stride");
 
-template <class AR, int NP, bool SYM>
+// RHS of one row: pairs k = 1..NP at offsets (k, -k) about the row (STG = 0), or about a
+// half point: (k, 1 - k) (STG = +1, edges to cells) or (k - 1, -k) (STG = -1, cells to edges)
+template <class AR, int NP, bool SYM, int STG = 0>
 __device__ __forceinline__ typename AR::V line_stencil(const typename AR::V* __restrict__ p,
                                                       const typename AR::V (&c)[NP], typename AR::V c0) {
     typename AR::V acc;
-    if constexpr (SYM) {
+    if constexpr (STG != 0) {
+        constexpr int sh = STG > 0 ? 0 : -1;
+        acc = SYM ? AR::mul(AR::add(p[1 + sh], p[sh]), c[0]) : AR::mul(AR::sub(p[1 + sh], p[sh]), c[0]);
+#pragma unroll
+        for (int k = 2; k <= NP; k++) {
+            const typename AR::V d = SYM ? AR::add(p[k + sh], p[1 - k + sh]) : AR::sub(p[k + sh], p[1 - k + sh]);
+            acc = AR::add(acc, AR::mul(d, c[k - 1]));
+        }
+    } else if constexpr (SYM) {
         acc = AR::mul(p[0], c0);
 #pragma unroll
         for (int k = 1; k <= NP; k++) acc = AR::add(acc, AR::mul(AR::add(p[k], p[-k]), c[k - 1]));
@@ -71,7 +81,7 @@ __host__ __device__ constexpr int line_min_blocks(bool circ, int m, bool alias) 
 // Number of per-row tables of a banded line: g a1 a2 b1 b2 pf1 pf2 pb1 pb2.
 constexpr int kRowTables = 9;
 
-template <class AR, int Q, int NP, bool SYM, bool CIRC, int M, int NT, bool ALIAS>
+template <class AR, int Q, int NP, bool SYM, bool CIRC, int M, int NT, bool ALIAS, int STG = 0>
 __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
     k_line(const StencilParams cp, const typename AR::IO* __restrict__ f, typename AR::IO* __restrict__ out,
            const LineSet ls, unsigned* __restrict__ status) {
@@ -245,6 +255,13 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
             if constexpr (CIRC) {
                 win[-h] = tile[main_pos(l, p < 0 ? p + ns : p)];
                 win[M - 1 + h] = tile[main_pos(l, q >= ns ? q - ns : q)];
+                if constexpr (STG > 0 && AR::kScaled) {
+                    if (q == ns && cp.xdup) {
+                        const double v = __ldg(f + base_in[l] + (long)ns * ls.fp);
+                        bad |= (unsigned)(bexp(v) == 2047);
+                        win[M - 1 + h] = df_from_double_shift(v, lexp[l] - 1023);
+                    }
+                }
             } else {
                 win[-h] = p < 0 ? AR::zero() : tile[main_pos(l, p)];
                 win[M - 1 + h] = q >= ns ? AR::zero() : tile[main_pos(l, q)];
@@ -281,14 +298,14 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
         for (int j = 0; j < M; j++) {
             V y;
             if constexpr (CIRC) {
-                const V r = line_stencil<AR, NP, SYM>(win + j, cc, c0);
+                const V r = line_stencil<AR, NP, SYM, STG>(win + j, cc, c0);
                 y = (Q == 2) ? AR::fms2(r, a1, s1, a2, s2) : AR::fms1(r, a1, s1);
             } else {
                 const int i = t * M + j;
                 V r;
                 if (i < nlo) r = edge[l * ne + i];
                 else if (i >= ehi) r = edge[l * ne + nlo + (i - ehi)];
-                else r = line_stencil<AR, NP, SYM>(win + j, cc, c0);
+                else r = line_stencil<AR, NP, SYM, STG>(win + j, cc, c0);
                 r = AR::mul(r, rt[j]);
                 y = (Q == 2) ? AR::fms2(r, rt[PW + j], s1, rt[2 * PW + j], s2) : AR::fms1(r, rt[PW + j], s1);
             }
@@ -469,14 +486,14 @@ size_t line_smem(const StencilParams& c) {
     return sizeof(typename AR::V) * (tabs + (size_t)c.L * line_stride(c.P * Lay::S) + work + edges);
 }
 
-template <class AR, int Q, int NP, bool SYM, bool CIRC, int M, bool ALIAS>
+template <class AR, int Q, int NP, bool SYM, bool CIRC, int M, bool ALIAS, int STG = 0>
 int launch_line_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                   cudaStream_t s) {
     using IO = typename AR::IO;
     constexpr int NT = CIRC ? kLineThreadsCirc : kLineThreadsBand;
     const long blocks = (ls.nlines + c.L - 1) / c.L;
     const size_t smem = line_smem<AR, CIRC, NP, M, ALIAS>(c);
-    auto kern = k_line<AR, Q, NP, SYM, CIRC, M, NT, ALIAS>;
+    auto kern = k_line<AR, Q, NP, SYM, CIRC, M, NT, ALIAS, STG>;
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return PS_ECUDA;
@@ -517,5 +534,8 @@ int launch_line_f32_circ(int shape, const StencilParams& c, const void* f, void*
                          unsigned* status, cudaStream_t s);
 int launch_line_f32_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                          unsigned* status, cudaStream_t s);
+// the staggered shapes (double-float, circulant, chunks of 32)
+int launch_line_stagg(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                      unsigned* status, cudaStream_t s);
 
 }  // namespace pade

@@ -77,6 +77,24 @@ def test_two_steps_match_oracle(oracle, kw):
             assert float(g.field("nu_sgs_C").min()) >= 0.0
 
 
+def test_two_steps_native_fp64_transforms(oracle, native_lib):
+    """The same step with the FP64 transform kernels, which take the fields and their x
+    gradients from separate y transforms (the double-float path shares one)."""
+    from padeops_gb300 import _lib as L
+
+    old = native_lib.pade_fft_get_arith()
+    L.check(native_lib.pade_fft_set_arith(L.FFT_FP64))
+    try:
+        g, ref = _pair(16, oracle)
+        _compare(g, ref, 1e-12)
+        for _ in range(2):
+            g.timeAdvance(use_graph=False)
+            ref.tvd_rk3()
+            _compare(g, ref, 1e-10)
+    finally:
+        native_lib.pade_fft_set_arith(old)
+
+
 def test_graph_replay_equals_eager(oracle):
     ga, _ = _pair(16, oracle)
     gb, _ = _pair(16, oracle)

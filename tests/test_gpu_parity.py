@@ -169,7 +169,7 @@ def stagg_shapes(n, op, n1=10, n2=9):
 
 
 @pytest.mark.parametrize("op", STAGG_PER)
-@pytest.mark.parametrize("n", [5, 32, 257])
+@pytest.mark.parametrize("n", [5, 32, 128, 257])
 def test_stagg_periodic(oracle, op, n):
     dx = 1.0 / n
     o = P.cd06stagg()
@@ -181,6 +181,23 @@ def test_stagg_periodic(oracle, op, n):
     for path in PATHS:
         out = run(o, L.STAGG_OPS.index(op), 3, f, sout, path=path)
         assert relerr(out, ref) < tol64(2 if op.startswith("d2") else 1, f, ref, dx), path
+
+
+@pytest.mark.parametrize("op", ["ddz_E2C", "InterpZ_E2C"])
+@pytest.mark.parametrize("n", [16, 64, 96])
+def test_stagg_periodic_edge_point_as_given(oracle, op, n):
+    """Periodic edges to cells read the (n+1)-th edge as stored (cd06stagg.F90:319, 544),
+    whether or not it repeats the first: the line kernels (n a multiple of 32) and the
+    generic chunked kernel (n = 16) alike."""
+    dx = 1.0 / n
+    o = P.cd06stagg()
+    assert o.init(n, dx) == 0
+    sin, sout = stagg_shapes(n, op)
+    f = field(sin, 12)
+    assert np.abs(f[:, :, -1] - f[:, :, 0]).max() > 0.1
+    ref = oracle.stagg(f, n, dx, op, periodic=True)
+    out = run(o, L.STAGG_OPS.index(op), 3, f, sout, path=L.PATH_DF)
+    assert relerr(out, ref) < tol64(1, f, ref, dx)
 
 
 @pytest.mark.parametrize("op", list(L.STAGG_OPS))
