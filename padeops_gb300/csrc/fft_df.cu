@@ -196,6 +196,16 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
     }
 }
 
+// c * 2^k as FP64: d(h) + d(l) with the shift on the exponent bits when |k| <= 800 (exact,
+// the same value as shifting the sum), else the checked shift of the sum
+__device__ __forceinline__ double2 cstore(cdf c, int k) {
+    if (k >= -800 && k <= 800) {  // both parts scaled on their exponent bits, no range checks
+        const unsigned kadd = (unsigned)(896 + k) << 20;
+        return make_double2(df_to_double_kadd(c.r, kadd), df_to_double_kadd(c.i, kadd));
+    }
+    return make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
+}
+
 template <int IN, int OUT, int KIND>
 __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const FftLines ls,
                                                 const float4* __restrict__ twg, int logn, int lb, int sign,
@@ -360,7 +370,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
         cdf c = ldc(smf, l * lsd + swz(KIND == FK_PLAIN ? brev(p, logn) : p, z));
         if (use_scale_df) c = cscale(c, sdf);
         const int k = emax[l] - 1023 + scale_exp;
-        const double2 v = make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
+        const double2 v = cstore(c, k);
         if (OUT == OUT_REAL) {
             reinterpret_cast<double*>(out)[o] = v.x;
         } else {
@@ -382,9 +392,6 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
 __device__ __forceinline__ cdf cconj(cdf a) { return cdf{a.r, df_neg(a.i)}; }
 __device__ __forceinline__ cdf chalf(cdf a) {
     return cdf{dfv{0.5f * a.r.h, 0.5f * a.r.l}, dfv{0.5f * a.i.h, 0.5f * a.i.l}};
-}
-__device__ __forceinline__ double2 cstore(cdf c, int k) {
-    return make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
 }
 
 // Real transforms along x lines (fp == 1) of N = 2^logN points through one complex transform
