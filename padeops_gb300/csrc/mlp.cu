@@ -5,10 +5,12 @@
 //
 // Kernels
 //  * k_mlp_infer: per point, the features (9 velocity gradients / |S|, ln(1 + Delta/eta))
-//    from the nine FP64 gradient arrays, the MLP on the tensor cores (mma.sync m16n8k16,
-//    BF16 operands, FP32 accumulation; layer-1 accumulators are re-used in registers as
-//    layer-2 operands), softplus, and nu = Cs^2 Delta^2 |S| written in FP64.  80 B/point
-//    of HBM traffic against ~10 kflop/point.
+//    from the nine FP64 gradient arrays, computed in FP32 from an integer FP64 -> FP32
+//    conversion (the FP64 pipe is 1/64 of the FP32 rate on this part and the network reads
+//    BF16), the MLP on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32
+//    accumulation; layer-1 accumulators are re-used in registers as layer-2 operands; GELU
+//    with the hardware tanh approximation), softplus, and nu = Cs^2 Delta^2 |S| written in
+//    FP64.  80 B/point of HBM traffic against ~10 kflop/point.
 //  * k_mlp_train_tile: forward and backward of a 128-sample tile in FP32 (shared memory
 //    activations), writing the tile's partial gradient; k_mlp_reduce sums the tiles in a
 //    fixed order (deterministic); k_mlp_adamw applies AdamW.
@@ -41,6 +43,15 @@ __device__ __forceinline__ float gelu_grad(float x) {
     const float t = tanhf(C_GELU * (x + 0.044715f * x * x * x));
     return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * C_GELU * (1.0f + 3.0f * 0.044715f * x * x);
 }
+// GELU with the hardware tanh approximation (inference, whose activations are then BF16)
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu_fast(float x) {
+    return 0.5f * x * (1.0f + tanh_approx(C_GELU * (x + 0.044715f * x * x * x)));
+}
 __device__ __forceinline__ float softplus(float z) { return z > 20.0f ? z : log1pf(expf(z)); }
 __device__ __forceinline__ float sigmoid(float z) { return 0.5f * (1.0f + tanhf(0.5f * z)); }
 
@@ -48,19 +59,50 @@ struct Grad9 {
     const double* p[9];
 };
 
-// features of point e; returns |S|
-__device__ __forceinline__ double point_features(const Grad9& d, long e, double delta, double nu, float* x) {
-    double g[9];
+// FP64 -> FP32 on the bits (rounded half up; zero below the FP32 normal range, infinity
+// above it): integer work, no FP64 instructions
+__device__ __forceinline__ float d2f_bits(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const int e = (int)((hi >> 20) & 0x7FFu);
+    const unsigned sign = hi & 0x80000000u;
+    if (e < 897) return __uint_as_float(sign);
+    if (e > 1150) return __uint_as_float(sign | 0x7F800000u);
+    const unsigned b = sign | ((unsigned)(e - 896) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    return __uint_as_float(b + ((lo >> 28) & 1u));
+}
+
+// 2^k as a float, -126 <= k <= 127
+__device__ __forceinline__ float pow2f(int k) { return __uint_as_float((unsigned)(k + 127) << 23); }
+
+// Features of point e in FP32 (the network sees them in BF16): the nine gradients over
+// |S| = sqrt(2 S_ij S_ij), and ln(1 + Delta sqrt(|S| / nu)).  The gradients are scaled by a
+// power of two near their largest magnitude first, so S_ij S_ij cannot overflow.  Returns |S|.
+__device__ __forceinline__ float point_features(const Grad9& d, long e, float delta, float nu, float* x) {
+    float g[9];
+    float gm = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 9; i++) g[i] = d.p[i][e];
-    const double s1 = g[0], s2 = 0.5 * (g[1] + g[3]), s3 = 0.5 * (g[2] + g[6]), s4 = g[4],
-                 s5 = 0.5 * (g[5] + g[7]), s6 = g[8];
-    const double s = s1 * s1 + 2.0 * s2 * s2 + 2.0 * s3 * s3 + s4 * s4 + 2.0 * s5 * s5 + s6 * s6;
-    const double mag = sqrt(2.0 * s);
-    const double inv = mag > 0.0 ? 1.0 / mag : 0.0;
+    for (int i = 0; i < 9; i++) {
+        g[i] = d2f_bits(d.p[i][e]);
+        gm = fmaxf(gm, fabsf(g[i]));
+    }
+    if (!(gm > 0.0f) || !(gm <= 3.0e38f)) {  // zero gradients (or non-finite ones): zero features
 #pragma unroll
-    for (int i = 0; i < 9; i++) x[i] = (float)(g[i] * inv);
-    x[9] = (float)log1p(delta * sqrt(mag / nu));
+        for (int i = 0; i < NIN; i++) x[i] = 0.0f;
+        return gm > 0.0f ? gm : 0.0f;
+    }
+    const int k = (int)((__float_as_uint(gm) >> 23) & 0xFFu) - 127;  // gm in [2^k, 2^(k+1))
+    const float sc = pow2f(max(-126, -k));
+#pragma unroll
+    for (int i = 0; i < 9; i++) g[i] *= sc;
+    const float s1 = g[0], s2 = 0.5f * (g[1] + g[3]), s3 = 0.5f * (g[2] + g[6]), s4 = g[4],
+                s5 = 0.5f * (g[5] + g[7]), s6 = g[8];
+    const float s = s1 * s1 + 2.0f * s2 * s2 + 2.0f * s3 * s3 + s4 * s4 + 2.0f * s5 * s5 + s6 * s6;
+    const float ms = sqrtf(2.0f * s);  // |S| * sc
+    const float inv = ms > 0.0f ? 1.0f / ms : 0.0f;
+#pragma unroll
+    for (int i = 0; i < 9; i++) x[i] = g[i] * inv;
+    const float mag = ms / sc;
+    x[9] = log1pf(delta * sqrtf(mag / nu));
     return mag;
 }
 
@@ -94,7 +136,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
                                                    float* __restrict__ cs2_out) {
     __shared__ InferWeights W;
     __shared__ __align__(16) __nv_bfloat16 X[TILE * XS];
-    __shared__ double mag[TILE];
+    __shared__ float mag[TILE];
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(wg);
         uint32_t* dst = reinterpret_cast<uint32_t*>(&W);
@@ -103,14 +145,15 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
     const double d2 = delta * delta;
+    const float delta_f = (float)delta, nu_f = (float)nu;
     for (long base = (long)blockIdx.x * TILE; base < n; base += (long)gridDim.x * TILE) {
         __syncthreads();  // weights loaded / previous tile consumed
         {
             const long e = base + threadIdx.x;
             float x[NIN];
-            double m = 0.0;
+            float m = 0.0f;
             if (e < n) {
-                m = point_features(d, e, delta, nu, x);
+                m = point_features(d, e, delta_f, nu_f, x);
             } else {
 #pragma unroll
                 for (int i = 0; i < NIN; i++) x[i] = 0.0f;
@@ -141,10 +184,10 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
                 const uint32_t* wr = reinterpret_cast<const uint32_t*>(W.w1 + (nt * 8 + g) * XS);
                 mma_bf16(h[nt], a, wr[t], wr[t + 4]);
                 const int c = nt * 8 + 2 * t;
-                h[nt][0] = gelu(h[nt][0] + W.b1[c]);
-                h[nt][1] = gelu(h[nt][1] + W.b1[c + 1]);
-                h[nt][2] = gelu(h[nt][2] + W.b1[c]);
-                h[nt][3] = gelu(h[nt][3] + W.b1[c + 1]);
+                h[nt][0] = gelu_fast(h[nt][0] + W.b1[c]);
+                h[nt][1] = gelu_fast(h[nt][1] + W.b1[c + 1]);
+                h[nt][2] = gelu_fast(h[nt][2] + W.b1[c]);
+                h[nt][3] = gelu_fast(h[nt][3] + W.b1[c + 1]);
             }
             // layer 2: the layer-1 accumulators of n-tiles (2kt, 2kt+1) form the A operand of k-tile kt
             float o[8][4];
@@ -168,8 +211,8 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
 #pragma unroll
             for (int nt = 0; nt < 8; nt++) {
                 const int c = nt * 8 + 2 * t;
-                z0 += W.w3[c] * gelu(o[nt][0] + W.b2[c]) + W.w3[c + 1] * gelu(o[nt][1] + W.b2[c + 1]);
-                z1 += W.w3[c] * gelu(o[nt][2] + W.b2[c]) + W.w3[c + 1] * gelu(o[nt][3] + W.b2[c + 1]);
+                z0 += W.w3[c] * gelu_fast(o[nt][0] + W.b2[c]) + W.w3[c + 1] * gelu_fast(o[nt][1] + W.b2[c + 1]);
+                z1 += W.w3[c] * gelu_fast(o[nt][2] + W.b2[c]) + W.w3[c + 1] * gelu_fast(o[nt][3] + W.b2[c + 1]);
             }
             z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
             z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
@@ -182,7 +225,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
                     const long e = base + r;
                     if (e < n) {
                         const float cs2 = softplus((hr ? z1 : z0) + W.b3);
-                        nu_out[e] = (double)cs2 * d2 * mag[r];
+                        nu_out[e] = (double)cs2 * d2 * (double)mag[r];
                         if (cs2_out) cs2_out[e] = cs2;
                     }
                 }
@@ -195,7 +238,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
 __global__ void k_mlp_features(Grad9 d, long n, double delta, double nu, float* __restrict__ X) {
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
         float x[NIN];
-        point_features(d, e, delta, nu, x);
+        point_features(d, e, (float)delta, (float)nu, x);
 #pragma unroll
         for (int i = 0; i < NIN; i++) X[e * NIN + i] = x[i];
     }
