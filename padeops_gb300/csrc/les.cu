@@ -316,7 +316,14 @@ __global__ void k_clip_neg(double* __restrict__ x, long n) {
 
 // tau = -2 nu Sij(idx)  (sgsmod_igrid.F90:188-193)
 __global__ void k_tau(Ptr9 d, int idx, const double* __restrict__ nu, double* __restrict__ out, long n) {
-    GRID_STRIDE(e, n) { out[e] = -mul(2.0 * nu[e], sij(d.p, idx, e)); }
+    // off-diagonal: 2 nu * (0.5 (a + b)) is nu * (a + b) exactly (power-of-two scalings), two
+    // FP64 instructions instead of four (the kernel runs at the FP64 issue rate)
+    const int ia = idx == 1 ? 1 : (idx == 2 ? 2 : 5), ib = idx == 1 ? 3 : (idx == 2 ? 6 : 7);
+    if (idx == 1 || idx == 2 || idx == 4) {
+        GRID_STRIDE(e, n) { out[e] = -mul(nu[e], add(d.p[ia][e], d.p[ib][e])); }
+    } else {
+        GRID_STRIDE(e, n) { out[e] = -mul(2.0 * nu[e], sij(d.p, idx, e)); }
+    }
 }
 
 // a -= i k(a) X ; b -= i k(b) X  (mtimes_ik then subtraction, sgsmod_igrid.F90:213-260);

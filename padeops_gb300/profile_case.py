@@ -5,6 +5,7 @@
     python -m padeops_gb300.profile_case --family spectral --n 256 --repeat 3   # fft + ifft
     python -m padeops_gb300.profile_case --family projection --n 256 --repeat 3
     python -m padeops_gb300.profile_case --family les --n 128 --repeat 2        # TVD-RK3 steps
+    python -m padeops_gb300.profile_case --family les_learned --n 256 --repeat 1  # learned closure
 
 Used for Nsight Compute captures of a single kernel on a bounded case; prints the mean
 CUDA-event time per application and the implied HBM throughput at 16 B/point.
@@ -19,7 +20,7 @@ import numpy as np
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--family", default="cd10",
-                    choices=["cd06", "cd10", "cf90", "gaussian", "spectral", "projection", "les"])
+                    choices=["cd06", "cd10", "cf90", "gaussian", "spectral", "projection", "les", "les_learned"])
     ap.add_argument("--opcode", type=int, default=1)
     ap.add_argument("--dir", type=int, default=1)
     ap.add_argument("--n", type=int, default=256)
@@ -37,7 +38,7 @@ def main(argv=None):
     from padeops_gb300 import build as B
 
     B.build()
-    if a.family in ("spectral", "projection", "les"):
+    if a.family in ("spectral", "projection", "les", "les_learned"):
         return spectral_case(a, torch, P)
     path = {"df": L.PATH_DF, "native": L.PATH_NATIVE, "fp32": L.PATH_FP32}[a.path]
     dt = torch.float32 if path == L.PATH_FP32 else torch.float64
@@ -82,16 +83,22 @@ def spectral_case(a, torch, P):
     n = a.n
     d = 2 * np.pi / n
     g = torch.Generator(device="cuda").manual_seed(0)
-    if a.family == "les":
+    if a.family in ("les", "les_learned"):
         from padeops_gb300.synthetic import hit_initial_field
 
         u, v, w = hit_initial_field(n, seed=4)
         grid = P.igrid()
-        grid.init(n, n, n)
+        if a.family == "les_learned":  # an untrained network: the cost does not depend on the weights
+            from padeops_gb300.sgs_learned import LearnedClosure, init_params
+
+            grid.init(n, n, n, learnedSGS=True, JudgeFreq=0)
+            grid.set_mlp(LearnedClosure(init_params(0)))
+        else:
+            grid.init(n, n, n)
         dev = lambda x: torch.from_numpy(np.ascontiguousarray(x.T)).cuda()  # noqa: E731
         grid.set_fields(dev(u), dev(v), dev(w))
         ms = _timed(torch, lambda: grid.timeAdvance(use_graph=False), a.repeat)
-        print(f"les n={n}: {ms:.3f} ms/step")
+        print(f"{a.family} n={n}: {ms:.3f} ms/step")
         return
     sp = P.spectral()
     sp.init(n, n, n, d, d)
