@@ -440,6 +440,11 @@ struct pade_les_s {
     double2 *whatC = nullptr, *uEhat = nullptr, *vEhat = nullptr;
     double2 *d2u = nullptr, *d2v = nullptr, *d2w = nullptr;
     double2 *tC1 = nullptr, *tE1 = nullptr;
+    // second stream of the RHS and its scratch (the v / w chains and every other tau chain)
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double2 *tC1b = nullptr, *tE1b = nullptr;
+    double *rC1b = nullptr, *rE1b = nullptr;
     double2 *uhat_cur = nullptr, *vhat_cur = nullptr, *what_cur = nullptr;  // fields project_and_prep acts on
     // physical fields
     double *u = nullptr, *v = nullptr, *wC = nullptr, *w = nullptr, *uE = nullptr, *vE = nullptr;
@@ -608,10 +613,45 @@ int dynamic_procedure(pade_les h, cudaStream_t s) {
     return PS_OK;
 }
 
-int sgs_rhs(pade_les h, cudaStream_t s) {
+// b waits for the work enqueued so far on a (event slot e)
+int after(pade_les h, int e, cudaStream_t a, cudaStream_t b) {
+    if (cudaEventRecord(h->ev[e], a) != cudaSuccess) return PS_ECUDA;
+    return cudaStreamWaitEvent(b, h->ev[e], 0) == cudaSuccess ? PS_OK : PS_ECUDA;
+}
+
+// Whether the eddy viscosity is pointwise in the gradients and needs no scratch, so that it
+// can run beside the nonlinear terms: every model but the plane-averaged learned one.
+bool nu_pointwise(pade_les h) { return !(h->prm.learnedSGS && h->prm.learnedPlaneAvg); }
+
+// nuC (and Dsgs, the dynamic procedure's |S|) of the pointwise models
+int sgs_nu_pointwise(pade_les h, cudaStream_t s) {
+    const long n = h->NC;
+    const unsigned g = grid_for(n);
+    const Ptr9 dC = p9(h->dC);
+    if (h->prm.learnedSGS) {
+        if (!h->mlp) return PS_EINVAL;
+        const double* grads[9];
+        for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
+        return pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, s);
+    }
+    const bool dyn = h->prm.dynamic != 0;
+    if (h->prm.SGSModelID == 1) {
+        k_sigma_kernel<<<g, 256, 0, s>>>(dC, h->nuC, n);
+    } else if (h->prm.SGSModelID == 2) {
+        k_amd_kernel<<<g, 256, 0, s>>>(dC, h->camd_x, h->camd_y, h->camd_z, h->nuC, n);
+    } else {
+        k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
+    }
+    KCHECK();
+    return PS_OK;
+}
+
+// the rest of the eddy viscosity (dynamic procedure, plane averages, model constant) and
+// its interpolation to the edges
+int sgs_nu_rest(pade_les h, cudaStream_t s) {
     const long n = h->NC, nE = h->NE;
-    const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC), gsE = grid_for(h->SE);
-    const Ptr9 dC = p9(h->dC), dE = p9(h->dE);
+    const unsigned g = grid_for(n), gE = grid_for(nE);
+    const Ptr9 dC = p9(h->dC);
     const bool learned = h->prm.learnedSGS != 0;
     const bool dyn = h->prm.dynamic != 0 && !learned;
     if (learned) {
@@ -622,11 +662,11 @@ int sgs_rhs(pade_les h, cudaStream_t s) {
             KCHECK();
             CK(dynamic_procedure(h, s));
         }
-        const double* grads[9];
-        for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
         if (h->prm.learnedPlaneAvg) {
             // nu = <Cs^2 Delta^2>_xy |S|: the closure's coefficient through the dynamic
             // procedure's plane average (Cs^2 as FP32 in the rC1 scratch)
+            const double* grads[9];
+            for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
             float* cs2 = reinterpret_cast<float*>(h->rC1);
             CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, cs2, s));
             k_cs2_delta2<<<g, 256, 0, s>>>(cs2, h->deltaLES * h->deltaLES, h->rC2, n);
@@ -640,18 +680,8 @@ int sgs_rhs(pade_les h, cudaStream_t s) {
             KCHECK();
             k_scale_nu<<<g, 256, 0, s>>>(h->nuC, h->lamL, 0.0, h->plane, n);
             KCHECK();
-        } else {
-            CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, s));
         }
     } else {
-        if (h->prm.SGSModelID == 1) {
-            k_sigma_kernel<<<g, 256, 0, s>>>(dC, h->nuC, n);
-        } else if (h->prm.SGSModelID == 2) {
-            k_amd_kernel<<<g, 256, 0, s>>>(dC, h->camd_x, h->camd_y, h->camd_z, h->nuC, n);
-        } else {
-            k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
-        }
-        KCHECK();
         if (dyn && h->newTimeStep && h->mstep % std::max(1, h->prm.DynProcFreq) == 0) CK(dynamic_procedure(h, s));
         k_scale_nu<<<g, 256, 0, s>>>(h->nuC, dyn ? h->lambda : nullptr, h->cmodel_global, h->plane, n);
         KCHECK();
@@ -662,88 +692,104 @@ int sgs_rhs(pade_les h, cudaStream_t s) {
         KCHECK();
     }
     if (h->newTimeStep) h->mstep++;
-    const double* k1 = h->spC->d_k1;
-    const double* k2 = h->spC->d_k2;
-    const long nxh = h->nxh, nxy = h->splane;
-    // ddx(tau11) -> urhs
-    k_tau<<<g, 256, 0, s>>>(dC, 0, h->nuC, h->rC1, n);
-    KCHECK();
-    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
-    k_sub_ik<<<gs, 256, 0, s>>>(h->urhs, 1, nullptr, 0, h->tC1, k1, k2, nxh, nxy, h->SC);
-    KCHECK();
-    // ddy(tau22) -> vrhs
-    k_tau<<<g, 256, 0, s>>>(dC, 3, h->nuC, h->rC1, n);
-    KCHECK();
-    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
-    k_sub_ik<<<gs, 256, 0, s>>>(h->vrhs, 2, nullptr, 0, h->tC1, k1, k2, nxh, nxy, h->SC);
-    KCHECK();
-    // ddz(tau33) -> wrhs
-    k_tau<<<g, 256, 0, s>>>(dC, 5, h->nuC, h->rC1, n);
-    KCHECK();
-    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
-    CK(zop(h, OP_DDZ_C2E, 1, h->tC1, h->tE1, s));
-    k_csub2<<<gsE, 256, 0, s>>>(h->wrhs, h->tE1, h->SE);
-    KCHECK();
-    // tau12: vrhs -= ik1 X, urhs -= ik2 X
-    k_tau<<<g, 256, 0, s>>>(dC, 1, h->nuC, h->rC1, n);
-    KCHECK();
-    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
-    k_sub_ik<<<gs, 256, 0, s>>>(h->vrhs, 1, h->urhs, 2, h->tC1, k1, k2, nxh, nxy, h->SC);
-    KCHECK();
-    // tau13 (edges): urhs -= ddz_E2C(X), wrhs -= ik1 X
-    k_tau<<<gE, 256, 0, s>>>(dE, 2, h->nuE, h->rE1, nE);
-    KCHECK();
-    CK(spectral_fft(h->spE, h->rE1, h->tE1, s));
-    CK(zop(h, OP_DDZ_E2C, 1, h->tE1, h->tC1, s));
-    k_csub2<<<gs, 256, 0, s>>>(h->urhs, h->tC1, h->SC);
-    KCHECK();
-    k_sub_ik<<<gsE, 256, 0, s>>>(h->wrhs, 1, nullptr, 0, h->tE1, k1, k2, nxh, nxy, h->SE);
-    KCHECK();
-    // tau23 (edges): vrhs -= ddz_E2C(X), wrhs -= ik2 X
-    k_tau<<<gE, 256, 0, s>>>(dE, 4, h->nuE, h->rE1, nE);
-    KCHECK();
-    CK(spectral_fft(h->spE, h->rE1, h->tE1, s));
-    CK(zop(h, OP_DDZ_E2C, 1, h->tE1, h->tC1, s));
-    k_csub2<<<gs, 256, 0, s>>>(h->vrhs, h->tC1, h->SC);
-    KCHECK();
-    k_sub_ik<<<gsE, 256, 0, s>>>(h->wrhs, 2, nullptr, 0, h->tE1, k1, k2, nxh, nxy, h->SE);
-    KCHECK();
     return PS_OK;
 }
 
+// The divergence of tau into the right-hand sides: six chains (tau component, its x-y
+// transform, the z operator where one applies, then the subtraction from the RHS).  Chains
+// alternate between two streams with their own scratch, so one chain's FP64-bound tau and
+// subtraction kernels run beside the other's transforms; the subtractions keep the
+// sequential order (each waits for the previous one), so the sums are those of one stream.
+int sgs_tau_rhs(pade_les h, cudaStream_t s) {
+    const long n = h->NC, nE = h->NE;
+    const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC), gsE = grid_for(h->SE);
+    const Ptr9 dC = p9(h->dC), dE = p9(h->dE);
+    const double* k1 = h->spC->d_k1;
+    const double* k2 = h->spC->d_k2;
+    const long nxh = h->nxh, nxy = h->splane;
+    struct Scr {
+        double *rC, *rE;
+        double2 *tC, *tE;
+        cudaStream_t st;
+    };
+    const Scr A{h->rC1, h->rE1, h->tC1, h->tE1, s}, B{h->rC1b, h->rE1b, h->tC1b, h->tE1b, h->s2};
+    CK(after(h, 0, s, h->s2));  // nuC / nuE are ready
+    for (int c = 0; c < 6; c++) {
+        const Scr& X = (c % 2 == 0) ? A : B;
+        const cudaStream_t t = X.st;
+        // tau component, transform, z operator
+        if (c < 4) {
+            static const int idx[4] = {0, 3, 5, 1};  // tau11, tau22, tau33, tau12
+            k_tau<<<g, 256, 0, t>>>(dC, idx[c], h->nuC, X.rC, n);
+            KCHECK();
+            CK(spectral_fft(h->spC, X.rC, X.tC, t));
+            if (c == 2) CK(zop(h, OP_DDZ_C2E, 1, X.tC, X.tE, t));
+        } else {
+            k_tau<<<gE, 256, 0, t>>>(dE, c == 4 ? 2 : 4, h->nuE, X.rE, nE);  // tau13, tau23 (edges)
+            KCHECK();
+            CK(spectral_fft(h->spE, X.rE, X.tE, t));
+            CK(zop(h, OP_DDZ_E2C, 1, X.tE, X.tC, t));
+        }
+        // the subtractions, after the previous chain's
+        if (c > 0) CK(after(h, 3, (c % 2 == 0) ? B.st : A.st, t));
+        switch (c) {
+            case 0: k_sub_ik<<<gs, 256, 0, t>>>(h->urhs, 1, nullptr, 0, X.tC, k1, k2, nxh, nxy, h->SC); break;
+            case 1: k_sub_ik<<<gs, 256, 0, t>>>(h->vrhs, 2, nullptr, 0, X.tC, k1, k2, nxh, nxy, h->SC); break;
+            case 2: k_csub2<<<gsE, 256, 0, t>>>(h->wrhs, X.tE, h->SE); break;
+            case 3: k_sub_ik<<<gs, 256, 0, t>>>(h->vrhs, 1, h->urhs, 2, X.tC, k1, k2, nxh, nxy, h->SC); break;
+            default:
+                k_csub2<<<gs, 256, 0, t>>>(c == 4 ? h->urhs : h->vrhs, X.tC, h->SC);
+                KCHECK();
+                k_sub_ik<<<gsE, 256, 0, t>>>(h->wrhs, c == 4 ? 1 : 2, nullptr, 0, X.tE, k1, k2, nxh, nxy, h->SE);
+                break;
+        }
+        KCHECK();
+    }
+    return after(h, 2, h->s2, s);  // join
+}
+
+// RHS of one stage (addNonLinearTerm_Rot, addViscousTerm, getRHS_SGS; igrid.F90:1497-1571,
+// 1793-1951).  The u chain runs on s, the v and w chains on the second stream with their
+// own scratch, and the pointwise eddy viscosity beside them.
 int populate_rhs(pade_les h, cudaStream_t s) {
     const long n = h->NC, nE = h->NE;
     const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC), gsE = grid_for(h->SE);
     const Ptr9 dC = p9(h->dC), dE = p9(h->dE);
-    k_nl_c<<<g, 256, 0, s>>>(dC, h->u, h->v, h->rC1, h->rC2, n);
-    KCHECK();
-    k_nl_e<<<gE, 256, 0, s>>>(dE, h->w, h->uE, h->vE, h->rE1, h->rE2, h->rE3, nE);
-    KCHECK();
     const int visc = h->prm.isInviscid ? 0 : 1;
     const double r = 1.0 / h->prm.Re;
     const double* k1 = h->spC->d_k1;
     const double* k2 = h->spC->d_k2;
+    const cudaStream_t s2 = h->s2;
+    const bool early = h->prm.useSGS && nu_pointwise(h);
+    CK(after(h, 0, s, s2));  // fork
+    if (early) CK(sgs_nu_pointwise(h, s2));
+    k_nl_c<<<g, 256, 0, s>>>(dC, h->u, h->v, h->rC1, h->rC2, n);
+    KCHECK();
+    k_nl_e<<<gE, 256, 0, s>>>(dE, h->w, h->uE, h->vE, h->rE1, h->rE2, h->rE3, nE);
+    KCHECK();
+    CK(after(h, 1, s, s2));  // the products are ready
+    // v and w (second stream, scratch tC1b / tE1b)
+    CK(spectral_fft(h->spC, h->rC2, h->tC1b, s2));
+    CK(spectral_fft(h->spE, h->rE2, h->tE1b, s2));
+    CK(zop(h, OP_I_E2C, 1, h->tE1b, h->vrhs, s2));
+    k_rhs_finish<<<gs, 256, 0, s2>>>(h->vrhs, h->tC1b, h->vhat_cur, h->d2v, k1, k2, h->nxh, h->splane, r, visc, h->SC);
+    KCHECK();
+    CK(spectral_fft(h->spE, h->rE3, h->wrhs, s2));
+    if (visc) {
+        k_rhs_finish<<<gsE, 256, 0, s2>>>(h->wrhs, nullptr, h->what_cur, h->d2w, k1, k2, h->nxh, h->splane, r, 1,
+                                           h->SE);
+        KCHECK();
+    }
     // u
     CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
     CK(spectral_fft(h->spE, h->rE1, h->tE1, s));
     CK(zop(h, OP_I_E2C, 1, h->tE1, h->urhs, s));
     k_rhs_finish<<<gs, 256, 0, s>>>(h->urhs, h->tC1, h->uhat_cur, h->d2u, k1, k2, h->nxh, h->splane, r, visc, h->SC);
     KCHECK();
-    // v
-    CK(spectral_fft(h->spC, h->rC2, h->tC1, s));
-    CK(spectral_fft(h->spE, h->rE2, h->tE1, s));
-    CK(zop(h, OP_I_E2C, 1, h->tE1, h->vrhs, s));
-    k_rhs_finish<<<gs, 256, 0, s>>>(h->vrhs, h->tC1, h->vhat_cur, h->d2v, k1, k2, h->nxh, h->splane, r, visc, h->SC);
-    KCHECK();
-    // w
-    CK(spectral_fft(h->spE, h->rE3, h->wrhs, s));
-    if (visc) {
-        k_rhs_finish<<<gsE, 256, 0, s>>>(h->wrhs, nullptr, h->what_cur, h->d2w, k1, k2, h->nxh, h->splane, r, 1,
-                                          h->SE);
-        KCHECK();
-    }
-    if (h->prm.useSGS) CK(sgs_rhs(h, s));
-    return PS_OK;
+    CK(after(h, 2, s2, s));  // join
+    if (!h->prm.useSGS) return PS_OK;
+    CK(sgs_nu_rest(h, s));
+    return sgs_tau_rhs(h, s);
 }
 
 int compute_dt(pade_les h, cudaStream_t s) {
@@ -851,6 +897,9 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
     if (rc == PS_OK) rc = pade_spectral_init(&h->spE, h->nx, h->ny, h->nz + 1, h->dx, h->dy, 0);
     if (rc == PS_OK) rc = pade_poisson_periodic_init(&h->po, h->spC, h->dx, h->dy, h->dz);
     if (rc == PS_OK) rc = pade_cd06stagg_init_periodic(&h->stagg, h->nz, h->dz);
+    if (rc == PS_OK && cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking) != cudaSuccess) rc = PS_ECUDA;
+    for (int i = 0; i < 4 && rc == PS_OK; i++)
+        if (cudaEventCreateWithFlags(&h->ev[i], cudaEventDisableTiming) != cudaSuccess) rc = PS_ECUDA;
     if (rc == PS_OK) {
         std::vector<double> k3 = wavenums(h->nz, h->dz);
         k3[h->nz / 2] = -k3[h->nz / 2];
@@ -859,14 +908,14 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
     }
     const size_t c16 = sizeof(double2), r8 = sizeof(double);
     double2** cC[] = {&h->uhat, &h->vhat, &h->uhat1, &h->vhat1, &h->urhs, &h->vrhs, &h->whatC, &h->d2u, &h->d2v,
-                      &h->tC1};
-    double2** cE[] = {&h->what, &h->what1, &h->wrhs, &h->uEhat, &h->vEhat, &h->d2w, &h->tE1};
+                      &h->tC1, &h->tC1b};
+    double2** cE[] = {&h->what, &h->what1, &h->wrhs, &h->uEhat, &h->vEhat, &h->d2w, &h->tE1, &h->tE1b};
     for (auto pp : cC)
         if (rc == PS_OK) rc = al(h, pp, c16 * h->SC);
     for (auto pp : cE)
         if (rc == PS_OK) rc = al(h, pp, c16 * h->SE);
-    double** rCl[] = {&h->u, &h->v, &h->wC, &h->rC1, &h->rC2, &h->nuC, &h->div};
-    double** rEl[] = {&h->w, &h->uE, &h->vE, &h->rE1, &h->rE2, &h->rE3, &h->nuE};
+    double** rCl[] = {&h->u, &h->v, &h->wC, &h->rC1, &h->rC2, &h->nuC, &h->div, &h->rC1b};
+    double** rEl[] = {&h->w, &h->uE, &h->vE, &h->rE1, &h->rE2, &h->rE3, &h->nuE, &h->rE1b};
     for (auto pp : rCl)
         if (rc == PS_OK) rc = al(h, pp, r8 * h->NC);
     for (auto pp : rEl)
@@ -906,6 +955,9 @@ int pade_les_destroy(pade_les h) {
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->graph) cudaGraphDestroy(h->graph);
     for (void* p : h->allocs) cudaFree(p);
+    for (cudaEvent_t e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->s2) cudaStreamDestroy(h->s2);
     if (h->stagg) pade_destroy(h->stagg);
     if (h->po) pade_poisson_destroy(h->po);
     if (h->spE) pade_spectral_destroy(h->spE);
