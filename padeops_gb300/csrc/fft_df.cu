@@ -283,6 +283,10 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     // ---- load (FP64, natural order) and the per-line maximum exponent; kLoadBatch elements
     // per thread are read before any is stored, so their global loads overlap
     int ls_l = threadIdx.x % nl, ls_p = threadIdx.x / nl;
+    // strided lines with nl dividing the block: every element of a thread is on its line
+    // threadIdx.x % nl, so the thread keeps the maximum and updates emax once
+    const bool own_line = !pin && sl == 0;
+    int my_max = 0;
     for (int e0 = threadIdx.x; e0 < total; e0 += kLoadBatch * blockDim.x) {
         double2 vb[kLoadBatch];
         int lidx[kLoadBatch], pidx[kLoadBatch];
@@ -306,9 +310,15 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             if (e0 + u * blockDim.x >= total) continue;
             const double2 v = vb[u];
             smd[lidx[u] * lsd + swz(pidx[u], z)] = v;
-            emax_update(emax, lidx[u], max(bexp(v.x), bexp(v.y)), pin && logn >= 5);
+            const int m = max(bexp(v.x), bexp(v.y));
+            if (own_line) {
+                my_max = max(my_max, m);
+            } else {
+                emax_update(emax, lidx[u], m, pin && logn >= 5);
+            }
         }
     }
+    if (own_line && threadIdx.x < total) atomicMax(&emax[threadIdx.x % nl], my_max);
     __syncthreads();
     // ---- split in place, each line scaled by 2^-(emax - 1023)
     for (int e = threadIdx.x; e < total; e += blockDim.x) {

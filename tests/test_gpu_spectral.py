@@ -54,7 +54,7 @@ def arith(request, native_lib):
 
 
 @pytest.mark.parametrize("dir", [1, 2, 3])
-@pytest.mark.parametrize("n", [2, 4, 32, 256, 1024])
+@pytest.mark.parametrize("n", [2, 4, 32, 128, 256, 1024, 2048, 8192])
 @pytest.mark.parametrize("sign", [-1, 1])
 def test_c2c_matches_numpy(native_lib, arith, dir, n, sign):
     tol = FFT_TOL[arith]
@@ -74,7 +74,7 @@ def test_c2c_matches_numpy(native_lib, arith, dir, n, sign):
     assert relerr(host(x), ref) < tol
 
 
-@pytest.mark.parametrize("nx", [2, 8, 64, 512])
+@pytest.mark.parametrize("nx", [2, 8, 64, 512, 4096])
 def test_r2c_c2r_x(native_lib, arith, nx):
     tol = FFT_TOL[arith]
     rng = np.random.default_rng(nx)
