@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -560,6 +561,118 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     }
 }
 
+// ---- 256-point complex transforms of strided lines in registers (the y transforms) ----
+// Four-step form n = 16 x 16: thread (l, j) of a CTA of 16 lines loads x[16 p1 + j],
+// p1 = 0..15, runs a 16-point DFT over p1 in registers, multiplies by W256^(j k1), and
+// exchanges through shared memory once; thread (l, k1) then runs the 16-point DFT over j and
+// stores X[k1 + 16 k2].  Each 16-point DFT is radix-4 x radix-4 (W16^(q r) between), so per
+// point one shared-memory store and load replace the four passes of k_fft_df.
+
+// y0..y3 = the 4-point DFT of x0..x3 (W4 = -i forward, +i backward)
+__device__ __forceinline__ void radix4(const cdf& x0, const cdf& x1, const cdf& x2, const cdf& x3, bool inv, cdf& y0,
+                                       cdf& y1, cdf& y2, cdf& y3) {
+    const cdf s02 = cadd(x0, x2), d02 = csub(x0, x2), s13 = cadd(x1, x3);
+    const cdf c = mul_mi(csub(x1, x3), inv);
+    y0 = cadd(s02, s13);
+    y1 = cadd(d02, c);
+    y2 = csub(s02, s13);
+    y3 = csub(d02, c);
+}
+
+// in place: a[k] = sum_m a[m] W16^(m k); tw is the 256-point table (W16^e = tw[16 e])
+__device__ __forceinline__ void dft16(cdf (&a)[16], bool inv, const float4* tw) {
+    cdf b[16];  // b[4 q + r]: the 4-point DFT over m of a[q + 4 m], times W16^(q r)
+#pragma unroll
+    for (int q = 0; q < 4; q++) radix4(a[q], a[q + 4], a[q + 8], a[q + 12], inv, b[4 * q], b[4 * q + 1], b[4 * q + 2], b[4 * q + 3]);
+#pragma unroll
+    for (int q = 1; q < 4; q++)
+#pragma unroll
+        for (int r = 1; r < 4; r++) {
+            const int e = q * r;
+            b[4 * q + r] = e == 4 ? mul_mi(b[4 * q + r], inv) : cmulw(b[4 * q + r], tw[16 * e], inv);
+        }
+#pragma unroll
+    for (int r = 0; r < 4; r++) radix4(b[r], b[4 + r], b[8 + r], b[12 + r], inv, a[r], a[r + 4], a[r + 8], a[r + 12]);
+}
+
+__global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out, const FftLines ls,
+                                                       const float4* __restrict__ twg, int sign, int scale_exp,
+                                                       float2 scale_df, int use_scale_df, const FftExtra ex) {
+    constexpr int LSD = 257;  // shared line stride (float4): consecutive lines on distinct banks
+    extern __shared__ __align__(16) float4 smf[];
+    float4* tw = smf + 16 * LSD;  // W256^t, t < 256
+    __shared__ int emax[16];
+    __shared__ long lbin[16], lbout[16];
+    __shared__ int la[16];
+    const bool inv = sign > 0;
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) tw[t] = twiddle_ext(twg, t, 128);
+    const long l0 = (long)blockIdx.x * 16;
+    const int nl = (int)min(16L, ls.nlines - l0);
+    if (threadIdx.x < nl) {
+        const long lg = l0 + threadIdx.x, a = lg % ls.na, b = lg / ls.na;
+        emax[threadIdx.x] = 0;
+        lbin[threadIdx.x] = a * ls.fa + b * ls.fb;
+        lbout[threadIdx.x] = a * ls.oa + b * ls.ob;
+        la[threadIdx.x] = (int)a;
+    }
+    __syncthreads();
+    const int l = threadIdx.x & 15, j = threadIdx.x >> 4;
+    const bool act = l < nl;
+    // ---- load x[16 p1 + j] (FP64) with the load-time multiplier, and the line maximum
+    double2 v[16];
+    int mx = 0;
+    if (act) {
+        const double2* src = reinterpret_cast<const double2*>(in) + lbin[l];
+#pragma unroll
+        for (int p1 = 0; p1 < 16; p1++) v[p1] = src[(long)(16 * p1 + j) * ls.fp];
+#pragma unroll
+        for (int p1 = 0; p1 < 16; p1++) {
+            const int p = 16 * p1 + j;
+            if (ex.mul == MUL_MASK_AP) {
+                if (!(fabs(ex.ka[la[l]]) < ex.cut_a && fabs(ex.kb[p]) < ex.cut_b)) v[p1] = make_double2(0.0, 0.0);
+            } else if (ex.mul != MUL_NONE) {
+                const double k = ex.km[ex.mul == MUL_IK_A ? la[l] : p];
+                v[p1] = make_double2(-k * v[p1].y, k * v[p1].x);
+            }
+            mx = max(mx, max(bexp(v[p1].x), bexp(v[p1].y)));
+        }
+        atomicMax(&emax[l], mx);
+    }
+    __syncthreads();
+    const int ke = emax[l] - 1023;
+    cdf a[16];
+#pragma unroll
+    for (int p1 = 0; p1 < 16; p1++)
+        a[p1] = cdf{df_from_double_shift(v[p1].x, ke), df_from_double_shift(v[p1].y, ke)};
+    // ---- DFT over p1, twiddles and exchange; then the DFT over j.  One copy of the DFT code
+    // serves both stages (a loop that is not unrolled): the unrolled kernel outgrew the
+    // instruction cache.
+#pragma unroll 1
+    for (int stage = 0; stage < 2; stage++) {
+        dft16(a, inv, tw);
+        if (stage == 1) break;
+#pragma unroll
+        for (int k1 = 1; k1 < 16; k1++) a[k1] = cmulw(a[k1], tw[j * k1], inv);
+#pragma unroll
+        for (int k1 = 0; k1 < 16; k1++) stc(smf, l * LSD + 16 * k1 + j, a[k1]);
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) a[jj] = ldc(smf, l * LSD + 16 * j + jj);  // this thread: k1 = j
+    }
+    // ---- store X[k1 + 16 k2]
+    if (act) {
+        const dfv sdf{scale_df.x, scale_df.y};
+        const int ks = ke + scale_exp;
+        double2* dst = reinterpret_cast<double2*>(out) + lbout[l];
+#pragma unroll
+        for (int k2 = 0; k2 < 16; k2++) {
+            cdf c = a[k2];
+            if (use_scale_df) c = cscale(c, sdf);
+            dst[(long)(j + 16 * k2) * ls.op] = cstore(c, ks);
+        }
+    }
+}
+
 std::mutex g_twdf_mu;
 std::map<std::pair<int, int>, float4*> g_twdf;  // (device, n) -> df exp(-2 pi i t / n), t < n/2
 
@@ -616,6 +729,15 @@ int launch_df_t(const void* in, void* out, const FftLines& ls, const float4* tw,
 
 }  // namespace
 
+// the four-step 256-point kernel unless PADE_FFT_FOURSTEP=0 (a tuning override: k_fft_df instead)
+bool fourstep_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("PADE_FFT_FOURSTEP");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, double scale, int oddball, const void* in,
                   void* out, const FftLines& ls, const FftExtra& ex, cudaStream_t s) {
     const int n = 1 << logn;
@@ -642,6 +764,16 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
                                                                   s);
     if (kind == FK_DEALIAS)
         return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_DEALIAS>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
+    if (in_mode == IN_COMPLEX && out_mode == OUT_COMPLEX && logn == 8 && ls.fp != 1 && ls.op != 1 && fourstep_enabled()) {
+        // strided 256-point lines (the y transforms): the register-resident four-step kernel
+        const size_t smem = sizeof(float4) * (16 * 257 + 256);
+        if (cudaFuncSetAttribute(k_fft_df256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return PS_ECUDA;
+        const long blocks = (ls.nlines + 15) / 16;
+        if (blocks > 0x7fffffffL) return PS_ENOTSUP;
+        k_fft_df256<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, sign, sexp, sdf, use, ex);
+        return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+    }
     if (in_mode == IN_COMPLEX && out_mode == OUT_COMPLEX)
         return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_PLAIN>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
     // 16-byte pair loads (r2c input) / stores (c2r output) need aligned real lines
