@@ -199,12 +199,15 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
 
 // c * 2^k as FP64: d(h) + d(l) with the shift on the exponent bits when |k| <= 800 (exact,
 // the same value as shifting the sum), else the checked shift of the sum
+__device__ __noinline__ double2 cstore_checked(cdf c, int k) {  // out of line: rare, keeps kernels small
+    return make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
+}
 __device__ __forceinline__ double2 cstore(cdf c, int k) {
     if (k >= -800 && k <= 800) {  // both parts scaled on their exponent bits, no range checks
         const unsigned kadd = (unsigned)(896 + k) << 20;
         return make_double2(df_to_double_kadd(c.r, kadd), df_to_double_kadd(c.i, kadd));
     }
-    return make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
+    return cstore_checked(c, k);
 }
 
 template <int IN, int OUT, int KIND>
@@ -595,6 +598,7 @@ __device__ __forceinline__ void dft16(cdf (&a)[16], bool inv, const float4* tw) 
     for (int r = 0; r < 4; r++) radix4(b[r], b[4 + r], b[8 + r], b[12 + r], inv, a[r], a[r + 4], a[r + 8], a[r + 12]);
 }
 
+template <int MUL>  // the load-time multiplier (FftMul), one instantiation each: smaller code
 __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out, const FftLines ls,
                                                        const float4* __restrict__ twg, int sign, int scale_exp,
                                                        float2 scale_df, int use_scale_df, const FftExtra ex) {
@@ -628,10 +632,10 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
 #pragma unroll
         for (int p1 = 0; p1 < 16; p1++) {
             const int p = 16 * p1 + j;
-            if (ex.mul == MUL_MASK_AP) {
+            if (MUL == MUL_MASK_AP) {
                 if (!(fabs(ex.ka[la[l]]) < ex.cut_a && fabs(ex.kb[p]) < ex.cut_b)) v[p1] = make_double2(0.0, 0.0);
-            } else if (ex.mul != MUL_NONE) {
-                const double k = ex.km[ex.mul == MUL_IK_A ? la[l] : p];
+            } else if (MUL != MUL_NONE) {
+                const double k = ex.km[MUL == MUL_IK_A ? la[l] : p];
                 v[p1] = make_double2(-k * v[p1].y, k * v[p1].x);
             }
             mx = max(mx, max(bexp(v[p1].x), bexp(v[p1].y)));
@@ -767,11 +771,15 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
     if (in_mode == IN_COMPLEX && out_mode == OUT_COMPLEX && logn == 8 && ls.fp != 1 && ls.op != 1 && fourstep_enabled()) {
         // strided 256-point lines (the y transforms): the register-resident four-step kernel
         const size_t smem = sizeof(float4) * (16 * 257 + 256);
-        if (cudaFuncSetAttribute(k_fft_df256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        auto kern = ex.mul == MUL_MASK_AP ? k_fft_df256<MUL_MASK_AP>
+                    : ex.mul == MUL_IK_A  ? k_fft_df256<MUL_IK_A>
+                    : ex.mul == MUL_IK_P  ? k_fft_df256<MUL_IK_P>
+                                          : k_fft_df256<MUL_NONE>;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return PS_ECUDA;
         const long blocks = (ls.nlines + 15) / 16;
         if (blocks > 0x7fffffffL) return PS_ENOTSUP;
-        k_fft_df256<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, sign, sexp, sdf, use, ex);
+        kern<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, sign, sexp, sdf, use, ex);
         return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
     }
     if (in_mode == IN_COMPLEX && out_mode == OUT_COMPLEX)
