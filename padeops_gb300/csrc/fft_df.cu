@@ -15,6 +15,11 @@
 // frequency (bit-reversed result); the fused kinds multiply in that order and transform
 // back by decimation in time, so no reordering pass is needed.
 //
+// Kernels: k_fft_df (any length 2..8192, radix-4 passes through shared memory, the fused z
+// kinds), k_fft_df_real (r2c / c2r along x through a half-length complex transform), and
+// k_fft_df256 (strided 256-point complex lines, a four-step 16 x 16 transform held in
+// registers with one shared-memory exchange).
+//
 // Same modes, kinds and conventions as k_fft (fft.cu).
 #include <cuda_runtime.h>
 
