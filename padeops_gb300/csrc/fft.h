@@ -47,6 +47,8 @@ struct FftExtra {
     const double* km;
     double cut_a, cut_b, cut_c;  // FK_DEALIAS: keep |ka| < cut_a and |kb| < cut_b and |kc| < cut_c
     int edge_copy;     // FK_DEALIAS: also store point 0 at point n (periodic edge plane)
+    const double* mtab;  // FK_PROJECT / FK_POISSON3D, double-float kernel: the multiplier of
+                         // each (line, bit-reversed position), fft_df_mult_table; null: computed
 };
 
 FftLines fft_lines(int dir, long n1, long n2, long n3, long in_len, long out_len);
@@ -56,6 +58,13 @@ FftLines fft_lines(int dir, long n1, long n2, long n3, long in_len, long out_len
 // oddball (IN_HALF only) zeroes the Nyquist entry before the complex-to-real transform.
 int fft_launch(int in_mode, int out_mode, int kind, int n, int sign, double scale, int oddball, const void* in,
                void* out, const FftLines& ls, const FftExtra& ex, cudaStream_t s);
+
+// The multipliers of FK_PROJECT (-1/|k|^2, 0 where |k|^2 <= 1e-14) or FK_POISSON3D
+// (-1/(|k|^2 + 1e-20), 0 for the zero mode) of z lines (i, j) of nz points (a power of two),
+// as the double-float kernel reads them: table[(i + nxh j) nz + q] for bit-reversed position
+// q (frequency brev(q)).  Allocates *out (nxh ny nz doubles) and fills it on stream s.
+int fft_df_mult_table(int kind, const double* ka, const double* kb, const double* kc, int nxh, int ny, int nz,
+                      double** out, cudaStream_t s);
 
 // The same transform in double-float arithmetic (fft_df.cu); logn = log2(n)
 int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, double scale, int oddball, const void* in,

@@ -105,6 +105,25 @@ __device__ __forceinline__ double ksq(double a, double b, double c) {
     return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
 }
 
+// the multiplier of the fused kinds at wavenumbers (a, b, c); zero_mode: the (0, 0, 0) point
+template <int KIND>
+__device__ __forceinline__ double fk_mult(double a, double b, double c, bool zero_mode) {
+    const double kr = ksq(a, b, c);
+    if (KIND == FK_PROJECT) return kr <= 1e-14 ? 0.0 : -(1.0 / kr);
+    return zero_mode ? 0.0 : -1.0 / __dadd_rn(kr, 1e-20);
+}
+
+template <int KIND>
+__global__ void k_mult_table(const double* __restrict__ ka, const double* __restrict__ kb,
+                             const double* __restrict__ kc, int nxh, int logn, long nlines, double* __restrict__ out) {
+    const long total = nlines << logn;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const long lg = e >> logn;
+        const int q = (int)(e & ((1 << logn) - 1)), f = brev(q, logn);
+        out[e] = fk_mult<KIND>(ka[lg % nxh], kb[lg / nxh], kc[f], lg == 0 && f == 0);
+    }
+}
+
 // decimation in frequency: natural order -> bit-reversed.  tw holds exp(-2 pi i t / (n 2^tws)),
 // so a table made for a longer transform serves with stride 2^tws; it extends to 3/4 of that
 // transform's length (W^(t + N/2) = -W^t) for the radix-4 twiddle W^3k.  Line l starts at
@@ -352,13 +371,11 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
                 const bool keep = fabs(ex.ka[i]) < ex.cut_a && fabs(ex.kb[j]) < ex.cut_b && fabs(ex.kc[f]) < ex.cut_c;
                 if (!keep) stc(smf, se, cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}});
             } else {
-                const double kr = ksq(ex.ka[i], ex.kb[j], ex.kc[f]);
                 double m;
-                if (KIND == FK_PROJECT) {
-                    m = kr <= 1e-14 ? 0.0 : -(1.0 / kr);
+                if (ex.mtab) {
+                    m = ex.mtab[lg * n + swz(qs, z)];
                 } else {
-                    m = -1.0 / __dadd_rn(kr, 1e-20);
-                    if (lg == 0 && f == 0) m = 0.0;
+                    m = fk_mult<KIND>(ex.ka[i], ex.kb[j], ex.kc[f], lg == 0 && f == 0);
                 }
                 unsigned bad = 0;
                 stc(smf, se, cscale(ldc(smf, se), df_from_double(m, bad)));
@@ -737,6 +754,27 @@ int launch_df_t(const void* in, void* out, const FftLines& ls, const float4* tw,
 }
 
 }  // namespace
+
+int fft_df_mult_table(int kind, const double* ka, const double* kb, const double* kc, int nxh, int ny, int nz,
+                      double** out, cudaStream_t s) {
+    *out = nullptr;
+    int logn = 0;
+    while ((1 << logn) < nz) logn++;
+    if ((1 << logn) != nz || (kind != FK_PROJECT && kind != FK_POISSON3D)) return PS_EINVAL;
+    const long nlines = (long)nxh * ny;
+    if (cudaMalloc(reinterpret_cast<void**>(out), sizeof(double) * (size_t)(nlines << logn)) != cudaSuccess) {
+        *out = nullptr;
+        cudaGetLastError();
+        return PS_ENOMEM;
+    }
+    const unsigned g = 152 * 8;
+    if (kind == FK_PROJECT) {
+        k_mult_table<FK_PROJECT><<<g, 256, 0, s>>>(ka, kb, kc, nxh, logn, nlines, *out);
+    } else {
+        k_mult_table<FK_POISSON3D><<<g, 256, 0, s>>>(ka, kb, kc, nxh, logn, nlines, *out);
+    }
+    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+}
 
 // the four-step 256-point kernel unless PADE_FFT_FOURSTEP=0 (a tuning override: k_fft_df instead)
 bool fourstep_enabled() {

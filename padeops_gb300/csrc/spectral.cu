@@ -211,6 +211,7 @@ int projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStream_t 
     ex.v = static_cast<double2*>(vhat);
     ex.nxh = nxh;
     ex.plane = (long)nxh * ny;
+    ex.mtab = h->d_mtab;
     FftLines lz = fft_lines(3, nxh, ny, nz, nz, nz);
     rc = fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PROJECT, nz, -1, 1.0 / (double)nz, 0, h->f2d, h->f2d, lz, ex, s);
     if (rc != PS_OK) return rc;
@@ -381,6 +382,9 @@ int pade_poisson_periodic_init(pade_poisson* out, pade_spectral sp, double dx, d
     if (rc == PS_OK) rc = dalloc((void**)&h->f2d, sizeof(double2) * plane * h->nz);
     if (rc == PS_OK) rc = dalloc((void**)&h->dwE, sizeof(double2) * plane * (h->nz + 1));
     if (rc == PS_OK) rc = dalloc((void**)&h->part, sizeof(double) * kMaxPartials);
+    if (rc == PS_OK) rc = fft_df_mult_table(FK_PROJECT, h->d_k1r, h->d_k2r, h->d_k3m, h->nxh, h->ny, h->nz, &h->d_mtab,
+                                            nullptr);
+    if (rc == PS_OK && cudaStreamSynchronize(nullptr) != cudaSuccess) rc = PS_ECUDA;
     if (rc != PS_OK) {
         pade_poisson_destroy(h);
         return rc;
@@ -424,7 +428,7 @@ int pade_poisson_destroy(pade_poisson h) {
     if (h->stagg) pade_destroy(h->stagg);
     void* bufs[] = {h->d_k1r, h->d_k2r, h->d_k3m, h->f2d, h->dwE, h->part, h->d_k3e, h->d_k3mc, h->d_k3mp,
                     h->fext, h->wext, h->d_den, h->d_coshb, h->d_cosht, h->d_sinhb, h->d_sinht, h->d_chats,
-                    h->su, h->sv, h->sw};
+                    h->su, h->sv, h->sw, h->d_mtab};
     for (void* b : bufs) cudaFree(b);
     delete h;
     return PS_OK;
@@ -512,6 +516,8 @@ int pade_poisson3d_init(pade_poisson3d* out, int nx, int ny, int nz, double dx, 
     if (rc == PS_OK) rc = upload(&h->d_ky, h->ky);
     if (rc == PS_OK) rc = upload(&h->d_kz, h->kz);
     if (rc == PS_OK) rc = dalloc((void**)&h->hat, sizeof(double2) * (size_t)h->nxh * ny * nz);
+    if (rc == PS_OK) rc = fft_df_mult_table(FK_POISSON3D, h->d_kx, h->d_ky, h->d_kz, h->nxh, ny, nz, &h->d_mtab, nullptr);
+    if (rc == PS_OK && cudaStreamSynchronize(nullptr) != cudaSuccess) rc = PS_ECUDA;
     if (rc != PS_OK) {
         pade_poisson3d_destroy(h);
         return rc;
@@ -526,6 +532,7 @@ int pade_poisson3d_destroy(pade_poisson3d h) {
     cudaFree(h->d_ky);
     cudaFree(h->d_kz);
     cudaFree(h->hat);
+    cudaFree(h->d_mtab);
     delete h;
     return PS_OK;
 }
@@ -546,6 +553,7 @@ int pade_poisson3d_solve(pade_poisson3d h, const double* rhs, double* f, void* s
     ex.kc = h->d_kz;
     ex.nxh = nxh;
     ex.plane = (long)nxh * ny;
+    ex.mtab = h->d_mtab;
     FftLines lz = fft_lines(3, nxh, ny, nz, nz, nz);
     if ((rc = fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_POISSON3D, nz, -1, 1.0, 0, h->hat, h->hat, lz, ex, s)) != PS_OK)
         return rc;

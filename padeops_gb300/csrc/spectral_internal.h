@@ -28,6 +28,7 @@ struct pade_poisson_s {
     double2* f2d = nullptr;    // (nxh, ny, nz): dwdz, then the pressure
     double2* dwE = nullptr;    // (nxh, ny, nz+1)
     double* part = nullptr;    // kMaxPartials
+    double* d_mtab = nullptr;  // periodic: the fused z kernel's -1/|k|^2 per (line, position)
     // walls at z = 0 and Lz (PeriodicInZ false): stagg is then the odd-odd operator
     int periodic = 1, stokes = 0;
     double* d_k3e = nullptr;    // CD06-stagg modified wavenumbers of the 2 nz extension
@@ -53,6 +54,7 @@ struct pade_poisson3d_s {
     double* d_ky = nullptr;
     double* d_kz = nullptr;
     double2* hat = nullptr;  // (nxh, ny, nz)
+    double* d_mtab = nullptr;  // the fused z kernel's multiplier per (line, position)
 };
 
 namespace pade {
