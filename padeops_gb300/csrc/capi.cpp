@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -124,6 +125,21 @@ int grow(void** buf, size_t* cur, size_t need) {
 
 constexpr size_t kPipeMinBytes = 8u << 20;
 
+}  // namespace
+
+namespace pade {
+int pipe_chunks() {
+    static const int n = [] {
+        const char* e = std::getenv("PADE_PIPE_CHUNKS");
+        const int v = e ? std::atoi(e) : 0;
+        return (v >= 1 && v <= kPipeChunks) ? v : 8;
+    }();
+    return n;
+}
+}  // namespace pade
+
+namespace {
+
 int ensure_pipe(pade_op h) {
     if (h->pipe_ok) return PS_OK;
     for (int i = 0; i < 3; i++)
@@ -148,7 +164,8 @@ int apply_host_pipelined(pade_op h, const DevicePlan& P, int path, const void* f
     const long nl = ls.nlines;
     const int mode = ls.fb != 0 ? 0 : (ls.fp == 1 ? 1 : 2);
     const long units = mode == 0 ? nl / ls.na : nl;  // b-rows or lines
-    const long per = (units + kPipeChunks - 1) / kPipeChunks;
+    const int nch = pipe_chunks();
+    const long per = (units + nch - 1) / nch;
     const unsigned char* fh = static_cast<const unsigned char*>(f);
     unsigned char* oh = static_cast<unsigned char*>(out);
     unsigned char* fd = static_cast<unsigned char*>(h->stage_in);

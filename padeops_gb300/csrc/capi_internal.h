@@ -18,8 +18,10 @@ inline bool bc_valid(int bc) { return bc == 0 || bc == 1 || bc == -1; }
 // plans are keyed by opcode * 16 + bc index (bcid(bc1) * 3 + bcid(bcn))
 inline int plan_key(int opcode, int bc1, int bcn) { return opcode * 16 + bcid(bc1) * 3 + bcid(bcn); }
 
-// chunks of the host-buffer copy-in / compute / copy-out pipeline (capi.cpp)
-constexpr int kPipeChunks = 8;
+// chunks of the host-buffer copy-in / compute / copy-out pipeline (capi.cpp): at most
+// kPipeChunks; pipe_chunks() is the number used (8, or PADE_PIPE_CHUNKS as a tuning override)
+constexpr int kPipeChunks = 32;
+int pipe_chunks();
 
 }  // namespace pade
 
