@@ -224,8 +224,8 @@ int apply_host_pipelined(pade_op h, const DevicePlan& P, int path, const void* f
 
 int apply(pade_op h, int opcode, int dir, int cplx, const void* f, void* out, int na, int nb, int bc1, int bcn,
           int path, void* stream) {
-    if (!h || !f || !out) return PS_EINVAL;
-    if (dir < 1 || dir > 3 || na < 1 || nb < 1) return PS_EINVAL;
+    if (!h) return PS_EINVAL;
+    if (dir < 1 || dir > 3 || na < 0 || nb < 0) return PS_EINVAL;
     if (path < PATH_DF || path > PATH_FP32) return PS_EINVAL;
     if (h->family == F_CD10 || h->family == F_CF90 || h->family == F_GAUSS) {
         if (!bc_valid(bc1) || !bc_valid(bcn)) return PS_EREF_BC;
@@ -239,6 +239,8 @@ int apply(pade_op h, int opcode, int dir, int cplx, const void* f, void* out, in
     const DevicePlan& P = *it->second;
     const OpDef& d = P.host().def;
     if (cplx && path == PATH_FP32) return PS_ENOTSUP;
+    if (na == 0 || nb == 0) return PS_OK;  // empty arrays: nothing to do (the reference's loops run zero times)
+    if (!f || !out) return PS_EINVAL;
     cudaStream_t s = (cudaStream_t)stream;
     LineSet ls = make_lines(dir, cplx, d.m, d.nout, na, nb);
     const size_t esz = path == PATH_FP32 ? sizeof(float) : sizeof(double);

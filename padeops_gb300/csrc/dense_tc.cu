@@ -724,8 +724,9 @@ extern "C" {
 
 int pade_dense_apply(pade_op h, int opcode, int dir, const double* f, double* out, int na, int nb, int bc1, int bcn,
                      void* stream) {
-    if (!h || na < 1 || nb < 1) return PS_EINVAL;
+    if (!h || na < 0 || nb < 0) return PS_EINVAL;
     if (dir < 1 || dir > 3) return PS_EINVAL;
+    if (na == 0 || nb == 0) return PS_OK;  // empty arrays: nothing to do
     if (!device_ptr(f) || !device_ptr(out)) return PS_EINVAL;
     if (h->family == F_CD10 || h->family == F_CF90 || h->family == F_GAUSS) {
         if (!bc_valid(bc1) || !bc_valid(bcn)) return PS_EREF_BC;

@@ -97,8 +97,8 @@ pade::LineSet lines_of(int dir, int cplx, long m, long nout, long na, long nb) {
 extern "C" int pade_apply_noalloc(pade_op h, int opcode, int dir, int is_complex, const void* f, void* out, int na,
                                   int nb, int bc1, int bcn, void* stream) {
     using namespace pade;
-    if (!h || !f || !out) return PS_EINVAL;
-    if (dir < 1 || dir > 3 || na < 1 || nb < 1) return PS_EINVAL;
+    if (!h) return PS_EINVAL;
+    if (dir < 1 || dir > 3 || na < 0 || nb < 0) return PS_EINVAL;
     if (h->family == F_CD10 || h->family == F_CF90 || h->family == F_GAUSS) {
         if (!bc_valid(bc1) || !bc_valid(bcn)) return PS_EREF_BC;
         if (h->periodic) bc1 = bcn = 0;
@@ -111,6 +111,8 @@ extern "C" int pade_apply_noalloc(pade_op h, int opcode, int dir, int is_complex
     if (it == h->plans.end()) return PS_EINVAL;
     const DevicePlan& P = *it->second;
     const OpDef& d = P.host().def;
+    if (na == 0 || nb == 0) return PS_OK;  // empty arrays: nothing to do
+    if (!f || !out) return PS_EINVAL;
     const int cplx = is_complex ? 1 : 0;
     const size_t in_bytes = sizeof(double) * (size_t)d.m * na * nb * (cplx ? 2 : 1);
     const size_t out_bytes = sizeof(double) * (size_t)d.nout * na * nb * (cplx ? 2 : 1);

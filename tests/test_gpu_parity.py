@@ -333,6 +333,28 @@ def test_range_flag_for_non_finite_input(oracle):
     assert e.value.code == L.PADE_ERANGE
 
 
+def test_empty_line_sets_are_no_ops(native_lib):
+    """No lines (na or nb = 0): success and nothing done, as the reference's loops over
+    empty arrays; null field pointers are accepted then.  Negative counts stay errors."""
+    import ctypes
+
+    h = ctypes.c_void_p()
+    assert native_lib.pade_cd10_init(ctypes.byref(h), 32, 0.1, 1, 0, 0) == 0
+    try:
+        for na, nb in ((0, 4), (4, 0), (0, 0)):
+            assert native_lib.pade_apply(h, 1, 1, 0, None, None, na, nb, 0, 0, L.PATH_DF, None) == 0
+            assert native_lib.pade_apply_noalloc(h, 1, 2, 0, None, None, na, nb, 0, 0, None) == 0
+        assert native_lib.pade_apply(h, 1, 1, 0, None, None, -1, 4, 0, 0, L.PATH_DF, None) == L.PADE_EINVAL
+        assert native_lib.pade_apply(h, 1, 1, 0, None, None, 4, 4, 0, 0, L.PATH_DF, None) == L.PADE_EINVAL
+        c = P.cd10()
+        assert c.init(32, 0.1, True) == 0
+        f = np.zeros((32, 0, 3), order="F")
+        df = np.zeros_like(f, order="F")
+        c.dd1(f, df, 0, 3)
+    finally:
+        native_lib.pade_destroy(h)
+
+
 def test_reference_error_codes():
     c = P.cd10()
     assert c.init(7, 0.1, True) == L.PADE_EREF_NONPERIODIC_N
