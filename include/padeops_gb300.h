@@ -130,7 +130,8 @@ int pade_set_path(pade_op op, int path);
 /* Generic entry: family operation `opcode` (cd06/cd10: 1 = first, 2 = second derivative;
  * cf90/gaussian: 0; cd06stagg: 0 ddz_E2C, 1 ddz_C2E, 2 ddz_C2C, 3 ddz_E2E, 4 d2dz2_C2C,
  * 5 d2dz2_E2E, 6 InterpZ_E2C, 7 InterpZ_C2E) along direction `dir` (1, 2, 3) of an array
- * whose other two extents are na, nb.  path PADE_PATH_FP32 takes float arrays. */
+ * whose other two extents are na, nb (either 0: nothing to do, f and out may be null).
+ * path PADE_PATH_FP32 takes float arrays. */
 int pade_apply(pade_op op, int opcode, int dir, int is_complex, const void* f, void* out, int na, int nb, int bc1,
                int bcn, int path, void* stream);
 /* No counterpart in the reference.  The FP64 operator application of pade_apply (the
