@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     // kinds its (x, y) wavenumber indices (one division per line, none per element)
     __shared__ long lbin[64], lbout[64];
     __shared__ int la[64], lxi[64], lyj[64];
+    __shared__ bool keep_ij[64];  // FK_DEALIAS: the x-y cut-offs of each line
     const int n = 1 << logn, half = n >> 1;
     const int lsd = n + 1;  // shared-memory line stride: lines at one point apart start on distinct banks
     const Swz z = make_swz(logn);  // point p of line l sits at l * lsd + swz(p)
@@ -265,6 +266,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             lxi[l] = (int)(lg % ex.nxh);
             lyj[l] = (int)(lg / ex.nxh);
         }
+        if (KIND == FK_DEALIAS) keep_ij[l] = fabs(ex.ka[lxi[l]]) < ex.cut_a && fabs(ex.kb[lyj[l]]) < ex.cut_b;
     }
     __syncthreads();
     // element e = (l, p): e = l n + p on contiguous lines, e = p nl + l on strided lines
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             const long lg = l0 + l;
             const int i = lxi[l], j = lyj[l];
             if (KIND == FK_DEALIAS) {
-                const bool keep = fabs(ex.ka[i]) < ex.cut_a && fabs(ex.kb[j]) < ex.cut_b && fabs(ex.kc[f]) < ex.cut_c;
+                const bool keep = keep_ij[l] && fabs(ex.kc[f]) < ex.cut_c;
                 if (!keep) stc(smf, se, cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}});
             } else {
                 double m;
@@ -630,8 +632,12 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
     __shared__ int emax[16];
     __shared__ long lbin[16], lbout[16];
     __shared__ int la[16];
+    __shared__ bool keep_a[16], keep_p[256];  // MUL_MASK_AP: the two cut-offs, once per line / position
     const bool inv = sign > 0;
-    for (int t = threadIdx.x; t < 256; t += blockDim.x) tw[t] = twiddle_ext(twg, t, 128);
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+        tw[t] = twiddle_ext(twg, t, 128);
+        if (MUL == MUL_MASK_AP) keep_p[t] = fabs(ex.kb[t]) < ex.cut_b;
+    }
     const long l0 = (long)blockIdx.x * 16;
     const int nl = (int)min(16L, ls.nlines - l0);
     if (threadIdx.x < nl) {
@@ -640,6 +646,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
         lbin[threadIdx.x] = a * ls.fa + b * ls.fb;
         lbout[threadIdx.x] = a * ls.oa + b * ls.ob;
         la[threadIdx.x] = (int)a;
+        if (MUL == MUL_MASK_AP) keep_a[threadIdx.x] = fabs(ex.ka[a]) < ex.cut_a;
     }
     __syncthreads();
     const int l = threadIdx.x & 15, j = threadIdx.x >> 4;
@@ -655,7 +662,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
         for (int p1 = 0; p1 < 16; p1++) {
             const int p = 16 * p1 + j;
             if (MUL == MUL_MASK_AP) {
-                if (!(fabs(ex.ka[la[l]]) < ex.cut_a && fabs(ex.kb[p]) < ex.cut_b)) v[p1] = make_double2(0.0, 0.0);
+                if (!(keep_a[l] && keep_p[p])) v[p1] = make_double2(0.0, 0.0);
             } else if (MUL != MUL_NONE) {
                 const double k = ex.km[MUL == MUL_IK_A ? la[l] : p];
                 v[p1] = make_double2(-k * v[p1].y, k * v[p1].x);
