@@ -633,10 +633,15 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
     __shared__ long lbin[16], lbout[16];
     __shared__ int la[16];
     __shared__ bool keep_a[16], keep_p[256];  // MUL_MASK_AP: the two cut-offs, once per line / position
+    __shared__ dfv kdf[256];  // MUL_IK_P: km per position, MUL_IK_A: per line, as double-float
     const bool inv = sign > 0;
     for (int t = threadIdx.x; t < 256; t += blockDim.x) {
         tw[t] = twiddle_ext(twg, t, 128);
         if (MUL == MUL_MASK_AP) keep_p[t] = fabs(ex.kb[t]) < ex.cut_b;
+        if (MUL == MUL_IK_P) {
+            unsigned bad = 0;
+            kdf[t] = df_from_double(ex.km[t], bad);
+        }
     }
     const long l0 = (long)blockIdx.x * 16;
     const int nl = (int)min(16L, ls.nlines - l0);
@@ -647,6 +652,10 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
         lbout[threadIdx.x] = a * ls.oa + b * ls.ob;
         la[threadIdx.x] = (int)a;
         if (MUL == MUL_MASK_AP) keep_a[threadIdx.x] = fabs(ex.ka[a]) < ex.cut_a;
+        if (MUL == MUL_IK_A) {
+            unsigned bad = 0;
+            kdf[threadIdx.x] = df_from_double(ex.km[a], bad);
+        }
     }
     __syncthreads();
     const int l = threadIdx.x & 15, j = threadIdx.x >> 4;
@@ -663,9 +672,6 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
             const int p = 16 * p1 + j;
             if (MUL == MUL_MASK_AP) {
                 if (!(keep_a[l] && keep_p[p])) v[p1] = make_double2(0.0, 0.0);
-            } else if (MUL != MUL_NONE) {
-                const double k = ex.km[MUL == MUL_IK_A ? la[l] : p];
-                v[p1] = make_double2(-k * v[p1].y, k * v[p1].x);
             }
             mx = max(mx, max(bexp(v[p1].x), bexp(v[p1].y)));
         }
@@ -675,8 +681,13 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
     const int ke = emax[l] - 1023;
     cdf a[16];
 #pragma unroll
-    for (int p1 = 0; p1 < 16; p1++)
+    for (int p1 = 0; p1 < 16; p1++) {
         a[p1] = cdf{df_from_double_shift(v[p1].x, ke), df_from_double_shift(v[p1].y, ke)};
+        if (MUL == MUL_IK_A || MUL == MUL_IK_P) {  // i k x in double-float (the FP64 products ran on the FP64 pipe)
+            const dfv k = kdf[MUL == MUL_IK_A ? l : 16 * p1 + j];
+            a[p1] = cdf{df_neg(df_norm(df_mul(a[p1].i, k))), df_norm(df_mul(a[p1].r, k))};
+        }
+    }
     // ---- DFT over p1, twiddles and exchange; then the DFT over j.  One copy of the DFT code
     // serves both stages (a loop that is not unrolled): the unrolled kernel outgrew the
     // instruction cache.
