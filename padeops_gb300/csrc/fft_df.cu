@@ -717,6 +717,121 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
     }
 }
 
+// The fused z kinds on strided 256-point lines, four-step: forward (16 x 16 in registers, one
+// exchange), the kind's multiplier at natural frequency f = j + 16 k2 (thread (line, j) then
+// holds X[j + 16 k2], which is exactly the input layout of the backward four-step), backward,
+// store; the same loads, multipliers and stores as k_fft_df's fused kinds.
+template <int KIND>
+__global__ void __launch_bounds__(256, 2) k_fft_df256_fk(const void* in, void* out, const FftLines ls,
+                                                          const float4* __restrict__ twg, int scale_exp,
+                                                          float2 scale_df, int use_scale_df, const FftExtra ex) {
+    constexpr int LSD = 257;
+    extern __shared__ __align__(16) float4 smf[];
+    float4* tw = smf + 16 * LSD;  // W256^t, t < 256
+    __shared__ int emax[16];
+    __shared__ long lbin[16], lbout[16];
+    __shared__ int lxi[16], lyj[16];
+    __shared__ bool keep_ij[16];  // FK_DEALIAS: the x-y cut-offs of each line
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) tw[t] = twiddle_ext(twg, t, 128);
+    const long l0 = (long)blockIdx.x * 16;
+    const int nl = (int)min(16L, ls.nlines - l0);
+    if (threadIdx.x < nl) {
+        const long lg = l0 + threadIdx.x, a = lg % ls.na, b = lg / ls.na;
+        emax[threadIdx.x] = 0;
+        lbin[threadIdx.x] = a * ls.fa + b * ls.fb;
+        lbout[threadIdx.x] = a * ls.oa + b * ls.ob;
+        lxi[threadIdx.x] = (int)(lg % ex.nxh);
+        lyj[threadIdx.x] = (int)(lg / ex.nxh);
+        if (KIND == FK_DEALIAS)
+            keep_ij[threadIdx.x] = fabs(ex.ka[lxi[threadIdx.x]]) < ex.cut_a && fabs(ex.kb[lyj[threadIdx.x]]) < ex.cut_b;
+    }
+    __syncthreads();
+    const int l = threadIdx.x & 15, j = threadIdx.x >> 4;
+    const bool act = l < nl;
+    const long lg = l0 + l;
+    // ---- load x[16 p1 + j] (the projection adds i (k1 uhat + k2 vhat) to dw/dz)
+    double2 v[16];
+    int mx = 0;
+    if (act) {
+        const double2* src = reinterpret_cast<const double2*>(in) + lbin[l];
+#pragma unroll
+        for (int p1 = 0; p1 < 16; p1++) v[p1] = src[(long)(16 * p1 + j) * ls.fp];
+        if (KIND == FK_PROJECT) {
+            const double k1 = ex.k1[lxi[l]], k2 = ex.k2[lyj[l]];
+#pragma unroll
+            for (int p1 = 0; p1 < 16; p1++) {
+                const long idx = lg + (long)(16 * p1 + j) * ex.plane;
+                const double2 uu = ex.u[idx], vv = ex.v[idx];
+                const double tx = __dadd_rn(__dmul_rn(k1, uu.x), __dmul_rn(k2, vv.x));
+                const double ty = __dadd_rn(__dmul_rn(k1, uu.y), __dmul_rn(k2, vv.y));
+                v[p1] = make_double2(v[p1].x - ty, v[p1].y + tx);
+            }
+        }
+#pragma unroll
+        for (int p1 = 0; p1 < 16; p1++) mx = max(mx, max(bexp(v[p1].x), bexp(v[p1].y)));
+        atomicMax(&emax[l], mx);
+    }
+    __syncthreads();
+    const int ke = emax[l] - 1023;
+    cdf a[16];
+#pragma unroll
+    for (int p1 = 0; p1 < 16; p1++) a[p1] = cdf{df_from_double_shift(v[p1].x, ke), df_from_double_shift(v[p1].y, ke)};
+    // ---- forward (stages 0, 1), multiplier, backward (stages 2, 3): one copy of the DFT code
+#pragma unroll 1
+    for (int st = 0; st < 4; st++) {
+        const bool inv = st >= 2;
+        dft16(a, inv, tw);
+        if (st == 3) break;
+        if (st == 1) {  // a[k2] = X[j + 16 k2]; lines past the end have no table entries
+#pragma unroll
+            for (int k2 = 0; k2 < 16 && act; k2++) {
+                const int f = j + 16 * k2;
+                if (KIND == FK_DEALIAS) {
+                    if (!(keep_ij[l] && fabs(ex.kc[f]) < ex.cut_c)) a[k2] = cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}};
+                } else {
+                    const double m = ex.mtab ? ex.mtab[lg * 256 + brev(f, 8)]
+                                             : fk_mult<KIND>(ex.ka[lxi[l]], ex.kb[lyj[l]], ex.kc[f], lg == 0 && f == 0);
+                    unsigned bad = 0;
+                    a[k2] = cscale(a[k2], df_from_double(m, bad));
+                }
+            }
+            continue;
+        }
+#pragma unroll
+        for (int k1 = 1; k1 < 16; k1++) a[k1] = cmulw(a[k1], tw[j * k1], inv);
+        if (st == 2) __syncthreads();  // the first exchange's reads are done
+#pragma unroll
+        for (int k1 = 0; k1 < 16; k1++) stc(smf, l * LSD + 16 * k1 + j, a[k1]);
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) a[jj] = ldc(smf, l * LSD + 16 * j + jj);
+    }
+    // ---- store x[j + 16 k2] (the projection also updates uhat and vhat)
+    if (act) {
+        const dfv sdf{scale_df.x, scale_df.y};
+        const int ks = ke + scale_exp;
+        double2* dst = reinterpret_cast<double2*>(out) + lbout[l];
+        const double k1 = KIND == FK_PROJECT ? ex.k1[lxi[l]] : 0.0, k2 = KIND == FK_PROJECT ? ex.k2[lyj[l]] : 0.0;
+#pragma unroll
+        for (int k2i = 0; k2i < 16; k2i++) {
+            const int p = j + 16 * k2i;
+            cdf c = a[k2i];
+            if (use_scale_df) c = cscale(c, sdf);
+            const double2 r = cstore(c, ks);
+            dst[(long)p * ls.op] = r;
+            if (KIND == FK_DEALIAS && ex.edge_copy && p == 0) dst[256L * ls.op] = r;
+            if (KIND == FK_PROJECT) {
+                const long idx = lg + (long)p * ex.plane;
+                double2 uu = ex.u[idx], vv = ex.v[idx];
+                uu = make_double2(uu.x + k1 * r.y, uu.y - k1 * r.x);
+                vv = make_double2(vv.x + k2 * r.y, vv.y - k2 * r.x);
+                ex.u[idx] = uu;
+                ex.v[idx] = vv;
+            }
+        }
+    }
+}
+
 std::mutex g_twdf_mu;
 std::map<std::pair<int, int>, float4*> g_twdf;  // (device, n) -> df exp(-2 pi i t / n), t < n/2
 
@@ -821,6 +936,18 @@ int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, doubl
         use = 1;
         sdf.x = (float)scale;
         sdf.y = (float)(scale - (double)sdf.x);
+    }
+    if (kind != FK_PLAIN && logn == 8 && ls.fp != 1 && ls.op != 1 && fourstep_enabled()) {
+        const size_t smem = sizeof(float4) * (16 * 257 + 256);
+        auto kern = kind == FK_PROJECT ? k_fft_df256_fk<FK_PROJECT>
+                    : kind == FK_POISSON3D ? k_fft_df256_fk<FK_POISSON3D>
+                                           : k_fft_df256_fk<FK_DEALIAS>;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return PS_ECUDA;
+        const long blocks = (ls.nlines + 15) / 16;
+        if (blocks > 0x7fffffffL) return PS_ENOTSUP;
+        kern<<<(unsigned)blocks, 256, smem, s>>>(in, out, ls, tw, sexp, sdf, use, ex);
+        return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
     }
     if (kind == FK_PROJECT)
         return launch_df_t<IN_COMPLEX, OUT_COMPLEX, FK_PROJECT>(in, out, ls, tw, logn, lb, sign, sexp, sdf, use, 0, ex, s);
