@@ -832,6 +832,104 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256_fk(const void* in, void* o
     }
 }
 
+// A field and its x derivative from one half spectrum along x (N = 256): both outputs are
+// real, so the two c2r transforms run as one complex inverse transform of length N,
+//   Z[q] = X'[q] + i Y'[q],  Z[N - q] = conj X'[q] + i conj Y'[q],  Y = i km X,
+// (X', Y': the imaginary parts at q = 0 and N/2 dropped, as c2r does), out1 = Re z,
+// out2 = Im z.  The complex transform is the four-step 16 x 16 of k_fft_df256 with thread
+// (line, j) on consecutive points of a contiguous line (coalesced loads and stores).
+__device__ __forceinline__ double dstore(dfv a, int k) {
+    if (k >= -800 && k <= 800) return df_to_double_kadd(a, (unsigned)(896 + k) << 20);
+    return shift_up(df_to_double(a), k);
+}
+
+__global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __restrict__ in, double* __restrict__ out1,
+                                                                double* __restrict__ out2, const FftLines ls,
+                                                                const float4* __restrict__ twg,
+                                                                const double* __restrict__ km, int scale_exp,
+                                                                float2 scale_df, int use_scale_df) {
+    constexpr int LSD = 16 * 17 + 1;  // rows of 17 (the exchange's reads then hit distinct banks)
+    extern __shared__ __align__(16) float4 smf[];
+    float4* tw = smf + 16 * LSD;  // W256^t, t < 256
+    __shared__ int emax[16];
+    __shared__ long lbin[16], lbout[16];
+    __shared__ dfv kdf[129];
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+        tw[t] = twiddle_ext(twg, t, 128);
+        if (t <= 128) {
+            unsigned bad = 0;
+            kdf[t] = df_from_double(km[t], bad);
+        }
+    }
+    const long l0 = (long)blockIdx.x * 16;
+    const int nl = (int)min(16L, ls.nlines - l0);
+    if (threadIdx.x < nl) {
+        const long lg = l0 + threadIdx.x, a = lg % ls.na, b = lg / ls.na;
+        emax[threadIdx.x] = 0;
+        lbin[threadIdx.x] = a * ls.fa + b * ls.fb;
+        lbout[threadIdx.x] = a * ls.oa + b * ls.ob;
+    }
+    __syncthreads();
+    const int l = threadIdx.x >> 4, j = threadIdx.x & 15;
+    const bool act = l < nl;
+    // ---- load X[q] for the points q' = 16 p1 + j (q = q' up to N/2, else N - q')
+    double2 v[16];
+    int mx = 0;
+    if (act) {
+        const double2* src = in + lbin[l];
+#pragma unroll
+        for (int p1 = 0; p1 < 16; p1++) {
+            const int qp = 16 * p1 + j;
+            v[p1] = src[qp <= 128 ? qp : 256 - qp];
+            mx = max(mx, max(bexp(v[p1].x), bexp(v[p1].y)));
+        }
+        atomicMax(&emax[l], mx);
+    }
+    __syncthreads();
+    const int ke = emax[l] - 1023;
+    cdf a[16];
+#pragma unroll
+    for (int p1 = 0; p1 < 16; p1++) {
+        const int qp = 16 * p1 + j, q = qp <= 128 ? qp : 256 - qp;
+        const bool edge = q == 0 || q == 128;
+        const dfv xr = df_from_double_shift(v[p1].x, ke), xi0 = df_from_double_shift(v[p1].y, ke);
+        const dfv xi = edge ? df_zero() : xi0;
+        const dfv k = kdf[q];
+        const dfv yr = df_neg(df_norm(df_mul(xi0, k)));          // Re(i k X) (from the stored X)
+        const dfv yi = edge ? df_zero() : df_norm(df_mul(xr, k));  // Im(i k X)
+        a[p1] = qp <= 128 ? cdf{df_norm(df_sub(xr, yi)), df_norm(df_add(xi, yr))}
+                          : cdf{df_norm(df_add(xr, yi)), df_norm(df_sub(yr, xi))};
+    }
+    // ---- backward four-step (one copy of the DFT code for both stages)
+#pragma unroll 1
+    for (int stage = 0; stage < 2; stage++) {
+        dft16(a, true, tw);
+        if (stage == 1) break;
+#pragma unroll
+        for (int k1 = 1; k1 < 16; k1++) a[k1] = cmulw(a[k1], tw[j * k1], true);
+#pragma unroll
+        for (int k1 = 0; k1 < 16; k1++) stc(smf, l * LSD + 17 * k1 + j, a[k1]);
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) a[jj] = ldc(smf, l * LSD + 17 * j + jj);  // this thread: k1 = j
+    }
+    // ---- store z[j + 16 k2]: real part to out1, imaginary part to out2
+    if (act) {
+        const dfv sdf{scale_df.x, scale_df.y};
+        const int ks = ke + scale_exp;
+        double* d1 = out1 + lbout[l];
+        double* d2 = out2 + lbout[l];
+#pragma unroll
+        for (int k2 = 0; k2 < 16; k2++) {
+            cdf c = a[k2];
+            if (use_scale_df) c = cscale(c, sdf);
+            const long o = (long)(j + 16 * k2) * ls.op;
+            d1[o] = dstore(c.r, ks);
+            d2[o] = dstore(c.i, ks);
+        }
+    }
+}
+
 std::mutex g_twdf_mu;
 std::map<std::pair<int, int>, float4*> g_twdf;  // (device, n) -> df exp(-2 pi i t / n), t < n/2
 
@@ -916,6 +1014,35 @@ bool fourstep_enabled() {
         return !(e && e[0] == '0');
     }();
     return on;
+}
+
+int fft_c2r_pair_df(const void* in, double* out1, double* out2, const FftLines& ls, int n, double scale,
+                    const double* km, cudaStream_t s) {
+    if (n != 256 || ls.fp != 1 || ls.op != 1 || !km || !fourstep_enabled()) return PS_ENOTSUP;
+    if (ls.nlines <= 0) return PS_OK;
+    const float4* tw = nullptr;
+    int rc = twiddles_df(n, &tw);
+    if (rc != PS_OK) return rc;
+    int e2 = 0;
+    const double mant = std::frexp(scale, &e2);
+    int sexp = 0, use = 0;
+    float2 sdf = make_float2(1.0f, 0.0f);
+    if (mant == 0.5) {
+        sexp = e2 - 1;
+    } else {
+        use = 1;
+        sdf.x = (float)scale;
+        sdf.y = (float)(scale - (double)sdf.x);
+    }
+    const size_t smem = sizeof(float4) * ((16 * 17 + 1) * 16 + 256);
+    if (cudaFuncSetAttribute(k_fft_df_c2r_pair256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return PS_ECUDA;
+    const long blocks = (ls.nlines + 15) / 16;
+    if (blocks > 0x7fffffffL) return PS_ENOTSUP;
+    k_fft_df_c2r_pair256<<<(unsigned)blocks, 256, smem, s>>>(static_cast<const double2*>(in), out1, out2, ls, tw, km,
+                                                             sexp, sdf, use);
+    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
 int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, double scale, int oddball, const void* in,

@@ -162,6 +162,9 @@ int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out
     if (rc != PS_OK) return rc;
     FftLines lx = fft_lines(1, h->nx, h->ny, h->nz, h->nxh, h->nx);
     const double norm = 1.0 / ((double)h->nx * (double)h->ny);
+    // both real outputs from one complex transform where that kernel applies
+    rc = fft_c2r_pair(h->work, out, out_dx, lx, h->nx, norm, h->d_k1, s);
+    if (rc != PS_ENOTSUP) return rc;
     rc = fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, h->work, out, lx, ex, s);
     if (rc != PS_OK) return rc;
     // i k1 on the y-transformed half spectrum: k1 depends on the x index alone, so it
