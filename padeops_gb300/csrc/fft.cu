@@ -276,10 +276,10 @@ FftLines fft_lines(int dir, long n1, long n2, long n3, long in_len, long out_len
     return s;
 }
 
-int fft_c2r_pair(const void* in, double* out1, double* out2, const FftLines& ls, int n, double scale,
+int fft_c2r_pair(const void* in, const void* in2, double* out1, double* out2, const FftLines& ls, int n, double scale,
                  const double* km, cudaStream_t s) {
     if (g_arith.load() != FFT_ARITH_DF) return PS_ENOTSUP;
-    return fft_c2r_pair_df(in, out1, out2, ls, n, scale, km, s);
+    return fft_c2r_pair_df(in, in2, out1, out2, ls, n, scale, km, s);
 }
 
 void fft_set_arith(int a) { g_arith.store(a == FFT_ARITH_FP64 ? FFT_ARITH_FP64 : FFT_ARITH_DF); }

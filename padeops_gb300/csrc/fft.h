@@ -66,13 +66,14 @@ int fft_launch(int in_mode, int out_mode, int kind, int n, int sign, double scal
 int fft_df_mult_table(int kind, const double* ka, const double* kb, const double* kc, int nxh, int ny, int nz,
                       double** out, cudaStream_t s);
 
-// out1 = c2r(X) and out2 = c2r(i km X) of half-spectrum lines along x (IN_HALF -> OUT_REAL
-// lines ls, n = 256, oddball 0), both times scale, in one launch; PS_ENOTSUP where this
-// path does not apply (other lengths, strided lines, FP64 arithmetic): use two fft_launch.
-int fft_c2r_pair(const void* in, double* out1, double* out2, const FftLines& ls, int n, double scale,
+// out1 = c2r(X) and out2 = c2r(Y) of half-spectrum lines along x (IN_HALF -> OUT_REAL lines
+// ls, n = 256, oddball 0), Y = in2 or, with in2 null, i km X; both times scale, in one
+// launch.  PS_ENOTSUP where this path does not apply (other lengths, strided lines, FP64
+// arithmetic): use two fft_launch.
+int fft_c2r_pair(const void* in, const void* in2, double* out1, double* out2, const FftLines& ls, int n, double scale,
                  const double* km, cudaStream_t s);
-int fft_c2r_pair_df(const void* in, double* out1, double* out2, const FftLines& ls, int n, double scale,
-                    const double* km, cudaStream_t s);
+int fft_c2r_pair_df(const void* in, const void* in2, double* out1, double* out2, const FftLines& ls, int n,
+                    double scale, const double* km, cudaStream_t s);
 
 // The same transform in double-float arithmetic (fft_df.cu); logn = log2(n)
 int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, double scale, int oddball, const void* in,

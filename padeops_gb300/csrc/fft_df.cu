@@ -832,9 +832,10 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256_fk(const void* in, void* o
     }
 }
 
-// A field and its x derivative from one half spectrum along x (N = 256): both outputs are
-// real, so the two c2r transforms run as one complex inverse transform of length N,
-//   Z[q] = X'[q] + i Y'[q],  Z[N - q] = conj X'[q] + i conj Y'[q],  Y = i km X,
+// Two real fields from two half spectra along x (N = 256; the second one given, or i km X,
+// the x derivative of the first): both outputs are real, so the two c2r transforms run as one
+// complex inverse transform of length N,
+//   Z[q] = X'[q] + i Y'[q],  Z[N - q] = conj X'[q] + i conj Y'[q],
 // (X', Y': the imaginary parts at q = 0 and N/2 dropped, as c2r does), out1 = Re z,
 // out2 = Im z.  The complex transform is the four-step 16 x 16 of k_fft_df256 with thread
 // (line, j) on consecutive points of a contiguous line (coalesced loads and stores).
@@ -843,9 +844,10 @@ __device__ __forceinline__ double dstore(dfv a, int k) {
     return shift_up(df_to_double(a), k);
 }
 
-__global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __restrict__ in, double* __restrict__ out1,
-                                                                double* __restrict__ out2, const FftLines ls,
-                                                                const float4* __restrict__ twg,
+template <bool DERIV>  // Y = i km X (DERIV) or the second half spectrum in2
+__global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __restrict__ in, const double2* __restrict__ in2,
+                                                                double* __restrict__ out1, double* __restrict__ out2,
+                                                                const FftLines ls, const float4* __restrict__ twg,
                                                                 const double* __restrict__ km, int scale_exp,
                                                                 float2 scale_df, int use_scale_df) {
     constexpr int LSD = 16 * 17 + 1;  // rows of 17 (the exchange's reads then hit distinct banks)
@@ -856,7 +858,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
     __shared__ dfv kdf[129];
     for (int t = threadIdx.x; t < 256; t += blockDim.x) {
         tw[t] = twiddle_ext(twg, t, 128);
-        if (t <= 128) {
+        if (DERIV && t <= 128) {
             unsigned bad = 0;
             kdf[t] = df_from_double(km[t], bad);
         }
@@ -873,6 +875,8 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
     const int l = threadIdx.x >> 4, j = threadIdx.x & 15;
     const bool act = l < nl;
     // ---- load X[q] for the points q' = 16 p1 + j (q = q' up to N/2, else N - q')
+    // (two inputs: the maximum first, then the values are read again after the barrier, so
+    // that the 32 raw values need not stay in registers)
     double2 v[16];
     int mx = 0;
     if (act) {
@@ -882,6 +886,15 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
             const int qp = 16 * p1 + j;
             v[p1] = src[qp <= 128 ? qp : 256 - qp];
             mx = max(mx, max(bexp(v[p1].x), bexp(v[p1].y)));
+        }
+        if (!DERIV) {
+            const double2* src2 = in2 + lbin[l];
+#pragma unroll
+            for (int p1 = 0; p1 < 16; p1++) {
+                const int qp = 16 * p1 + j;
+                const double2 w = src2[qp <= 128 ? qp : 256 - qp];
+                mx = max(mx, max(bexp(w.x), bexp(w.y)));
+            }
         }
         atomicMax(&emax[l], mx);
     }
@@ -894,9 +907,16 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
         const bool edge = q == 0 || q == 128;
         const dfv xr = df_from_double_shift(v[p1].x, ke), xi0 = df_from_double_shift(v[p1].y, ke);
         const dfv xi = edge ? df_zero() : xi0;
-        const dfv k = kdf[q];
-        const dfv yr = df_neg(df_norm(df_mul(xi0, k)));          // Re(i k X) (from the stored X)
-        const dfv yi = edge ? df_zero() : df_norm(df_mul(xr, k));  // Im(i k X)
+        dfv yr, yi;
+        if (DERIV) {
+            const dfv k = kdf[q];
+            yr = df_neg(df_norm(df_mul(xi0, k)));          // Re(i k X) (from the stored X)
+            yi = edge ? df_zero() : df_norm(df_mul(xr, k));  // Im(i k X)
+        } else {
+            const double2 w = act ? in2[lbin[l] + q] : make_double2(0.0, 0.0);
+            yr = df_from_double_shift(w.x, ke);
+            yi = edge ? df_zero() : df_from_double_shift(w.y, ke);
+        }
         a[p1] = qp <= 128 ? cdf{df_norm(df_sub(xr, yi)), df_norm(df_add(xi, yr))}
                           : cdf{df_norm(df_add(xr, yi)), df_norm(df_sub(yr, xi))};
     }
@@ -1016,9 +1036,9 @@ bool fourstep_enabled() {
     return on;
 }
 
-int fft_c2r_pair_df(const void* in, double* out1, double* out2, const FftLines& ls, int n, double scale,
-                    const double* km, cudaStream_t s) {
-    if (n != 256 || ls.fp != 1 || ls.op != 1 || !km || !fourstep_enabled()) return PS_ENOTSUP;
+int fft_c2r_pair_df(const void* in, const void* in2, double* out1, double* out2, const FftLines& ls, int n,
+                    double scale, const double* km, cudaStream_t s) {
+    if (n != 256 || ls.fp != 1 || ls.op != 1 || (!km && !in2) || !fourstep_enabled()) return PS_ENOTSUP;
     if (ls.nlines <= 0) return PS_OK;
     const float4* tw = nullptr;
     int rc = twiddles_df(n, &tw);
@@ -1035,13 +1055,13 @@ int fft_c2r_pair_df(const void* in, double* out1, double* out2, const FftLines& 
         sdf.y = (float)(scale - (double)sdf.x);
     }
     const size_t smem = sizeof(float4) * ((16 * 17 + 1) * 16 + 256);
-    if (cudaFuncSetAttribute(k_fft_df_c2r_pair256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+    auto kern = in2 ? k_fft_df_c2r_pair256<false> : k_fft_df_c2r_pair256<true>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return PS_ECUDA;
     const long blocks = (ls.nlines + 15) / 16;
     if (blocks > 0x7fffffffL) return PS_ENOTSUP;
-    k_fft_df_c2r_pair256<<<(unsigned)blocks, 256, smem, s>>>(static_cast<const double2*>(in), out1, out2, ls, tw, km,
-                                                             sexp, sdf, use);
+    kern<<<(unsigned)blocks, 256, smem, s>>>(static_cast<const double2*>(in), static_cast<const double2*>(in2), out1,
+                                             out2, ls, tw, km, sexp, sdf, use);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 

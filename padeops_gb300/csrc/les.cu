@@ -530,32 +530,30 @@ int dealias(pade_les h, double2* f, int edge, cudaStream_t s) {
     return fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_DEALIAS, h->nz, -1, 1.0 / (double)h->nz, 0, f, f, lz, ex, s);
 }
 
-// the y and z gradients; the x gradients come with the fields from prep_physical
+// the y and z gradients (the x gradients come with the fields from prep_physical), two
+// inverse transforms per call (their x passes paired in one launch); tC1b / tE1b are free here
 int compute_duidxj(pade_les h, cudaStream_t s) {
     pade_spectral C = h->spC, E = h->spE;
-    CK(spectral_ifft(C, h->uhat_cur, h->dC[1], 0, s, MUL_IK_P));
-    CK(spectral_ifft(E, h->uEhat, h->dE[1], 0, s, MUL_IK_P));
-    CK(spectral_ifft(C, h->vhat_cur, h->dC[4], 0, s, MUL_IK_P));
-    CK(spectral_ifft(E, h->vEhat, h->dE[4], 0, s, MUL_IK_P));
-    CK(spectral_ifft(C, h->whatC, h->dC[7], 0, s, MUL_IK_P));
-    CK(spectral_ifft(E, h->what_cur, h->dE[7], 0, s, MUL_IK_P));
-    // dwdz at C and E, d2wdz2 at E
+    // d/dy of u and v
+    CK(spectral_ifft_two(C, h->uhat_cur, MUL_IK_P, h->vhat_cur, MUL_IK_P, h->dC[1], h->dC[4], C->work, h->tC1b, s));
+    CK(spectral_ifft_two(E, h->uEhat, MUL_IK_P, h->vEhat, MUL_IK_P, h->dE[1], h->dE[4], E->work, h->tE1b, s));
+    // dw/dy with dw/dz (dw/dz at C, then at E; the scratch transforms in place)
     CK(zop(h, OP_DDZ_E2C, 1, h->what_cur, h->tC1, s));
-    CK(spectral_ifft(C, h->tC1, h->dC[8], 0, s));
     CK(zop(h, OP_I_C2E, 1, h->tC1, h->tE1, s));
-    CK(spectral_ifft(E, h->tE1, h->dE[8], 0, s));
+    CK(spectral_ifft_two(C, h->whatC, MUL_IK_P, h->tC1, MUL_NONE, h->dC[7], h->dC[8], C->work, h->tC1, s));
+    CK(spectral_ifft_two(E, h->what_cur, MUL_IK_P, h->tE1, MUL_NONE, h->dE[7], h->dE[8], E->work, h->tE1, s));
     if (!h->prm.isInviscid) CK(zop(h, OP_D2_E2E, 1, h->what_cur, h->d2w, s));
-    // dudz, d2udz2; dvdz, d2vdz2
+    // du/dz with dv/dz, at E and at C
     CK(zop(h, OP_DDZ_C2E, 1, h->uhat_cur, h->tE1, s));
-    CK(spectral_ifft(E, h->tE1, h->dE[2], 0, s));
-    if (!h->prm.isInviscid) CK(zop(h, OP_D2_C2C, 1, h->uhat_cur, h->d2u, s));
+    CK(zop(h, OP_DDZ_C2E, 1, h->vhat_cur, h->tE1b, s));
+    if (!h->prm.isInviscid) {
+        CK(zop(h, OP_D2_C2C, 1, h->uhat_cur, h->d2u, s));
+        CK(zop(h, OP_D2_C2C, 1, h->vhat_cur, h->d2v, s));
+    }
     CK(zop(h, OP_I_E2C, 1, h->tE1, h->tC1, s));
-    CK(spectral_ifft(C, h->tC1, h->dC[2], 0, s));
-    CK(zop(h, OP_DDZ_C2E, 1, h->vhat_cur, h->tE1, s));
-    CK(spectral_ifft(E, h->tE1, h->dE[5], 0, s));
-    if (!h->prm.isInviscid) CK(zop(h, OP_D2_C2C, 1, h->vhat_cur, h->d2v, s));
-    CK(zop(h, OP_I_E2C, 1, h->tE1, h->tC1, s));
-    return spectral_ifft(C, h->tC1, h->dC[5], 0, s);
+    CK(zop(h, OP_I_E2C, 1, h->tE1b, h->tC1b, s));
+    CK(spectral_ifft_two(E, h->tE1, MUL_NONE, h->tE1b, MUL_NONE, h->dE[2], h->dE[5], h->tE1, h->tE1b, s));
+    return spectral_ifft_two(C, h->tC1, MUL_NONE, h->tC1b, MUL_NONE, h->dC[2], h->dC[5], h->tC1, h->tC1b, s);
 }
 
 // physical fields and their x gradients (one y transform per pair), then the other gradients

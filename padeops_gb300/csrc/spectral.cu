@@ -163,7 +163,7 @@ int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out
     FftLines lx = fft_lines(1, h->nx, h->ny, h->nz, h->nxh, h->nx);
     const double norm = 1.0 / ((double)h->nx * (double)h->ny);
     // both real outputs from one complex transform where that kernel applies
-    rc = fft_c2r_pair(h->work, out, out_dx, lx, h->nx, norm, h->d_k1, s);
+    rc = fft_c2r_pair(h->work, nullptr, out, out_dx, lx, h->nx, norm, h->d_k1, s);
     if (rc != PS_ENOTSUP) return rc;
     rc = fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, h->work, out, lx, ex, s);
     if (rc != PS_OK) return rc;
@@ -174,6 +174,27 @@ int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out
     rc = fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, h->work, out_dx, lx, ex, s);
     if (rc != PS_ENOTSUP) return rc;
     return spectral_ifft(h, in, out_dx, 0, s, MUL_IK_A);  // transforms without that multiplier
+}
+
+int spectral_ifft_two(pade_spectral h, const void* in1, int mul1, const void* in2, int mul2, double* out1,
+                      double* out2, void* w1, void* w2, cudaStream_t s) {
+    FftLines ly = fft_lines(2, h->nxh, h->ny, h->nz, h->ny, h->ny);
+    for (int t = 0; t < 2; t++) {
+        FftExtra ex{};
+        ex.mul = t == 0 ? mul1 : mul2;
+        ex.km = ex.mul == MUL_IK_A ? h->d_k1 : h->d_k2;
+        const int rc = fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PLAIN, h->ny, 1, 1.0, 0, t == 0 ? in1 : in2,
+                                  t == 0 ? w1 : w2, ly, ex, s);
+        if (rc != PS_OK) return rc;
+    }
+    FftLines lx = fft_lines(1, h->nx, h->ny, h->nz, h->nxh, h->nx);
+    const double norm = 1.0 / ((double)h->nx * (double)h->ny);
+    int rc = fft_c2r_pair(w1, w2, out1, out2, lx, h->nx, norm, nullptr, s);
+    if (rc != PS_ENOTSUP) return rc;
+    FftExtra ex{};
+    rc = fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, w1, out1, lx, ex, s);
+    if (rc != PS_OK) return rc;
+    return fft_launch(IN_HALF, OUT_REAL, FK_PLAIN, h->nx, 1, norm, 0, w2, out2, lx, ex, s);
 }
 
 int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s) {

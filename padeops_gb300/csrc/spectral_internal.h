@@ -90,6 +90,11 @@ int wall_projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStre
 int wall_pressure(pade_poisson h, cudaStream_t s);
 // out = ifft2(in) and out_dx = ifft2(i k1 in) from one y transform (oddball 0)
 int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out_dx, cudaStream_t s);
+// out1 = ifft2(in1 [times i k: mul1]) and out2 = ifft2(in2 [mul2]) (oddball 0), the y
+// transforms into w1 and w2 (which may be in1 and in2: those are then overwritten), the two
+// x transforms in one launch where the paired kernel applies
+int spectral_ifft_two(pade_spectral h, const void* in1, int mul1, const void* in2, int mul2, double* out1,
+                      double* out2, void* w1, void* w2, cudaStream_t s);
 // ifft of fhat * G, G = 1 where |k1| < cut1 and |k2| < cut2 (the test filter's TestFilter_oop)
 int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s);
 
