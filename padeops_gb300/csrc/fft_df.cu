@@ -853,21 +853,26 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
     constexpr int LSD = 16 * 17 + 1;  // rows of 17 (the exchange's reads then hit distinct banks)
     extern __shared__ __align__(16) float4 smf[];
     float4* tw = smf + 16 * LSD;  // W256^t, t < 256
-    __shared__ int emax[16];
+    // each of the two fields is scaled by its own line maximum (emax1 / emax2) before the
+    // packing, so either keeps its full relative precision whatever the other's magnitude
+    __shared__ int emax1[16], emax2[16];
     __shared__ long lbin[16], lbout[16];
     __shared__ dfv kdf[129];
+    __shared__ int kexp[129];  // DERIV: an exponent bound of km[q] (-2000 for 0)
     for (int t = threadIdx.x; t < 256; t += blockDim.x) {
         tw[t] = twiddle_ext(twg, t, 128);
         if (DERIV && t <= 128) {
             unsigned bad = 0;
             kdf[t] = df_from_double(km[t], bad);
+            kexp[t] = km[t] == 0.0 ? -2000 : bexp(km[t]) - 1022;
         }
     }
     const long l0 = (long)blockIdx.x * 16;
     const int nl = (int)min(16L, ls.nlines - l0);
     if (threadIdx.x < nl) {
         const long lg = l0 + threadIdx.x, a = lg % ls.na, b = lg / ls.na;
-        emax[threadIdx.x] = 0;
+        emax1[threadIdx.x] = 0;
+        emax2[threadIdx.x] = 0;
         lbin[threadIdx.x] = a * ls.fa + b * ls.fb;
         lbout[threadIdx.x] = a * ls.oa + b * ls.ob;
     }
@@ -878,14 +883,16 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
     // (two inputs: the maximum first, then the values are read again after the barrier, so
     // that the 32 raw values need not stay in registers)
     double2 v[16];
-    int mx = 0;
+    int mx = 0, my = 0;
     if (act) {
         const double2* src = in + lbin[l];
 #pragma unroll
         for (int p1 = 0; p1 < 16; p1++) {
-            const int qp = 16 * p1 + j;
-            v[p1] = src[qp <= 128 ? qp : 256 - qp];
-            mx = max(mx, max(bexp(v[p1].x), bexp(v[p1].y)));
+            const int qp = 16 * p1 + j, q = qp <= 128 ? qp : 256 - qp;
+            v[p1] = src[q];
+            const int bx = max(bexp(v[p1].x), bexp(v[p1].y));
+            mx = max(mx, bx);
+            if (DERIV && bx > 0) my = max(my, bx + kexp[q]);  // |k X| < 2^(that - 1023)
         }
         if (!DERIV) {
             const double2* src2 = in2 + lbin[l];
@@ -893,13 +900,18 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
             for (int p1 = 0; p1 < 16; p1++) {
                 const int qp = 16 * p1 + j;
                 const double2 w = src2[qp <= 128 ? qp : 256 - qp];
-                mx = max(mx, max(bexp(w.x), bexp(w.y)));
+                my = max(my, max(bexp(w.x), bexp(w.y)));
             }
         }
-        atomicMax(&emax[l], mx);
+        atomicMax(&emax1[l], mx);
+        atomicMax(&emax2[l], min(max(my, 0), 2046));
     }
     __syncthreads();
-    const int ke = emax[l] - 1023;
+    const int ke = emax1[l] - 1023, ke2 = emax2[l] - 1023;
+    // DERIV: i k X formed from X at the first scale, then moved to the second by 2^(ke - ke2)
+    const int dsh = ke - ke2;
+    const bool sh_ok = dsh >= -126 && dsh <= 127;
+    const float shf = sh_ok ? __uint_as_float((unsigned)(dsh + 127) << 23) : 1.0f;
     cdf a[16];
 #pragma unroll
     for (int p1 = 0; p1 < 16; p1++) {
@@ -910,12 +922,20 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
         dfv yr, yi;
         if (DERIV) {
             const dfv k = kdf[q];
-            yr = df_neg(df_norm(df_mul(xi0, k)));          // Re(i k X) (from the stored X)
-            yi = edge ? df_zero() : df_norm(df_mul(xr, k));  // Im(i k X)
+            dfv xr2 = xr, xi2 = xi0;
+            if (sh_ok) {
+                xr2 = dfv{xr.h * shf, xr.l * shf};
+                xi2 = dfv{xi0.h * shf, xi0.l * shf};
+            } else {
+                xr2 = df_from_double_shift(v[p1].x, ke2);
+                xi2 = df_from_double_shift(v[p1].y, ke2);
+            }
+            yr = df_neg(df_norm(df_mul(xi2, k)));           // Re(i k X) (from the stored X)
+            yi = edge ? df_zero() : df_norm(df_mul(xr2, k));  // Im(i k X)
         } else {
             const double2 w = act ? in2[lbin[l] + q] : make_double2(0.0, 0.0);
-            yr = df_from_double_shift(w.x, ke);
-            yi = edge ? df_zero() : df_from_double_shift(w.y, ke);
+            yr = df_from_double_shift(w.x, ke2);
+            yi = edge ? df_zero() : df_from_double_shift(w.y, ke2);
         }
         a[p1] = qp <= 128 ? cdf{df_norm(df_sub(xr, yi)), df_norm(df_add(xi, yr))}
                           : cdf{df_norm(df_add(xr, yi)), df_norm(df_sub(yr, xi))};
@@ -936,7 +956,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
     // ---- store z[j + 16 k2]: real part to out1, imaginary part to out2
     if (act) {
         const dfv sdf{scale_df.x, scale_df.y};
-        const int ks = ke + scale_exp;
+        const int ks = ke + scale_exp, ks2 = ke2 + scale_exp;
         double* d1 = out1 + lbout[l];
         double* d2 = out2 + lbout[l];
 #pragma unroll
@@ -945,7 +965,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
             if (use_scale_df) c = cscale(c, sdf);
             const long o = (long)(j + 16 * k2) * ls.op;
             d1[o] = dstore(c.r, ks);
-            d2[o] = dstore(c.i, ks);
+            d2[o] = dstore(c.i, ks2);
         }
     }
 }

@@ -58,6 +58,21 @@ def test_init_sequence_matches_oracle(oracle):
     _compare(g, ref, 1e-12)
 
 
+def test_init_sequence_with_disparate_magnitudes(oracle):
+    """Velocity components 1e6 apart: transforms that share a launch keep each field's own
+    scaling, so the small component's gradients stay at full relative precision."""
+    n, L_ = 16, 2 * np.pi
+    u, v, w = hit_initial_field(n, seed=4)
+    v = 1e-6 * v
+    w = 1e3 * w
+    ref = LesOracle(n, n, n, L_, L_, L_)
+    ref.init_fields(u, v, w)
+    g = P.igrid()
+    g.init(n, n, n)
+    g.set_fields(dev(u), dev(v), dev(w))
+    _compare(g, ref, 1e-12)
+
+
 @pytest.mark.parametrize("kw", [dict(dynamic=True), dict(dynamic=False), dict(useSGS=False),
                                 dict(useSGS=False, isInviscid=True), dict(dynamic=False, SGSModelID=1),
                                 dict(dynamic=False, SGSModelID=2)])
