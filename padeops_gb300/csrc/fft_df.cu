@@ -17,8 +17,10 @@
 //
 // Kernels: k_fft_df (any length 2..8192, radix-4 passes through shared memory, the fused z
 // kinds), k_fft_df_real (r2c / c2r along x through a half-length complex transform), and
-// k_fft_df256 (strided 256-point complex lines, a four-step 16 x 16 transform held in
-// registers with one shared-memory exchange).
+// for 256-point lines the register four-step 16 x 16 (one shared-memory exchange):
+// k_fft_df256 (strided complex lines, the y transforms), k_fft_df256_fk (the fused z kinds),
+// k_fft_df_c2r_pair256 (two c2r transforms of contiguous x lines as one complex transform).
+// PADE_FFT_FOURSTEP=0 (a tuning override) keeps the radix-4 kernels everywhere.
 //
 // Same modes, kinds and conventions as k_fft (fft.cu).
 #include <cuda_runtime.h>
