@@ -841,9 +841,14 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256_fk(const void* in, void* o
 // (X', Y': the imaginary parts at q = 0 and N/2 dropped, as c2r does), out1 = Re z,
 // out2 = Im z.  The complex transform is the four-step 16 x 16 of k_fft_df256 with thread
 // (line, j) on consecutive points of a contiguous line (coalesced loads and stores).
+__device__ __noinline__ double dstore_checked(dfv a, int k) { return shift_up(df_to_double(a), k); }
 __device__ __forceinline__ double dstore(dfv a, int k) {
     if (k >= -800 && k <= 800) return df_to_double_kadd(a, (unsigned)(896 + k) << 20);
-    return shift_up(df_to_double(a), k);
+    return dstore_checked(a, k);  // out of line: rare, keeps the kernel small
+}
+// X split at line scale 2^k (the rare path of the derivative pair, out of line)
+__device__ __noinline__ cdf split_at(double2 x, int k) {
+    return cdf{df_from_double_shift(x.x, k), df_from_double_shift(x.y, k)};
 }
 
 template <bool DERIV>  // Y = i km X (DERIV) or the second half spectrum in2
@@ -929,8 +934,9 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
                 xr2 = dfv{xr.h * shf, xr.l * shf};
                 xi2 = dfv{xi0.h * shf, xi0.l * shf};
             } else {
-                xr2 = df_from_double_shift(v[p1].x, ke2);
-                xi2 = df_from_double_shift(v[p1].y, ke2);
+                const cdf x2 = split_at(v[p1], ke2);
+                xr2 = x2.r;
+                xi2 = x2.i;
             }
             yr = df_neg(df_norm(df_mul(xi2, k)));           // Re(i k X) (from the stored X)
             yi = edge ? df_zero() : df_norm(df_mul(xr2, k));  // Im(i k X)
