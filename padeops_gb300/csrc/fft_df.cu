@@ -115,6 +115,12 @@ __device__ __forceinline__ double fk_mult(double a, double b, double c, bool zer
     return zero_mode ? 0.0 : -1.0 / __dadd_rn(kr, 1e-20);
 }
 
+// out of line for the unrolled four-step kernel (its tables make this path rare)
+template <int KIND>
+__device__ __noinline__ double fk_mult_call(double a, double b, double c, bool zero_mode) {
+    return fk_mult<KIND>(a, b, c, zero_mode);
+}
+
 template <int KIND>
 __global__ void k_mult_table(const double* __restrict__ ka, const double* __restrict__ kb,
                              const double* __restrict__ kc, int nxh, int logn, long nlines, double* __restrict__ out) {
@@ -792,7 +798,8 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256_fk(const void* in, void* o
                     if (!(keep_ij[l] && fabs(ex.kc[f]) < ex.cut_c)) a[k2] = cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}};
                 } else {
                     const double m = ex.mtab ? ex.mtab[lg * 256 + brev(f, 8)]
-                                             : fk_mult<KIND>(ex.ka[lxi[l]], ex.kb[lyj[l]], ex.kc[f], lg == 0 && f == 0);
+                                             : fk_mult_call<KIND>(ex.ka[lxi[l]], ex.kb[lyj[l]], ex.kc[f],
+                                                                  lg == 0 && f == 0);
                     unsigned bad = 0;
                     a[k2] = cscale(a[k2], df_from_double(m, bad));
                 }
