@@ -282,6 +282,12 @@ int fft_c2r_pair(const void* in, const void* in2, double* out1, double* out2, co
     return fft_c2r_pair_df(in, in2, out1, out2, ls, n, scale, km, s);
 }
 
+int fft_r2c_pair(const double* in1, const double* in2, void* out1, void* out2, const FftLines& ls, int n,
+                 double scale, cudaStream_t s) {
+    if (g_arith.load() != FFT_ARITH_DF) return PS_ENOTSUP;
+    return fft_r2c_pair_df(in1, in2, out1, out2, ls, n, scale, s);
+}
+
 void fft_set_arith(int a) { g_arith.store(a == FFT_ARITH_FP64 ? FFT_ARITH_FP64 : FFT_ARITH_DF); }
 int fft_get_arith() { return g_arith.load(); }
 

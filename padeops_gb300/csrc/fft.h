@@ -74,6 +74,12 @@ int fft_c2r_pair(const void* in, const void* in2, double* out1, double* out2, co
                  const double* km, cudaStream_t s);
 int fft_c2r_pair_df(const void* in, const void* in2, double* out1, double* out2, const FftLines& ls, int n,
                     double scale, const double* km, cudaStream_t s);
+// out1 = r2c(in1), out2 = r2c(in2) of real lines along x (IN_REAL -> OUT_HALF lines ls, n =
+// 256), both times scale, in one launch; PS_ENOTSUP where this path does not apply.
+int fft_r2c_pair(const double* in1, const double* in2, void* out1, void* out2, const FftLines& ls, int n,
+                 double scale, cudaStream_t s);
+int fft_r2c_pair_df(const double* in1, const double* in2, void* out1, void* out2, const FftLines& ls, int n,
+                    double scale, cudaStream_t s);
 
 // The same transform in double-float arithmetic (fft_df.cu); logn = log2(n)
 int fft_launch_df(int in_mode, int out_mode, int kind, int logn, int sign, double scale, int oddball, const void* in,

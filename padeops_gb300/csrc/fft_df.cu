@@ -985,6 +985,85 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
     }
 }
 
+// Two real fields along x (N = 256) to their half spectra with one complex transform:
+// z = x1 2^-e1 + i x2 2^-e2 (each field scaled by its own line maximum), Z = FFT(z), and for
+// k = 0..N/2: X1 = (Z[k] + conj Z[N-k]) / 2, X2 = -i (Z[k] - conj Z[N-k]) / 2, each stored
+// with its own exponent.  The transform is the register four-step 16 x 16.
+__global__ void __launch_bounds__(256, 2) k_fft_df_r2c_pair256(const double* __restrict__ in1,
+                                                                const double* __restrict__ in2,
+                                                                double2* __restrict__ out1, double2* __restrict__ out2,
+                                                                const FftLines ls, const float4* __restrict__ twg,
+                                                                int scale_exp, float2 scale_df, int use_scale_df) {
+    constexpr int LSD = 16 * 17 + 1;
+    extern __shared__ __align__(16) float4 smf[];
+    float4* tw = smf + 16 * LSD;  // W256^t, t < 256
+    __shared__ int emax1[16], emax2[16];
+    __shared__ long lbin[16], lbout[16];
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) tw[t] = twiddle_ext(twg, t, 128);
+    const long l0 = (long)blockIdx.x * 16;
+    const int nl = (int)min(16L, ls.nlines - l0);
+    if (threadIdx.x < nl) {
+        const long lg = l0 + threadIdx.x, a = lg % ls.na, b = lg / ls.na;
+        emax1[threadIdx.x] = 0;
+        emax2[threadIdx.x] = 0;
+        lbin[threadIdx.x] = a * ls.fa + b * ls.fb;
+        lbout[threadIdx.x] = a * ls.oa + b * ls.ob;
+    }
+    __syncthreads();
+    const int l = threadIdx.x >> 4, j = threadIdx.x & 15;
+    const bool act = l < nl;
+    double2 v[16];  // (x1, x2) at point 16 p1 + j
+    if (act) {
+        int m1 = 0, m2 = 0;
+#pragma unroll
+        for (int p1 = 0; p1 < 16; p1++) {
+            const long o = lbin[l] + 16 * p1 + j;
+            v[p1] = make_double2(in1[o], in2[o]);
+            m1 = max(m1, bexp(v[p1].x));
+            m2 = max(m2, bexp(v[p1].y));
+        }
+        atomicMax(&emax1[l], m1);
+        atomicMax(&emax2[l], m2);
+    }
+    __syncthreads();
+    const int ke1 = emax1[l] - 1023, ke2 = emax2[l] - 1023;
+    cdf a[16];
+#pragma unroll
+    for (int p1 = 0; p1 < 16; p1++) a[p1] = cdf{df_from_double_shift(v[p1].x, ke1), df_from_double_shift(v[p1].y, ke2)};
+#pragma unroll 1
+    for (int stage = 0; stage < 2; stage++) {
+        dft16(a, false, tw);
+        if (stage == 1) break;
+#pragma unroll
+        for (int k1 = 1; k1 < 16; k1++) a[k1] = cmulw(a[k1], tw[j * k1], false);
+#pragma unroll
+        for (int k1 = 0; k1 < 16; k1++) stc(smf, l * LSD + 17 * k1 + j, a[k1]);
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) a[jj] = ldc(smf, l * LSD + 17 * j + jj);  // this thread: k1 = j
+    }
+    // ---- Z in natural order, then the two half spectra
+    __syncthreads();  // the exchange's reads are done
+#pragma unroll
+    for (int k2 = 0; k2 < 16; k2++) stc(smf, l * LSD + j + 16 * k2, a[k2]);
+    __syncthreads();
+    if (act) {
+        const dfv sdf{scale_df.x, scale_df.y};
+        const int ks1 = ke1 + scale_exp, ks2 = ke2 + scale_exp;
+        for (int k = j; k <= 128; k += 16) {
+            const cdf zk = ldc(smf, l * LSD + k), zn = ldc(smf, l * LSD + ((256 - k) & 255));
+            cdf x1 = chalf(cdf{df_norm(df_add(zk.r, zn.r)), df_norm(df_sub(zk.i, zn.i))});
+            cdf x2 = chalf(cdf{df_norm(df_add(zk.i, zn.i)), df_norm(df_sub(zn.r, zk.r))});
+            if (use_scale_df) {
+                x1 = cscale(x1, sdf);
+                x2 = cscale(x2, sdf);
+            }
+            out1[lbout[l] + (long)k * ls.op] = cstore(x1, ks1);
+            out2[lbout[l] + (long)k * ls.op] = cstore(x2, ks2);
+        }
+    }
+}
+
 std::mutex g_twdf_mu;
 std::map<std::pair<int, int>, float4*> g_twdf;  // (device, n) -> df exp(-2 pi i t / n), t < n/2
 
@@ -1069,6 +1148,35 @@ bool fourstep_enabled() {
         return !(e && e[0] == '0');
     }();
     return on;
+}
+
+int fft_r2c_pair_df(const double* in1, const double* in2, void* out1, void* out2, const FftLines& ls, int n,
+                    double scale, cudaStream_t s) {
+    if (n != 256 || ls.fp != 1 || ls.op != 1 || !fourstep_enabled()) return PS_ENOTSUP;
+    if (ls.nlines <= 0) return PS_OK;
+    const float4* tw = nullptr;
+    int rc = twiddles_df(n, &tw);
+    if (rc != PS_OK) return rc;
+    int e2 = 0;
+    const double mant = std::frexp(scale, &e2);
+    int sexp = 0, use = 0;
+    float2 sdf = make_float2(1.0f, 0.0f);
+    if (mant == 0.5) {
+        sexp = e2 - 1;
+    } else {
+        use = 1;
+        sdf.x = (float)scale;
+        sdf.y = (float)(scale - (double)sdf.x);
+    }
+    const size_t smem = sizeof(float4) * ((16 * 17 + 1) * 16 + 256);
+    if (cudaFuncSetAttribute(k_fft_df_r2c_pair256, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return PS_ECUDA;
+    const long blocks = (ls.nlines + 15) / 16;
+    if (blocks > 0x7fffffffL) return PS_ENOTSUP;
+    k_fft_df_r2c_pair256<<<(unsigned)blocks, 256, smem, s>>>(in1, in2, static_cast<double2*>(out1),
+                                                             static_cast<double2*>(out2), ls, tw, sexp, sdf, use);
+    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
 int fft_c2r_pair_df(const void* in, const void* in2, double* out1, double* out2, const FftLines& ls, int n,

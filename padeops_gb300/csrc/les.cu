@@ -459,7 +459,7 @@ struct pade_les_s {
     double2 *tC1 = nullptr, *tE1 = nullptr;
     // second stream of the RHS and its scratch (the v / w chains and every other tau chain)
     cudaStream_t s2 = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     double2 *tC1b = nullptr, *tE1b = nullptr;
     double *rC1b = nullptr, *rE1b = nullptr;
     double2 *uhat_cur = nullptr, *vhat_cur = nullptr, *what_cur = nullptr;  // fields project_and_prep acts on
@@ -765,7 +765,8 @@ int sgs_tau_rhs(pade_les h, cudaStream_t s) {
 
 // RHS of one stage (addNonLinearTerm_Rot, addViscousTerm, getRHS_SGS; igrid.F90:1497-1571,
 // 1793-1951).  The u chain runs on s, the v and w chains on the second stream with their
-// own scratch, and the pointwise eddy viscosity beside them.
+// own scratch (the u and v products transformed in pairs, one per grid and stream), and the
+// pointwise eddy viscosity beside them.
 int populate_rhs(pade_les h, cudaStream_t s) {
     const long n = h->NC, nE = h->NE;
     const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC), gsE = grid_for(h->SE);
@@ -783,21 +784,24 @@ int populate_rhs(pade_les h, cudaStream_t s) {
     k_nl_e<<<gE, 256, 0, s>>>(dE, h->w, h->uE, h->vE, h->rE1, h->rE2, h->rE3, nE);
     KCHECK();
     CK(after(h, 1, s, s2));  // the products are ready
-    // v and w (second stream, scratch tC1b / tE1b)
-    CK(spectral_fft(h->spC, h->rC2, h->tC1b, s2));
-    CK(spectral_fft(h->spE, h->rE2, h->tE1b, s2));
-    CK(zop(h, OP_I_E2C, 1, h->tE1b, h->vrhs, s2));
-    k_rhs_finish<<<gs, 256, 0, s2>>>(h->vrhs, h->tC1b, h->vhat_cur, h->d2v, k1, k2, h->nxh, h->splane, r, visc, h->SC);
-    KCHECK();
+    // the edge-grid products of u and v transformed as a pair (second stream), then w there;
+    // the cell-grid pair on s; each stream then waits for the other's pair
+    CK(spectral_fft_two(h->spE, h->rE1, h->rE2, h->tE1, h->tE1b, s2));
+    if (cudaEventRecord(h->ev[4], s2) != cudaSuccess) return PS_ECUDA;  // the edge-grid pair is done
     CK(spectral_fft(h->spE, h->rE3, h->wrhs, s2));
     if (visc) {
         k_rhs_finish<<<gsE, 256, 0, s2>>>(h->wrhs, nullptr, h->what_cur, h->d2w, k1, k2, h->nxh, h->splane, r, 1,
                                            h->SE);
         KCHECK();
     }
+    CK(spectral_fft_two(h->spC, h->rC1, h->rC2, h->tC1, h->tC1b, s));
+    CK(after(h, 5, s, s2));
+    // v (second stream, scratch tC1b / tE1b)
+    CK(zop(h, OP_I_E2C, 1, h->tE1b, h->vrhs, s2));
+    k_rhs_finish<<<gs, 256, 0, s2>>>(h->vrhs, h->tC1b, h->vhat_cur, h->d2v, k1, k2, h->nxh, h->splane, r, visc, h->SC);
+    KCHECK();
     // u
-    CK(spectral_fft(h->spC, h->rC1, h->tC1, s));
-    CK(spectral_fft(h->spE, h->rE1, h->tE1, s));
+    if (cudaStreamWaitEvent(s, h->ev[4], 0) != cudaSuccess) return PS_ECUDA;
     CK(zop(h, OP_I_E2C, 1, h->tE1, h->urhs, s));
     k_rhs_finish<<<gs, 256, 0, s>>>(h->urhs, h->tC1, h->uhat_cur, h->d2u, k1, k2, h->nxh, h->splane, r, visc, h->SC);
     KCHECK();
@@ -913,7 +917,7 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
     if (rc == PS_OK) rc = pade_poisson_periodic_init(&h->po, h->spC, h->dx, h->dy, h->dz);
     if (rc == PS_OK) rc = pade_cd06stagg_init_periodic(&h->stagg, h->nz, h->dz);
     if (rc == PS_OK && cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking) != cudaSuccess) rc = PS_ECUDA;
-    for (int i = 0; i < 4 && rc == PS_OK; i++)
+    for (int i = 0; i < 6 && rc == PS_OK; i++)
         if (cudaEventCreateWithFlags(&h->ev[i], cudaEventDisableTiming) != cudaSuccess) rc = PS_ECUDA;
     if (rc == PS_OK) {
         std::vector<double> k3 = wavenums(h->nz, h->dz);

@@ -176,6 +176,22 @@ int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out
     return spectral_ifft(h, in, out_dx, 0, s, MUL_IK_A);  // transforms without that multiplier
 }
 
+int spectral_fft_two(pade_spectral h, const double* in1, const double* in2, void* out1, void* out2, cudaStream_t s) {
+    FftLines lx = fft_lines(1, h->nx, h->ny, h->nz, h->nx, h->nxh);
+    int rc = fft_r2c_pair(in1, in2, out1, out2, lx, h->nx, 1.0, s);
+    if (rc == PS_ENOTSUP) {
+        rc = spectral_fft(h, in1, out1, s);
+        if (rc != PS_OK) return rc;
+        return spectral_fft(h, in2, out2, s);
+    }
+    if (rc != PS_OK) return rc;
+    const FftExtra ex{};
+    FftLines ly = fft_lines(2, h->nxh, h->ny, h->nz, h->ny, h->ny);
+    rc = fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PLAIN, h->ny, -1, 1.0, 0, out1, out1, ly, ex, s);
+    if (rc != PS_OK) return rc;
+    return fft_launch(IN_COMPLEX, OUT_COMPLEX, FK_PLAIN, h->ny, -1, 1.0, 0, out2, out2, ly, ex, s);
+}
+
 int spectral_ifft_two(pade_spectral h, const void* in1, int mul1, const void* in2, int mul2, double* out1,
                       double* out2, void* w1, void* w2, cudaStream_t s) {
     FftLines ly = fft_lines(2, h->nxh, h->ny, h->nz, h->ny, h->ny);

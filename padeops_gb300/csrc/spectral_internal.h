@@ -90,6 +90,9 @@ int wall_projection(pade_poisson h, void* uhat, void* vhat, void* what, cudaStre
 int wall_pressure(pade_poisson h, cudaStream_t s);
 // out = ifft2(in) and out_dx = ifft2(i k1 in) from one y transform (oddball 0)
 int spectral_ifft_pair(pade_spectral h, const void* in, double* out, double* out_dx, cudaStream_t s);
+// out1 = fft2(in1), out2 = fft2(in2); the two x transforms in one launch where the paired
+// kernel applies
+int spectral_fft_two(pade_spectral h, const double* in1, const double* in2, void* out1, void* out2, cudaStream_t s);
 // out1 = ifft2(in1 [times i k: mul1]) and out2 = ifft2(in2 [mul2]) (oddball 0), the y
 // transforms into w1 and w2 (which may be in1 and in2: those are then overwritten), the two
 // x transforms in one launch where the paired kernel applies
