@@ -71,6 +71,9 @@ def test_init_sequence_with_disparate_magnitudes(oracle):
     g.init(n, n, n)
     g.set_fields(dev(u), dev(v), dev(w))
     _compare(g, ref, 1e-12)
+    g.timeAdvance(use_graph=False)  # the right-hand sides pair transforms of u and v too
+    ref.tvd_rk3()
+    _compare(g, ref, 1e-10)
 
 
 @pytest.mark.parametrize("kw", [dict(dynamic=True), dict(dynamic=False), dict(useSGS=False),
