@@ -186,7 +186,8 @@ def run_device(args, P, torch):
         for k in range(nops):
             per_launch[k] += evs[s][k][0].elapsed_time(evs[s][k][1])
     per_launch /= args.steps
-    return ms / args.steps, per_launch, clocks, plan, f_host
+    del ins
+    return ms / args.steps, per_launch, clocks, plan, f_host, outs
 
 
 def run_e2e(args, P, torch, f_host):
@@ -240,11 +241,20 @@ def cpu_baseline(args, f_host, steps=None):
     n = steps or 1
     t = time.perf_counter()
     for _ in range(n):
-        for w in work:
-            w()
+        results = [w() for w in work]
     dt = (time.perf_counter() - t) / n
     gpts = len(work) * N ** 3 / dt / 1e9
-    return gpts, O.threads(), dt
+    return gpts, O.threads(), dt, results
+
+
+def parity(plan, outs, oracle_out):
+    """Normwise relative difference max|gpu - oracle| / max|oracle| of each application of
+    the timed step (the outputs of its last step) against the oracle on the same field."""
+    per = {}
+    for (obj, opc, d, name), o, r in zip(plan, outs, oracle_out):
+        g = o.cpu().numpy().T
+        per[name] = float(np.abs(g - r).max() / np.abs(r).max())
+    return max(per.values()), per
 
 
 def _time(torch, fn, reps, stream=None):
@@ -327,6 +337,165 @@ def les_stats(stats, n):
             "eps_sgs": {"dynamic": d["eps"][1], "learned": lr["eps"][1]}}
 
 
+def config1_extra(P, torch):
+    """Config 1: CD06 periodic ddx / ddy / ddz (cd06%dd1..dd3) on the 64^3 field of 32 modes
+    with |k_i| <= 16 (seed 1): errors against the oracle and the analytic derivative (the
+    oracle's own error against it beside), CUDA-event time per call.  The 4 MB working set
+    sits in L2, so the throughput is reported, not graded against HBM."""
+    from oracle import oracle as O
+    from padeops_gb300.synthetic import random_modes
+
+    n = 64
+    f, grad = random_modes(n, 32, 16, 1, gradient=True)
+    dx = 2 * np.pi / n
+    c = P.cd06()
+    assert c.init(n, dx, True, 0, 0) == 0
+    fd = torch.from_numpy(np.ascontiguousarray(f.T)).cuda()
+    od = torch.empty_like(fd)
+    res = {}
+    for d, fn in ((1, c.dd1), (2, c.dd2), (3, c.dd3)):
+        fn(fd, od, n, n)
+        torch.cuda.synchronize()
+        got = od.cpu().numpy().T
+        ref = O.cd06(f, dx, periodic=True, dir=d)
+        ex = grad[d - 1]
+        sc = np.abs(ex).max()
+        ms = _time(torch, lambda fn=fn: fn(fd, od, n, n), 50)
+        t = time.perf_counter()
+        O.cd06(f, dx, periodic=True, dir=d)
+        ms_cpu = (time.perf_counter() - t) * 1e3
+        res[f"dd{d}"] = {"relerr_vs_oracle": float(np.abs(got - ref).max() / np.abs(ref).max()),
+                         "relerr_vs_analytic": float(np.abs(got - ex).max() / sc),
+                         "oracle_relerr_vs_analytic": float(np.abs(ref - ex).max() / sc),
+                         "ms": ms, "Gpts_s": n ** 3 / (ms * 1e-3) / 1e9, "oracle_ms": ms_cpu}
+    return {"per_direction": res, "grid": [n, n, n],
+            "field": "32 modes, integer |k_i| <= 16, amplitudes N(0,1)|k|^-5/6, random phases, seed 1",
+            "note": "relerr normwise (max|a-b|/max|b|); the analytic error is CD06's truncation error at "
+                    "k dx <= pi/2; 4 MB per field fits in L2 (throughput not roofline-graded)"}
+
+
+def spectrum_velocity(torch, shape, kp, seed, dev):
+    """Three physical fields with independent random phases and the spectrum
+    E(k) ~ k^4 exp(-2 (k/kp)^2) (non-solenoidal): u_i = Re ifftn(sqrt(E/(4 pi k^2)) e^{i theta}),
+    the real part being the Hermitian-symmetrised field; scaled to u_rms = 1."""
+    nx, ny, nz = shape
+    g = torch.Generator(device=dev).manual_seed(seed)
+    kx = torch.fft.fftfreq(nx, 1.0 / nx, device=dev, dtype=torch.float64)
+    ky = torch.fft.fftfreq(ny, 1.0 / ny, device=dev, dtype=torch.float64)
+    kz = torch.fft.fftfreq(nz, 1.0 / nz, device=dev, dtype=torch.float64)
+    # (z, y, x) tensor order = Fortran (x, y, z) memory order
+    kk = torch.sqrt(kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2)
+    amp = torch.sqrt(kk ** 2 * torch.exp(-2.0 * (kk / kp) ** 2) / (4 * np.pi))
+    del kk
+    out = []
+    for _ in range(3):
+        th = torch.rand((nz, ny, nx), generator=g, device=dev, dtype=torch.float64) * (2 * np.pi)
+        c = torch.polar(amp, th)
+        del th
+        out.append(torch.fft.ifftn(c).real.contiguous() * float(nx * ny * nz))
+        del c
+    rms = torch.sqrt(sum((x ** 2).mean() for x in out) / 3.0)
+    return [x / rms for x in out]
+
+
+def config3_fields(P, torch, shape, dev):
+    """Config 3's spectral velocity on a grid of `shape`: uhat, vhat (nx/2+1, ny, nz) and what
+    on the nz+1 edges, from the cell fields by spectral%fft and Pade6stagg%interpz_C2E
+    (tests/test_PressureProj_PeriodicCD06.F90:66-83), fixOddball false."""
+    nx, ny, nz = shape
+    sp = P.spectral()
+    sp.init(nx, ny, nz, 2 * np.pi / nx, 2 * np.pi / ny, fixOddball=False)
+    u, v, wc = spectrum_velocity(torch, shape, 8.0, 3, dev)
+    hs = (nz, ny, nx // 2 + 1)
+    U = torch.empty(hs, dtype=torch.complex128, device=dev)
+    V = torch.empty_like(U)
+    WC = torch.empty_like(U)
+    sp.fft(u, U)
+    sp.fft(v, V)
+    sp.fft(wc, WC)
+    del u, v, wc
+    st = P.cd06stagg()
+    assert st.init(nz, 2 * np.pi / nz) == 0
+    W = torch.empty((nz + 1, ny, nx // 2 + 1), dtype=torch.complex128, device=dev)
+    st.InterpZ_C2E(WC, W, nx // 2 + 1, ny)
+    del WC
+    torch.cuda.synchronize()
+    return sp, U, V, W
+
+
+def config3_extra(P, torch, dev):
+    """Config 3 (512^3 periodic, E(k) ~ k^4 exp(-2 (k/8)^2), non-solenoidal): max |div u| of
+    the CD06 divergence before and after the projection, the projection's relative residual
+    against the oracle (on a 512 x 512 x 64 slab of the same construction: the numpy oracle
+    cannot hold 512^3 within the bench's time), and the transform and transpose times."""
+    from oracle import spectral_oracle as SO
+    from padeops_gb300 import decomp_2d as D
+
+    res = {}
+    n = 512
+    d = 2 * np.pi / n
+    sp, U, V, W = config3_fields(P, torch, (n, n, n), dev)
+    po = P.padepoisson()
+    po.init(d, d, d, sp)
+    div = torch.empty((n, n, n), dtype=torch.float64, device=dev)
+    po.DivergenceCheck(U, V, W, div)
+    torch.cuda.synchronize()
+    div0 = float(div.abs().max())
+    U1, V1, W1 = U.clone(), V.clone(), W.clone()
+    po.PressureProjection(U1, V1, W1)
+    po.DivergenceCheck(U1, V1, W1, div)
+    torch.cuda.synchronize()
+    div1 = float(div.abs().max())
+    umax = max(float(x.abs().max()) for x in (U1, V1, W1))
+    ms_p = _time(torch, lambda: po.PressureProjection(U1, V1, W1), 3)
+    ms_d = _time(torch, lambda: po.DivergenceCheck(U1, V1, W1, div), 3)
+    phys = torch.empty((n, n, n), dtype=torch.float64, device=dev)
+    ms_i = _time(torch, lambda: sp.ifft(U1, phys), 3)
+    ms_f = _time(torch, lambda: sp.fft(phys, U1), 3)
+    T = torch.empty_like(U)
+    ms_t = _time(torch, lambda: (D.transpose_y_to_z(U, T), D.transpose_z_to_y(T, U)), 3)
+    cbytes = 16 * (n // 2 + 1) * n * n
+    res["grid_512"] = {
+        "max_abs_div_before": div0, "max_abs_div_after": div1,
+        "max_abs_div_after_rel": div1 / div0,
+        "max_abs_velocity_hat": umax,
+        "PressureProjection_ms": ms_p, "DivergenceCheck_ms": ms_d,
+        "spectral_fft_ms": ms_f, "spectral_ifft_ms": ms_i,
+        "fft_three_fields_ms": 3 * ms_f,
+        "transpose_y_z_round_trip_ms": ms_t,
+        "projection_compulsory_GBps": 6 * cbytes / (ms_p * 1e-3) / 1e9}
+    del sp, po, U, V, W, U1, V1, W1, div, phys, T
+    torch.cuda.empty_cache()
+    # residual against the oracle on a slab of the same construction
+    shape = (512, 512, 64)
+    nx, ny, nz = shape
+    sp, U, V, W = config3_fields(P, torch, shape, dev)
+    uh, vh, wh = (np.asfortranarray(x.cpu().numpy().T) for x in (U, V, W))
+    po = P.padepoisson()
+    po.init(2 * np.pi / nx, 2 * np.pi / ny, 2 * np.pi / nz, sp)
+    po.PressureProjection(U, V, W)
+    div = torch.empty((nz, ny, nx), dtype=torch.float64, device=dev)
+    po.DivergenceCheck(U, V, W, div)
+    torch.cuda.synchronize()
+    ref = SO.PeriodicPoisson(nx, ny, nz, 2 * np.pi / nx, 2 * np.pi / ny, 2 * np.pi / nz, fixOddball=False)
+    ru, rv, rw, _ = ref.projection(uh, vh, wh)
+    rdiv = ref.divergence(ru, rv, rw)
+
+    def rel(t, r):
+        return float(np.abs(t.cpu().numpy().T - r).max() / np.abs(r).max())
+
+    res["slab_512x512x64"] = {"relerr_uhat": rel(U, ru), "relerr_vhat": rel(V, rv), "relerr_what": rel(W, rw),
+                              "relerr_divergence_abs": float(np.abs(div.cpu().numpy().T - rdiv).max()
+                                                             / max(np.abs(ru).max(), 1e-300)),
+                              "max_abs_div_after": float(div.abs().max())}
+    res["note"] = ("fixOddball false, w interpolated to the edges with the periodic CD06-stagg interpolation as in "
+                   "tests/test_PressureProj_PeriodicCD06.F90; relerr normwise against the numpy/C oracle; one GPU "
+                   "keeps one (i,j,k) layout, so the transposes are layout-preserving copies, timed for reference")
+    del sp, po, U, V, W, div
+    torch.cuda.empty_cache()
+    return res
+
+
 def extras(args, P, torch, f_host):
     """Secondary measurements of the other hot-path rows (rank 0): the FP32 and native-FP64
     paths of the same step, the 512^3 periodic projection, and the 256^3 LES step with the
@@ -400,29 +569,15 @@ def extras(args, P, torch, f_host):
     except Exception as ex:  # pragma: no cover
         out["dense_error"] = repr(ex)
     try:
-        n = 512
-        d = 2 * np.pi / n
-        sp = P.spectral()
-        sp.init(n, n, n, d, d, fixOddball=False)
-        po = P.padepoisson()
-        po.init(d, d, d, sp)
+        out["config1_cd06_64"] = config1_extra(P, torch)
+    except Exception as ex:  # pragma: no cover
+        out["config1_error"] = repr(ex)
+    try:
+        out["projection_512"] = config3_extra(P, torch, dev)
+    except Exception as ex:  # pragma: no cover
+        out["projection_512_error"] = repr(ex)
+    try:
         g = torch.Generator(device=dev).manual_seed(3)
-        U = torch.randn((n, n, n // 2 + 1), dtype=torch.complex128, device=dev, generator=g)
-        V = torch.randn_like(U)
-        W = torch.randn((n + 1, n, n // 2 + 1), dtype=torch.complex128, device=dev, generator=g)
-        ms_p = _time(torch, lambda: po.PressureProjection(U, V, W), 3)
-        div = torch.empty((n, n, n), dtype=torch.float64, device=dev)
-        ms_d = _time(torch, lambda: po.DivergenceCheck(U, V, W, div), 3)
-        phys = torch.randn((n, n, n), dtype=torch.float64, device=dev, generator=g)
-        ms_f = _time(torch, lambda: sp.fft(phys, U), 3)
-        ms_i = _time(torch, lambda: sp.ifft(U, phys), 3)
-        cbytes = 16 * (n // 2 + 1) * n * n
-        out["projection_512"] = {"PressureProjection_ms": ms_p, "DivergenceCheck_ms": ms_d,
-                                 "spectral_fft_ms": ms_f, "spectral_ifft_ms": ms_i,
-                                 "projection_compulsory_GBps": 6 * cbytes / (ms_p * 1e-3) / 1e9,
-                                 "note": "double-float radix-2 FFTs on the FP32 pipes (default arithmetic)"}
-        del U, V, W, div, phys, sp, po
-        torch.cuda.empty_cache()
         # walls at z = 0 and Lz (PeriodicInZ false), with and without the Stokes pressure, 256^3
         n = 256
         d = 2 * np.pi / n
@@ -563,7 +718,7 @@ def main():
         if rank != 0:
             return
         f_host = make_field()
-        gpts, cores, dt = cpu_baseline(args, f_host, steps=max(1, min(args.steps, 3)))
+        gpts, cores, dt, _ = cpu_baseline(args, f_host, steps=max(1, min(args.steps, 3)))
         line = {"metric": metric, "value": gpts, "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
@@ -584,7 +739,7 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    ms_step, per_launch, clocks, plan, f_host = run_device(args, P, torch)
+    ms_step, per_launch, clocks, plan, f_host, outs = run_device(args, P, torch)
     if world > 1:
         from padeops_gb300.replicas import max_over_ranks
 
@@ -606,17 +761,25 @@ def main():
             "algorithmic_bytes_per_launch": npts * BYTES_PER_POINT,
             "per_launch_ms": {p[3]: round(float(v), 4) for p, v in zip(plan, per_launch)}}
     cb = None
+    par = None
     if rank == 0:
-        gpts, cores, dt = cpu_baseline(args, f_host, steps=1)
+        gpts, cores, dt, oracle_out = cpu_baseline(args, f_host, steps=1)
         cb = {"value": gpts, "unit": "Gpts/s", "cores": cores, "kind": "port",
               "sample": "one full 256^3 step (9 applications), oracle C port with OpenMP over lines"}
+        par = parity(plan, outs, oracle_out)
+        del oracle_out
+    del outs
+    torch.cuda.empty_cache()
     ext = extras(args, P, torch, f_host) if (rank == 0 and not args.no_extras) else None
     if rank == 0:
         line = {"metric": metric, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64 (double-float arithmetic)", "data": "synthetic",
                 "config": config, "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": len(plan) * args.steps}
+                "gpu_launches": len(plan) * args.steps,
+                "parity_relerr": par[0], "parity_relerr_per_op": par[1],
+                "parity_note": "outputs of the last timed step against the oracle on the same field, "
+                               "max|gpu - oracle| / max|oracle| per application"}
         if ext is not None:
             line["extras"] = ext
         print(json.dumps(line), flush=True)

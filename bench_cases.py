@@ -1,14 +1,16 @@
-"""Run one compact operator repeatedly on a device-resident field (profiling driver).
+"""Single-kernel benchmark cases: one operation applied repeatedly to a device-resident
+field (the driver of the Nsight Compute captures summarised under profiles/).
 
-    python -m padeops_gb300.profile_case --family cd10 --opcode 1 --dir 1 --n 256 \
-        --other 256 320 --repeat 3 --path df
-    python -m padeops_gb300.profile_case --family spectral --n 256 --repeat 3   # fft + ifft
-    python -m padeops_gb300.profile_case --family projection --n 256 --repeat 3
-    python -m padeops_gb300.profile_case --family les --n 128 --repeat 2        # TVD-RK3 steps
-    python -m padeops_gb300.profile_case --family les_learned --n 256 --repeat 1  # learned closure
+    python bench_cases.py --family cd10 --opcode 1 --dir 1 --n 256 --other 256 320 --repeat 3 --path df
+    python bench_cases.py --family dense --opcode 1 --dir 1 --n 256 --other 256 256 --repeat 3
+    python bench_cases.py --family spectral --n 256 --repeat 3      # fft + ifft
+    python bench_cases.py --family projection --n 256 --repeat 3
+    python bench_cases.py --family les --n 128 --repeat 2           # TVD-RK3 steps
+    python bench_cases.py --family les_learned --n 256 --repeat 1   # learned closure
 
-Used for Nsight Compute captures of a single kernel on a bounded case; prints the mean
-CUDA-event time per application and the implied HBM throughput at 16 B/point.
+Prints the mean CUDA-event time per application and the implied HBM throughput at
+16 B/point (8 B/point for the FP32 path).  Not part of the library: a measurement tool
+beside bench.py.
 """
 import argparse
 import os
@@ -20,7 +22,8 @@ import numpy as np
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--family", default="cd10",
-                    choices=["cd06", "cd10", "cf90", "gaussian", "spectral", "projection", "les", "les_learned"])
+                    choices=["cd06", "cd10", "cf90", "gaussian", "dense", "spectral", "projection", "les",
+                             "les_learned"])
     ap.add_argument("--opcode", type=int, default=1)
     ap.add_argument("--dir", type=int, default=1)
     ap.add_argument("--n", type=int, default=256)
@@ -32,7 +35,7 @@ def main(argv=None):
     a = ap.parse_args(argv)
     import torch
 
-    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
     import padeops_gb300 as P
     from padeops_gb300 import _lib as L
     from padeops_gb300 import build as B
@@ -40,6 +43,8 @@ def main(argv=None):
     B.build()
     if a.family in ("spectral", "projection", "les", "les_learned"):
         return spectral_case(a, torch, P)
+    if a.family == "dense":
+        return dense_case(a, torch, P, L)
     path = {"df": L.PATH_DF, "native": L.PATH_NATIVE, "fp32": L.PATH_FP32}[a.path]
     dt = torch.float32 if path == L.PATH_FP32 else torch.float64
     n = a.n
@@ -65,6 +70,29 @@ def main(argv=None):
     bpp = 2 * f.element_size()
     print(f"{a.family} op{a.opcode} dir{a.dir} n={n} lines={na}x{nb} path={a.path}: {ms:.4f} ms/app, "
           f"{total / ms / 1e6:.1f} Gpts/s, {total * bpp / ms / 1e6:.1f} GB/s")
+
+
+def dense_case(a, torch, P, L):
+    """pade_dense_apply of a periodic cd10 operator (opcode 1 or 2) along a.dir."""
+    import ctypes
+
+    n = a.n
+    o = P.cd10()
+    assert o.init(n, 2 * np.pi / n, True) == 0
+    na, nb = a.other
+    total = n * na * nb
+    g = torch.Generator(device="cuda").manual_seed(0)
+    f = torch.randn(total, device="cuda", dtype=torch.float64, generator=g)
+    out = torch.empty_like(f)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def run():
+        L.check(L.lib().pade_dense_apply(o.handle, a.opcode, a.dir, ctypes.c_void_p(f.data_ptr()),
+                                         ctypes.c_void_p(out.data_ptr()), na, nb, 0, 0, s), "dense_apply")
+
+    ms = _timed(torch, run, a.repeat)
+    print(f"dense cd10 op{a.opcode} dir{a.dir} n={n} lines={na}x{nb}: {ms:.4f} ms/app, "
+          f"{total / ms / 1e6:.1f} Gpts/s, {total * 16 / ms / 1e6:.1f} GB/s")
 
 
 def _timed(torch, fn, repeat):

@@ -5,7 +5,7 @@
  * type (cd06, cd10, cf90, gaussian, cd06stagg) becomes an opaque `pade_op` handle; each
  * type-bound procedure becomes one function with the same argument meaning.  A Fortran
  * shim keeps the reference's module/type names, stores the handle as type(c_ptr) and
- * calls these functions through ISO_C_BINDING.
+ * calls these functions through ISO_C_BINDING (the modules under fortran/).
  *
  * Conventions
  *  - Arrays are column-major (Fortran order, x fastest), FP64, as in the reference.
@@ -141,8 +141,10 @@ int pade_apply(pade_op op, int opcode, int dir, int is_complex, const void* f, v
  * device array of PADE_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the library
  * until exit; host buffers larger than half of it return PADE_ESCRATCH.  All calls share
  * the array (the flag is cleared per call), so calls whose GPU work overlaps race.  The
- * first call on a device resolves the array's address (make it before any stream
- * capture).  Device-pointer calls are asynchronous and do not report PADE_ERANGE. */
+ * first call on a device resolves the array's address; under CUDA's lazy module loading
+ * the driver may load the module and create the array then.  A call with na or nb = 0 does
+ * only that set-up: make it before the time loop and before any stream capture.
+ * Device-pointer calls are asynchronous and do not report PADE_ERANGE. */
 #define PADE_NOALLOC_SCRATCH_BYTES (32u << 20)
 int pade_apply_noalloc(pade_op op, int opcode, int dir, int is_complex, const void* f, void* out, int na, int nb,
                        int bc1, int bcn, void* stream);
@@ -194,6 +196,28 @@ int pade_spectral_fft(pade_spectral sp, const double* in, void* out, void* strea
 /* complex (nx/2+1,ny,nz) -> real (nx,ny,nz): backward c2c y, c2r x, times 1/(nx ny);
  * set_oddball zeroes the x-Nyquist modes first (fft_3d.F90:633-635).  `in` is not modified. */
 int pade_spectral_ifft(pade_spectral sp, const void* in, double* out, int set_oddball, void* stream);
+
+/* The fused spectral layer: the transforms above with spectral's pointwise multipliers and
+ * pairings folded into their passes (the inputs are not modified).
+ * ifft(mTimes_ik1_oop(in)) (d = 1) or ifft(mTimes_ik2_oop(in)) (d = 2)
+ * (spectral.F90:235-273 then 1413-1452): the x or y derivative of a spectral field. */
+int pade_spectral_ifft_ik(pade_spectral sp, const void* in, double* out, int d, void* stream);
+/* ifft(in) and ifft(mTimes_ik1_oop(in)): a field and its x derivative (igrid compute_duidxj,
+ * igrid.F90:2553-2684), one complex x transform for both when nx = 256 */
+int pade_spectral_ifft_and_ddx(pade_spectral sp, const void* in, double* out, double* out_dx, void* stream);
+/* fft(in1) and fft(in2) of two real fields, the x transforms of both in one launch when
+ * nx = 256 (each field keeps its own scaling, whatever their magnitudes) */
+int pade_spectral_fft_two(pade_spectral sp, const double* in1, const double* in2, void* out1, void* out2,
+                          void* stream);
+/* ifft of two spectral fields, each with an optional multiplier d1, d2 (0 none, 1 i k1,
+ * 2 i k2), the x transforms of both in one launch when nx = 256; the first call allocates
+ * a second workspace of the handle */
+int pade_spectral_ifft_two(pade_spectral sp, const void* in1, int d1, const void* in2, int d2, double* out1,
+                           double* out2, void* stream);
+/* ifft(TestFilter_oop(in)): the sharp x-y cutoff of InitTestFilter(filtfact)
+ * (spectral.F90:1333-1367, 736-753) fused into the inverse transform.  The reference
+ * refuses its test filter for periodic-z problems; this entry has no such restriction. */
+int pade_spectral_ifft_testfilter(pade_spectral sp, const void* in, double* out, double filtfact, void* stream);
 
 /* padepoisson with PeriodicInZ (src/incompressible/PadePoisson.F90:130-200, 76-128): the
  * periodic staggered-CD06 projection.  Keeps a pointer to `sp` (which must outlive it). */

@@ -122,6 +122,11 @@ def lib():
         "pade_spectral_get_wavenumbers": [vp, dp, dp],
         "pade_spectral_fft": [vp, vp, vp, vp],
         "pade_spectral_ifft": [vp, vp, vp, i, vp],
+        "pade_spectral_ifft_ik": [vp, vp, vp, i, vp],
+        "pade_spectral_ifft_and_ddx": [vp, vp, vp, vp, vp],
+        "pade_spectral_fft_two": [vp, vp, vp, vp, vp, vp],
+        "pade_spectral_ifft_two": [vp, vp, i, vp, i, vp, vp, vp],
+        "pade_spectral_ifft_testfilter": [vp, vp, vp, d, vp],
         "pade_poisson_periodic_init": [pop, vp, d, d, d],
         "pade_poisson_wall_init": [pop, vp, d, d, d, d, i],
         "pade_poisson_get_pressure": [vp, vp, vp, vp, vp, vp],

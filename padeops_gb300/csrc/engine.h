@@ -74,6 +74,8 @@ struct StencilParams {
     F2 ca1, ca2;      // circulant recurrence constants (forward and backward)
     const int* tidx;  // banded edge rows: tap rows and coefficients (nlo + nhi rows x tw)
     const F2* tc;
+    const double* tcd;  // the same coefficients in FP64 (the double-float path evaluates the edge
+                        // rows in FP64 from the FP64 input: their one-sided sums cancel)
     const F2* rc;     // banded: ns x 5 (g, a1, a2, b1, b2)
     const F2* fscan;
     const F2* bscan;

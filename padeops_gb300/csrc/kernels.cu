@@ -353,6 +353,7 @@ int DevicePlan::upload(const HostPlan& hp) {
         const bool own = cline_.M != ch_.M;  // separate chunk tables for the line kernel
         cline_.tidx = cdf_.tidx;
         cline_.tc = cdf_.tc;
+        cline_.tcd = (const double*)(base + o_tc);
         cline_.rc = cdf_.rc;
         cline_.fscan = own ? (const F2*)(lb + o_lk[0]) : cdf_.fscan;
         cline_.bscan = own ? (const F2*)(lb + o_lk[1]) : cdf_.bscan;

@@ -19,8 +19,15 @@
 //    host threads calling concurrently) race on the array and must be ordered by the
 //    caller.
 //  * The first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress while that device is current; make that first call before any
+//    cudaGetSymbolAddress while that device is current.  Under CUDA's lazy module loading
+//    that lookup is also where the driver loads this module and creates the array, so the
+//    first call may make the driver allocate.  A call with na or nb = 0 does that set-up
+//    and nothing else: make it (or any first call) before the time loop and before any
 //    stream capture begins.
+//  * Device-pointer calls return without waiting, so an infinity or NaN in their input
+//    (PADE_ERANGE for host-pointer calls) is not reported: the flag in the status slot is
+//    cleared by the next call.  Callers that need the check pass host buffers or test
+//    their fields themselves.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -111,6 +118,9 @@ extern "C" int pade_apply_noalloc(pade_op h, int opcode, int dir, int is_complex
     if (it == h->plans.end()) return PS_EINVAL;
     const DevicePlan& P = *it->second;
     const OpDef& d = P.host().def;
+    void* base = nullptr;
+    int rc = scratch_address(&base);  // per-device set-up (once), also for empty calls
+    if (rc != PS_OK) return rc;
     if (na == 0 || nb == 0) return PS_OK;  // empty arrays: nothing to do
     if (!f || !out) return PS_EINVAL;
     const int cplx = is_complex ? 1 : 0;
@@ -119,9 +129,6 @@ extern "C" int pade_apply_noalloc(pade_op h, int opcode, int dir, int is_complex
     const bool din = device_pointer(f), dout = device_pointer(out);
     if ((!din && in_bytes > kStageBytes) || (!dout && out_bytes > kStageBytes)) return PADE_ESCRATCH;
 
-    void* base = nullptr;
-    int rc = scratch_address(&base);
-    if (rc != PS_OK) return rc;
     unsigned char* b = static_cast<unsigned char*>(base);
     unsigned* status = reinterpret_cast<unsigned*>(b);
     void* stage_in = b + kStatusBytes;

@@ -372,6 +372,7 @@ int pade_spectral_destroy(pade_spectral h) {
     cudaFree(h->d_k1);
     cudaFree(h->d_k2);
     cudaFree(h->work);
+    cudaFree(h->work2);
     delete h;
     return PS_OK;
 }
@@ -391,6 +392,51 @@ int pade_spectral_fft(pade_spectral h, const double* in, void* out, void* stream
 int pade_spectral_ifft(pade_spectral h, const void* in, double* out, int set_oddball, void* stream) {
     if (!h || !device_ptr(in) || !device_ptr(out)) return PS_EINVAL;
     return spectral_ifft(h, in, out, set_oddball ? 1 : 0, static_cast<cudaStream_t>(stream));
+}
+
+// ---------------------------------------------------------------- fused spectral layer
+namespace {
+int mul_of(int d) { return d == 1 ? MUL_IK_A : d == 2 ? MUL_IK_P : MUL_NONE; }
+}  // namespace
+
+int pade_spectral_ifft_ik(pade_spectral h, const void* in, double* out, int d, void* stream) {
+    if (!h || (d != 1 && d != 2) || !device_ptr(in) || !device_ptr(out)) return PS_EINVAL;
+    return spectral_ifft(h, in, out, 0, static_cast<cudaStream_t>(stream), mul_of(d));
+}
+
+int pade_spectral_ifft_and_ddx(pade_spectral h, const void* in, double* out, double* out_dx, void* stream) {
+    if (!h || !device_ptr(in) || !device_ptr(out) || !device_ptr(out_dx)) return PS_EINVAL;
+    return spectral_ifft_pair(h, in, out, out_dx, static_cast<cudaStream_t>(stream));
+}
+
+int pade_spectral_fft_two(pade_spectral h, const double* in1, const double* in2, void* out1, void* out2,
+                          void* stream) {
+    if (!h || !device_ptr(in1) || !device_ptr(in2) || !device_ptr(out1) || !device_ptr(out2)) return PS_EINVAL;
+    return spectral_fft_two(h, in1, in2, out1, out2, static_cast<cudaStream_t>(stream));
+}
+
+int pade_spectral_ifft_two(pade_spectral h, const void* in1, int d1, const void* in2, int d2, double* out1,
+                           double* out2, void* stream) {
+    if (!h || d1 < 0 || d1 > 2 || d2 < 0 || d2 > 2) return PS_EINVAL;
+    if (!device_ptr(in1) || !device_ptr(in2) || !device_ptr(out1) || !device_ptr(out2)) return PS_EINVAL;
+    if (!h->work2) {
+        const size_t bytes = sizeof(double2) * (size_t)h->nxh * h->ny * h->nz;
+        if (cudaMalloc(&h->work2, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            h->work2 = nullptr;
+            return PS_ENOMEM;
+        }
+    }
+    return spectral_ifft_two(h, in1, mul_of(d1), in2, mul_of(d2), out1, out2, h->work, h->work2,
+                             static_cast<cudaStream_t>(stream));
+}
+
+int pade_spectral_ifft_testfilter(pade_spectral h, const void* in, double* out, double filtfact, void* stream) {
+    if (!h || !(filtfact > 0) || !device_ptr(in) || !device_ptr(out)) return PS_EINVAL;
+    const double pi = 3.141592653589793238462643383279502884;
+    const double cut1 = ((2.0 / 3.0) * pi / h->dx) / filtfact;
+    const double cut2 = ((2.0 / 3.0) * pi / h->dy) / filtfact;
+    return spectral_ifft_masked(h, in, out, cut1, cut2, static_cast<cudaStream_t>(stream));
 }
 
 // ---------------------------------------------------------------- padepoisson

@@ -14,6 +14,7 @@ struct pade_spectral_s {
     double* d_k1 = nullptr;
     double* d_k2 = nullptr;
     double2* work = nullptr;  // (nxh, ny, nz): the ifft's y-transform output
+    double2* work2 = nullptr; // (nxh, ny, nz): second y-transform output of pade_spectral_ifft_two (on first use)
 };
 
 struct pade_poisson_s {

@@ -269,16 +269,30 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
         }
     }
     // ---- banded: RHS of the edge rows (explicit one-sided closures) ----
+    // The double-float path sums them in FP64 from the FP64 input (re-read, in L1/L2 after
+    // the staging): a one-sided second-derivative row adds terms ~1/h^2 larger than its
+    // result, and the 48-bit split of the input would lose 5 bits of that cancellation.
     if constexpr (!CIRC) {
         for (int it = tid; it < nl * ne; it += nth) {
             const int ll = it / ne, e = it - ll * ne;
-            V acc = AR::zero();
+            if constexpr (AR::kScaled) {
+                const double* src = reinterpret_cast<const double*>(f) + base_in[ll];
+                double acc = 0.0;
 #pragma unroll 1
-            for (int k = 0; k < cp.tw; k++) {
-                const int idx = __ldg(cp.tidx + e * cp.tw + k);
-                acc = AR::add(acc, AR::mul(tile[main_pos(ll, idx)], AR::coef(cp.tc[e * cp.tw + k])));
+                for (int k = 0; k < cp.tw; k++) {
+                    const int idx = __ldg(cp.tidx + e * cp.tw + k);
+                    acc = __fma_rn(__ldg(cp.tcd + e * cp.tw + k), __ldg(src + (long)idx * ls.fp), acc);
+                }
+                edge[it] = df_from_double_shift(acc, lexp[ll] - 1023);
+            } else {
+                V acc = AR::zero();
+#pragma unroll 1
+                for (int k = 0; k < cp.tw; k++) {
+                    const int idx = __ldg(cp.tidx + e * cp.tw + k);
+                    acc = AR::add(acc, AR::mul(tile[main_pos(ll, idx)], AR::coef(cp.tc[e * cp.tw + k])));
+                }
+                edge[it] = AR::norm(acc);
             }
-            edge[it] = AR::norm(acc);
         }
         __syncthreads();
     }

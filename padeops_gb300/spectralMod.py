@@ -77,6 +77,43 @@ class spectral:
         po, _, _ = _dev(arr_out, "arr_out")
         L.check(L.lib().pade_spectral_ifft(self.handle, pi, po, int(bool(setOddball)), s), "spectral.ifft")
 
+    # ---- the fused spectral layer (pointwise multipliers folded into the transforms) ----
+    def ifft_ik(self, arr_in, arr_out, d):
+        """ifft(mTimes_ik1_oop(arr_in)) for d = 1, ifft(mTimes_ik2_oop(arr_in)) for d = 2."""
+        pi, _, s = _dev(arr_in, "arr_in")
+        po, _, _ = _dev(arr_out, "arr_out")
+        L.check(L.lib().pade_spectral_ifft_ik(self.handle, pi, po, int(d), s), "spectral.ifft_ik")
+
+    def ifft_and_ddx(self, arr_in, arr_out, arr_out_dx):
+        """ifft(arr_in) and ifft(mTimes_ik1_oop(arr_in))."""
+        pi, _, s = _dev(arr_in, "arr_in")
+        po, _, _ = _dev(arr_out, "arr_out")
+        pd, _, _ = _dev(arr_out_dx, "arr_out_dx")
+        L.check(L.lib().pade_spectral_ifft_and_ddx(self.handle, pi, po, pd, s), "spectral.ifft_and_ddx")
+
+    def fft_two(self, in1, in2, out1, out2):
+        """fft(in1) -> out1 and fft(in2) -> out2."""
+        p1, _, s = _dev(in1, "in1")
+        p2, _, _ = _dev(in2, "in2")
+        q1, _, _ = _dev(out1, "out1")
+        q2, _, _ = _dev(out2, "out2")
+        L.check(L.lib().pade_spectral_fft_two(self.handle, p1, p2, q1, q2, s), "spectral.fft_two")
+
+    def ifft_two(self, in1, d1, in2, d2, out1, out2):
+        """ifft of (i k_d1) in1 and (i k_d2) in2 (d = 0: no multiplier)."""
+        p1, _, s = _dev(in1, "in1")
+        p2, _, _ = _dev(in2, "in2")
+        q1, _, _ = _dev(out1, "out1")
+        q2, _, _ = _dev(out2, "out2")
+        L.check(L.lib().pade_spectral_ifft_two(self.handle, p1, int(d1), p2, int(d2), q1, q2, s), "spectral.ifft_two")
+
+    def ifft_testfilter(self, arr_in, arr_out, filtfact=2.0):
+        """ifft(TestFilter_oop(arr_in)) with the cutoff of InitTestFilter(filtfact)."""
+        pi, _, s = _dev(arr_in, "arr_in")
+        po, _, _ = _dev(arr_out, "arr_out")
+        L.check(L.lib().pade_spectral_ifft_testfilter(self.handle, pi, po, float(filtfact), s),
+                "spectral.ifft_testfilter")
+
     def destroy(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             L.lib().pade_spectral_destroy(self._h)

@@ -7,10 +7,11 @@ reference's fields.
 import numpy as np
 
 
-def random_modes(n, nmodes, kmax, seed, z_nonperiodic=False, profile=False):
+def random_modes(n, nmodes, kmax, seed, z_nonperiodic=False, profile=False, gradient=False):
     """Sum of nmodes Fourier modes with integer wavevectors |k_i| <= kmax, amplitudes
     N(0,1)*|k|^(-5/6) and random phases on [0, 2pi)^3 (z on [0, 1] when z_nonperiodic,
-    times tanh(4(z - 0.5)) when profile)."""
+    times tanh(4(z - 0.5)) when profile).  gradient (periodic, no profile) also returns
+    the analytic derivatives (df/dx, df/dy, df/dz)."""
     rng = np.random.default_rng(seed)
     nx, ny, nz = (n, n, n) if np.isscalar(n) else n
     x = np.arange(nx) * 2 * np.pi / nx
@@ -20,7 +21,10 @@ def random_modes(n, nmodes, kmax, seed, z_nonperiodic=False, profile=False):
         z = 2 * np.pi * zz
     else:
         z = np.arange(nz) * 2 * np.pi / nz
+    if gradient and (z_nonperiodic or profile):
+        raise ValueError("analytic gradients of the periodic field only")
     f = np.zeros((nx, ny, nz), order="F")
+    grad = [np.zeros((nx, ny, nz), order="F") for _ in range(3)] if gradient else None
     X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
     for _ in range(nmodes):
         k = np.zeros(3)
@@ -28,31 +32,40 @@ def random_modes(n, nmodes, kmax, seed, z_nonperiodic=False, profile=False):
             k = rng.integers(-kmax, kmax + 1, size=3)
         amp = rng.standard_normal() * np.linalg.norm(k) ** (-5.0 / 6.0)
         ph = rng.uniform(0, 2 * np.pi)
-        f += amp * np.cos(k[0] * X + k[1] * Y + k[2] * Z + ph)
+        arg = k[0] * X + k[1] * Y + k[2] * Z + ph
+        f += amp * np.cos(arg)
+        if gradient:
+            s = np.sin(arg)
+            for i in range(3):
+                grad[i] -= amp * k[i] * s
     if profile:
         f *= np.tanh(4 * (np.linspace(0.0, 1.0, nz) - 0.5))[None, None, :]
+    if gradient:
+        return np.asfortranarray(f), [np.asfortranarray(g) for g in grad]
     return np.asfortranarray(f)
 
 
 def hit_initial_field(n, seed=4, kp=4.0, urms=1.0):
     """Seeded solenoidal-spectrum field on [0, 2pi)^3: E(k) ~ k^4 exp(-2 (k/kp)^2), random
     phases, scaled to u_rms; w returned on nz+1 edge planes (plane nz+1 = plane 1).  The
-    projection inside init_fields makes it discretely divergence free."""
+    projection inside init_fields makes it discretely divergence free.  n is the points
+    per direction, or (nx, ny, nz) for a box of unequal resolutions."""
     rng = np.random.default_rng(seed)
-    k = np.fft.fftfreq(n, 1.0 / n)
-    KX, KY, KZ = np.meshgrid(k, k, k, indexing="ij")
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+    KX, KY, KZ = np.meshgrid(np.fft.fftfreq(nx, 1.0 / nx), np.fft.fftfreq(ny, 1.0 / ny),
+                             np.fft.fftfreq(nz, 1.0 / nz), indexing="ij")
     kk = np.sqrt(KX ** 2 + KY ** 2 + KZ ** 2)
     kk[0, 0, 0] = 1.0
     E = kk ** 4 * np.exp(-2.0 * (kk / kp) ** 2)
     amp = np.sqrt(E / (4 * np.pi * kk ** 2))
     amp[0, 0, 0] = 0.0
-    amp[np.abs(KX) >= n // 3] = 0.0
-    amp[np.abs(KY) >= n // 3] = 0.0
-    amp[np.abs(KZ) >= n // 3] = 0.0
+    amp[np.abs(KX) >= nx // 3] = 0.0
+    amp[np.abs(KY) >= ny // 3] = 0.0
+    amp[np.abs(KZ) >= nz // 3] = 0.0
     comps = []
     for _ in range(3):
-        ph = rng.uniform(0, 2 * np.pi, (n, n, n))
-        comps.append(np.real(np.fft.ifftn(amp * np.exp(1j * ph))) * n ** 3)
+        ph = rng.uniform(0, 2 * np.pi, (nx, ny, nz))
+        comps.append(np.real(np.fft.ifftn(amp * np.exp(1j * ph))) * (nx * ny * nz))
     u, v, w = comps
     s = urms / np.sqrt((u ** 2 + v ** 2 + w ** 2).mean() / 3.0)
     u, v, w = (np.asfortranarray(c * s) for c in (u, v, w))
