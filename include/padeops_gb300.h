@@ -122,6 +122,55 @@ int pade_cd06stagg_d2dz2_E2E_cmplx(pade_op op, const double* fE, double* d2fE, i
 int pade_cd06stagg_InterpZ_E2C_cmplx(pade_op op, const double* fE, double* IfC, int n1, int n2, void* stream);
 int pade_cd06stagg_InterpZ_C2E_cmplx(pade_op op, const double* fC, double* IfE, int n1, int n2, void* stream);
 
+/* ---- Pade6stagg: igrid's staggered z-operator facade (src/incompressible/PadeDerOps.F90) ----
+ * replaces Pade6stagg%init(gpC, sp_gpC, gpE, sp_gpE, dz, scheme, isPeriodic) (PadeDerOps.F90:
+ * 57-124) with nz = gpC%zsz(3); the x-y extents (n1, n2) of each array are given per call.
+ * scheme: 1 cd06 (the compact sixth-order operators), 0 fd02 (modified wavenumbers and the
+ * Poincare constant only: its operators return PADE_ENOTSUP), 2 fourierColl (PADE_ENOTSUP:
+ * it needs the z transforms of spectral); other values return the reference's GracefulExit
+ * codes 434 (periodic) / 323 (non-periodic).  Non-periodic objects hold the nine cd06stagg
+ * objects of PadeDerOps.F90:92-110 and select one per call by (bot, top), each -1 (odd),
+ * 0 (one-sided) or 1 (even), as PadeDerOps.F90:146-995; periodic objects ignore them. */
+typedef struct pade_pade6stagg_s* pade_pade6stagg;
+int pade_pade6stagg_init(pade_pade6stagg* p, int nz, double dz, int scheme, int isPeriodic);
+int pade_pade6stagg_destroy(pade_pade6stagg p);
+/* generic entry: op 0 ddz_C2E, 1 ddz_E2C, 2 interpz_C2E, 3 interpz_E2C, 4 d2dz2_C2C,
+ * 5 d2dz2_E2E on (n1, n2, nz) cell / (n1, n2, nz + 1) edge arrays, real or complex(rkind).
+ * The combinations the reference has no operator for (d2dz2 with a one-sided end, codes
+ * outside {-1, 0, 1}) give a zero output, as PadeDerOps.F90 sets output = 0. */
+int pade_pade6stagg_apply(pade_pade6stagg p, int op, int is_complex, const double* in, double* out, int n1, int n2,
+                          int bot, int top, void* stream);
+/* the named procedures of the type (PadeDerOps.F90:146-995), REAL and CMPLX overloads */
+int pade_pade6stagg_ddz_C2E(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                            void* stream);
+int pade_pade6stagg_ddz_E2C(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                            void* stream);
+int pade_pade6stagg_interpz_C2E(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                                void* stream);
+int pade_pade6stagg_interpz_E2C(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                                void* stream);
+int pade_pade6stagg_d2dz2_C2C(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                              void* stream);
+int pade_pade6stagg_d2dz2_E2E(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                              void* stream);
+int pade_pade6stagg_ddz_C2E_cmplx(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                                  void* stream);
+int pade_pade6stagg_ddz_E2C_cmplx(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot, int top,
+                                  void* stream);
+int pade_pade6stagg_interpz_C2E_cmplx(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot,
+                                      int top, void* stream);
+int pade_pade6stagg_interpz_E2C_cmplx(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot,
+                                      int top, void* stream);
+int pade_pade6stagg_d2dz2_C2C_cmplx(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot,
+                                    int top, void* stream);
+int pade_pade6stagg_d2dz2_E2E_cmplx(pade_pade6stagg p, const double* in, double* out, int n1, int n2, int bot,
+                                    int top, void* stream);
+/* getModifiedWavenumbers (PadeDerOps.F90:997-1016): kp of the object's scheme for the n
+ * wavenumbers k (cd06: getmodCD06stagg 1034-1053; fd02: getmodFD02stagg 1055-1074).  Host. */
+int pade_pade6stagg_getModifiedWavenumbers(pade_pade6stagg p, const double* k, double* kp, int n);
+/* getApproxPoincareConstant (PadeDerOps.F90:1018-1032).  Host. */
+int pade_pade6stagg_getApproxPoincareConstant(pade_pade6stagg p, double* c);
+
 /* ---- common ---- */
 /* replaces the destroy procedure of every type above */
 int pade_destroy(pade_op op);

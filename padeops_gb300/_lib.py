@@ -33,6 +33,8 @@ PATH_FP32 = 2
 
 FAMILY = {"cd06": 0, "cd10": 1, "cf90": 2, "gaussian": 3, "cd06stagg": 4}
 STAGG_OPS = ("ddz_E2C", "ddz_C2E", "ddz_C2C", "ddz_E2E", "d2dz2_C2C", "d2dz2_E2E", "InterpZ_E2C", "InterpZ_C2E")
+# Pade6stagg operations in pade_pade6stagg_apply's numbering
+PADE6_OPS = ("ddz_C2E", "ddz_E2C", "interpz_C2E", "interpz_E2C", "d2dz2_C2C", "d2dz2_E2E")
 
 _lib = None
 
@@ -114,6 +116,16 @@ def lib():
     for nm in STAGG_OPS:
         sig[f"pade_cd06stagg_{nm}"] = [vp, vp, vp, i, i, vp]
         sig[f"pade_cd06stagg_{nm}_cmplx"] = [vp, vp, vp, i, i, vp]
+    sig.update({
+        "pade_pade6stagg_init": [pop, i, d, i, i],
+        "pade_pade6stagg_destroy": [vp],
+        "pade_pade6stagg_apply": [vp, i, i, vp, vp, i, i, i, i, vp],
+        "pade_pade6stagg_getModifiedWavenumbers": [vp, dp, dp, i],
+        "pade_pade6stagg_getApproxPoincareConstant": [vp, dp],
+    })
+    for nm in PADE6_OPS:
+        sig[f"pade_pade6stagg_{nm}"] = [vp, vp, vp, i, i, i, i, vp]
+        sig[f"pade_pade6stagg_{nm}_cmplx"] = [vp, vp, vp, i, i, i, i, vp]
     sig.update({
         "pade_wavenumbers": [i, d, dp],
         "pade_modified_wavenumbers_cd06stagg": [dp, i, d, dp],

@@ -276,14 +276,17 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
         for (int it = tid; it < nl * ne; it += nth) {
             const int ll = it / ne, e = it - ll * ne;
             if constexpr (AR::kScaled) {
+                // inputs scaled by the line's power of two first (exact), so no product or
+                // partial sum of a tiny line falls into the subnormal range
                 const double* src = reinterpret_cast<const double*>(f) + base_in[ll];
+                const double sc = scalbn(1.0, 1023 - lexp[ll]);
                 double acc = 0.0;
 #pragma unroll 1
                 for (int k = 0; k < cp.tw; k++) {
                     const int idx = __ldg(cp.tidx + e * cp.tw + k);
-                    acc = __fma_rn(__ldg(cp.tcd + e * cp.tw + k), __ldg(src + (long)idx * ls.fp), acc);
+                    acc = __fma_rn(__ldg(cp.tcd + e * cp.tw + k), __dmul_rn(__ldg(src + (long)idx * ls.fp), sc), acc);
                 }
-                edge[it] = df_from_double_shift(acc, lexp[ll] - 1023);
+                edge[it] = df_from_double_shift(acc, 0);
             } else {
                 V acc = AR::zero();
 #pragma unroll 1
