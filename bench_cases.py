@@ -22,7 +22,7 @@ import numpy as np
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--family", default="cd10",
-                    choices=["cd06", "cd10", "cf90", "gaussian", "dense", "spectral", "projection", "les",
+                    choices=["cd06", "cd10", "cf90", "gaussian", "stagg", "dense", "spectral", "projection", "les",
                              "les_learned"])
     ap.add_argument("--opcode", type=int, default=1)
     ap.add_argument("--dir", type=int, default=1)
@@ -49,15 +49,19 @@ def main(argv=None):
     dt = torch.float32 if path == L.PATH_FP32 else torch.float64
     n = a.n
     h = (2 * np.pi / n) if a.periodic else 1.0 / (n - 1)
-    cls = {"cd06": P.cd06, "cd10": P.cd10, "cf90": P.cf90, "gaussian": P.gaussian}[a.family]
+    cls = {"cd06": P.cd06, "cd10": P.cd10, "cf90": P.cf90, "gaussian": P.gaussian, "stagg": P.cd06stagg}[a.family]
     o = cls()
-    rc = o.init(n, h, bool(a.periodic)) if a.family in ("cd06", "cd10") else o.init(n, bool(a.periodic))
+    if a.family == "stagg":  # periodic cd06stagg; --opcode is the pade_apply stagg operation (0..7)
+        rc = o.init(n, h) if a.periodic else o.init(n, h, True, True)
+    else:
+        rc = o.init(n, h, bool(a.periodic)) if a.family in ("cd06", "cd10") else o.init(n, bool(a.periodic))
     assert rc == 0, rc
     na, nb = a.other
+    n_in, n_out = o.lengths(a.opcode)
     total = n * na * nb
     g = torch.Generator(device="cuda").manual_seed(0)
-    f = torch.randn(total, device="cuda", dtype=dt, generator=g)
-    out = torch.empty_like(f)
+    f = torch.randn(n_in * na * nb, device="cuda", dtype=dt, generator=g)
+    out = torch.empty(n_out * na * nb, device="cuda", dtype=dt)
     o.apply(a.opcode, a.dir, f, out, na, nb, a.bc[0], a.bc[1], path)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -85,6 +85,8 @@ struct StencilParams {
     const F2* phb;
 };
 
+struct RegParams;  // reg_kernel.cuh
+
 class DevicePlan {
    public:
     DevicePlan() = default;
@@ -101,6 +103,9 @@ class DevicePlan {
     int chunk_M() const { return ch_.M; }
     int line_shape() const { return line_shape_; }
     const StencilParams& line_params() const { return cline_; }
+    // register-resident periodic kernel (chunks of 32 rows), when the line shape allows it
+    bool reg_ok() const { return reg_ok_; }
+    const RegParams& reg_params() const { return *creg_; }
 
    private:
     HostPlan hp_;
@@ -111,6 +116,8 @@ class DevicePlan {
     ChunkParams cdf_{}, cf32_{};
     int line_shape_ = SHAPE_NONE;
     StencilParams cline_{};
+    bool reg_ok_ = false;
+    RegParams* creg_ = nullptr;
 };
 
 // Fixed-stencil kernel for a plan with line_shape() != SHAPE_NONE: double-float (FP64 in
@@ -118,6 +125,10 @@ class DevicePlan {
 int launch_line(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                 cudaStream_t s);
 int launch_line_f32(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                    unsigned* status, cudaStream_t s);
+// Register-resident periodic line kernel (reg_kernel.cuh): double-float (fp32 = 0, FP64
+// in and out) or FP32.  PS_ENOTSUP for shapes it does not instantiate.
+int launch_line_reg(int shape, const RegParams& c, int fp32, const void* f, void* out, const LineSet& ls,
                     unsigned* status, cudaStream_t s);
 
 // Launch the operator on a set of lines.  f/out are device pointers to double (FP64 paths)

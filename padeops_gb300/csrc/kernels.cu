@@ -10,6 +10,7 @@
 #include <cstring>
 
 #include "chunk_kernel.cuh"
+#include "reg_kernel.cuh"
 
 namespace pade {
 
@@ -121,6 +122,7 @@ F2 split(double v) {
 
 DevicePlan::~DevicePlan() {
     if (dev_) cudaFree(dev_);
+    delete creg_;
 }
 
 int DevicePlan::upload(const HostPlan& hp) {
@@ -268,6 +270,46 @@ int DevicePlan::upload(const HostPlan& hp) {
             line_shape_ = shape;
         }
     }
+    // register-resident periodic kernel: whole chunks of 32 rows, a power-of-two number of
+    // lanes per line; coefficients and fundamental solutions travel in the kernel parameters
+    size_t o_rg[4] = {0, 0, 0, 0};
+    reg_ok_ = false;
+    delete creg_;
+    creg_ = nullptr;
+    if (line_shape_ != SHAPE_NONE && ch_.circ && d.ns % 32 == 0) {
+        const int pr = d.ns / 32;
+        ChunkPlanHost cr;
+        if (pr >= 1 && pr <= kMaxLanes && (pr & (pr - 1)) == 0 && build_chunk_plan(hp, 32, cr) == PS_OK && cr.ok &&
+            cr.P == pr && cr.Pp == pr) {
+            creg_ = new RegParams{};
+            RegParams& r = *creg_;
+            r.ns = cr.ns;
+            r.nout = cr.nout;
+            r.P = cr.P;
+            r.nsteps = cr.nsteps;
+            r.xdup = cline_.xdup;
+            r.c0 = cline_.c0;
+            for (int k = 0; k < kMaxPairs; k++) r.c[k] = cline_.c[k];
+            r.ca1 = cline_.ca1;
+            r.ca2 = cline_.ca2;
+            for (int j = 0; j < 32; j++) {
+                r.phf[j][0] = split(cr.phf[(size_t)j * 2]);
+                r.phf[j][1] = split(cr.phf[(size_t)j * 2 + 1]);
+                r.phb[j][0] = split(cr.phb[(size_t)j * 2]);
+                r.phb[j][1] = split(cr.phb[(size_t)j * 2 + 1]);
+            }
+            auto put = [&](const std::vector<double>& src) {
+                std::vector<F2> o(src.size());
+                for (size_t k = 0; k < src.size(); k++) o[k] = split(src[k]);
+                return A.put(o.data(), o.size() * sizeof(F2));
+            };
+            o_rg[0] = put(cr.fscan);
+            o_rg[1] = put(cr.bscan);
+            o_rg[2] = put(cr.fwrap);
+            o_rg[3] = put(cr.bwrap);
+            reg_ok_ = true;
+        }
+    }
     const cudaError_t me = cudaMalloc(&dev_, A.host.size());
     if (me != cudaSuccess) {
         dev_ = nullptr;
@@ -348,6 +390,12 @@ int DevicePlan::upload(const HostPlan& hp) {
         }
     }
 
+    if (reg_ok_) {
+        creg_->fscan = (const F2*)(base + o_rg[0]);
+        creg_->bscan = (const F2*)(base + o_rg[1]);
+        creg_->fwrap = (const F2*)(base + o_rg[2]);
+        creg_->bwrap = (const F2*)(base + o_rg[3]);
+    }
     if (line_shape_ != SHAPE_NONE) {
         unsigned char* lb = base;
         const bool own = cline_.M != ch_.M;  // separate chunk tables for the line kernel
@@ -368,6 +416,22 @@ int DevicePlan::upload(const HostPlan& hp) {
 // ------------------------------------------------------------------------------------
 // launch
 // ------------------------------------------------------------------------------------
+// Which periodic line kernel runs: the register-resident one for the FP32 path; for
+// double-float the register kernel only on tridiagonal operators along strided lines
+// (measured 5-7 % faster there), the shared-memory k_line otherwise (the unrolled
+// pentadiagonal double-float code stalls on instruction fetch; contiguous lines stage
+// faster through shared memory).  PADE_LINE_KERNEL (a tuning override): "reg" the register
+// kernel everywhere, "shared" k_line everywhere.
+static int line_kernel_choice() {
+    static const int v = [] {
+        const char* e = std::getenv("PADE_LINE_KERNEL");
+        if (e && std::strcmp(e, "reg") == 0) return 1;
+        if (e && std::strcmp(e, "shared") == 0) return 2;
+        return 0;
+    }();
+    return v;
+}
+
 int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const LineSet& ls, unsigned* status,
                  cudaStream_t s) {
     if (ls.nlines <= 0) return PS_OK;
@@ -390,11 +454,21 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
     if (!p.chunk_ok()) return PS_ENOTSUP;
     const auto& h = p.chunk_host();
     if (path == PATH_DF) {
+        const int sh = p.line_shape();
+        const bool tri = sh == SHAPE_T2A || sh == SHAPE_T2S || sh >= SHAPE_T2A_E2C;
+        if (p.reg_ok() && (line_kernel_choice() == 1 || (line_kernel_choice() == 0 && tri && ls.fp != 1))) {
+            const int rc = launch_line_reg(sh, p.reg_params(), 0, f, out, ls, status, s);
+            if (rc != PS_ENOTSUP) return rc;
+        }
         if (p.line_shape() != SHAPE_NONE) return launch_line(p.line_shape(), p.line_params(), f, out, ls, status, s);
         return h.M == 16 ? launch_chunk_m<ArDF, 16>(h, p.chunk_df(), f, out, ls, status, s)
                          : launch_chunk_m<ArDF, 32>(h, p.chunk_df(), f, out, ls, status, s);
     }
     if (path == PATH_FP32) {
+        if (p.reg_ok() && line_kernel_choice() != 2 && p.line_shape() < SHAPE_T2A_E2C) {
+            const int rc = launch_line_reg(p.line_shape(), p.reg_params(), 1, f, out, ls, status, s);
+            if (rc != PS_ENOTSUP) return rc;
+        }
         if (p.line_shape() != SHAPE_NONE && p.line_shape() < SHAPE_T2A_E2C)
             return launch_line_f32(p.line_shape(), p.line_params(), f, out, ls, status, s);
         return h.M == 16 ? launch_chunk_m<ArF32, 16>(h, p.chunk_f32(), f, out, ls, status, s)
