@@ -355,14 +355,21 @@ typedef struct {
     double dealiasFact;    /* 2/3 rule by default */
     int t_DivergenceCheck; /* check/fix the divergence every t steps (0: never) */
     int learnedSGS;        /* 1: nu from the learned closure (pade_les_set_mlp) */
-    int JudgeFreq;         /* learnedSGS: run the dynamic procedure every JudgeFreq steps as a
-                              reference for the closure (lambda1d of pade_les_info); 0: never */
+    int JudgeFreq;         /* learnedSGS: run the dynamic procedure every JudgeFreq steps as the
+                              judge of the closure (pade_les_judge_info): its lambda(z) is compared
+                              with the closure's plane-averaged Cs^2 Delta^2 and becomes the fallback
+                              coefficient; 0: never (the fallback is then (Csgs Delta)^2) */
     int learnedPlaneAvg;   /* learnedSGS: 1 = the closure's coefficient averaged over each x-y plane
                               (nu = <Cs^2 Delta^2>_xy |S|, the dynamic procedure's form);
                               0 = pointwise (nu = Cs^2(x) Delta^2 |S|) */
     int SGSModelID;        /* eddy-viscosity kernel (init_destroy_sgs_igrid.F90:158-165): 0 Smagorinsky,
                               1 sigma (sigma.F90), 2 AMD (AMD.F90); 1 and 2 with constant coefficients
                               (DynamicProcedureType 0) */
+    double JudgeTol;       /* learnedSGS with JudgeFreq > 0: when the judge's relative error
+                              max_z |<Cs^2 Delta^2>_xy - lambda| / max_z lambda exceeds JudgeTol (> 0),
+                              every point takes the fallback (the dynamic lambda(z)) until the next
+                              judge step; 0: never.  Points whose features leave the closure's
+                              training range (pade_mlp_set_range) always take the fallback. */
 } pade_les_params;
 #define PADE_LES_UHAT 0
 #define PADE_LES_VHAT 1
@@ -390,6 +397,11 @@ int pade_les_info(pade_les les, double* dt, double* tsim, int* step, double* lam
 /* simulated time and step counter, as a restart sets them (igrid.F90:2719-2765 reads tsim;
  * the step continues from the restart's time index) */
 int pade_les_set_time(pade_les les, double tsim, int step);
+/* the learned closure's judge (no counterpart in the reference): the relative error of the
+ * last judge step (-1 before any), the closure's plane-averaged Cs^2 Delta^2 there (nz
+ * entries, may be NULL) and the number of point evaluations given the fallback coefficient
+ * since init; synchronises */
+int pade_les_judge_info(pade_les les, double* err, double* lambda_closure, long long* n_fallback);
 /* device pointer of an internal field (PADE_LES_*), valid until pade_les_destroy */
 int pade_les_field(pade_les les, int which, void** ptr);
 /* attach the learned closure used when learnedSGS is set (the object must outlive the
@@ -408,6 +420,10 @@ int pade_les_set_mlp(pade_les les, pade_mlp mlp);
 int pade_mlp_create(pade_mlp* mlp); /* parameters zero until pade_mlp_set_params */
 int pade_mlp_destroy(pade_mlp mlp);
 int pade_mlp_set_params(pade_mlp mlp, const float* host_params); /* also resets the AdamW state */
+/* training range of the 10 features (host arrays lo, hi; both NULL: no range).  Inside the
+ * LES, points whose features leave it take the fallback coefficient (the dynamic procedure's
+ * last lambda(z), or the constant Smagorinsky one); pade_mlp_infer_nu itself ignores it. */
+int pade_mlp_set_range(pade_mlp mlp, const float* lo, const float* hi);
 int pade_mlp_get_params(pade_mlp mlp, float* host_params);
 /* mean squared error of Cs^2 against y over B samples X (device, B x 10 row-major) and its
  * gradient (host, PADE_MLP_NPARAM); synchronises */

@@ -51,11 +51,14 @@ class igrid:
     def init(self, nx, ny, nz, Lx=2 * np.pi, Ly=2 * np.pi, Lz=2 * np.pi, Re=1000.0, isInviscid=False, CFL=0.5,
              dt=-1.0, useSGS=True, DynamicProcedureType=1, Csgs=0.17, deltaRatio=2.0, DynProcFreq=1,
              dealiasFact=2.0 / 3.0, t_DivergenceCheck=10, learnedSGS=False, JudgeFreq=0, learnedPlaneAvg=False,
-             SGSModelID=0):
+             SGSModelID=0, JudgeTol=0.0):
         """igrid init (igrid.F90:330-660) for PeriodicInZ with SGSModelID 0 (Smagorinsky).
 
         learnedSGS replaces the model coefficient by the learned closure (set_mlp), with the
-        dynamic procedure run every JudgeFreq steps as its reference (0: never);
+        dynamic procedure run every JudgeFreq steps as its judge (0: never): judge_info gives
+        the closure's error against it, its lambda(z) is the fallback coefficient of points
+        outside the closure's training range, and while the error exceeds JudgeTol (> 0)
+        every point takes that fallback;
         learnedPlaneAvg applies the closure's coefficient averaged over each x-y plane, the
         form of the dynamic procedure's lambda(z), instead of pointwise.  SGSModelID: 0
         Smagorinsky, 1 sigma, 2 AMD (the last two with DynamicProcedureType 0)."""
@@ -65,7 +68,7 @@ class igrid:
         p = L.LesParams(nx, ny, nz, Lx, Ly, Lz, Re, int(bool(isInviscid)), CFL, dt, int(bool(useSGS)),
                         int(DynamicProcedureType == 1), Csgs, deltaRatio, DynProcFreq, dealiasFact,
                         t_DivergenceCheck, int(bool(learnedSGS)), int(JudgeFreq), int(bool(learnedPlaneAvg)),
-                        int(SGSModelID))
+                        int(SGSModelID), float(JudgeTol))
         self.Lx, self.Ly, self.Lz, self.Re = Lx, Ly, Lz, Re
         h = ctypes.c_void_p(None)
         L.check(L.lib().pade_les_init(ctypes.byref(h), ctypes.byref(p)), "igrid.init")
@@ -100,6 +103,18 @@ class igrid:
         L.check(L.lib().pade_les_info(self.handle, ctypes.byref(dt), ctypes.byref(ts), ctypes.byref(st),
                                       lam.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return {"dt": dt.value, "tsim": ts.value, "step": st.value, "lambda": lam}
+
+    def judge_info(self):
+        """The learned closure's judge: relative error of the last judge step (-1 before
+        any), the closure's plane-averaged Cs^2 Delta^2 there, and the number of point
+        evaluations that took the fallback coefficient."""
+        err = ctypes.c_double()
+        lam = np.empty(self.nz)
+        nfb = ctypes.c_longlong()
+        L.check(L.lib().pade_les_judge_info(self.handle, ctypes.byref(err),
+                                            lam.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(nfb)),
+                "igrid.judge_info")
+        return {"err": err.value, "lambda_closure": lam, "n_fallback": nfb.value}
 
     def field(self, name):
         """A copy of an internal field as a CUDA tensor (Fortran-shaped view reversed)."""

@@ -48,7 +48,7 @@ class LesParams(ctypes.Structure):
                 ("Csgs", ctypes.c_double), ("deltaRatio", ctypes.c_double), ("DynProcFreq", ctypes.c_int),
                 ("dealiasFact", ctypes.c_double), ("t_DivergenceCheck", ctypes.c_int),
                 ("learnedSGS", ctypes.c_int), ("JudgeFreq", ctypes.c_int), ("learnedPlaneAvg", ctypes.c_int),
-                ("SGSModelID", ctypes.c_int)]
+                ("SGSModelID", ctypes.c_int), ("JudgeTol", ctypes.c_double)]
 
 
 MLP_NPARAM = 4929
@@ -165,6 +165,8 @@ def lib():
         "pade_les_info": [vp, dp, dp, pi, dp],
         "pade_les_set_time": [vp, d, i],
         "pade_les_field": [vp, i, pop],
+        "pade_les_judge_info": [vp, dp, dp, ctypes.POINTER(ctypes.c_longlong)],
+        "pade_mlp_set_range": [vp, fp, fp],
         "pade_les_set_mlp": [vp, vp],
         "pade_mlp_create": [pop],
         "pade_mlp_destroy": [vp],

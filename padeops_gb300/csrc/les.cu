@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "../../include/padeops_gb300.h"
+#include "dfmath.cuh"
 #include "fft.h"
 #include "operators.h"
 #include "spectral_internal.h"
@@ -57,33 +58,48 @@ __device__ __forceinline__ double sij(const double* const* d, int idx, long e) {
     }
 }
 
-// sqrt(2 Sij Sij) in the reference's summation order (smagorinsky.F90:39-67)
-__device__ __forceinline__ double smag(double s1, double s2, double s3, double s4, double s5, double s6) {
-    double s = mul(s1, s1);
-    s = add(s, 2.0 * mul(s2, s2));
-    s = add(s, 2.0 * mul(s3, s3));
-    s = add(s, mul(s4, s4));
-    s = add(s, 2.0 * mul(s5, s5));
-    s = add(s, mul(s6, s6));
-    return sqrt(2.0 * s);
-}
-
 struct Ptr9 {
     const double* p[9];
 };
 
-// smag() of the gradients' Sij: 2 (0.5 (a + b))^2 is 0.5 (a + b)^2 exactly (power-of-two
-// scalings), three FP64 instructions instead of four for each off-diagonal term
-__device__ __forceinline__ double smag_grads(const double* const* d, long e) {
-    const double g0 = d[0][e], g4 = d[4][e], g8 = d[8][e];
-    const double a = add(d[1][e], d[3][e]), b = add(d[2][e], d[6][e]), c = add(d[5][e], d[7][e]);
-    double s = mul(g0, g0);
-    s = add(s, 0.5 * mul(a, a));
-    s = add(s, 0.5 * mul(b, b));
-    s = add(s, mul(g4, g4));
-    s = add(s, 0.5 * mul(c, c));
-    s = add(s, mul(g8, g8));
-    return sqrt(2.0 * s);
+// ---- double-float forms of the pointwise kernels whose FP64 work exceeds their HBM traffic
+// (|S|, the Germano products, the RK and RHS updates).  GB300 issues FP64 at about 2 lanes
+// per SM cycle, so these ran at the FP64 rate; here each FP64 input is split into a df value
+// with integer instructions (48 significant bits; magnitudes below 2^-74 count as zero, far
+// below any field of the step), the arithmetic runs on the FP32 pipes and each result is
+// rounded once to FP64 (one FP64 add).  The results agree with the FP64 operation order to
+// ~1e-14 relative.
+__device__ __forceinline__ dfv dsp(double x) {
+    unsigned b = 0;
+    return df_from_double(x, b);
+}
+__device__ __forceinline__ double dfo(dfv a) { return df_to_double(df_norm(a)); }
+__device__ __forceinline__ dfv dmul(dfv a, dfv b) { return df_norm(df_mul(a, b)); }
+__device__ __forceinline__ dfv dscale(dfv a, float p2) { return dfv{a.h * p2, a.l * p2}; }  // p2 a power of two
+// an FP64 constant as df (its leading 48 bits)
+__device__ __forceinline__ dfv dconst(double c) { return dsp(c); }
+
+// sqrt of a non-negative df value: the FP32 root refined by one Newton (Heron) step with an
+// exact residual (TwoProduct by FMA): relative error ~2^-47
+__device__ __forceinline__ dfv df_sqrt(dfv x) {
+    if (!(x.h > 0.0f)) return df_zero();
+    const float r = __fsqrt_rn(x.h);
+    const float p = __fmul_rn(r, r);
+    const float e = __fmaf_rn(r, r, -p);
+    const float d = __fadd_rn(__fsub_rn(__fsub_rn(x.h, p), e), x.l);
+    const float c = __fdiv_rn(d, __fadd_rn(r, r));
+    return df_norm(dfv{r, c});
+}
+
+// sqrt(2 Sij Sij) of six Sij values (df), smagorinsky.F90:39-67
+__device__ __forceinline__ dfv df_smag(dfv s1, dfv s2, dfv s3, dfv s4, dfv s5, dfv s6) {
+    dfv s = df_mul(s1, s1);
+    s = df_add(s, dscale(df_mul(s2, s2), 2.0f));
+    s = df_add(s, dscale(df_mul(s3, s3), 2.0f));
+    s = df_add(s, df_mul(s4, s4));
+    s = df_add(s, dscale(df_mul(s5, s5), 2.0f));
+    s = df_add(s, df_mul(s6, s6));
+    return df_sqrt(dscale(df_norm(s), 2.0f));
 }
 
 // ---- addNonLinearTerm_Rot products (igrid.F90:1530-1557)
@@ -107,33 +123,50 @@ __global__ void k_nl_e(Ptr9 dE, const double* __restrict__ w, const double* __re
     }
 }
 
-// rhs = rhs + f1  [+ (1/Re)(-kabs_sq fhat + d2)]  (igrid.F90:1537-1538, 1924-1930)
+// rhs = rhs + f1  [+ (1/Re)(-kabs_sq fhat + d2)]  (igrid.F90:1537-1538, 1924-1930), double-float
 __global__ void k_rhs_finish(double2* __restrict__ rhs, const double2* __restrict__ f1,
                              const double2* __restrict__ fhat, const double2* __restrict__ d2,
                              const double* __restrict__ k1, const double* __restrict__ k2, long nxh, long nxy,
                              double oneByRe, int viscous, long n) {
+    const dfv re = dconst(oneByRe);
     GRID_STRIDE(e, n) {
-        double2 r = rhs[e];
+        const double2 r0 = rhs[e];
+        dfv rx = dsp(r0.x), ry = dsp(r0.y);
         if (f1) {
             const double2 a = f1[e];
-            r = make_double2(add(r.x, a.x), add(r.y, a.y));
+            rx = df_add(rx, dsp(a.x));
+            ry = df_add(ry, dsp(a.y));
         }
         if (viscous) {
             const long q = e % nxy;
-            const double ka = k1[q % nxh], kb = k2[q / nxh];
-            const double ks = add(mul(ka, ka), mul(kb, kb));
+            const dfv ka = dsp(k1[q % nxh]), kb = dsp(k2[q / nxh]);
+            const dfv ks = df_norm(df_add(df_mul(ka, ka), df_mul(kb, kb)));
             const double2 fh = fhat[e], dd = d2[e];
-            const double tx = add(mul(-ks, fh.x), dd.x), ty = add(mul(-ks, fh.y), dd.y);
-            r = make_double2(add(r.x, mul(oneByRe, tx)), add(r.y, mul(oneByRe, ty)));
+            const dfv tx = df_norm(df_sub(dsp(dd.x), df_mul(ks, dsp(fh.x))));
+            const dfv ty = df_norm(df_sub(dsp(dd.y), df_mul(ks, dsp(fh.y))));
+            rx = df_add(df_norm(rx), df_mul(re, tx));
+            ry = df_add(df_norm(ry), df_mul(re, ty));
         }
-        rhs[e] = r;
+        rhs[e] = make_double2(dfo(rx), dfo(ry));
     }
 }
 
-// |S| at cell centres (get_smagorinsky_kernel); optional copy for the dynamic procedure
+// |S| at cell centres (get_smagorinsky_kernel) in double-float; optional copy for the
+// dynamic procedure
 __global__ void k_nu_kernel(Ptr9 dC, double* __restrict__ nu, double* __restrict__ dsgs, long n) {
     GRID_STRIDE(e, n) {
-        const double v = smag_grads(dC.p, e);
+        const dfv g0 = dsp(dC.p[0][e]), g4 = dsp(dC.p[4][e]), g8 = dsp(dC.p[8][e]);
+        // Sij off-diagonal = 0.5 (a + b): 2 Sij^2 = 0.5 (a + b)^2
+        const dfv a = df_add(dsp(dC.p[1][e]), dsp(dC.p[3][e]));
+        const dfv b = df_add(dsp(dC.p[2][e]), dsp(dC.p[6][e]));
+        const dfv c = df_add(dsp(dC.p[5][e]), dsp(dC.p[7][e]));
+        dfv s = df_mul(g0, g0);
+        s = df_add(s, dscale(df_mul(a, a), 0.5f));
+        s = df_add(s, dscale(df_mul(b, b), 0.5f));
+        s = df_add(s, df_mul(g4, g4));
+        s = df_add(s, dscale(df_mul(c, c), 0.5f));
+        s = df_add(s, df_mul(g8, g8));
+        const double v = dfo(df_sqrt(dscale(df_norm(s), 2.0f)));
         nu[e] = v;
         if (dsgs) dsgs[e] = v;
     }
@@ -213,7 +246,9 @@ __global__ void k_amd_kernel(Ptr9 d, double cx, double cy, double cz, double* __
 // |S| of six arrays
 __global__ void k_smag6(const double* s0, const double* s1, const double* s2, const double* s3, const double* s4,
                         const double* s5, double* __restrict__ out, long n) {
-    GRID_STRIDE(e, n) { out[e] = smag(s0[e], s1[e], s2[e], s3[e], s4[e], s5[e]); }
+    GRID_STRIDE(e, n) {
+        out[e] = dfo(df_smag(dsp(s0[e]), dsp(s1[e]), dsp(s2[e]), dsp(s3[e]), dsp(s4[e]), dsp(s5[e])));
+    }
 }
 
 // out = [scale *] Sij(idx)
@@ -244,25 +279,24 @@ struct Ptr6 {
     const double* p[6];
 };
 
-// numerator / denominator of the Germano identity in the reference's order (139-154)
+// numerator / denominator of the Germano identity (standardDynamicProcedure.F90:139-154) in
+// double-float: Lij Mij and Mij Mij with the off-diagonal products (1, 2, 4) counted twice
 __global__ void k_num_den(Ptr6 L, Ptr6 M, double* __restrict__ num, double* __restrict__ den, long n) {
     GRID_STRIDE(e, n) {
-        // the off-diagonal products (1, 2, 4) enter twice; each is formed once
-        double lm[6], mm[6];
+        dfv a = df_zero(), b = df_zero();
 #pragma unroll
         for (int i = 0; i < 6; i++) {
-            const double m = M.p[i][e];
-            lm[i] = mul(L.p[i][e], m);
-            mm[i] = mul(m, m);
+            const dfv m = dsp(M.p[i][e]);
+            dfv lm = df_mul(dsp(L.p[i][e]), m), mm = df_mul(m, m);
+            if (i == 1 || i == 2 || i == 4) {
+                lm = dscale(lm, 2.0f);
+                mm = dscale(mm, 2.0f);
+            }
+            a = df_add(a, lm);
+            b = df_add(b, mm);
         }
-        double a = lm[0];
-        for (int i = 1; i < 6; i++) a = add(a, lm[i]);
-        a = add(add(add(a, lm[1]), lm[2]), lm[4]);
-        double b = mm[0];
-        for (int i = 1; i < 6; i++) b = add(b, mm[i]);
-        b = add(add(add(b, mm[1]), mm[2]), mm[4]);
-        num[e] = a;
-        den[e] = 2.0 * b;
+        num[e] = dfo(a);
+        den[e] = dfo(dscale(df_norm(b), 2.0f));
     }
 }
 
@@ -312,6 +346,22 @@ __global__ void k_lambda(const double* __restrict__ part, int chunks, double mea
     }
     const double nm = fmax(mul(x, meanfact), 0.0);
     lambda[k] = nm / add(mul(y, meanfact), 1e-18);
+}
+
+// the learned closure's judge: relative error of the closure's plane-averaged coefficient
+// lamL against the dynamic procedure's lambda, and the switch that sends every point to the
+// fallback while it exceeds tol (> 0)
+__global__ void k_judge(const double* __restrict__ lambda, const double* __restrict__ lamL, int nz, double tol,
+                        double* __restrict__ err, int* __restrict__ all) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double dm = 0.0, lm = 0.0;
+    for (int k = 0; k < nz; k++) {
+        dm = fmax(dm, fabs(lamL[k] - lambda[k]));
+        lm = fmax(lm, fabs(lambda[k]));
+    }
+    const double e = lm > 0.0 ? dm / lm : (dm > 0.0 ? INFINITY : 0.0);
+    *err = e;
+    *all = (tol > 0.0 && e > tol) ? 1 : 0;
 }
 
 // nu *= lambda(z) (dynamic) or cmodel_global
@@ -371,24 +421,25 @@ __global__ void k_csub2(double2* __restrict__ y, const double2* __restrict__ x, 
     }
 }
 
-// TVD-RK3 stage updates (igrid.F90:1128-1164); dt read from device memory
+// TVD-RK3 stage updates (igrid.F90:1128-1164), double-float; dt read from device memory
 __global__ void k_rk(int stage, double2* __restrict__ u0, double2* __restrict__ u1, const double2* __restrict__ r,
                      const double* __restrict__ dtp, long n) {
     const double dt = *dtp;
+    // stage weights (1, 1), (3/4, 1/4), (1/3, 2/3) and the dt factor, in double-float
+    const dfv c0 = dconst(stage == 2 ? 3.0 / 4.0 : 1.0 / 3.0), c1 = dconst(stage == 2 ? 1.0 / 4.0 : 2.0 / 3.0);
+    const dfv c2 = dmul(dconst(stage == 1 ? 1.0 : (stage == 2 ? 1.0 / 4.0 : 2.0 / 3.0)), dsp(dt));
     GRID_STRIDE(e, n) {
         const double2 a = u0[e], rr = r[e];
+        const dfv ax = dsp(a.x), ay = dsp(a.y);
         if (stage == 1) {
-            u1[e] = make_double2(add(a.x, mul(dt, rr.x)), add(a.y, mul(dt, rr.y)));
-        } else if (stage == 2) {
-            const double2 b = u1[e];
-            const double c0 = 3.0 / 4.0, c1 = 1.0 / 4.0, c2 = mul(1.0 / 4.0, dt);
-            u1[e] = make_double2(add(add(mul(c0, a.x), mul(c1, b.x)), mul(c2, rr.x)),
-                                 add(add(mul(c0, a.y), mul(c1, b.y)), mul(c2, rr.y)));
+            u1[e] = make_double2(dfo(df_add(ax, df_mul(c2, dsp(rr.x)))), dfo(df_add(ay, df_mul(c2, dsp(rr.y)))));
         } else {
             const double2 b = u1[e];
-            const double c0 = 1.0 / 3.0, c1 = 2.0 / 3.0, c2 = mul(2.0 / 3.0, dt);
-            u0[e] = make_double2(add(add(mul(c0, a.x), mul(c1, b.x)), mul(c2, rr.x)),
-                                 add(add(mul(c0, a.y), mul(c1, b.y)), mul(c2, rr.y)));
+            const dfv tx = df_add(df_norm(df_add(df_mul(c0, ax), df_mul(c1, dsp(b.x)))), df_mul(c2, dsp(rr.x)));
+            const dfv ty = df_add(df_norm(df_add(df_mul(c0, ay), df_mul(c1, dsp(b.y)))), df_mul(c2, dsp(rr.y)));
+            const double2 o = make_double2(dfo(tx), dfo(ty));
+            if (stage == 2) u1[e] = o;
+            else u0[e] = o;
         }
     }
 }
@@ -481,6 +532,10 @@ struct pade_les_s {
     cudaStream_t gstream = nullptr;
     pade_mlp mlp = nullptr;
     double deltaLES = 0;
+    // learned closure: fallback switch, fallback count, judge error
+    int* fball = nullptr;
+    unsigned long long* fbcount = nullptr;
+    double* judge_err = nullptr;
 };
 
 namespace {
@@ -629,6 +684,10 @@ int dynamic_procedure(pade_les h, cudaStream_t s) {
 }
 
 // b waits for the work enqueued so far on a (event slot e)
+// the learned closure's fallback: the last judged lambda(z) (initially (Csgs Delta)^2), every
+// point while the judge's switch is on
+MlpFallback fallback(pade_les h) { return MlpFallback{h->lambda, h->plane, h->fball, h->fbcount}; }
+
 int after(pade_les h, int e, cudaStream_t a, cudaStream_t b) {
     if (cudaEventRecord(h->ev[e], a) != cudaSuccess) return PS_ECUDA;
     return cudaStreamWaitEvent(b, h->ev[e], 0) == cudaSuccess ? PS_OK : PS_ECUDA;
@@ -647,7 +706,7 @@ int sgs_nu_pointwise(pade_les h, cudaStream_t s) {
         if (!h->mlp) return PS_EINVAL;
         const double* grads[9];
         for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
-        return pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, s);
+        return mlp_infer_nu_fb(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, nullptr, fallback(h), s);
     }
     const bool dyn = h->prm.dynamic != 0;
     if (h->prm.SGSModelID == 1) {
@@ -657,6 +716,20 @@ int sgs_nu_pointwise(pade_les h, cudaStream_t s) {
     } else {
         k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, (dyn && h->newTimeStep) ? h->Dsgs : nullptr, n);
     }
+    KCHECK();
+    return PS_OK;
+}
+
+// the closure's plane-averaged Cs^2 Delta^2 into lamL from Cs^2 (FP32) in cs2
+int closure_plane_average(pade_les h, const float* cs2, cudaStream_t s) {
+    const long n = h->NC;
+    const unsigned g = grid_for(n);
+    k_cs2_delta2<<<g, 256, 0, s>>>(cs2, h->deltaLES * h->deltaLES, h->rC2, n);
+    KCHECK();
+    dim3 grid(kPlaneChunks, h->nz);
+    k_plane_sums<<<grid, 256, 0, s>>>(h->rC2, nullptr, h->plane, h->part);
+    KCHECK();
+    k_lambda<<<(h->nz + 127) / 128, 128, 0, s>>>(h->part, kPlaneChunks, h->meanfact, h->nz, h->lamL);
     KCHECK();
     return PS_OK;
 }
@@ -671,26 +744,27 @@ int sgs_nu_rest(pade_les h, cudaStream_t s) {
     const bool dyn = h->prm.dynamic != 0 && !learned;
     if (learned) {
         if (!h->mlp) return PS_EINVAL;
-        // the dynamic procedure as a periodic reference for the closure (lambda1d)
+        const double* grads[9];
+        for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
+        float* cs2 = reinterpret_cast<float*>(h->rC1);
+        // the judge: the dynamic procedure's lambda(z) (then the fallback coefficient) against
+        // the closure's plane average on the same fields (standardDynamicProcedure.F90:74-244)
         if (h->newTimeStep && h->prm.JudgeFreq > 0 && h->mstep % h->prm.JudgeFreq == 0) {
             k_nu_kernel<<<g, 256, 0, s>>>(dC, h->rC2, h->Dsgs, n);
             KCHECK();
             CK(dynamic_procedure(h, s));
+            MlpFallback fb = fallback(h);
+            fb.count = nullptr;  // the judge's own evaluation is not counted
+            CK(mlp_infer_nu_fb(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->rC2, cs2, fb, s));
+            CK(closure_plane_average(h, cs2, s));
+            k_judge<<<1, 32, 0, s>>>(h->lambda, h->lamL, h->nz, h->prm.JudgeTol, h->judge_err, h->fball);
+            KCHECK();
         }
         if (h->prm.learnedPlaneAvg) {
             // nu = <Cs^2 Delta^2>_xy |S|: the closure's coefficient through the dynamic
             // procedure's plane average (Cs^2 as FP32 in the rC1 scratch)
-            const double* grads[9];
-            for (int i = 0; i < 9; i++) grads[i] = h->dC[i];
-            float* cs2 = reinterpret_cast<float*>(h->rC1);
-            CK(pade_mlp_infer_nu(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, cs2, s));
-            k_cs2_delta2<<<g, 256, 0, s>>>(cs2, h->deltaLES * h->deltaLES, h->rC2, n);
-            KCHECK();
-            dim3 grid(kPlaneChunks, h->nz);
-            k_plane_sums<<<grid, 256, 0, s>>>(h->rC2, nullptr, h->plane, h->part);
-            KCHECK();
-            k_lambda<<<(h->nz + 127) / 128, 128, 0, s>>>(h->part, kPlaneChunks, h->meanfact, h->nz, h->lamL);
-            KCHECK();
+            CK(mlp_infer_nu_fb(h->mlp, grads, n, h->deltaLES, 1.0 / h->prm.Re, h->nuC, cs2, fallback(h), s));
+            CK(closure_plane_average(h, cs2, s));
             k_nu_kernel<<<g, 256, 0, s>>>(dC, h->nuC, nullptr, n);
             KCHECK();
             k_scale_nu<<<g, 256, 0, s>>>(h->nuC, h->lamL, 0.0, h->plane, n);
@@ -950,15 +1024,31 @@ int pade_les_init(pade_les* out, const pade_les_params* p) {
         if (rc == PS_OK) rc = al(h, &h->Dsgs, r8 * h->NC);
         if (rc == PS_OK) rc = al(h, &h->part, r8 * 2 * kPlaneChunks * h->nz);
     }
-    if (p->useSGS && p->learnedSGS && p->learnedPlaneAvg) {
+    if (p->useSGS && p->learnedSGS) {
         if (!h->part && rc == PS_OK) rc = al(h, &h->part, r8 * 2 * kPlaneChunks * h->nz);
         if (rc == PS_OK) rc = al(h, &h->lamL, r8 * h->nz);
+        if (rc == PS_OK) rc = al(h, &h->fball, sizeof(int));
+        if (rc == PS_OK) rc = al(h, &h->fbcount, sizeof(unsigned long long));
+        if (rc == PS_OK) rc = al(h, &h->judge_err, r8);
+        if (rc == PS_OK && (cudaMemset(h->fball, 0, sizeof(int)) != cudaSuccess ||
+                            cudaMemset(h->fbcount, 0, sizeof(unsigned long long)) != cudaSuccess ||
+                            cudaMemset(h->lamL, 0, r8 * h->nz) != cudaSuccess))
+            rc = PS_ECUDA;
+        if (rc == PS_OK) {
+            const double m1 = -1.0;  // no judge step yet
+            if (cudaMemcpy(h->judge_err, &m1, r8, cudaMemcpyHostToDevice) != cudaSuccess) rc = PS_ECUDA;
+        }
     }
     if (rc == PS_OK) rc = al(h, &h->lambda, r8 * h->nz);
     if (rc == PS_OK) rc = al(h, &h->d_dt, r8);
     if (rc == PS_OK) rc = al(h, &h->d_tsim, r8);
     if (rc == PS_OK) rc = al(h, &h->cflpart, r8 * kCflBlocks);
     if (rc == PS_OK && cudaMemset(h->lambda, 0, r8 * h->nz) != cudaSuccess) rc = PS_ECUDA;
+    if (rc == PS_OK && p->useSGS && p->learnedSGS) {
+        // the closure's fallback before any judge step: the constant Smagorinsky coefficient
+        const std::vector<double> c(h->nz, h->cmodel_global);
+        if (cudaMemcpy(h->lambda, c.data(), r8 * h->nz, cudaMemcpyHostToDevice) != cudaSuccess) rc = PS_ECUDA;
+    }
     if (rc == PS_OK && cudaMemset(h->d_tsim, 0, r8) != cudaSuccess) rc = PS_ECUDA;
     if (rc == PS_OK && cudaMemset(h->d_dt, 0, r8) != cudaSuccess) rc = PS_ECUDA;
     if (rc != PS_OK) {
@@ -1082,6 +1172,22 @@ int pade_les_info(pade_les h, double* dt, double* tsim, int* step, double* lambd
     if (step) *step = h->step;
     if (lambda1d && cudaMemcpy(lambda1d, h->lambda, sizeof(double) * h->nz, cudaMemcpyDeviceToHost) != cudaSuccess)
         return PS_ECUDA;
+    return PS_OK;
+}
+
+int pade_les_judge_info(pade_les h, double* err, double* lambda_closure, long long* n_fallback) {
+    if (!h) return PS_EINVAL;
+    if (!h->prm.learnedSGS || !h->judge_err) return PS_ENOTSUP;
+    if (cudaDeviceSynchronize() != cudaSuccess) return PS_ECUDA;
+    if (err && cudaMemcpy(err, h->judge_err, sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) return PS_ECUDA;
+    if (lambda_closure &&
+        cudaMemcpy(lambda_closure, h->lamL, sizeof(double) * h->nz, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return PS_ECUDA;
+    if (n_fallback) {
+        unsigned long long c = 0;
+        if (cudaMemcpy(&c, h->fbcount, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) return PS_ECUDA;
+        *n_fallback = (long long)c;
+    }
     return PS_OK;
 }
 

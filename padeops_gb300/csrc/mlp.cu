@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdint>
 #include <vector>
 
@@ -129,14 +130,18 @@ struct InferWeights {
     __nv_bfloat16 w1[NH * XS];
     __nv_bfloat16 w2[NH * W2S];
     float b1[NH], b2[NH], w3[NH], b3;
+    // training range of the features (pade_mlp_set_range); has_range = 0: no range check
+    float lo[NIN], hi[NIN];
+    int has_range;
 };
 
 __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta, double nu,
                                                    const InferWeights* __restrict__ wg, double* __restrict__ nu_out,
-                                                   float* __restrict__ cs2_out) {
+                                                   float* __restrict__ cs2_out, const MlpFallback fb) {
     __shared__ InferWeights W;
     __shared__ __align__(16) __nv_bfloat16 X[TILE * XS];
     __shared__ float mag[TILE];
+    __shared__ unsigned char fbk[TILE];  // point takes the fallback coefficient
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(wg);
         uint32_t* dst = reinterpret_cast<uint32_t*>(&W);
@@ -146,6 +151,8 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
     const int g = lane >> 2, t = lane & 3;
     const double d2 = delta * delta;
     const float delta_f = (float)delta, nu_f = (float)nu;
+    const bool fb_on = fb.lam != nullptr;
+    const bool fb_all = fb_on && fb.all && *fb.all != 0;
     for (long base = (long)blockIdx.x * TILE; base < n; base += (long)gridDim.x * TILE) {
         __syncthreads();  // weights loaded / previous tile consumed
         {
@@ -159,6 +166,18 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
                 for (int i = 0; i < NIN; i++) x[i] = 0.0f;
             }
             mag[threadIdx.x] = m;
+            // features outside the training range (or the judge's switch) send the point to
+            // the fallback coefficient
+            bool out = fb_all;
+            if (fb_on && W.has_range) {
+#pragma unroll
+                for (int i = 0; i < NIN; i++) out = out || !(x[i] >= W.lo[i] && x[i] <= W.hi[i]);
+            }
+            fbk[threadIdx.x] = out ? 1 : 0;
+            if (fb.count) {
+                const unsigned bal = __ballot_sync(0xffffffffu, out && e < n);
+                if ((threadIdx.x & 31) == 0 && bal) atomicAdd(fb.count, (unsigned long long)__popc(bal));
+            }
             uint32_t* row = reinterpret_cast<uint32_t*>(X + threadIdx.x * XS);
 #pragma unroll
             for (int i = 0; i < 5; i++) row[i] = pack_bf16(x[2 * i], x[2 * i + 1]);
@@ -224,9 +243,15 @@ __global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta
                     const int r = r0 + g + 8 * hr;
                     const long e = base + r;
                     if (e < n) {
-                        const float cs2 = softplus((hr ? z1 : z0) + W.b3);
-                        nu_out[e] = (double)cs2 * d2 * (double)mag[r];
-                        if (cs2_out) cs2_out[e] = cs2;
+                        if (fbk[r]) {
+                            const double c = fb.lam[e / fb.plane];  // Cs^2 Delta^2 of the fallback
+                            nu_out[e] = c * (double)mag[r];
+                            if (cs2_out) cs2_out[e] = (float)(c / d2);
+                        } else {
+                            const float cs2 = softplus((hr ? z1 : z0) + W.b3);
+                            nu_out[e] = (double)cs2 * d2 * (double)mag[r];
+                            if (cs2_out) cs2_out[e] = cs2;
+                        }
                     }
                 }
             }
@@ -417,6 +442,7 @@ struct pade_mlp_s {
     int part_tiles = 0;
     InferWeights* iw = nullptr;
     bool packed = false;
+    int has_range = 0;
     int t = 0;  // AdamW step count
 };
 
@@ -463,6 +489,7 @@ int pade_mlp_create(pade_mlp* out) {
         if (rc == PS_OK) rc = dalloc((void**)p, sizeof(float) * NPARAM);
     if (rc == PS_OK) rc = dalloc((void**)&h->loss, sizeof(float));
     if (rc == PS_OK) rc = dalloc((void**)&h->iw, sizeof(InferWeights));
+    if (rc == PS_OK && cudaMemset(h->iw, 0, sizeof(InferWeights)) != cudaSuccess) rc = PS_ECUDA;  // no range
     if (rc == PS_OK) {
         for (float* p : {h->prm, h->m, h->v, h->grad})
             if (cudaMemset(p, 0, sizeof(float) * NPARAM) != cudaSuccess) rc = PS_ECUDA;
@@ -546,16 +573,43 @@ int pade_mlp_features(const double* const* duidxj, long n, double delta, double 
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
+int pade_mlp_set_range(pade_mlp h, const float* lo, const float* hi) {
+    if (!h || (!lo) != (!hi)) return PS_EINVAL;
+    InferWeights tmp;
+    int has = lo ? 1 : 0;
+    for (int i = 0; i < NIN; i++) {
+        tmp.lo[i] = lo ? lo[i] : 0.0f;
+        tmp.hi[i] = hi ? hi[i] : 0.0f;
+        if (lo && !(lo[i] <= hi[i])) return PS_EINVAL;
+    }
+    const size_t off = offsetof(InferWeights, lo);
+    const size_t bytes = sizeof(InferWeights) - off;
+    tmp.has_range = has;
+    if (cudaMemcpy(reinterpret_cast<char*>(h->iw) + off, reinterpret_cast<const char*>(&tmp) + off, bytes,
+                   cudaMemcpyHostToDevice) != cudaSuccess)
+        return PS_ECUDA;
+    h->has_range = has;
+    return PS_OK;
+}
+
 int pade_mlp_infer_nu(pade_mlp h, const double* const* duidxj, long n, double delta, double nu, double* nu_out,
                       float* cs2_out, void* stream) {
+    return mlp_infer_nu_fb(h, duidxj, n, delta, nu, nu_out, cs2_out, MlpFallback{nullptr, 1, nullptr, nullptr},
+                           static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"
+
+int pade::mlp_infer_nu_fb(pade_mlp h, const double* const* duidxj, long n, double delta, double nu, double* nu_out,
+                          float* cs2_out, const MlpFallback& fb, cudaStream_t s) {
     if (!h || !duidxj || n < 0 || !device_ptr(nu_out) || !(delta > 0) || !(nu > 0)) return PS_EINVAL;
+    if (fb.lam && fb.plane < 1) return PS_EINVAL;
     if (cs2_out && !device_ptr(cs2_out)) return PS_EINVAL;
     Grad9 d;
     for (int i = 0; i < 9; i++) {
         if (!device_ptr(duidxj[i])) return PS_EINVAL;
         d.p[i] = duidxj[i];
     }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (!h->packed) {
         k_mlp_pack_infer<<<1, 256, 0, s>>>(h->prm, h->iw);
         if (cudaGetLastError() != cudaSuccess) return PS_ECUDA;
@@ -564,8 +618,6 @@ int pade_mlp_infer_nu(pade_mlp h, const double* const* duidxj, long n, double de
     if (n == 0) return PS_OK;
     const long tiles = (n + TILE - 1) / TILE;
     const unsigned g = (unsigned)std::min<long>(tiles, 152L * 8);
-    k_mlp_infer<<<g, 128, 0, s>>>(d, n, delta, nu, h->iw, nu_out, cs2_out);
+    k_mlp_infer<<<g, 128, 0, s>>>(d, n, delta, nu, h->iw, nu_out, cs2_out, fb);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
-
-}  // extern "C"

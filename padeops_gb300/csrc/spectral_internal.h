@@ -102,4 +102,16 @@ int spectral_ifft_two(pade_spectral h, const void* in1, int mul1, const void* in
 // ifft of fhat * G, G = 1 where |k1| < cut1 and |k2| < cut2 (the test filter's TestFilter_oop)
 int spectral_ifft_masked(pade_spectral h, const void* in, double* out, double cut1, double cut2, cudaStream_t s);
 
+// Learned closure inside the LES (mlp.cu, called by les.cu): points whose features leave
+// the training range (pade_mlp_set_range), or every point while *all is nonzero, take the
+// fallback coefficient Cs^2 Delta^2 = lam[z plane] instead of the network's.
+struct MlpFallback {
+    const double* lam;          // per z plane; null: no fallback
+    long plane;                 // points per z plane
+    const int* all;             // device flag (may be null)
+    unsigned long long* count;  // device counter of the points given the fallback (may be null)
+};
+int mlp_infer_nu_fb(pade_mlp h, const double* const* duidxj, long n, double delta, double nu, double* nu_out,
+                    float* cs2_out, const MlpFallback& fb, cudaStream_t s);
+
 }  // namespace pade

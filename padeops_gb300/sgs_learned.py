@@ -70,6 +70,18 @@ class LearnedClosure:
         L.check(L.lib().pade_mlp_get_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
         return p
 
+    def set_range(self, lo, hi):
+        """Training range of the 10 features (None, None: no range).  Inside the LES, points
+        outside it take the fallback coefficient instead of the network's."""
+        if lo is None and hi is None:
+            L.check(L.lib().pade_mlp_set_range(self._h, None, None), "pade_mlp_set_range")
+            return
+        lo = np.ascontiguousarray(lo, dtype=np.float32)
+        hi = np.ascontiguousarray(hi, dtype=np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.check(L.lib().pade_mlp_set_range(self._h, lo.ctypes.data_as(fp), hi.ctypes.data_as(fp)),
+                "pade_mlp_set_range")
+
     def loss_grad(self, X, y):
         loss = ctypes.c_float()
         g = np.empty(NPARAM, dtype=np.float32)
@@ -135,8 +147,16 @@ def training_set(grid, closure, nsteps, every=1, max_samples=None, seed=0):
     return X, y
 
 
-def train(closure, X, y, epochs=5, batch=4096, lr=2e-3, wd=0.0, seed=0):
-    """Mini-batch AdamW over (X, y); returns the mean loss of each epoch."""
+def feature_range(X):
+    """Per-feature minimum and maximum of a training set X (n x 10)."""
+    return X.min(dim=0).values.cpu().numpy(), X.max(dim=0).values.cpu().numpy()
+
+
+def train(closure, X, y, epochs=5, batch=4096, lr=2e-3, wd=0.0, seed=0, set_range=True):
+    """Mini-batch AdamW over (X, y); returns the mean loss of each epoch.  set_range records
+    the training set's feature range in the closure (its fallback test inside the LES)."""
+    if set_range:
+        closure.set_range(*feature_range(X))
     g = torch.Generator(device="cpu").manual_seed(seed)
     n = X.shape[0]
     hist = []
@@ -150,3 +170,90 @@ def train(closure, X, y, epochs=5, batch=4096, lr=2e-3, wd=0.0, seed=0):
             nb += 1
         hist.append(tot / max(nb, 1))
     return hist
+
+
+def box_filter(f, r):
+    """Mean over r x r x r blocks of a field held as a (nz, ny, nx) tensor (a Fortran array
+    with reversed dimensions); every extent a multiple of r."""
+    nz, ny, nx = f.shape
+    return f.reshape(nz // r, r, ny // r, r, nx // r, r).mean(dim=(1, 3, 5))
+
+
+def dns_training_set(n_dns=512, ratio=4, nsteps=60, snapshots=2, every=20, seed=5, kp=8.0, Re=1000.0,
+                     cs2_max=0.25, max_samples=None):
+    """Training pairs from a direct simulation (the a priori procedure): the solver without an
+    SGS model on n_dns^3 from the seeded spectrum E(k) ~ k^4 exp(-2 (k/kp)^2), run nsteps
+    steps; then `snapshots` times, `every` steps apart, its velocity is box-filtered by
+    `ratio` onto the LES grid n_dns/ratio.  Targets: the local Smagorinsky coefficient that
+    matches the resolved-to-subgrid energy flux of the filtered DNS,
+        Cs^2 = max(0, -tau_ij S_ij) / (2 Delta^2 |S| S_ij S_ij),  tau_ij = <u_i u_j> - <u_i><u_j>
+    (clipped to [0, cs2_max]), with S_ij and the features from the filtered field's gradients
+    as the LES computes them (the filtered field passed through igrid's init sequence).
+    Returns (X, y, info): CUDA float32 tensors and a dict of the run's figures."""
+    from .IncompressibleGrid import igrid
+    from .PadeDerOps import Pade6stagg
+    from .synthetic import hit_initial_field_torch
+
+    n_les = n_dns // ratio
+    L_ = 2 * np.pi
+    g = igrid()
+    g.init(n_dns, n_dns, n_dns, Re=Re, useSGS=False)
+    u, v, w = hit_initial_field_torch(n_dns, seed=seed, kp=kp)
+    g.set_fields(u, v, w)
+    del u, v, w
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        g.timeAdvance(use_graph=False)
+        for _ in range(nsteps - 1):
+            g.timeAdvance(use_graph=True)
+    side.synchronize()
+    les = igrid()
+    les.init(n_les, n_les, n_les, Re=Re, useSGS=False)
+    interp = Pade6stagg()
+    L.check(interp.init(n_les, L_ / n_les, 1, True), "Pade6stagg.init")
+    dl = delta_les(L_ / n_les, L_ / n_les, L_ / n_les)
+    clo = LearnedClosure()
+    Xs, ys = [], []
+    for snap in range(snapshots):
+        if snap:
+            with torch.cuda.stream(side):
+                for _ in range(every):
+                    g.timeAdvance(use_graph=True)
+            side.synchronize()
+        uu = [g.field(nm) for nm in ("u", "v", "wC")]
+        fu = [box_filter(a, ratio) for a in uu]
+        tau = {}
+        for i in range(3):
+            for j in range(i, 3):
+                tau[(i, j)] = box_filter(uu[i] * uu[j], ratio) - fu[i] * fu[j]
+        del uu
+        wE = torch.empty((n_les + 1, n_les, n_les), dtype=torch.float64, device="cuda")
+        interp.interpz_C2E(fu[2].contiguous(), wE, 0, 0)
+        les.set_fields(fu[0].contiguous(), fu[1].contiguous(), wE)
+        grads = [les.field(f"duidxjC{i + 1}") for i in range(9)]
+        G = [[grads[3 * i + j] for j in range(3)] for i in range(3)]  # G[i][j] = du_i/dx_j
+        S = {(i, j): 0.5 * (G[i][j] + G[j][i]) for i in range(3) for j in range(i, 3)}
+        w2 = {(i, j): (1.0 if i == j else 2.0) for (i, j) in S}
+        SS = sum(w2[k] * S[k] * S[k] for k in S)
+        Smag = torch.sqrt(2.0 * SS)
+        flux = -sum(w2[k] * tau[k] * S[k] for k in S)
+        den = 2.0 * dl * dl * Smag * SS
+        cs2 = torch.where(den > 0, flux / torch.where(den > 0, den, torch.ones_like(den)), torch.zeros_like(den))
+        cs2 = cs2.clamp(0.0, cs2_max)
+        X = clo.features(grads, dl, 1.0 / Re)
+        Xs.append(X)
+        ys.append(cs2.reshape(-1).float())
+        del tau, grads, G, S, SS, Smag, flux, den
+    X = torch.cat(Xs)
+    y = torch.cat(ys)
+    info = {"n_dns": n_dns, "n_les": n_les, "steps": nsteps + every * (snapshots - 1), "tsim": g.info()["tsim"],
+            "samples": int(X.shape[0]), "cs2_mean": float(y.mean()), "cs2_zero_fraction": float((y == 0).float().mean())}
+    g.destroy()
+    les.destroy()
+    interp.destroy()
+    clo.destroy()
+    if max_samples is not None and X.shape[0] > max_samples:
+        gen = torch.Generator(device="cpu").manual_seed(seed)
+        idx = torch.randperm(X.shape[0], generator=gen)[:max_samples].to(X.device)
+        X, y = X[idx].contiguous(), y[idx].contiguous()
+    return X, y, info

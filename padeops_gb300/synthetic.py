@@ -71,3 +71,34 @@ def hit_initial_field(n, seed=4, kp=4.0, urms=1.0):
     u, v, w = (np.asfortranarray(c * s) for c in (u, v, w))
     wE = np.asfortranarray(np.concatenate([w, w[:, :, :1]], axis=2))
     return u, v, wE
+
+
+def hit_initial_field_torch(n, seed=4, kp=4.0, urms=1.0, device="cuda"):
+    """hit_initial_field built on the device (torch FFTs; independent phases from a seeded
+    torch generator, so not the same realisation as the numpy version): u, v (nz, ny, nx)
+    and w on nz+1 edge planes, as CUDA tensors holding Fortran-ordered arrays (x fastest).
+    For grids whose numpy construction would be slow (512^3)."""
+    import torch
+
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+    g = torch.Generator(device=device).manual_seed(seed)
+    f = lambda m: torch.fft.fftfreq(m, 1.0 / m, device=device, dtype=torch.float64)  # noqa: E731
+    kx, ky, kz = f(nx), f(ny), f(nz)
+    # (z, y, x) tensor order = Fortran (x, y, z) memory order
+    KZ, KY, KX = kz[:, None, None], ky[None, :, None], kx[None, None, :]
+    kk = torch.sqrt(KX ** 2 + KY ** 2 + KZ ** 2)
+    kk[0, 0, 0] = 1.0
+    amp = torch.sqrt(kk ** 4 * torch.exp(-2.0 * (kk / kp) ** 2) / (4 * np.pi * kk ** 2))
+    amp[0, 0, 0] = 0.0
+    amp = amp * (KX.abs() < nx // 3) * (KY.abs() < ny // 3) * (KZ.abs() < nz // 3)
+    del kk
+    comps = []
+    for _ in range(3):
+        ph = torch.rand((nz, ny, nx), generator=g, device=device, dtype=torch.float64) * (2 * np.pi)
+        comps.append(torch.fft.ifftn(torch.polar(amp, ph)).real.contiguous() * float(nx * ny * nz))
+        del ph
+    u, v, w = comps
+    s = urms / torch.sqrt((u ** 2 + v ** 2 + w ** 2).mean() / 3.0)
+    u, v, w = u * s, v * s, w * s
+    wE = torch.cat([w, w[:1]], dim=0).contiguous()
+    return u.contiguous(), v.contiguous(), wE
