@@ -7,6 +7,7 @@ field (the driver of the Nsight Compute captures summarised under profiles/).
     python bench_cases.py --family projection --n 256 --repeat 3
     python bench_cases.py --family les --n 128 --repeat 2           # TVD-RK3 steps
     python bench_cases.py --family les_learned --n 256 --repeat 1   # learned closure
+    python bench_cases.py --family mlp --n 256 --repeat 5           # closure inference alone
 
 Prints the mean CUDA-event time per application and the implied HBM throughput at
 16 B/point (8 B/point for the FP32 path).  Not part of the library: a measurement tool
@@ -23,7 +24,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--family", default="cd10",
                     choices=["cd06", "cd10", "cf90", "gaussian", "stagg", "dense", "spectral", "projection", "les",
-                             "les_learned"])
+                             "les_learned", "mlp"])
     ap.add_argument("--opcode", type=int, default=1)
     ap.add_argument("--dir", type=int, default=1)
     ap.add_argument("--n", type=int, default=256)
@@ -45,6 +46,8 @@ def main(argv=None):
         return spectral_case(a, torch, P)
     if a.family == "dense":
         return dense_case(a, torch, P, L)
+    if a.family == "mlp":
+        return mlp_case(a, torch)
     path = {"df": L.PATH_DF, "native": L.PATH_NATIVE, "fp32": L.PATH_FP32}[a.path]
     dt = torch.float32 if path == L.PATH_FP32 else torch.float64
     n = a.n
@@ -97,6 +100,18 @@ def dense_case(a, torch, P, L):
     ms = _timed(torch, run, a.repeat)
     print(f"dense cd10 op{a.opcode} dir{a.dir} n={n} lines={na}x{nb}: {ms:.4f} ms/app, "
           f"{total / ms / 1e6:.1f} Gpts/s, {total * 16 / ms / 1e6:.1f} GB/s")
+
+
+def mlp_case(a, torch):
+    """Learned-closure inference (pade_mlp_infer_nu) on n^3 points of random gradients."""
+    from padeops_gb300.sgs_learned import LearnedClosure, init_params
+
+    n3 = a.n ** 3
+    g = torch.Generator(device="cuda").manual_seed(0)
+    grads = [torch.randn(n3, device="cuda", dtype=torch.float64, generator=g) for _ in range(9)]
+    c = LearnedClosure(init_params(0))
+    ms = _timed(torch, lambda: c.infer_nu(grads, 2 * np.pi / a.n, 1e-3), a.repeat)
+    print(f"mlp inference n^3={n3}: {ms:.4f} ms/launch, {n3 * 80 / ms / 1e6:.1f} GB/s at 80 B/point")
 
 
 def _timed(torch, fn, repeat):

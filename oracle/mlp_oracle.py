@@ -111,13 +111,15 @@ def bf16(x):
 
 
 def infer_bf16(p, X):
-    """The inference kernel's arithmetic: BF16 inputs, weights W1/W2 and hidden layer 1,
-    FP32-exact products, FP64 sums standing in for FP32 accumulation."""
+    """The inference kernel's arithmetic: BF16 inputs, weights and activations (both hidden
+    layers and w3), FP32-exact products, FP64 sums standing in for FP32 accumulation.  The
+    kernel evaluates GELU in BF16 arithmetic with an approximate tanh; here GELU is exact and
+    rounded once, so the two differ by a few BF16 ulps per activation."""
     w = unpack(p)
     xb = bf16(X)
     z1 = xb @ bf16(w["W1"]).T + np.asarray(w["b1"], dtype=np.float32)
     h1 = bf16(gelu(z1))
     z2 = h1 @ bf16(w["W2"]).T + np.asarray(w["b2"], dtype=np.float32)
-    h2 = gelu(z2)
-    z3 = h2 @ np.asarray(w["w3"], dtype=np.float32) + np.float32(w["b3"][0])
+    h2 = bf16(gelu(z2))
+    z3 = h2 @ bf16(np.asarray(w["w3"], dtype=np.float32)) + np.float32(w["b3"][0])
     return softplus(z3)

@@ -21,7 +21,7 @@ CUDA_SOURCES = ["kernels.cu", "kernels_df16.cu", "kernels_df32.cu", "kernels_f32
                 "spectral.cu", "poisson_wall.cu", "les.cu", "mlp.cu",
                 "dense_tc.cu"]
 HEADERS = ["operators.h", "plan.h", "chunkplan.h", "engine.h", "dfmath.cuh", "chunk_kernel.cuh", "stencil_kernel.cuh", "reg_kernel.cuh", "capi_internal.h",
-           "fft.h", "spectral_internal.h"]
+           "fft.h", "spectral_internal.h", "tc_common.cuh"]
 
 
 def _nvcc():

@@ -4,13 +4,13 @@
 // DoStandardDynamicProcedure (sgsmod_igrid.F90:176-183).
 //
 // Kernels
-//  * k_mlp_infer: per point, the features (9 velocity gradients / |S|, ln(1 + Delta/eta))
+//  * k_mlp_infer_tc: per point, the features (9 velocity gradients / |S|, ln(1 + Delta/eta))
 //    from the nine FP64 gradient arrays, computed in FP32 from an integer FP64 -> FP32
 //    conversion (the FP64 pipe is 1/64 of the FP32 rate on this part and the network reads
-//    BF16), the MLP on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32
-//    accumulation; layer-1 accumulators are re-used in registers as layer-2 operands; GELU
-//    with the hardware tanh approximation), softplus, and nu = Cs^2 Delta^2 |S| written in
-//    FP64.  80 B/point of HBM traffic against ~10 kflop/point.
+//    BF16); the three layers as tcgen05.mma (BF16 operands from shared memory, FP32
+//    accumulators in tensor memory, biases folded into the MMAs); GELU on BF16 pairs between
+//    the layers; softplus; nu = Cs^2 Delta^2 |S| written in FP64.  84 B/point of HBM traffic
+//    (72 read, 8 written, plus 4 when Cs^2 is kept) against ~10 kflop/point.
 //  * k_mlp_train_tile: forward and backward of a 128-sample tile in FP32 (shared memory
 //    activations), writing the tile's partial gradient; k_mlp_reduce sums the tiles in a
 //    fixed order (deterministic); k_mlp_adamw applies AdamW.
@@ -24,10 +24,13 @@
 #include <vector>
 
 #include "../../include/padeops_gb300.h"
+#include "dfmath.cuh"
 #include "operators.h"
 #include "spectral_internal.h"
+#include "tc_common.cuh"
 
 using namespace pade;
+using namespace pade::tc;
 
 namespace {
 
@@ -43,15 +46,6 @@ __device__ __forceinline__ float gelu(float x) {
 __device__ __forceinline__ float gelu_grad(float x) {
     const float t = tanhf(C_GELU * (x + 0.044715f * x * x * x));
     return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * C_GELU * (1.0f + 3.0f * 0.044715f * x * x);
-}
-// GELU with the hardware tanh approximation (inference, whose activations are then BF16)
-__device__ __forceinline__ float tanh_approx(float x) {
-    float y;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float gelu_fast(float x) {
-    return 0.5f * x * (1.0f + tanh_approx(C_GELU * (x + 0.044715f * x * x * x)));
 }
 __device__ __forceinline__ float softplus(float z) { return z > 20.0f ? z : log1pf(expf(z)); }
 __device__ __forceinline__ float sigmoid(float z) { return 0.5f * (1.0f + tanhf(0.5f * z)); }
@@ -75,15 +69,16 @@ __device__ __forceinline__ float d2f_bits(double d) {
 // 2^k as a float, -126 <= k <= 127
 __device__ __forceinline__ float pow2f(int k) { return __uint_as_float((unsigned)(k + 127) << 23); }
 
-// Features of point e in FP32 (the network sees them in BF16): the nine gradients over
-// |S| = sqrt(2 S_ij S_ij), and ln(1 + Delta sqrt(|S| / nu)).  The gradients are scaled by a
-// power of two near their largest magnitude first, so S_ij S_ij cannot overflow.  Returns |S|.
-__device__ __forceinline__ float point_features(const Grad9& d, long e, float delta, float nu, float* x) {
+// Features of one point in FP32 (the network sees them in BF16) from its nine FP64
+// gradients g: the gradients over |S| = sqrt(2 S_ij S_ij), and ln(1 + Delta sqrt(|S| / nu)).
+// The gradients are scaled by a power of two near their largest magnitude first, so
+// S_ij S_ij cannot overflow.  Returns |S|.
+__device__ __forceinline__ float point_features(const double* gd, float delta, float nu, float* x) {
     float g[9];
     float gm = 0.0f;
 #pragma unroll
     for (int i = 0; i < 9; i++) {
-        g[i] = d2f_bits(d.p[i][e]);
+        g[i] = d2f_bits(gd[i]);
         gm = fmaxf(gm, fabsf(g[i]));
     }
     if (!(gm > 0.0f) || !(gm <= 3.0e38f)) {  // zero gradients (or non-finite ones): zero features
@@ -108,162 +103,242 @@ __device__ __forceinline__ float point_features(const Grad9& d, long e, float de
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-    const __nv_bfloat16 a = __float2bfloat16_rn(lo), b = __float2bfloat16_rn(hi);
-    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // lo in the low half (lower address)
+    return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
+// ---- inference on the tensor cores (tcgen05, BF16 operands, FP32 accumulation in TMEM)
+//
+// A CTA of 128 threads takes tiles of 128 points; thread r owns point r of the tile, which
+// is row r of every MMA's A operand and lane r of tensor memory.  Per tile:
+//   features -> X (128 x 16 BF16: 10 features, then 1, 1 at K = 10, 11 to carry the biases)
+//   D  = X W1ext^T                         (1 MMA, N = 64)      -> GELU -> H (128 x 64 BF16)
+//   D  = H W2^T + X B2ext^T                (4 + 1 MMAs, N = 64) -> GELU -> H
+//   D  = H W3ext^T + X B3ext^T             (4 + 1 MMAs, N = 16) -> z = column 0
+//   Cs^2 = softplus(z), nu = Cs^2 Delta^2 |S|.
+// Each bias is split into two BF16 parts (value and remainder, ~2^-17 relative) that
+// multiply the two 1-features, so the tensor cores add it.  The three D share 64 TMEM
+// columns (each is read out before the next MMA overwrites it).  GELU runs on BF16 pairs
+// (packed FMA and the hardware tanh approximation on two values per instruction), the
+// activations being BF16 anyway.  The next tile's gradients are loaded while the current
+// one goes through the network; four CTAs share an SM.  Thread 0 waits on the MMA barrier
+// (bounded: a timeout sets g_mlp_err, the CTA frees its tensor memory and returns) while
+// the other threads sleep in the CTA barrier that follows.
+constexpr int TILE = 128;              // points per tile (MMA M)
+constexpr uint32_t kTmemCols = 64;     // one FP32 accumulator of N <= 64
+constexpr int kInferCtasPerSm = 4;
+constexpr unsigned kMlpWaitLimit = 1u << 22;
 
-constexpr int TILE = 128;  // points per CTA iteration (4 warps x 2 m-tiles of 16)
-constexpr int XS = 24;     // bf16 row stride of the feature tile and W1 (bank-conflict padding)
-constexpr int W2S = 72;    // bf16 row stride of W2
-
-// weights for inference: W1 (64 x 16, k padded with zeros) and W2 (64 x 64) as BF16,
-// biases and w3 in FP32
-struct InferWeights {
-    __nv_bfloat16 w1[NH * XS];
-    __nv_bfloat16 w2[NH * W2S];
-    float b1[NH], b2[NH], w3[NH], b3;
+// Inference weights: pre-swizzled shared-memory images (K-major rows of 128 bytes) of the
+// MMAs' B operands, then the features' training range.
+//   wsmall, 64 rows:  K 0..15  W1 row n (K 0..9), b1[n] as BF16 value + remainder (K 10, 11)
+//                     K 16..31 b2[n] the same way (K 26, 27)
+//                     K 32..47 rows 0..15: b3 (row 0, K 42, 43), zeros elsewhere
+//   w2, 64 rows:      W2[n][k]
+//   w3, 16 rows:      row 0 = w3, rows 1..15 zero (N = 16 is the smallest M = 128 shape)
+struct TcWeights {
+    uint8_t wsmall[64 * 128];
+    uint8_t w2[64 * 128];
+    uint8_t w3[16 * 128];
     // training range of the features (pade_mlp_set_range); has_range = 0: no range check
     float lo[NIN], hi[NIN];
     int has_range;
 };
+constexpr size_t kImgBytes = 64 * 128 + 64 * 128 + 16 * 128;
+static_assert(offsetof(TcWeights, lo) == kImgBytes, "image layout");
+static_assert(kImgBytes % 1024 == 0, "tiles after the images stay 1024-byte aligned");
+constexpr size_t kInferSmem = 1024 + kImgBytes + 2 * (size_t)TILE * 128;  // alignment slack, images, X, H
 
-__global__ void __launch_bounds__(128) k_mlp_infer(Grad9 d, long n, double delta, double nu,
-                                                   const InferWeights* __restrict__ wg, double* __restrict__ nu_out,
-                                                   float* __restrict__ cs2_out, const MlpFallback fb) {
-    __shared__ InferWeights W;
-    __shared__ __align__(16) __nv_bfloat16 X[TILE * XS];
-    __shared__ float mag[TILE];
-    __shared__ unsigned char fbk[TILE];  // point takes the fallback coefficient
-    {
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(wg);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(&W);
-        for (int i = threadIdx.x; i < (int)(sizeof(InferWeights) / 4); i += blockDim.x) dst[i] = src[i];
+__device__ unsigned g_mlp_err;  // 1: a tensor-core wait timed out
+
+__device__ __forceinline__ uint32_t bf2_u32(__nv_bfloat162 v) { return *reinterpret_cast<const uint32_t*>(&v); }
+__device__ __forceinline__ __nv_bfloat162 u32_bf2(uint32_t u) { return *reinterpret_cast<const __nv_bfloat162*>(&u); }
+
+// GELU (tanh form) of two BF16 values, in BF16 arithmetic
+__device__ __forceinline__ uint32_t gelu_bf2(uint32_t xu) {
+    const __nv_bfloat162 x = u32_bf2(xu);
+    const __nv_bfloat162 k1 = __float2bfloat162_rn(C_GELU * 0.044715f), k0 = __float2bfloat162_rn(C_GELU);
+    const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
+    const __nv_bfloat162 u = __hmul2(x, __hfma2(__hmul2(x, x), k1, k0));  // sqrt(2/pi) (x + 0.044715 x^3)
+    uint32_t t;
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(bf2_u32(u)));
+    return bf2_u32(__hmul2(x, __hfma2(u32_bf2(t), half, half)));
+}
+
+// D (64 FP32 columns of this thread's lane) -> GELU -> row r of the BF16 tile H
+__device__ __forceinline__ void gelu_row(uint32_t trow, uint8_t* H, int r) {
+#pragma unroll
+    for (int cb = 0; cb < 4; cb++) {
+        uint32_t v[16];
+        tmem_ld16(trow + (uint32_t)(cb * 16), v);
+        uint32_t w[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) w[i] = gelu_bf2(pack_bf16(__uint_as_float(v[2 * i]), __uint_as_float(v[2 * i + 1])));
+        *reinterpret_cast<uint4*>(H + swz(r, 2 * cb)) = make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4*>(H + swz(r, 2 * cb + 1)) = make_uint4(w[4], w[5], w[6], w[7]);
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
+}
+
+__device__ __forceinline__ bool mlp_wait(uint64_t* bar, unsigned phase) {
+    unsigned it = 0;
+    while (!mbar_try_wait(bar, phase))
+        if (++it > kMlpWaitLimit) return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(TILE, kInferCtasPerSm)
+    k_mlp_infer_tc(Grad9 d, long n, double delta, double nu, const TcWeights* __restrict__ wg,
+                   double* __restrict__ nu_out, float* __restrict__ cs2_out, const MlpFallback fb) {
+    extern __shared__ uint8_t sm_raw[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    __shared__ float lo_s[NIN], hi_s[NIN];
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(sm_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t* Wsm = base;
+    uint8_t* W2 = base + 64 * 128;
+    uint8_t* W3 = base + 2 * 64 * 128;
+    uint8_t* X = base + kImgBytes;
+    uint8_t* H = X + TILE * 128;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(wg);
+        uint4* dst = reinterpret_cast<uint4*>(base);
+        for (int i = tid; i < (int)(kImgBytes / 16); i += TILE) dst[i] = __ldg(src + i);
+    }
+    if (tid < NIN) {
+        lo_s[tid] = wg->lo[tid];
+        hi_s[tid] = wg->hi[tid];
+    }
+    const bool has_range = wg->has_range != 0;
+    if (warp == 0) tmem_alloc(&tslot, kTmemCols);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    fence_async_smem();  // the weight images, written by the threads, are read by the tensor cores
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+    constexpr uint32_t id64 = idesc_bf16_m128(64), id16 = idesc_bf16_m128(16);
+    const uint32_t ONES = 0x3F803F80u;  // two BF16 1.0
+    const float delta_f = (float)delta, nu_f = (float)nu, d2f = (float)(delta * delta);
     const double d2 = delta * delta;
-    const float delta_f = (float)delta, nu_f = (float)nu;
     const bool fb_on = fb.lam != nullptr;
     const bool fb_all = fb_on && fb.all && *fb.all != 0;
-    for (long base = (long)blockIdx.x * TILE; base < n; base += (long)gridDim.x * TILE) {
-        __syncthreads();  // weights loaded / previous tile consumed
-        {
-            const long e = base + threadIdx.x;
-            float x[NIN];
-            float m = 0.0f;
-            if (e < n) {
-                m = point_features(d, e, delta_f, nu_f, x);
-            } else {
+    const long ntiles = (n + TILE - 1) / TILE;
+    unsigned ph = 0;
+    int tout = 0;  // this thread's wait timed out
+
+    double g[9];
+    auto load = [&](long t) {
+        const long e = t * TILE + tid;
+        const bool ok = t < ntiles && e < n;
 #pragma unroll
-                for (int i = 0; i < NIN; i++) x[i] = 0.0f;
-            }
-            mag[threadIdx.x] = m;
-            // features outside the training range (or the judge's switch) send the point to
-            // the fallback coefficient
-            bool out = fb_all;
-            if (fb_on && W.has_range) {
+        for (int i = 0; i < 9; i++) g[i] = ok ? __ldg(d.p[i] + e) : 0.0;
+    };
+    load(blockIdx.x);
+    for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long e = tile * TILE + tid;
+        float x[NIN];
+        float mag = 0.0f;
+        if (e < n) {
+            mag = point_features(g, delta_f, nu_f, x);
+        } else {
 #pragma unroll
-                for (int i = 0; i < NIN; i++) out = out || !(x[i] >= W.lo[i] && x[i] <= W.hi[i]);
-            }
-            fbk[threadIdx.x] = out ? 1 : 0;
-            if (fb.count) {
-                const unsigned bal = __ballot_sync(0xffffffffu, out && e < n);
-                if ((threadIdx.x & 31) == 0 && bal) atomicAdd(fb.count, (unsigned long long)__popc(bal));
-            }
-            uint32_t* row = reinterpret_cast<uint32_t*>(X + threadIdx.x * XS);
-#pragma unroll
-            for (int i = 0; i < 5; i++) row[i] = pack_bf16(x[2 * i], x[2 * i + 1]);
-#pragma unroll
-            for (int i = 5; i < 8; i++) row[i] = 0u;
+            for (int i = 0; i < NIN; i++) x[i] = 0.0f;
         }
-        __syncthreads();
-#pragma unroll 1
-        for (int mt = 0; mt < 2; mt++) {
-            const int r0 = warp * 32 + mt * 16;  // first row of this m-tile
-            uint32_t a[4];
-            const uint32_t* xr0 = reinterpret_cast<const uint32_t*>(X + (r0 + g) * XS);
-            const uint32_t* xr1 = reinterpret_cast<const uint32_t*>(X + (r0 + g + 8) * XS);
-            a[0] = xr0[t];
-            a[1] = xr1[t];
-            a[2] = xr0[t + 4];
-            a[3] = xr1[t + 4];
-            // layer 1: 8 n-tiles of 8 hidden units
-            float h[8][4];
+        // features outside the training range (or the judge's switch) send the point to the
+        // fallback coefficient
+        bool out = fb_all;
+        if (fb_on && has_range) {
 #pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                h[nt][0] = h[nt][1] = h[nt][2] = h[nt][3] = 0.0f;
-                const uint32_t* wr = reinterpret_cast<const uint32_t*>(W.w1 + (nt * 8 + g) * XS);
-                mma_bf16(h[nt], a, wr[t], wr[t + 4]);
-                const int c = nt * 8 + 2 * t;
-                h[nt][0] = gelu_fast(h[nt][0] + W.b1[c]);
-                h[nt][1] = gelu_fast(h[nt][1] + W.b1[c + 1]);
-                h[nt][2] = gelu_fast(h[nt][2] + W.b1[c]);
-                h[nt][3] = gelu_fast(h[nt][3] + W.b1[c + 1]);
-            }
-            // layer 2: the layer-1 accumulators of n-tiles (2kt, 2kt+1) form the A operand of k-tile kt
-            float o[8][4];
+            for (int i = 0; i < NIN; i++) out = out || !(x[i] >= lo_s[i] && x[i] <= hi_s[i]);
+        }
+        if (fb.count) {
+            const unsigned bal = __ballot_sync(0xffffffffu, out && e < n);
+            if ((tid & 31) == 0 && bal) atomicAdd(fb.count, (unsigned long long)__popc(bal));
+        }
+        *reinterpret_cast<uint4*>(X + swz(tid, 0)) =
+            make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
+        *reinterpret_cast<uint4*>(X + swz(tid, 1)) = make_uint4(pack_bf16(x[8], x[9]), ONES, 0u, 0u);
+        load(tile + gridDim.x);  // the next tile's gradients load while this one runs
+        fence_async_smem();
+        tc_fence_before();
+        if (__syncthreads_or(tout)) break;
+        // layer 1
+        if (tid == 0) {
+            tc_fence_after();
+            mma_f16(tmem, desc_sw128(su32(X)), desc_sw128(su32(Wsm)), id64, 0u);
+            mma_commit(&bar);
+        }
+        if (tid == 0 && !mlp_wait(&bar, ph)) tout = 1;  // one waiter; the others sleep in the barrier
+        ph ^= 1u;
+        if (__syncthreads_or(tout)) break;
+        tc_fence_after();
+        gelu_row(trow, H, tid);
+        fence_async_smem();
+        tc_fence_before();
+        if (__syncthreads_or(tout)) break;
+        // layer 2 (+ b2 from the 1-features)
+        if (tid == 0) {
+            tc_fence_after();
 #pragma unroll
-            for (int nt = 0; nt < 8; nt++) o[nt][0] = o[nt][1] = o[nt][2] = o[nt][3] = 0.0f;
+            for (int kk = 0; kk < 4; kk++)
+                mma_f16(tmem, desc_sw128(su32(H + kk * 32)), desc_sw128(su32(W2 + kk * 32)), id64, kk > 0 ? 1u : 0u);
+            mma_f16(tmem, desc_sw128(su32(X)), desc_sw128(su32(Wsm + 32)), id64, 1u);
+            mma_commit(&bar);
+        }
+        if (tid == 0 && !mlp_wait(&bar, ph)) tout = 1;  // one waiter; the others sleep in the barrier
+        ph ^= 1u;
+        if (__syncthreads_or(tout)) break;
+        tc_fence_after();
+        gelu_row(trow, H, tid);
+        fence_async_smem();
+        tc_fence_before();
+        if (__syncthreads_or(tout)) break;
+        // layer 3 (+ b3)
+        if (tid == 0) {
+            tc_fence_after();
 #pragma unroll
-            for (int kt = 0; kt < 4; kt++) {
-                uint32_t a2[4];
-                a2[0] = pack_bf16(h[2 * kt][0], h[2 * kt][1]);
-                a2[1] = pack_bf16(h[2 * kt][2], h[2 * kt][3]);
-                a2[2] = pack_bf16(h[2 * kt + 1][0], h[2 * kt + 1][1]);
-                a2[3] = pack_bf16(h[2 * kt + 1][2], h[2 * kt + 1][3]);
-#pragma unroll
-                for (int nt = 0; nt < 8; nt++) {
-                    const uint32_t* wr = reinterpret_cast<const uint32_t*>(W.w2 + (nt * 8 + g) * W2S + kt * 16);
-                    mma_bf16(o[nt], a2, wr[t], wr[t + 4]);
-                }
-            }
-            // layer 3 (FP32): rows g and g+8, this lane's 16 columns, then the 4 lanes of the row
-            float z0 = 0.0f, z1 = 0.0f;
-#pragma unroll
-            for (int nt = 0; nt < 8; nt++) {
-                const int c = nt * 8 + 2 * t;
-                z0 += W.w3[c] * gelu_fast(o[nt][0] + W.b2[c]) + W.w3[c + 1] * gelu_fast(o[nt][1] + W.b2[c + 1]);
-                z1 += W.w3[c] * gelu_fast(o[nt][2] + W.b2[c]) + W.w3[c + 1] * gelu_fast(o[nt][3] + W.b2[c + 1]);
-            }
-            z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
-            z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
-            z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
-            z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
-            if (t == 0) {
-#pragma unroll
-                for (int hr = 0; hr < 2; hr++) {
-                    const int r = r0 + g + 8 * hr;
-                    const long e = base + r;
-                    if (e < n) {
-                        if (fbk[r]) {
-                            const double c = fb.lam[e / fb.plane];  // Cs^2 Delta^2 of the fallback
-                            nu_out[e] = c * (double)mag[r];
-                            if (cs2_out) cs2_out[e] = (float)(c / d2);
-                        } else {
-                            const float cs2 = softplus((hr ? z1 : z0) + W.b3);
-                            nu_out[e] = (double)cs2 * d2 * (double)mag[r];
-                            if (cs2_out) cs2_out[e] = cs2;
-                        }
-                    }
-                }
+            for (int kk = 0; kk < 4; kk++)
+                mma_f16(tmem, desc_sw128(su32(H + kk * 32)), desc_sw128(su32(W3 + kk * 32)), id16, kk > 0 ? 1u : 0u);
+            mma_f16(tmem, desc_sw128(su32(X)), desc_sw128(su32(Wsm + 64)), id16, 1u);
+            mma_commit(&bar);
+        }
+        if (tid == 0 && !mlp_wait(&bar, ph)) tout = 1;  // one waiter; the others sleep in the barrier
+        ph ^= 1u;
+        if (__syncthreads_or(tout)) break;
+        tc_fence_after();
+        const float z = __uint_as_float(tmem_ld1(trow));
+        tc_fence_before();
+        if (e < n) {
+            if (out) {
+                const double c = fb.lam[e / fb.plane];  // Cs^2 Delta^2 of the fallback
+                nu_out[e] = c * (double)mag;
+                if (cs2_out) cs2_out[e] = (float)(c / d2);
+            } else {
+                const float cs2 = softplus(z);
+                nu_out[e] = float_bits_to_double(cs2 * d2f * mag);  // exact FP32 -> FP64 on the bits
+                if (cs2_out) cs2_out[e] = cs2;
             }
         }
     }
+    tc_fence_before();
+    __syncthreads();
+    if (tout) atomicOr(&g_mlp_err, 1u);
+    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
 // features of n points into X (row-major n x 10, FP32) for building training sets
 __global__ void k_mlp_features(Grad9 d, long n, double delta, double nu, float* __restrict__ X) {
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        double gd[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) gd[i] = d.p[i][e];
         float x[NIN];
-        point_features(d, e, (float)delta, (float)nu, x);
+        point_features(gd, (float)delta, (float)nu, x);
 #pragma unroll
         for (int i = 0; i < NIN; i++) X[e * NIN + i] = x[i];
     }
@@ -412,21 +487,31 @@ __global__ void k_mlp_adamw(float* __restrict__ prm, const float* __restrict__ g
     prm[p] = prm[p] - lr * (mh / (sqrtf(vh) + eps) + wd * prm[p]);
 }
 
-__global__ void k_mlp_pack_infer(const float* __restrict__ prm, InferWeights* __restrict__ w) {
-    for (int i = threadIdx.x; i < NH * XS; i += blockDim.x) {
-        const int j = i / XS, k = i % XS;
-        w->w1[i] = __float2bfloat16_rn(k < NIN ? prm[OFF_W1 + j * NIN + k] : 0.0f);
-    }
-    for (int i = threadIdx.x; i < NH * W2S; i += blockDim.x) {
-        const int j = i / W2S, k = i % W2S;
-        w->w2[i] = __float2bfloat16_rn(k < NH ? prm[OFF_W2 + j * NH + k] : 0.0f);
-    }
+// BF16 value v at (row, K index k) of a 128-byte-swizzled K-major image
+__device__ __forceinline__ void put_bf16(uint8_t* img, int row, int k, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(img + swz(row, k >> 3) + ((k & 7) << 1)) = __float2bfloat16_rn(v);
+}
+
+// bias b as a BF16 value and its BF16 remainder at K = k, k + 1 of row n
+__device__ __forceinline__ void put_bias(uint8_t* img, int row, int k, float b) {
+    const float h = __bfloat162float(__float2bfloat16_rn(b));
+    put_bf16(img, row, k, h);
+    put_bf16(img, row, k + 1, b - h);
+}
+
+// the parameters (FP32, flat) -> the inference images (one CTA)
+__global__ void k_mlp_pack_tc(const float* __restrict__ prm, TcWeights* __restrict__ w) {
+    uint32_t* z = reinterpret_cast<uint32_t*>(w);
+    for (int i = threadIdx.x; i < (int)(kImgBytes / 4); i += blockDim.x) z[i] = 0u;
+    __syncthreads();
+    for (int i = threadIdx.x; i < NH * NIN; i += blockDim.x) put_bf16(w->wsmall, i / NIN, i % NIN, prm[OFF_W1 + i]);
+    for (int i = threadIdx.x; i < NH * NH; i += blockDim.x) put_bf16(w->w2, i / NH, i % NH, prm[OFF_W2 + i]);
     for (int i = threadIdx.x; i < NH; i += blockDim.x) {
-        w->b1[i] = prm[OFF_B1 + i];
-        w->b2[i] = prm[OFF_B2 + i];
-        w->w3[i] = prm[OFF_W3 + i];
+        put_bias(w->wsmall, i, 10, prm[OFF_B1 + i]);
+        put_bias(w->wsmall, i, 26, prm[OFF_B2 + i]);
+        put_bf16(w->w3, 0, i, prm[OFF_W3 + i]);
     }
-    if (threadIdx.x == 0) w->b3 = prm[OFF_B3];
+    if (threadIdx.x == 0) put_bias(w->wsmall, 0, 42, prm[OFF_B3]);
 }
 
 }  // namespace
@@ -440,7 +525,7 @@ struct pade_mlp_s {
     float* part = nullptr;
     float* loss_part = nullptr;
     int part_tiles = 0;
-    InferWeights* iw = nullptr;
+    TcWeights* iw = nullptr;
     bool packed = false;
     int has_range = 0;
     int t = 0;  // AdamW step count
@@ -488,8 +573,8 @@ int pade_mlp_create(pade_mlp* out) {
     for (float** p : {&h->prm, &h->m, &h->v, &h->grad})
         if (rc == PS_OK) rc = dalloc((void**)p, sizeof(float) * NPARAM);
     if (rc == PS_OK) rc = dalloc((void**)&h->loss, sizeof(float));
-    if (rc == PS_OK) rc = dalloc((void**)&h->iw, sizeof(InferWeights));
-    if (rc == PS_OK && cudaMemset(h->iw, 0, sizeof(InferWeights)) != cudaSuccess) rc = PS_ECUDA;  // no range
+    if (rc == PS_OK) rc = dalloc((void**)&h->iw, sizeof(TcWeights));
+    if (rc == PS_OK && cudaMemset(h->iw, 0, sizeof(TcWeights)) != cudaSuccess) rc = PS_ECUDA;  // no range
     if (rc == PS_OK) {
         for (float* p : {h->prm, h->m, h->v, h->grad})
             if (cudaMemset(p, 0, sizeof(float) * NPARAM) != cudaSuccess) rc = PS_ECUDA;
@@ -575,15 +660,15 @@ int pade_mlp_features(const double* const* duidxj, long n, double delta, double 
 
 int pade_mlp_set_range(pade_mlp h, const float* lo, const float* hi) {
     if (!h || (!lo) != (!hi)) return PS_EINVAL;
-    InferWeights tmp;
+    TcWeights tmp;
     int has = lo ? 1 : 0;
     for (int i = 0; i < NIN; i++) {
         tmp.lo[i] = lo ? lo[i] : 0.0f;
         tmp.hi[i] = hi ? hi[i] : 0.0f;
         if (lo && !(lo[i] <= hi[i])) return PS_EINVAL;
     }
-    const size_t off = offsetof(InferWeights, lo);
-    const size_t bytes = sizeof(InferWeights) - off;
+    const size_t off = offsetof(TcWeights, lo);
+    const size_t bytes = sizeof(TcWeights) - off;
     tmp.has_range = has;
     if (cudaMemcpy(reinterpret_cast<char*>(h->iw) + off, reinterpret_cast<const char*>(&tmp) + off, bytes,
                    cudaMemcpyHostToDevice) != cudaSuccess)
@@ -611,13 +696,27 @@ int pade::mlp_infer_nu_fb(pade_mlp h, const double* const* duidxj, long n, doubl
         d.p[i] = duidxj[i];
     }
     if (!h->packed) {
-        k_mlp_pack_infer<<<1, 256, 0, s>>>(h->prm, h->iw);
+        k_mlp_pack_tc<<<1, 256, 0, s>>>(h->prm, h->iw);
         if (cudaGetLastError() != cudaSuccess) return PS_ECUDA;
         h->packed = true;
     }
     if (n == 0) return PS_OK;
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+            return PS_ECUDA;
+    }
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem) !=
+            cudaSuccess)
+            return PS_ECUDA;
+        attr = true;
+    }
     const long tiles = (n + TILE - 1) / TILE;
-    const unsigned g = (unsigned)std::min<long>(tiles, 152L * 8);
-    k_mlp_infer<<<g, 128, 0, s>>>(d, n, delta, nu, h->iw, nu_out, cs2_out, fb);
+    const unsigned g = (unsigned)std::min<long>(tiles, (long)nsm * kInferCtasPerSm);
+    k_mlp_infer_tc<<<g, TILE, kInferSmem, s>>>(d, n, delta, nu, h->iw, nu_out, cs2_out, fb);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }

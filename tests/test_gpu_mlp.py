@@ -2,7 +2,9 @@
 
 Tolerances: FP32 training kernels vs FP64 oracle 1e-4 (loss, gradient) and 1e-5 (AdamW
 parameters); features 1e-6; BF16 tensor-core inference 5e-3 of nu (BF16 carries 8 bits
-of mantissa; the oracle rounds operands the same way but sums in a different order).
+of mantissa; the oracle rounds operands and activations the same way but sums in a
+different order and evaluates GELU exactly, where the kernel uses BF16 arithmetic and an
+approximate tanh: about 1e-3 on these networks).
 """
 import numpy as np
 import pytest
