@@ -621,15 +621,44 @@ def extras(args, P, torch, f_host):
         nsamp = int(X.shape[0])
         del X, y
         torch.cuda.empty_cache()
+        # the closure's inference kernel alone on 256^3 points (9 FP64 gradients in, nu out)
+        n3 = 256 ** 3
+        gen = torch.Generator(device=dev).manual_seed(11)
+        grads = [torch.randn(n3, device=dev, dtype=torch.float64, generator=gen) for _ in range(9)]
+        nu_buf = torch.empty(n3, device=dev, dtype=torch.float64)
+        import ctypes as _ct
+
+        from padeops_gb300 import _lib as _L
+        from padeops_gb300.sgs_learned import _grads
+
+        garr = _grads(grads)
+
+        def infer_once():
+            _L.check(_L.lib().pade_mlp_infer_nu(clo._h, garr, n3, 2 * np.pi / 256, 1e-3,
+                                                _ct.c_void_p(nu_buf.data_ptr()), None,
+                                                _ct.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+        ms_inf = _time(torch, infer_once, 20)
+        pk_gbs, pk_src = peaks()
+        out["mlp_infer_256"] = {"ms_per_launch": ms_inf, "points": n3, "Gpts_s": n3 / ms_inf / 1e6,
+                                "bytes_per_point": 80, "achieved_GBps": n3 * 80 / ms_inf / 1e6,
+                                "frac_of_hbm_peak": n3 * 80 / ms_inf / 1e6 / pk_gbs,
+                                "peak_source": pk_src,
+                                "kernel": "k_mlp_infer_tc (tcgen05 kind::f16, BF16 operands, FP32 accumulation "
+                                          "in tensor memory; GELU on BF16 pairs)"}
+        del grads, nu_buf, garr
+        torch.cuda.empty_cache()
         # developed flow: dynamic and learned (judged every 10 steps) from seed 5, 300 steps at 64^3
         n0, nrun = 64, 300
         u, v, w = hit_initial_field(n0, seed=5)
         st64 = {}
         judge64 = {}
-        for mode in ("dynamic", "learned", "learned_planeavg"):
+        for mode in ("dynamic", "learned", "learned_planeavg", "learned_tol"):
             g1 = P.igrid()
             if mode != "dynamic":
-                g1.init(n0, n0, n0, learnedSGS=True, JudgeFreq=10, learnedPlaneAvg=mode == "learned_planeavg")
+                # learned_tol: the judge switches every point to lambda(z) while its error is above 0.25
+                g1.init(n0, n0, n0, learnedSGS=True, JudgeFreq=10, learnedPlaneAvg=mode == "learned_planeavg",
+                        JudgeTol=0.25 if mode == "learned_tol" else 0.0)
                 g1.set_mlp(clo)
             else:
                 g1.init(n0, n0, n0)
@@ -647,10 +676,13 @@ def extras(args, P, torch, f_host):
         out["les_64_developed"] = {
             "pointwise": les_stats(st64, n0),
             "plane_averaged": les_stats({"dynamic": st64["dynamic"], "learned": st64["learned_planeavg"]}, n0),
+            "judge_switch_tol_0.25": les_stats({"dynamic": st64["dynamic"], "learned": st64["learned_tol"]}, n0),
             "judge": judge64,
             "note": "closure trained a priori on the filtered 512^3 DNS; compared with the dynamic procedure from "
                     "seed 5 after 300 steps; judged every 10 steps (its lambda(z) the fallback outside the training "
-                    "range); pointwise nu = Cs^2(x) Delta^2 |S|, plane_averaged nu = <Cs^2 Delta^2>_xy |S|"}
+                    "range); pointwise nu = Cs^2(x) Delta^2 |S|, plane_averaged nu = <Cs^2 Delta^2>_xy |S|; "
+                    "judge_switch_tol_0.25: pointwise, with every point on lambda(z) while the judge's relative "
+                    "difference exceeds 0.25"}
         n = 256
         nstat = 30  # steps from the same initial field before the statistics are compared
         u, v, w = hit_initial_field(n, seed=4)

@@ -366,7 +366,9 @@ typedef struct {
                               1 sigma (sigma.F90), 2 AMD (AMD.F90); 1 and 2 with constant coefficients
                               (DynamicProcedureType 0) */
     double JudgeTol;       /* learnedSGS with JudgeFreq > 0: when the judge's relative error
-                              max_z |<Cs^2 Delta^2>_xy - lambda| / max_z lambda exceeds JudgeTol (> 0),
+                              max_z |<Cs^2 Delta^2>_xy - lambda| / max(max_z |lambda|,
+                              max_z <Cs^2 Delta^2>_xy) (0: agree, 1: one of them is zero) exceeds
+                              JudgeTol (> 0),
                               every point takes the fallback (the dynamic lambda(z)) until the next
                               judge step; 0: never.  Points whose features leave the closure's
                               training range (pade_mlp_set_range) always take the fallback. */

@@ -351,15 +351,19 @@ __global__ void k_lambda(const double* __restrict__ part, int chunks, double mea
 // the learned closure's judge: relative error of the closure's plane-averaged coefficient
 // lamL against the dynamic procedure's lambda, and the switch that sends every point to the
 // fallback while it exceeds tol (> 0)
+// The judge: relative difference of the closure's plane-averaged coefficient lamL(z) and the
+// dynamic procedure's lambda(z), max_z |lamL - lambda| / max(max_z |lambda|, max_z |lamL|)
+// (0 when both vanish, 1 when only one does); above tol every point takes lambda(z) until
+// the next judge step.
 __global__ void k_judge(const double* __restrict__ lambda, const double* __restrict__ lamL, int nz, double tol,
                         double* __restrict__ err, int* __restrict__ all) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double dm = 0.0, lm = 0.0;
     for (int k = 0; k < nz; k++) {
         dm = fmax(dm, fabs(lamL[k] - lambda[k]));
-        lm = fmax(lm, fabs(lambda[k]));
+        lm = fmax(lm, fmax(fabs(lambda[k]), fabs(lamL[k])));
     }
-    const double e = lm > 0.0 ? dm / lm : (dm > 0.0 ? INFINITY : 0.0);
+    const double e = lm > 0.0 ? dm / lm : 0.0;
     *err = e;
     *all = (tol > 0.0 && e > tol) ? 1 : 0;
 }

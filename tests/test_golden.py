@@ -136,7 +136,7 @@ def test_cuda_path_matches_golden(dir):
     assert relerr(_gpu_apply(c, 1, G["cd06_p256_f"], dir).ravel(), G["cd06_p256_oracle"]) < 1e-12
     f = P.cf90()
     assert f.init(32, False) == 0
-    assert relerr(_gpu_apply(f, 0, G["cf90_np32_f"], dir).ravel(), G["cf90_np32_oracle"]) < 1e-11
+    assert relerr(_gpu_apply(f, 0, G["cf90_np32_f"], dir).ravel(), G["cf90_np32_oracle"]) < 1e-12
     for case in _seed_cases():
         fl = G[f"seed_{case}_f"]
         n = fl.shape[0]
@@ -160,7 +160,7 @@ def test_cuda_path_matches_golden(dir):
             obj, opc = P.gaussian(), 0
             assert obj.init(n, False) == 0
         out = _gpu_apply(obj, opc, fl, dir, bc)
-        tol = 1e-10 if "_d2" in case else (1e-11 if fam == "cf90" else 1e-12)
+        tol = 1e-10 if "_d2" in case else 1e-12
         assert relerr(out, G[f"seed_{case}_oracle"]) < tol, case
 
 

@@ -68,7 +68,9 @@ def test_judge_error_and_switch_to_the_dynamic_coefficient():
     lam = g.info()["lambda"]
     lc = j["lambda_closure"]
     assert np.isfinite(lc).all() and lc.min() >= 0
-    assert j["err"] == pytest.approx(np.abs(lc - lam).max() / np.abs(lam).max(), rel=1e-12)
+    scale = max(np.abs(lam).max(), np.abs(lc).max())
+    assert j["err"] == pytest.approx(np.abs(lc - lam).max() / scale, rel=1e-12)
+    assert 0.0 <= j["err"] <= 1.0
     assert j["err"] > 1e-12
     # the switch is on after stage 1: stages 2 and 3 took lambda(z) |S| at every point
     assert j["n_fallback"] == 2 * n ** 3

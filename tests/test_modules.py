@@ -100,5 +100,5 @@ def test_filters_dispatch_matches_oracle(oracle):
     for fn, kw, ref in cases:
         fn(fd, out, **kw)
         torch.cuda.synchronize()
-        assert relerr(_host(out), ref) < 1e-11, (fn.__name__, kw)
+        assert relerr(_host(out), ref) < 1e-12, (fn.__name__, kw)
     flt.destroy()
