@@ -439,6 +439,9 @@ int pade_mlp_features(const double* const* duidxj, long n, double delta, double 
 /* nu_out = Cs^2 Delta^2 |S| per point (FP64); cs2_out (may be NULL) receives Cs^2 */
 int pade_mlp_infer_nu(pade_mlp mlp, const double* const* duidxj, long n, double delta, double nu, double* nu_out,
                       float* cs2_out, void* stream);
+/* 1 in *timed_out if an inference launch since the last call gave up waiting on its tensor
+ * cores (its outputs are then incomplete); clears the word; synchronises */
+int pade_mlp_status(int* timed_out);
 
 /* ---- host-only plan inspection (no GPU needed; never called by the entry points above) ----
  * family: 0 cd06, 1 cd10, 2 cf90, 3 gaussian, 4 cd06stagg.

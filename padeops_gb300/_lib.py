@@ -176,6 +176,7 @@ def lib():
         "pade_mlp_train_step": [vp, vp, vp, i, ctypes.c_float, ctypes.c_float, fp, vp],
         "pade_mlp_features": [pop, ctypes.c_long, d, d, vp, vp],
         "pade_mlp_infer_nu": [vp, pop, ctypes.c_long, d, d, vp, vp, vp],
+        "pade_mlp_status": [pi],
     })
     for name, args in sig.items():
         fn = getattr(L, name)

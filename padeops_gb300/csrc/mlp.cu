@@ -677,6 +677,18 @@ int pade_mlp_set_range(pade_mlp h, const float* lo, const float* hi) {
     return PS_OK;
 }
 
+int pade_mlp_status(int* timed_out) {
+    if (!timed_out) return PS_EINVAL;
+    unsigned v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_mlp_err, sizeof(unsigned)) != cudaSuccess) return PS_ECUDA;
+    *timed_out = (int)v;
+    if (v) {
+        const unsigned z = 0;
+        if (cudaMemcpyToSymbol(g_mlp_err, &z, sizeof(unsigned)) != cudaSuccess) return PS_ECUDA;
+    }
+    return PS_OK;
+}
+
 int pade_mlp_infer_nu(pade_mlp h, const double* const* duidxj, long n, double delta, double nu, double* nu_out,
                       float* cs2_out, void* stream) {
     return mlp_infer_nu_fb(h, duidxj, n, delta, nu, nu_out, cs2_out, MlpFallback{nullptr, 1, nullptr, nullptr},

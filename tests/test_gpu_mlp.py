@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import padeops_gb300 as P
+from padeops_gb300 import _lib as L
 from oracle import mlp_oracle as M
 from padeops_gb300.synthetic import hit_initial_field
 from padeops_gb300.sgs_learned import LearnedClosure, delta_les, init_params, train, training_set
@@ -68,6 +69,10 @@ def test_features_and_inference_match_oracle():
     rX, mag = M.features(d, delta, nu)
     assert relerr(X, rX) < 1e-6
     out, cs2 = c.infer_nu(dd, delta, nu, want_cs2=True)
+    import ctypes
+
+    flag = ctypes.c_int(-1)
+    assert L.lib().pade_mlp_status(ctypes.byref(flag)) == 0 and flag.value == 0  # no tensor-core wait gave up
     rcs2 = M.infer_bf16(p.astype(np.float64), rX.astype(np.float32).astype(np.float64))
     assert relerr(cs2.cpu().numpy(), rcs2) < 5e-3
     assert relerr(out.cpu().numpy(), rcs2 * delta ** 2 * mag) < 5e-3
