@@ -125,12 +125,13 @@ int pade_cd06stagg_InterpZ_C2E_cmplx(pade_op op, const double* fC, double* IfE, 
 /* ---- Pade6stagg: igrid's staggered z-operator facade (src/incompressible/PadeDerOps.F90) ----
  * replaces Pade6stagg%init(gpC, sp_gpC, gpE, sp_gpE, dz, scheme, isPeriodic) (PadeDerOps.F90:
  * 57-124) with nz = gpC%zsz(3); the x-y extents (n1, n2) of each array are given per call.
- * scheme: 1 cd06 (the compact sixth-order operators), 0 fd02 (modified wavenumbers and the
- * Poincare constant only: its operators return PADE_ENOTSUP), 2 fourierColl (PADE_ENOTSUP:
- * it needs the z transforms of spectral); other values return the reference's GracefulExit
- * codes 434 (periodic) / 323 (non-periodic).  Non-periodic objects hold the nine cd06stagg
- * objects of PadeDerOps.F90:92-110 and select one per call by (bot, top), each -1 (odd),
- * 0 (one-sided) or 1 (even), as PadeDerOps.F90:146-995; periodic objects ignore them. */
+ * scheme: 1 cd06 (the compact sixth-order operators), 0 fd02 (the second-order staggered
+ * operators of staggOps.F90, nz >= 3), 2 fourierColl (PADE_ENOTSUP: it needs the z transforms
+ * of spectral); other values return the reference's GracefulExit codes 434 (periodic) / 323
+ * (non-periodic).  Non-periodic cd06 objects hold the nine cd06stagg objects of
+ * PadeDerOps.F90:92-110 and select one per call by (bot, top), each -1 (odd), 0 (one-sided)
+ * or 1 (even), as PadeDerOps.F90:146-995; fd02 objects apply the per-code choices of the
+ * same routines' fd02 branches; periodic objects ignore the codes. */
 typedef struct pade_pade6stagg_s* pade_pade6stagg;
 int pade_pade6stagg_init(pade_pade6stagg* p, int nz, double dz, int scheme, int isPeriodic);
 int pade_pade6stagg_destroy(pade_pade6stagg p);
@@ -444,14 +445,17 @@ int pade_mlp_infer_nu(pade_mlp mlp, const double* const* duidxj, long n, double 
 int pade_mlp_status(int* timed_out);
 
 /* ---- host-only plan inspection (no GPU needed; never called by the entry points above) ----
- * family: 0 cd06, 1 cd10, 2 cf90, 3 gaussian, 4 cd06stagg.
+ * family: 0 cd06, 1 cd10, 2 cf90, 3 gaussian, 4 cd06stagg, 5 Pade6stagg's fd02 (bc1, bcn =
+ * the boundary codes bot, top; opcodes as pade_apply's staggered operations).
  * params: cd06/cd10 {n, dx, periodic}; cf90/gaussian {n, periodic};
- *         cd06stagg {n, dx, periodic, isTopEven, isBotEven, isTopSided, isBotSided}. */
+ *         cd06stagg {n, dx, periodic, isTopEven, isBotEven, isTopSided, isBotSided};
+ *         fd02 {nz, dz, periodic}. */
 #define PADE_FAMILY_CD06 0
 #define PADE_FAMILY_CD10 1
 #define PADE_FAMILY_CF90 2
 #define PADE_FAMILY_GAUSSIAN 3
 #define PADE_FAMILY_CD06STAGG 4
+#define PADE_FAMILY_FD02 5
 /* Apply the device plan's arithmetic (banded LU + cyclic correction) in FP64 on the CPU to
  * `nlines` contiguous lines; lets tests validate operator plans without a GPU. */
 int pade_plan_check(int family, const double* params, int opcode, int bc1, int bcn, const double* f, double* out,

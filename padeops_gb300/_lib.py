@@ -31,7 +31,7 @@ PATH_DF = 0
 PATH_NATIVE = 1
 PATH_FP32 = 2
 
-FAMILY = {"cd06": 0, "cd10": 1, "cf90": 2, "gaussian": 3, "cd06stagg": 4}
+FAMILY = {"cd06": 0, "cd10": 1, "cf90": 2, "gaussian": 3, "cd06stagg": 4, "fd02": 5}
 STAGG_OPS = ("ddz_E2C", "ddz_C2E", "ddz_C2C", "ddz_E2E", "d2dz2_C2C", "d2dz2_E2E", "InterpZ_E2C", "InterpZ_C2E")
 # Pade6stagg operations in pade_pade6stagg_apply's numbering
 PADE6_OPS = ("ddz_C2E", "ddz_E2C", "interpz_C2E", "interpz_E2C", "d2dz2_C2C", "d2dz2_E2E")

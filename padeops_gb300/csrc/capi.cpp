@@ -34,6 +34,7 @@ int define(int family, int n, double dx, int periodic, const StaggCfg& sc, int o
     case F_CF90: return def_cf90(n, periodic != 0, bc1, bcn, d);
     case F_GAUSS: return def_gaussian(n, periodic != 0, bc1, bcn, d);
     case F_STAGG: return def_stagg(sc, opcode, d);
+    case F_FD02: return def_fd02(n, dx, periodic != 0, bc1, bcn, opcode, d);
     }
     return PS_EINVAL;
 }
@@ -227,7 +228,7 @@ int apply(pade_op h, int opcode, int dir, int cplx, const void* f, void* out, in
     if (!h) return PS_EINVAL;
     if (dir < 1 || dir > 3 || na < 0 || nb < 0) return PS_EINVAL;
     if (path < PATH_DF || path > PATH_FP32) return PS_EINVAL;
-    if (h->family == F_CD10 || h->family == F_CF90 || h->family == F_GAUSS) {
+    if (h->family == F_CD10 || h->family == F_CF90 || h->family == F_GAUSS || h->family == F_FD02) {
         if (!bc_valid(bc1) || !bc_valid(bcn)) return PS_EREF_BC;
     } else {
         bc1 = bcn = 0;
@@ -417,6 +418,34 @@ static int stagg_init(pade_op* op, const StaggCfg& c) {
     }
     return finish_init(h, op);
 }
+}  // extern "C"
+
+int pade::fd02_init(pade_op* op, int nz, double dz, int periodic) {
+    if (!op) return PS_EINVAL;
+    *op = nullptr;
+    if (!(dz > 0.0) || nz < 3) return PS_EINVAL;
+    auto* h = new pade_op_s();
+    h->family = F_FD02;
+    h->n = nz;
+    h->dx = dz;
+    h->periodic = periodic ? 1 : 0;
+    const int ops[6] = {D1_E2C, D1_C2E, D2_C2C, D2_E2E, I_E2C, I_C2E};
+    for (int o : ops) {
+        for (int b = -1; b <= 1; b++)
+            for (int t = -1; t <= 1; t++) {
+                if (h->periodic && (b != 0 || t != 0)) continue;  // periodic calls use codes (0, 0)
+                const int rc = add_plan(h, o, b, t);
+                if (rc != PS_OK) {
+                    delete h;
+                    return rc;
+                }
+            }
+    }
+    return finish_init(h, op);
+}
+
+extern "C" {
+
 int pade_cd06stagg_init_periodic(pade_op* op, int n, double dx) {
     StaggCfg c;
     c.n = n;
@@ -530,6 +559,7 @@ static int host_def(int family, const double* p, int opcode, int bc1, int bcn, O
     int periodic = 1;
     if (family == F_CD06 || family == F_CD10) { dx = p[1]; periodic = (int)p[2]; }
     else if (family == F_CF90 || family == F_GAUSS) periodic = (int)p[1];
+    else if (family == F_FD02) { dx = p[1]; periodic = (int)p[2]; }
     else if (family == F_STAGG) {
         sc.n = n;
         sc.dx = p[1];

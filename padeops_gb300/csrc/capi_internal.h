@@ -11,7 +11,7 @@
 
 namespace pade {
 
-enum Family { F_CD06 = 0, F_CD10 = 1, F_CF90 = 2, F_GAUSS = 3, F_STAGG = 4 };
+enum Family { F_CD06 = 0, F_CD10 = 1, F_CF90 = 2, F_GAUSS = 3, F_STAGG = 4, F_FD02 = 5 };
 
 inline int bcid(int bc) { return bc == 0 ? 0 : (bc == 1 ? 1 : 2); }
 inline bool bc_valid(int bc) { return bc == 0 || bc == 1 || bc == -1; }
@@ -28,6 +28,10 @@ int pipe_chunks();
 namespace pade {
 // frees the dense (tensor-core path) matrices cached for a handle (dense_tc.cu)
 void dense_release(const void* h);
+// Pade6stagg's fd02 operators on nz cells (capi.cpp): one handle holding every operator for
+// every boundary-code pair (bot, top) in {-1, 0, 1}^2 (passed as pade_apply's bc1, bc2), or
+// the periodic operators
+int fd02_init(struct pade_op_s** op, int nz, double dz, int periodic);
 }  // namespace pade
 
 struct pade_op_s {

@@ -685,6 +685,100 @@ int def_stagg(const StaggCfg& c, int op, OpDef& o) {
 
 // Dense nout x m matrix of the operator (A^-1 B with copied rows), by band elimination in
 // long double on the dense B.  Host-side only; O(ns * q * m).
+// Pade6stagg fd02 (PadeDerOps.F90:146-995, fd02 branches) over staggOps (staggOps.F90:54-448).
+// Every operator is explicit (q = 0), written row by row on the true input/output lengths
+// (cells n, edges n + 1), the periodic wrap as explicit column indices.
+int def_fd02(int n, double dz, bool periodic, int bot, int top, int op, OpDef& o) {
+    if (n < 3) return PS_EINVAL;
+    const bool inE = (op == D1_E2C || op == D2_E2E || op == I_E2C);
+    const bool outE = (op == D1_C2E || op == D2_E2E || op == I_C2E);
+    if (op != D1_E2C && op != D1_C2E && op != D2_C2C && op != D2_E2E && op != I_E2C && op != I_C2E) return PS_ENOTSUP;
+    o = OpDef();
+    o.m = inE ? n + 1 : n;
+    o.nout = outE ? n + 1 : n;
+    o.ns = o.nout;
+    o.q = 0;
+    o.cyclic = false;
+    o.rhs.assign(o.ns, LinForm());
+    o.lhs.assign(o.ns, {0, 0, 1, 0, 0});
+    auto F = [](int i) { return LinForm(i - 1, 1.0); };  // 1-based
+    auto R = [&](int i) -> LinForm& { return o.rhs[i - 1]; };
+    const double dzi = 1.0 / dz, dzi2 = 1.0 / (dz * dz);
+    const bool codes = bot >= -1 && bot <= 1 && top >= -1 && top <= 1;
+    switch (op) {
+    case D1_E2C:  // staggOps.F90:54-64; the same operator for every (bot, top) (PadeDerOps.F90:583-585)
+        for (int i = 1; i <= n; i++) R(i) = dzi * (F(i + 1) - F(i));
+        o.io = {0, 1};
+        o.ic = {-dzi, dzi};
+        break;
+    case I_E2C:  // staggOps.F90:390-399
+        for (int i = 1; i <= n; i++) R(i) = 0.5 * (F(i) + F(i + 1));
+        o.io = {0, 1};
+        o.ic = {0.5, 0.5};
+        break;
+    case D1_C2E: {  // staggOps.F90:78-107; evenness flags of PadeDerOps.F90:419-445
+        for (int i = 2; i <= n; i++) R(i) = dzi * (F(i) - F(i - 1));
+        if (periodic) {
+            R(1) = dzi * (F(1) - F(n));
+            R(n + 1) = R(1);
+        } else {
+            if (!codes) return zero_op(o, n, false), o.m = n, o.nout = n + 1, o.ns = n + 1, PS_OK;
+            const bool be = bot != -1, te = top == 1 || (top == 0 && bot == -1);
+            R(1) = be ? LinForm() : (2.0 * dzi) * F(1);
+            R(n + 1) = te ? LinForm() : (-2.0 * dzi) * F(n);
+        }
+        o.io = {-1, 0};
+        o.ic = {-dzi, dzi};
+        break;
+    }
+    case I_C2E: {  // staggOps.F90:431-448 with the overrides of PadeDerOps.F90:703-738
+        for (int i = 2; i <= n; i++) R(i) = 0.5 * (F(i - 1) + F(i));
+        if (periodic) {
+            R(1) = 0.5 * (F(1) + F(n));
+            R(n + 1) = R(1);
+        } else {
+            if (!codes) return zero_op(o, n, false), o.m = n, o.nout = n + 1, o.ns = n + 1, PS_OK;
+            // bottom: -1 the zero BotVal, 0 2 f1 - e2 (one-sided), 1 f1; top likewise
+            R(1) = bot == -1 ? LinForm() : (bot == 0 ? 2.0 * F(1) - 0.5 * (F(1) + F(2)) : F(1));
+            R(n + 1) = top == -1 ? LinForm() : (top == 0 ? 2.0 * F(n) - 0.5 * (F(n - 1) + F(n)) : F(n));
+        }
+        o.io = {-1, 0};
+        o.ic = {0.5, 0.5};
+        break;
+    }
+    case D2_C2C: {  // staggOps.F90:235-264 (the interior reads f(k-1), f(k), f(k+1)); PadeDerOps.F90:159-183
+        for (int i = 2; i <= n - 1; i++) R(i) = dzi2 * (F(i + 1) - 2.0 * F(i) + F(i - 1));
+        if (periodic) {
+            R(1) = dzi2 * (F(2) - 2.0 * F(1) + F(n));
+            R(n) = dzi2 * (F(1) - 2.0 * F(n) + F(n - 1));
+        } else {
+            if (!codes || bot == 0 || top == 0) return zero_op(o, n, false), PS_OK;
+            R(1) = dzi2 * (bot == 1 ? F(2) - F(1) : F(2) - 3.0 * F(1));
+            R(n) = dzi2 * (top == 1 ? F(n - 1) - F(n) : F(n - 1) - 3.0 * F(n));
+        }
+        o.io = {-1, 0, 1};
+        o.ic = {dzi2, -2.0 * dzi2, dzi2};
+        break;
+    }
+    case D2_E2E: {  // staggOps.F90:297-326; PadeDerOps.F90:283-312
+        const int nE = n + 1;
+        for (int i = 2; i <= nE - 1; i++) R(i) = dzi2 * (F(i + 1) - 2.0 * F(i) + F(i - 1));
+        if (periodic) {
+            R(1) = dzi2 * (F(2) - 2.0 * F(1) + F(nE - 1));
+            R(nE) = dzi2 * (F(2) - 2.0 * F(nE) + F(nE - 1));
+        } else {
+            if (!codes || bot == 0 || top == 0) return zero_op(o, nE, false), PS_OK;
+            R(1) = bot == 1 ? (2.0 * dzi2) * (F(2) - F(1)) : LinForm();
+            R(nE) = top == 1 ? (2.0 * dzi2) * (F(nE - 1) - F(nE)) : LinForm();
+        }
+        o.io = {-1, 0, 1};
+        o.ic = {dzi2, -2.0 * dzi2, dzi2};
+        break;
+    }
+    }
+    return PS_OK;
+}
+
 int dense_operator(const OpDef& d, std::vector<double>& M) {
     M.assign((size_t)d.nout * d.m, 0.0);
     if (d.zero) return PS_OK;

@@ -79,6 +79,11 @@ struct StaggCfg {
     bool periodic = true, topEven = false, botEven = false, topSided = false, botSided = false;
 };
 int def_stagg(const StaggCfg& cfg, int op, OpDef& out);
+// Pade6stagg's second-order staggered scheme (fd02: staggOps.F90 operators selected as
+// PadeDerOps.F90 does per boundary-code pair (bot, top), each -1, 0 or 1; periodic lines
+// ignore the codes).  op: D1_E2C, D1_C2E, D2_C2C, D2_E2E, I_E2C, I_C2E (StaggOp numbering);
+// combinations the reference has no operator for give the zero operator.
+int def_fd02(int n, double dz, bool periodic, int bot, int top, int op, OpDef& out);
 
 // Dense restatement of an operator (nout x m matrix of A^-1 B including copied rows),
 // used by host-side tests and by the dense tensor-core path.  Returns 0 on success.

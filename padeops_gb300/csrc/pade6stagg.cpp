@@ -1,26 +1,34 @@
 // Pade6stagg: igrid's staggered z-operator facade (src/incompressible/PadeDerOps.F90).
 //
-// Periodic lines use one periodic cd06stagg object; non-periodic lines hold the nine
-// cd06stagg objects of PadeDerOps.F90:92-110 and pick one per call from the boundary codes
-// (bot, top), each -1 (odd), 0 (one-sided) or 1 (even), as PadeDerOps.F90:146-995 do.  The
-// second derivatives have no one-sided variant: like the reference, a 0 (or any code outside
-// {-1, 0, 1}) gives a zero output.  Only the sixth-order compact scheme (scheme 1) has
-// operators here; the second-order scheme (0) keeps its modified wavenumbers and Poincare
-// constant, and its operators return PADE_ENOTSUP.
+// Scheme cd06 (1): periodic lines use one periodic cd06stagg object; non-periodic lines hold
+// the nine cd06stagg objects of PadeDerOps.F90:92-110 and pick one per call from the
+// boundary codes (bot, top), each -1 (odd), 0 (one-sided) or 1 (even), as
+// PadeDerOps.F90:146-995 do.  The second derivatives have no one-sided variant: like the
+// reference, a 0 (or any code outside {-1, 0, 1}) gives a zero output.
+// Scheme fd02 (0): the second-order staggered operators of staggOps.F90, with the per-code
+// choices of PadeDerOps.F90's fd02 branches, in one handle (operators.cpp def_fd02); its
+// ddz_E2C and interpz_E2C ignore the codes, as the reference's do.
+// Scheme fourierColl (2) needs the spectral z transforms of a spectral object and returns
+// PADE_ENOTSUP.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "../../include/padeops_gb300.h"
+#include "capi_internal.h"
 
 struct pade_pade6stagg_s {
     int nz = 0, scheme = 1, periodic = 1;
     double dz = 1.0;
     pade_op per = nullptr;   // periodic object
     pade_op der[3][3] = {};  // non-periodic objects, [bot + 1][top + 1]
+    pade_op fd = nullptr;    // fd02: every operator and code pair, built at the first call
+    std::mutex mu;
     ~pade_pade6stagg_s() {
         if (per) pade_destroy(per);
+        if (fd) pade_destroy(fd);
         for (auto& r : der)
             for (auto& o : r)
                 if (o) pade_destroy(o);
@@ -76,6 +84,10 @@ int pade_pade6stagg_init(pade_pade6stagg* out, int nz, double dz, int scheme, in
     h->dz = dz;
     h->scheme = scheme;
     h->periodic = isPeriodic ? 1 : 0;
+    if (scheme == kFD02 && nz < 3) {
+        delete h;
+        return PADE_EINVAL;
+    }
     if (scheme == kCD06) {
         int rc = PADE_OK;
         if (h->periodic) {
@@ -106,13 +118,36 @@ int pade_pade6stagg_destroy(pade_pade6stagg p) {
 int pade_pade6stagg_apply(pade_pade6stagg p, int op, int is_complex, const double* in, double* out, int n1, int n2,
                           int bot, int top, void* stream) {
     if (!p || op < 0 || op > 5 || n1 < 0 || n2 < 0) return PADE_EINVAL;
-    if (p->scheme != kCD06) return PADE_ENOTSUP;
+    if (p->scheme != kCD06 && p->scheme != kFD02) return PADE_ENOTSUP;
     if (n1 == 0 || n2 == 0) return PADE_OK;
     if (!in || !out) return PADE_EINVAL;
+    const bool codes = bot >= -1 && bot <= 1 && top >= -1 && top <= 1;
+    if (p->scheme == kFD02) {
+        {
+            std::lock_guard<std::mutex> lock(p->mu);
+            if (!p->fd) {
+                const int rc = pade::fd02_init(&p->fd, p->nz, p->dz, p->periodic);
+                if (rc != PADE_OK) return rc;
+            }
+        }
+        int b = 0, t = 0;
+        if (!p->periodic) {
+            if (op == 1 || op == 3) {
+                b = t = 1;  // ddz_E2C, interpz_E2C: one operator whatever the codes
+            } else if (codes) {
+                b = bot;
+                t = top;
+            } else {
+                b = 2;  // no operator: zero output below
+            }
+        }
+        if (b != 2) return pade_apply(p->fd, kStaggOpcode[op], 3, is_complex ? 1 : 0, in, out, n1, n2, b, t,
+                                      PADE_PATH_DF, stream);
+    }
     pade_op o = p->per;
-    if (!p->periodic) {
+    if (!p->periodic || p->scheme == kFD02) {
         const bool d2 = op >= 4;
-        const bool valid = (bot >= -1 && bot <= 1 && top >= -1 && top <= 1) && !(d2 && (bot == 0 || top == 0));
+        const bool valid = p->scheme == kCD06 && codes && !(d2 && (bot == 0 || top == 0));
         if (!valid) {
             // PadeDerOps.F90: output = 0 for the combinations it has no operator for
             const int nout = (op == 0 || op == 2 || op == 5) ? p->nz + 1 : p->nz;

@@ -136,3 +136,40 @@ def test_invalid_codes_give_zero_output(oracle):
     out = np.ones((3, 2, nz + 1), order="F")
     p.ddz_C2E(f, out, 2, -1)  # bot outside {-1, 0, 1}: case default, output = 0
     assert np.all(out == 0)
+
+
+# ---- the second-order scheme (fd02: staggOps.F90 through PadeDerOps.F90's fd02 branches) ----
+FD02_INDEX = {"ddz_C2E": 0, "ddz_E2C": 1, "interpz_C2E": 2, "interpz_E2C": 3, "d2dz2_C2C": 4, "d2dz2_E2E": 5}
+
+
+@pytest.mark.parametrize("periodic", [False, True], ids=["walls", "periodic"])
+@pytest.mark.parametrize("cplx", [False, True], ids=["real", "cmplx"])
+@pytest.mark.parametrize("name", list(OPS))
+def test_fd02_every_code_pair(name, cplx, periodic):
+    from oracle import fd02_oracle as FO
+
+    nz, n1, n2 = 40, 5, 4
+    dz = 1.0 / nz
+    p = P.Pade6stagg()
+    assert p.init(nz, dz, P.PadeDerOps.fd02, periodic) == 0
+    _, e_in, e_out = OPS[name]
+    f = field((n1, n2, nz + (1 if e_in else 0)), 7, cplx)
+    oshape = (n1, n2, nz + (1 if e_out else 0))
+    dt = torch.complex128 if cplx else torch.float64
+    pairs = [(b, t) for b in (-1, 0, 1) for t in (-1, 0, 1)] + [(2, 1), (-1, 5)]
+    for bot, top in pairs:
+        ref = FO.apply(FD02_INDEX[name], f, dz, periodic, bot, top)
+        out = torch.full(tuple(reversed(oshape)), 7.0, dtype=dt, device="cuda")
+        getattr(p, name)(to_dev(f), out, bot, top)
+        torch.cuda.synchronize()
+        got = to_host(out)
+        if not np.any(ref):
+            assert np.all(got == 0), (bot, top)
+        else:
+            assert relerr(got, ref) < tol(name, f, ref, dz), (bot, top)
+    # host buffers through the named C entry point
+    ref = FO.apply(FD02_INDEX[name], f, dz, periodic, 1, -1)
+    out = np.zeros(oshape, dtype=f.dtype, order="F")
+    getattr(p, name)(f, out, 1, -1)
+    assert relerr(out, ref) < tol(name, f, ref, dz) if np.any(ref) else np.all(out == 0)
+    p.destroy()

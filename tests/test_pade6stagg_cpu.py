@@ -15,11 +15,7 @@ def test_fd02_modified_wavenumbers_and_constants():
     k = np.linspace(0, np.pi / dz, 17)
     assert np.allclose(p.getModifiedWavenumbers(k), 2 * np.sin(k * dz / 2) / dz, rtol=1e-15, atol=0)
     assert p.getApproxPoincareConstant() == 1.0 / np.sqrt(3.0)
-    f = np.zeros((2, 2, 40), order="F")
-    out = np.zeros((2, 2, 41), order="F")
-    with pytest.raises(L.PadeError) as e:
-        p.ddz_C2E(f, out, 0, 0)
-    assert e.value.code == L.PADE_ENOTSUP
+    assert P.Pade6stagg().init(2, dz, P.PadeDerOps.fd02, False) == L.PADE_EINVAL  # fd02 needs nz >= 3
 
 
 def test_init_error_codes():
