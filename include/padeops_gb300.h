@@ -126,9 +126,10 @@ int pade_cd06stagg_InterpZ_C2E_cmplx(pade_op op, const double* fC, double* IfE, 
  * replaces Pade6stagg%init(gpC, sp_gpC, gpE, sp_gpE, dz, scheme, isPeriodic) (PadeDerOps.F90:
  * 57-124) with nz = gpC%zsz(3); the x-y extents (n1, n2) of each array are given per call.
  * scheme: 1 cd06 (the compact sixth-order operators), 0 fd02 (the second-order staggered
- * operators of staggOps.F90, nz >= 3), 2 fourierColl (PADE_ENOTSUP: it needs the z transforms
- * of spectral); other values return the reference's GracefulExit codes 434 (periodic) / 323
- * (non-periodic).  Non-periodic cd06 objects hold the nine cd06stagg objects of
+ * operators of staggOps.F90, nz >= 3), 2 fourierColl (periodic only, as the reference: the
+ * spectral layer's z operators of spectral.F90:365-700; nz a power of two, otherwise
+ * PADE_ENOTSUP; device arrays only); other values return the reference's GracefulExit codes
+ * 434 (periodic) / 323 (non-periodic).  Non-periodic cd06 objects hold the nine cd06stagg objects of
  * PadeDerOps.F90:92-110 and select one per call by (bot, top), each -1 (odd), 0 (one-sided)
  * or 1 (even), as PadeDerOps.F90:146-995; fd02 objects apply the per-code choices of the
  * same routines' fd02 branches; periodic objects ignore the codes. */

@@ -226,3 +226,25 @@ def poisson_periodic(rhs, dx, dy, dz, modk=(None, None, None)):
     R = R * (-1.0 / (kabs + 1e-20))
     R[0, 0, 0] = 0.0
     return np.fft.irfft(np.fft.ifft(np.fft.ifft(R, axis=2), axis=1), n=nx, axis=0)
+
+
+def fourier_coll(op, f, nz, dz):
+    """Pade6stagg's fourierColl scheme: the spectral layer's periodic-z operators
+    (spectral.F90:365-700, factors from its init 843-856).  op in Pade6stagg order (0 ddz_C2E,
+    1 ddz_E2C, 2 interpz_C2E, 3 interpz_E2C, 4 d2dz2_C2C, 5 d2dz2_E2E); f Fortran-shaped with z
+    last (nz cells or nz + 1 edges, of which the first nz planes are transformed).  Real input:
+    r2c, modes 0 .. nz/2 - 1 multiplied (the Nyquist mode passes), c2r; complex input: c2c,
+    every mode multiplied; edge outputs repeat plane 0 as plane nz."""
+    k = GetWaveNums(nz, dz)
+    em, ep = np.exp(-1j * k * dz / 2.0), np.exp(1j * k * dz / 2.0)
+    fac = {0: 1j * k * em, 1: 1j * k * ep, 2: em, 3: ep, 4: -(k ** 2), 5: -(k ** 2)}[op]
+    x = np.asarray(f)[..., :nz]
+    if np.iscomplexobj(x):
+        out = np.fft.ifft(np.fft.fft(x, axis=-1) * fac, axis=-1)
+    else:
+        X = np.fft.rfft(x, axis=-1)
+        X[..., :nz // 2] *= fac[:nz // 2]
+        out = np.fft.irfft(X, n=nz, axis=-1)
+    if op in (0, 2, 5):
+        out = np.concatenate([out, out[..., :1]], axis=-1)
+    return out

@@ -8,8 +8,9 @@
 // Scheme fd02 (0): the second-order staggered operators of staggOps.F90, with the per-code
 // choices of PadeDerOps.F90's fd02 branches, in one handle (operators.cpp def_fd02); its
 // ddz_E2C and interpz_E2C ignore the codes, as the reference's do.
-// Scheme fourierColl (2) needs the spectral z transforms of a spectral object and returns
-// PADE_ENOTSUP.
+// Scheme fourierColl (2), periodic only (the reference's GracefulExit 323 otherwise): the
+// spectral layer's periodic-z operators (fourier_coll.cu), for nz a power of two, on device
+// arrays only (the spectral layer's rule).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -18,6 +19,7 @@
 
 #include "../../include/padeops_gb300.h"
 #include "capi_internal.h"
+#include "spectral_internal.h"
 
 struct pade_pade6stagg_s {
     int nz = 0, scheme = 1, periodic = 1;
@@ -25,10 +27,12 @@ struct pade_pade6stagg_s {
     pade_op per = nullptr;   // periodic object
     pade_op der[3][3] = {};  // non-periodic objects, [bot + 1][top + 1]
     pade_op fd = nullptr;    // fd02: every operator and code pair, built at the first call
+    pade::FourierColl* fc = nullptr;  // fourierColl: mode factors, built at the first call
     std::mutex mu;
     ~pade_pade6stagg_s() {
         if (per) pade_destroy(per);
         if (fd) pade_destroy(fd);
+        if (fc) pade::fourier_coll_destroy(fc);
         for (auto& r : der)
             for (auto& o : r)
                 if (o) pade_destroy(o);
@@ -78,7 +82,10 @@ int pade_pade6stagg_init(pade_pade6stagg* out, int nz, double dz, int scheme, in
     if (!(dz > 0.0) || nz < 1) return PADE_EINVAL;
     if (scheme != kFD02 && scheme != kCD06 && scheme != kFourier)
         return isPeriodic ? 434 : 323;  // PadeDerOps.F90:83, 118 GracefulExit codes
-    if (scheme == kFourier) return isPeriodic ? PADE_ENOTSUP : 323;  // needs spectral z transforms
+    if (scheme == kFourier) {
+        if (!isPeriodic) return 323;                                      // PadeDerOps.F90:118
+        if (nz < 2 || nz > 8192 || (nz & (nz - 1)) != 0) return PADE_ENOTSUP;  // FFT lengths
+    }
     auto* h = new pade_pade6stagg_s();
     h->nz = nz;
     h->dz = dz;
@@ -118,9 +125,19 @@ int pade_pade6stagg_destroy(pade_pade6stagg p) {
 int pade_pade6stagg_apply(pade_pade6stagg p, int op, int is_complex, const double* in, double* out, int n1, int n2,
                           int bot, int top, void* stream) {
     if (!p || op < 0 || op > 5 || n1 < 0 || n2 < 0) return PADE_EINVAL;
-    if (p->scheme != kCD06 && p->scheme != kFD02) return PADE_ENOTSUP;
     if (n1 == 0 || n2 == 0) return PADE_OK;
     if (!in || !out) return PADE_EINVAL;
+    if (p->scheme == kFourier) {
+        {
+            std::lock_guard<std::mutex> lock(p->mu);
+            if (!p->fc) {
+                const int rc = pade::fourier_coll_create(p->nz, p->dz, &p->fc);
+                if (rc != PADE_OK) return rc;
+            }
+        }
+        return pade::fourier_coll_apply(p->fc, op, is_complex ? 1 : 0, in, out, n1, n2,
+                                        static_cast<cudaStream_t>(stream));
+    }
     const bool codes = bot >= -1 && bot <= 1 && top >= -1 && top <= 1;
     if (p->scheme == kFD02) {
         {
@@ -184,6 +201,10 @@ P6(pade_pade6stagg_d2dz2_E2E_cmplx, 5, 1)
 int pade_pade6stagg_getModifiedWavenumbers(pade_pade6stagg p, const double* k, double* kp, int n) {
     if (!p || n < 0 || (n > 0 && (!k || !kp))) return PADE_EINVAL;
     if (p->scheme == kCD06) return pade_modified_wavenumbers_cd06stagg(k, n, p->dz, kp);
+    if (p->scheme == kFourier) {  // PadeDerOps.F90:1004-1005: kp = k
+        for (int i = 0; i < n; i++) kp[i] = k[i];
+        return PADE_OK;
+    }
     // getmodFD02stagg (PadeDerOps.F90:1055-1074): alpha = beta = b = c = 0, a = 1
     for (int i = 0; i < n; i++) {
         const double w = k[i] * p->dz;

@@ -65,6 +65,15 @@ constexpr int kMaxPartials = 152 * 8;
 std::vector<double> wavenums(int n, double dx);
 void modk_cd06stagg(const double* k, int n, double dx, double* kp);
 bool device_ptr(const void* p);
+
+// Pade6stagg's Fourier-collocation z operators (fourier_coll.cu): op in Pade6stagg order
+// (0 ddz_C2E, 1 ddz_E2C, 2 interpz_C2E, 3 interpz_E2C, 4 d2dz2_C2C, 5 d2dz2_E2E) on device
+// arrays of (n1, n2) lines; nz a power of two (PADE_ENOTSUP otherwise)
+struct FourierColl;
+int fourier_coll_create(int nz, double dz, FourierColl** out);
+void fourier_coll_destroy(FourierColl* fc);
+int fourier_coll_apply(FourierColl* fc, int op, int cplx, const double* in, double* out, int n1, int n2,
+                       cudaStream_t s);
 unsigned grid_for(long n);
 int dalloc(void** p, size_t bytes);
 // copy a host vector into a new device array

@@ -173,3 +173,31 @@ def test_fd02_every_code_pair(name, cplx, periodic):
     getattr(p, name)(f, out, 1, -1)
     assert relerr(out, ref) < tol(name, f, ref, dz) if np.any(ref) else np.all(out == 0)
     p.destroy()
+
+
+# ---- Fourier collocation in z (periodic; spectral.F90's z operators) ----
+@pytest.mark.parametrize("nz", [32, 256])
+@pytest.mark.parametrize("cplx", [False, True], ids=["real", "cmplx"])
+@pytest.mark.parametrize("name", list(OPS))
+def test_fourier_collocation(name, cplx, nz):
+    n1, n2 = 6, 5
+    dz = 2 * np.pi / nz
+    p = P.Pade6stagg()
+    assert p.init(nz, dz, P.PadeDerOps.fourierColl, True) == 0
+    _, e_in, e_out = OPS[name]
+    rng = np.random.default_rng(nz + 3 * cplx)
+    z = np.arange(nz + (1 if e_in else 0)) * dz
+    f = np.cos(3 * z)[None, None, :] + 0.3 * np.sin(7 * z + rng.standard_normal((n1, n2, 1))) + \
+        0.01 * rng.standard_normal((n1, n2, z.size))
+    if cplx:
+        f = f + 1j * (np.sin(2 * z)[None, None, :] + 0.01 * rng.standard_normal((n1, n2, z.size)))
+    f = np.asfortranarray(f)
+    ref = SO.fourier_coll(FD02_INDEX[name], f, nz, dz)
+    dt = torch.complex128 if cplx else torch.float64
+    out = torch.zeros(tuple(reversed(ref.shape)), dtype=dt, device="cuda")
+    for bot, top in ((0, 0), (-1, 1), (9, 9)):  # periodic: the codes are ignored
+        getattr(p, name)(to_dev(f), out, bot, top)
+        torch.cuda.synchronize()
+        assert relerr(to_host(out), ref) < 1e-12, (bot, top)
+    assert np.allclose(p.getModifiedWavenumbers(SO.GetWaveNums(nz, dz)), SO.GetWaveNums(nz, dz), rtol=0, atol=0)
+    assert p.getApproxPoincareConstant() == 1.0 / np.sqrt(12.0)

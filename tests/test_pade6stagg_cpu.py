@@ -22,5 +22,6 @@ def test_init_error_codes():
     assert P.Pade6stagg().init(16, 0.1, 7, True) == 434
     assert P.Pade6stagg().init(16, 0.1, 7, False) == 323
     assert P.Pade6stagg().init(16, 0.1, P.PadeDerOps.fourierColl, False) == 323
-    assert P.Pade6stagg().init(16, 0.1, P.PadeDerOps.fourierColl, True) == L.PADE_ENOTSUP
+    assert P.Pade6stagg().init(16, 0.1, P.PadeDerOps.fourierColl, True) == 0
+    assert P.Pade6stagg().init(24, 0.1, P.PadeDerOps.fourierColl, True) == L.PADE_ENOTSUP  # FFT lengths: 2^k
     assert P.Pade6stagg().init(16, -1.0, P.PadeDerOps.cd06, True) == L.PADE_EINVAL
