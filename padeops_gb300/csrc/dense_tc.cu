@@ -107,7 +107,7 @@ template <int STAGES, bool XL>
 __global__ void __launch_bounds__(NTHR) k_dense_tf32(const double* __restrict__ f, double* __restrict__ out,
                                                     const float* __restrict__ Dh, const float* __restrict__ Dl,
                                                     int nin, int nout, const LineSet ls,
-                                                    unsigned* __restrict__ rangeflag) {
+                                                    unsigned* __restrict__ rangeflag, int resid) {
     const long nlines = ls.nlines;
     extern __shared__ uint8_t dsm_raw[];
     __shared__ uint64_t mbar[2];
@@ -265,10 +265,11 @@ __global__ void __launch_bounds__(NTHR) k_dense_tf32(const double* __restrict__ 
                     if (line >= nlines) continue;
                     const double v = float_bits_to_double(__uint_as_float(r[j]));
                     if (XL) {
-                        out[line * ls.oa + row] = v;
+                        out[line * ls.oa + row] = resid ? __ldg(f + line * ls.fa + row) - v : v;
                     } else {
                         const long a = line % ls.na, b = line / ls.na;
-                        out[a * ls.oa + b * ls.ob + (long)row * ls.op] = v;
+                        out[a * ls.oa + b * ls.ob + (long)row * ls.op] =
+                            resid ? __ldg(f + a * ls.fa + b * ls.fb + (long)row * ls.fp) - v : v;
                     }
                 }
             }
@@ -322,7 +323,7 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
 template <bool XL>
 __global__ void __launch_bounds__(WS_THREADS, 1)
     k_dense_ws(const double* __restrict__ f, double* __restrict__ out, const float* __restrict__ Dimg, int nin,
-               int nout, const LineSet ls, long ntiles, unsigned* __restrict__ rangeflag) {
+               int nout, const LineSet ls, long ntiles, unsigned* __restrict__ rangeflag, int resid) {
     constexpr int NACC = 2;  // accumulator buffers: the epilogue of a tile overlaps the next
     const long nlines = ls.nlines;
     extern __shared__ uint8_t dsm_raw[];
@@ -436,7 +437,9 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     // rows of a line (contiguous).  y, z lines: a thread holds 16 consecutive lines of one
     // row, contiguous when the lines do not wrap in a (na % 16 == 0): 16-byte stores.
     const bool vec16 = !XL && ls.oa == 1 && ls.na % 16 == 0 && ls.op % 2 == 0 && ls.ob % 2 == 0 &&
-                       (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+                       (reinterpret_cast<uintptr_t>(out) & 15) == 0 &&
+                       (!resid || (ls.fa == 1 && ls.fp % 2 == 0 && ls.fb % 2 == 0 &&
+                                   (reinterpret_cast<uintptr_t>(f) & 15) == 0));
     auto epilogue = [&](long it, int b) {
         const long l0 = tile_of(it) * NT;
         const int lq = warp & 3;
@@ -446,26 +449,38 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
                 uint32_t r[16];
                 tmem_ld16(tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(b * nout + mh * NT + cb * 16), r);
                 const long line0 = l0 + cb * 16;
+                // residual form (filters): the accumulator holds (I - D) f, the output is f minus it
                 if (XL) {
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
                         const long line = line0 + j;
-                        if (line < nlines) out[line * ls.oa + row] = float_bits_to_double(__uint_as_float(r[j]));
+                        if (line >= nlines) continue;
+                        const double v = float_bits_to_double(__uint_as_float(r[j]));
+                        out[line * ls.oa + row] = resid ? __ldg(f + line * ls.fa + row) - v : v;
                     }
                 } else if (vec16 && line0 + 16 <= nlines) {
                     const long a = line0 % ls.na, bb = line0 / ls.na;
                     double* o = out + a + bb * ls.ob + (long)row * ls.op;
+                    const double* fi = f + a + bb * ls.fb + (long)row * ls.fp;
 #pragma unroll
-                    for (int j = 0; j < 16; j += 2)
-                        *reinterpret_cast<double2*>(o + j) = make_double2(float_bits_to_double(__uint_as_float(r[j])),
-                                                                          float_bits_to_double(__uint_as_float(r[j + 1])));
+                    for (int j = 0; j < 16; j += 2) {
+                        double2 v = make_double2(float_bits_to_double(__uint_as_float(r[j])),
+                                                 float_bits_to_double(__uint_as_float(r[j + 1])));
+                        if (resid) {
+                            const double2 x = __ldg(reinterpret_cast<const double2*>(fi + j));
+                            v = make_double2(x.x - v.x, x.y - v.y);
+                        }
+                        *reinterpret_cast<double2*>(o + j) = v;
+                    }
                 } else {
 #pragma unroll
                     for (int j = 0; j < 16; j++) {
                         const long line = line0 + j;
                         if (line >= nlines) continue;
                         const long a = line % ls.na, bb = line / ls.na;
-                        out[a * ls.oa + bb * ls.ob + (long)row * ls.op] = float_bits_to_double(__uint_as_float(r[j]));
+                        const double v = float_bits_to_double(__uint_as_float(r[j]));
+                        out[a * ls.oa + bb * ls.ob + (long)row * ls.op] =
+                            resid ? __ldg(f + a * ls.fa + bb * ls.fb + (long)row * ls.fp) - v : v;
                     }
                 }
             }
@@ -572,6 +587,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
 }
 
 struct DenseMat {
+    int resid = 0;  // the matrix is I - A^-1 B of a filter in residual form (output f - M f)
     float* Dh = nullptr;
     float* Dl = nullptr;
     float* Dimg = nullptr;  // per K chunk: hi then lo, nout rows of 128 bytes, swizzled as in shared memory
@@ -609,6 +625,14 @@ int dense_for(pade_op h, int opcode, int bc1, int bcn, DenseMat** out) {
     DenseMat dm;
     dm.nin = d.m;
     dm.nout = d.nout;
+    // filters in residual form (cf90): the tensor cores apply I - A^-1 B, whose result is
+    // small next to f, and the epilogue subtracts it from f in FP64, so the FP32
+    // accumulation's rounding scales with the small part only
+    if (d.resid && d.m == d.nout) {
+        dm.resid = 1;
+        for (int i = 0; i < d.nout; i++)
+            for (int j = 0; j < d.m; j++) M[(size_t)i * d.m + j] = (i == j ? 1.0 : 0.0) - M[(size_t)i * d.m + j];
+    }
     std::vector<float> hi(M.size()), lo(M.size());
     for (size_t i = 0; i < M.size(); i++) {
         hi[i] = tf32_host(M[i]);
@@ -713,14 +737,14 @@ int pade_dense_apply(pade_op h, int opcode, int dir, const double* f, double* ou
             return PS_ECUDA;
         const long grid = std::min<long>(blocks, nsm);
         kw<<<(unsigned)grid, WS_THREADS, smem_ws, s>>>(f, out, D->Dimg, D->nin, D->nout, ls, blocks,
-                                                                 h->status);
+                                                                 h->status, D->resid);
         return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
     }
     auto kern = dir == 1 ? (stages == 2 ? k_dense_tf32<2, true> : k_dense_tf32<1, true>)
                          : (stages == 2 ? k_dense_tf32<2, false> : k_dense_tf32<1, false>);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return PS_ECUDA;
-    kern<<<(unsigned)blocks, NTHR, smem, s>>>(f, out, D->Dh, D->Dl, D->nin, D->nout, ls, h->status);
+    kern<<<(unsigned)blocks, NTHR, smem, s>>>(f, out, D->Dh, D->Dl, D->nin, D->nout, ls, h->status, D->resid);
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 

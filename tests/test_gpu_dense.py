@@ -3,7 +3,9 @@ along x (contiguous lines) and y, z (strided lines).
 
 Tolerance: 3e-6 normwise relative (max|a-b| / max|b|).  The FP32 accumulation of
 256 products bounds the error by ~2^-24 sum|D||f| and the dropped lo*lo term by
-~2^-22 |D||f|; sum|D||f| / max|D f| is O(1-10) for these operators and fields.
+~2^-22 |D||f|; sum|D||f| / max|D f| is O(1-10) for these operators and fields.  CF90 runs
+in residual form (the tensor cores apply I - D, the epilogue subtracts the result from f in
+FP64), so its error scales with the small high-pass part: 3e-7, along every direction.
 """
 import ctypes
 
@@ -62,7 +64,7 @@ def test_dense_cf90_and_nonperiodic(oracle):
     f = field(n, na, nb, 5)
     c = P.cf90()
     assert c.init(n, True) == 0
-    assert relerr(dense(c, 0, f), oracle.cf90(f, periodic=True, dir=1)) < 3e-6
+    assert relerr(dense(c, 0, f), oracle.cf90(f, periodic=True, dir=1)) < 3e-7
     z = P.cd10()
     dz = 1.0 / (n - 1)
     assert z.init(n, dz, False) == 0
@@ -133,3 +135,22 @@ def test_dense_many_tiles_per_cta(dir, n, other):
         assert bool(torch.isfinite(od).all())
         err = float((od - ref).abs().max() / ref.abs().max())
         assert err < 3e-6, (dir, order, err)
+
+
+@pytest.mark.parametrize("dir,other", [(2, (32, 9)), (3, (16, 4)), (2, (7, 5)), (3, (9, 6))])
+def test_dense_cf90_residual_strided(oracle, dir, other):
+    """CF90 in residual form along y and z, with (na % 16 == 0) and without the 16-byte
+    epilogue stores."""
+    n = 256
+    c = P.cf90()
+    assert c.init(n, True) == 0
+    shape = list(other)
+    shape.insert(dir - 1, n)
+    rng = np.random.default_rng(dir + other[0])
+    x = np.arange(n) * 2 * np.pi / n
+    prof = np.cos(3 * x) + 0.2 * np.sin(40 * x + 1.0)
+    sh = [1, 1, 1]
+    sh[dir - 1] = n
+    f = np.asfortranarray(prof.reshape(sh) + 0.01 * rng.standard_normal(shape))
+    out = dense(c, 0, f, dir=dir)
+    assert relerr(out, oracle.cf90(f, periodic=True, dir=dir)) < 3e-7
