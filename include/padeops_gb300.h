@@ -406,6 +406,21 @@ int pade_les_set_time(pade_les les, double tsim, int step);
  * entries, may be NULL) and the number of point evaluations given the fallback coefficient
  * since init; synchronises */
 int pade_les_judge_info(pade_les les, double* err, double* lambda_closure, long long* n_fallback);
+/* Scalar SGS flux divergence for a scalar T carried by the caller beside the LES
+ * (getRHS_SGS_Scalar / getQjSGS, sgsmod_igrid.F90:268-335): Trhs -= i k1 q1^ + i k2 q2^ +
+ * ddz_E2C(q3^) with q1 = -kappa dT/dx, q2 = -kappa dT/dy at the cells and q3 = -kappa dT/dz at
+ * the edges.  dynamic = 0: kappa = nu_sgs / Pr, the LES's eddy viscosity at the cells and
+ * edges as its last stage computed it.  dynamic = 1 (Smagorinsky kernel only):
+ * DoStandardDynamicProcedureScalar (standardDynamicProcedure.F90:1-71): kappa = Beta(z) |S|,
+ * Beta(z) the planar ratio <R_i P_i> / <R_i R_i> of the test-filtered fluxes, with |S|, its
+ * test-filtered value and the test-filtered velocities taken from the LES's current fields
+ * (the state the next pade_les_step starts from); Beta(z) is copied to beta1d (nz, host or
+ * device, may be NULL; synchronises).  T: physical cells (nx, ny, nz); That: its x-y spectrum
+ * (nx/2+1, ny, nz, complex); dTdxC, dTdyC, dTdzC: cells; dTdzE: edges (nx, ny, nz + 1);
+ * Trhs: spectral cells, updated in place; device pointers, ordered on stream. */
+int pade_les_scalar_sgs(pade_les les, const double* T, const void* That, const double* dTdxC, const double* dTdyC,
+                        const double* dTdzC, const double* dTdzE, void* Trhs, double Pr, int dynamic,
+                        double* beta1d, void* stream);
 /* device pointer of an internal field (PADE_LES_*), valid until pade_les_destroy */
 int pade_les_field(pade_les les, int which, void** ptr);
 /* attach the learned closure used when learnedSGS is set (the object must outlive the

@@ -277,6 +277,41 @@ class LesOracle:
         nm = np.maximum(num.sum(axis=(0, 1)) * self.meanfact, 0.0)
         self.lambda1d = nm / (den.sum(axis=(0, 1)) * self.meanfact + 1e-18)
 
+    def scalar_sgs_rhs(self, T, That, dT, dTdzE, Trhs, Pr=1.0, dynamic=False, fields=None):
+        """getRHS_SGS_Scalar / getQjSGS (sgsmod_igrid.F90:268-335) and, when dynamic,
+        DoStandardDynamicProcedureScalar (standardDynamicProcedure.F90:1-71) with
+        planarAverage_and_TakeRatio (221-244).  fields: the LES state to use, a dict with u, v,
+        wC, uhat, vhat, whatC (spectral at the cells), duidxjC (9 arrays), nuC, nuE; dT the
+        three cell gradients of T.  Returns (Trhs, Beta(z) or None)."""
+        F = fields
+        beta = None
+        if dynamic:
+            SC = self.sij(F["duidxjC"])
+            Dsgs = self.smag_kernel(SC)                       # |S| (the Smagorinsky kernel)
+            Sf = [self.test_filter_r2r(s) for s in SC]
+            Df = self.smag_kernel(Sf)                         # |S| of the filtered strain
+            G = self.GTestFilt
+            uf = [self.ifft(F["uhat"] * G), self.ifft(F["vhat"] * G), self.ifft(F["whatC"] * G)]
+            dr2 = self.deltaRat * self.deltaRat
+            dTf = [self.test_filter_r2r(g) for g in dT]                                     # step 1
+            R = [self.test_filter_r2r(Dsgs * dT[i]) - dr2 * Df * dTf[i] for i in range(3)]    # step 3
+            Tf = self.ifft(That * G)                                                          # step 4
+            U = [F["u"], F["v"], F["wC"]]
+            Pf = [self.test_filter_r2r(U[i] * T) - uf[i] * Tf for i in range(3)]              # step 5
+            num = R[0] * Pf[0] + R[1] * Pf[1] + R[2] * Pf[2]
+            den = R[0] * R[0] + R[1] * R[1] + R[2] * R[2]
+            nm = np.maximum(num.sum(axis=(0, 1)) * self.meanfact, 0.0)
+            beta = nm / (den.sum(axis=(0, 1)) * self.meanfact + 1e-18)
+            kC = Dsgs * beta[None, None, :]
+            kE = self.sz(kC, "InterpZ_C2E")                   # interpolate_kappaSGS
+        else:
+            kC, kE = F["nuC"] / Pr, F["nuE"] / Pr
+        q1, q2, q3 = -kC * dT[0], -kC * dT[1], -kE * dTdzE
+        Trhs = Trhs - self.ik1(self.fft(q1))
+        Trhs = Trhs - self.ik2(self.fft(q2))
+        Trhs = Trhs - self.sz(self.fft(q3), "ddz_E2C")
+        return Trhs, beta
+
     def sgs_rhs(self, urhs, vrhs, wrhs):
         SC = self.sij(self.duidxjC)
         SE = self.sij(self.duidxjE)

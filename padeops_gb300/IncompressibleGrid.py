@@ -140,6 +140,25 @@ class igrid:
                                        torch.cuda.current_stream().cuda_stream))
         return (t.view(torch.complex128) if cplx else t).view(shape)
 
+    def scalar_sgs(self, T, That, dTdxC, dTdyC, dTdzC, dTdzE, Trhs, Pr=1.0, dynamic=False):
+        """getRHS_SGS_Scalar (sgsmod_igrid.F90:268-335) for a scalar carried beside the LES:
+        Trhs (its x-y spectrum at the cells, complex) loses the divergence of the SGS flux
+        -kappa grad T; kappa = nu_sgs / Pr, or Beta(z) |S| from the scalar dynamic procedure
+        (standardDynamicProcedure.F90:1-71).  CUDA tensors in the layout of field(); returns
+        Beta(z) (numpy) when dynamic."""
+        beta = np.zeros(self.nz) if dynamic else None
+
+        def vp(t):
+            return ctypes.c_void_p(t.data_ptr())
+
+        bp = beta.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if dynamic else None
+        L.check(L.lib().pade_les_scalar_sgs(self.handle, vp(T), vp(That), vp(dTdxC), vp(dTdyC), vp(dTdzC),
+                                            vp(dTdzE), vp(Trhs), float(Pr), int(bool(dynamic)),
+                                            ctypes.cast(bp, ctypes.c_void_p) if dynamic else None,
+                                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                "igrid.scalar_sgs")
+        return beta
+
     def set_time(self, tsim, step):
         L.check(L.lib().pade_les_set_time(self.handle, float(tsim), int(step)), "igrid.set_time")
 

@@ -165,6 +165,7 @@ def lib():
         "pade_les_info": [vp, dp, dp, pi, dp],
         "pade_les_set_time": [vp, d, i],
         "pade_les_field": [vp, i, pop],
+        "pade_les_scalar_sgs": [vp, vp, vp, vp, vp, vp, vp, vp, d, i, vp, vp],
         "pade_les_judge_info": [vp, dp, dp, ctypes.POINTER(ctypes.c_longlong)],
         "pade_mlp_set_range": [vp, fp, fp],
         "pade_les_set_mlp": [vp, vp],

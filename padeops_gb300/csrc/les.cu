@@ -279,6 +279,30 @@ struct Ptr6 {
     const double* p[6];
 };
 
+// scalar dynamic procedure (standardDynamicProcedure.F90:57-63): num = R . P, den = R . R
+__global__ void k_num_den3(const double* __restrict__ r0, const double* __restrict__ r1,
+                           const double* __restrict__ r2, const double* __restrict__ p0,
+                           const double* __restrict__ p1, const double* __restrict__ p2, double* __restrict__ num,
+                           double* __restrict__ den, long n) {
+    GRID_STRIDE(e, n) {
+        const double a = r0[e], b = r1[e], c = r2[e];
+        num[e] = add(add(mul(a, p0[e]), mul(b, p1[e])), mul(c, p2[e]));
+        den[e] = add(add(mul(a, a), mul(b, b)), mul(c, c));
+    }
+}
+
+// kappa = beta(z) Dsgs (beta per z plane) or nu / Pr (getQjSGS, sgsmod_igrid.F90:318-326)
+__global__ void k_kappa(const double* __restrict__ a, const double* __restrict__ beta, double pr_inv, long plane,
+                        double* __restrict__ kappa, long n) {
+    GRID_STRIDE(e, n) { kappa[e] = beta ? mul(a[e], beta[e / plane]) : mul(a[e], pr_inv); }
+}
+
+// q = -kappa dT  (sgsmod_igrid.F90:330-332)
+__global__ void k_negmul(const double* __restrict__ kappa, const double* __restrict__ g, double* __restrict__ q,
+                         long n) {
+    GRID_STRIDE(e, n) { q[e] = -mul(kappa[e], g[e]); }
+}
+
 // numerator / denominator of the Germano identity (standardDynamicProcedure.F90:139-154) in
 // double-float: Lij Mij and Mij Mij with the off-diagonal products (1, 2, 4) counted twice
 __global__ void k_num_den(Ptr6 L, Ptr6 M, double* __restrict__ num, double* __restrict__ den, long n) {
@@ -527,6 +551,7 @@ struct pade_les_s {
     // dynamic procedure
     double *Sf[6] = {nullptr}, *M[6] = {nullptr}, *Lm[6] = {nullptr}, *uf[3] = {nullptr};
     double *Df = nullptr, *Dsgs = nullptr, *lambda = nullptr, *part = nullptr, *lamL = nullptr;
+    double* betaT = nullptr;  // the scalar dynamic procedure's Beta(z) (pade_les_scalar_sgs)
     double *d_dt = nullptr, *d_tsim = nullptr, *cflpart = nullptr;
     std::vector<void*> allocs;
     int step = 0, mstep = 0;
@@ -1191,6 +1216,117 @@ int pade_les_judge_info(pade_les h, double* err, double* lambda_closure, long lo
         unsigned long long c = 0;
         if (cudaMemcpy(&c, h->fbcount, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) return PS_ECUDA;
         *n_fallback = (long long)c;
+    }
+    return PS_OK;
+}
+
+int pade_les_scalar_sgs(pade_les h, const double* T, const void* That_, const double* dTdxC, const double* dTdyC,
+                        const double* dTdzC, const double* dTdzE, void* Trhs_, double Pr, int dynamic,
+                        double* beta1d, void* stream) {
+    if (!h || !h->prm.useSGS) return PS_EINVAL;
+    for (const void* q : {(const void*)T, That_, (const void*)dTdxC, (const void*)dTdyC, (const void*)dTdzC,
+                          (const void*)dTdzE, (const void*)Trhs_})
+        if (!q || !device_ptr(q)) return PS_EINVAL;
+    if (dynamic && h->prm.SGSModelID != 0) return PS_ENOTSUP;  // Dsgs is the Smagorinsky kernel
+    if (!dynamic && !(Pr > 0.0)) return PS_EINVAL;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const double2* That = static_cast<const double2*>(That_);
+    double2* Trhs = static_cast<double2*>(Trhs_);
+    const long n = h->NC, nE = h->NE;
+    const unsigned g = grid_for(n), gE = grid_for(nE), gs = grid_for(h->SC);
+    double* kC = h->rC1b;  // kappa at cells and edges (the second stream's scratch is free between steps)
+    double* kE = h->rE1b;
+    if (dynamic) {
+        // the momentum procedure's arrays (kept when the LES itself is dynamic; allocated here otherwise)
+        const size_t r8 = sizeof(double);
+        int rc = PS_OK;
+        for (int i = 0; i < 6 && rc == PS_OK; i++)
+            if (!h->Sf[i]) rc = al(h, &h->Sf[i], r8 * n);
+        for (int i = 0; i < 6 && rc == PS_OK; i++)
+            if (!h->Lm[i]) rc = al(h, &h->Lm[i], r8 * n);
+        for (int i = 0; i < 3 && rc == PS_OK; i++)
+            if (!h->uf[i]) rc = al(h, &h->uf[i], r8 * n);
+        if (rc == PS_OK && !h->Df) rc = al(h, &h->Df, r8 * n);
+        if (rc == PS_OK && !h->Dsgs) rc = al(h, &h->Dsgs, r8 * n);
+        if (rc == PS_OK && !h->part) rc = al(h, &h->part, r8 * 2 * kPlaneChunks * h->nz);
+        if (rc == PS_OK && !h->betaT) rc = al(h, &h->betaT, r8 * h->nz);
+        if (rc != PS_OK) return rc;
+        const Ptr9 dC = p9(h->dC);
+        // Dsgs = |S|, the test-filtered |S| and velocities of the current fields
+        // (standardDynamicProcedure.F90:88-105, as the momentum procedure computes them)
+        k_nu_kernel<<<g, 256, 0, s>>>(dC, h->rC2, h->Dsgs, n);
+        KCHECK();
+        for (int i = 0; i < 6; i++) {
+            k_sij<<<g, 256, 0, s>>>(dC, i, nullptr, h->rC1, n);
+            KCHECK();
+            CK(test_filter(h, h->rC1, h->Sf[i], s));
+        }
+        k_smag6<<<g, 256, 0, s>>>(h->Sf[0], h->Sf[1], h->Sf[2], h->Sf[3], h->Sf[4], h->Sf[5], h->Df, n);
+        KCHECK();
+        CK(spectral_ifft_masked(h->spC, h->uhat_cur, h->uf[0], h->tf_x, h->tf_y, s));
+        CK(spectral_ifft_masked(h->spC, h->vhat_cur, h->uf[1], h->tf_x, h->tf_y, s));
+        CK(spectral_ifft_masked(h->spC, h->whatC, h->uf[2], h->tf_x, h->tf_y, s));
+        // DoStandardDynamicProcedureScalar (standardDynamicProcedure.F90:22-68); the filtered
+        // gradients take Sf[0..2], the filtered T Sf[3], R and P the arrays Lm
+        const double dr2 = h->prm.deltaRatio * h->prm.deltaRatio;
+        const double* dT[3] = {dTdxC, dTdyC, dTdzC};
+        for (int i = 0; i < 3; i++) CK(test_filter(h, dT[i], h->Sf[i], s));
+        for (int i = 0; i < 3; i++) {
+            k_prod<<<g, 256, 0, s>>>(h->Dsgs, dT[i], h->rC1, n);
+            KCHECK();
+            CK(test_filter(h, h->rC1, h->rC2, s));
+            k_mij<<<g, 256, 0, s>>>(h->rC2, h->Df, h->Sf[i], dr2, h->Lm[i], n);
+            KCHECK();
+        }
+        CK(spectral_ifft_masked(h->spC, That, h->Sf[3], h->tf_x, h->tf_y, s));
+        const double* U[3] = {h->u, h->v, h->wC};
+        for (int i = 0; i < 3; i++) {
+            k_prod<<<g, 256, 0, s>>>(U[i], T, h->rC1, n);
+            KCHECK();
+            CK(test_filter(h, h->rC1, h->rC2, s));
+            k_lij<<<g, 256, 0, s>>>(h->rC2, h->uf[i], h->Sf[3], h->Lm[3 + i], n);
+            KCHECK();
+        }
+        k_num_den3<<<g, 256, 0, s>>>(h->Lm[0], h->Lm[1], h->Lm[2], h->Lm[3], h->Lm[4], h->Lm[5], h->rC1, h->rC2, n);
+        KCHECK();
+        dim3 grid(kPlaneChunks, h->nz);
+        k_plane_sums<<<grid, 256, 0, s>>>(h->rC1, h->rC2, h->plane, h->part);
+        KCHECK();
+        k_lambda<<<(h->nz + 127) / 128, 128, 0, s>>>(h->part, kPlaneChunks, h->meanfact, h->nz, h->betaT);
+        KCHECK();
+        // kappa = Dsgs Beta(z), interpolated to the edges (interpolate_kappaSGS, eddyViscosity.F90:120-129)
+        k_kappa<<<g, 256, 0, s>>>(h->Dsgs, h->betaT, 0.0, h->plane, kC, n);
+        KCHECK();
+        CK(zop(h, OP_I_C2E, 0, kC, kE, s));
+    } else {
+        k_kappa<<<g, 256, 0, s>>>(h->nuC, nullptr, 1.0 / Pr, h->plane, kC, n);
+        KCHECK();
+        k_kappa<<<gE, 256, 0, s>>>(h->nuE, nullptr, 1.0 / Pr, h->plane, kE, nE);
+        KCHECK();
+    }
+    // getRHS_SGS_Scalar (sgsmod_igrid.F90:282-301): Trhs -= ik1 q1hat + ik2 q2hat + ddz_E2C(q3hat)
+    const double* k1 = h->spC->d_k1;
+    const double* k2 = h->spC->d_k2;
+    k_negmul<<<g, 256, 0, s>>>(kC, dTdxC, h->rC2, n);
+    KCHECK();
+    CK(spectral_fft(h->spC, h->rC2, h->tC1, s));
+    k_sub_ik<<<gs, 256, 0, s>>>(Trhs, 1, nullptr, 0, h->tC1, k1, k2, h->nxh, h->splane, h->SC);
+    KCHECK();
+    k_negmul<<<g, 256, 0, s>>>(kC, dTdyC, h->rC2, n);
+    KCHECK();
+    CK(spectral_fft(h->spC, h->rC2, h->tC1, s));
+    k_sub_ik<<<gs, 256, 0, s>>>(Trhs, 2, nullptr, 0, h->tC1, k1, k2, h->nxh, h->splane, h->SC);
+    KCHECK();
+    k_negmul<<<gE, 256, 0, s>>>(kE, dTdzE, h->rE2, nE);
+    KCHECK();
+    CK(spectral_fft(h->spE, h->rE2, h->tE1, s));
+    CK(zop(h, OP_DDZ_E2C, 1, h->tE1, h->tC1, s));
+    k_csub2<<<gs, 256, 0, s>>>(Trhs, h->tC1, h->SC);
+    KCHECK();
+    if (beta1d && dynamic) {
+        if (cudaMemcpyAsync(beta1d, h->betaT, sizeof(double) * h->nz, cudaMemcpyDefault, s) != cudaSuccess)
+            return PS_ECUDA;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return PS_ECUDA;
     }
     return PS_OK;
 }
