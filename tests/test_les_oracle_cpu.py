@@ -127,3 +127,22 @@ def test_amd_kernel_against_contraction():
     nu = LO.amd_kernel(_grad_list(G), Sl, c)
     assert np.max(np.abs(nu - ref)) < 1e-14 * np.max(np.abs(ref))
     assert np.count_nonzero(nu) > 10 and np.count_nonzero(nu == 0) > 10  # both signs of num occur
+
+
+def test_scalar_sgs_restatement_known_answer():
+    """With a constant kappa = nu / Pr, the flux divergence of -kappa grad T adds kappa
+    d2T/dx2 to the scalar's right-hand side (a single x mode here)."""
+    from oracle.les_oracle import LesOracle
+
+    n, L_ = 16, 2 * np.pi
+    o = LesOracle(n, n, n, L_, L_, L_)
+    x = (np.arange(n) * L_ / n)[:, None, None] * np.ones((1, n, n))
+    T = np.asfortranarray(np.cos(2 * x))
+    dT = [-2 * np.sin(2 * x), np.zeros_like(x), np.zeros_like(x)]
+    nu = 0.3
+    fields = {"nuC": np.full((n, n, n), nu), "nuE": np.full((n, n, n + 1), nu)}
+    Trhs0 = np.zeros((n // 2 + 1, n, n), dtype=complex)
+    Trhs, beta = o.scalar_sgs_rhs(T, o.fft(T), dT, np.zeros((n, n, n + 1)), Trhs0, Pr=0.6, fields=fields)
+    assert beta is None
+    want = o.fft((nu / 0.6) * (-4.0) * np.cos(2 * x))
+    assert np.abs(Trhs - want).max() <= 1e-12 * np.abs(want).max()
