@@ -141,10 +141,11 @@ __global__ void __launch_bounds__(256, 3)
                     mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
                     bad |= (unsigned)(mx == 2047);  // infinity or NaN in the line
                     if (lane == 0) lexp[l] = mx;
+                    const SplitK sk = split_consts(mx - 1023);
 #pragma unroll
                     for (int u = 0; u < kStageRegs; u++) {
                         const int p = lane + 32 * u;
-                        if (u < U && p < cp.m) dst[spos<M>(p)] = df_from_double_shift(v[u], mx - 1023);
+                        if (u < U && p < cp.m) dst[spos<M>(p)] = df_split_line(v[u], sk);
                     }
                 }
             }
@@ -171,10 +172,11 @@ __global__ void __launch_bounds__(256, 3)
                     const int k = lexp[l] - 1023;
                     bad |= (unsigned)(lexp[l] == 2047);
                     V* dst = tile + l * cp.LS;
+                    const SplitK sk = split_consts(k);
 #pragma unroll
                     for (int u = 0; u < kStageRegs; u++) {
                         const int p = q0 + pstep * u;
-                        if (u < U && p < cp.m) dst[spos<M>(p)] = df_from_double_shift(v[u], k);
+                        if (u < U && p < cp.m) dst[spos<M>(p)] = df_split_line(v[u], sk);
                     }
                 }
             }
@@ -250,9 +252,10 @@ __global__ void __launch_bounds__(256, 3)
                 const int k = lexp[ll] - 1023;
                 bad |= (unsigned)(lexp[ll] == 2047);  // infinity or NaN in the line
                 V* row = tile + ll * cp.LS;
+                const SplitK sk = split_consts(k);
                 for (int p = lane; p < cp.m; p += 32) {
                     const int ps = spos<M>(p);
-                    row[ps] = df_from_double_shift(reinterpret_cast<const double*>(row)[ps], k);
+                    row[ps] = df_split_line(reinterpret_cast<const double*>(row)[ps], sk);
                 }
             }
         }

@@ -79,6 +79,37 @@ __device__ __forceinline__ dfv df_from_double_shift(double d, int k) {
     return dfv{ok ? __uint_as_float(hb) : 0.0f, ok ? lo : 0.0f};
 }
 
+// The split of df_from_double_shift for values already scaled below 2 (a line's maximum in
+// [1, 2) after the shift by k): about half the instructions.  The FP64 exponent's low 9 bits
+// and the top 23 mantissa bits are shifted together into the FP32 layout and rebased by one
+// integer add (the shifted exponent e - k - 896 lies in [53, 127], so the 9-bit field cannot
+// carry); values below 2^-74 of the maximum (and zeros) give zero.  Per-line constants:
+struct SplitK {
+    unsigned kb, kc, thr;
+};
+
+__device__ __forceinline__ SplitK split_consts(int k) {
+    SplitK s;
+    s.kb = (unsigned)(-(k + 896)) << 23;
+    s.kc = (unsigned)(-(k + 948)) << 23;
+    s.thr = (unsigned)max(949 + k, 1) << 20;
+    return s;
+}
+
+__device__ __forceinline__ dfv df_split_line(double d, const SplitK& s) {
+    const unsigned lo32 = (unsigned)__double2loint(d);
+    const unsigned hi32 = (unsigned)__double2hiint(d);
+    const unsigned sign = hi32 & 0x80000000u;
+    // mantissa top 23 bits below the low 8 exponent bits: (hi32 << 3) | (lo32 >> 29)
+    const unsigned t = __funnelshift_l(lo32, hi32, 3);
+    const unsigned hb = (t + s.kb) | sign;  // exponent e - k - 896 in [53, 127] fits the field
+    const float lf = __uint2float_rn(lo32 & 0x1FFFFFFFu);
+    const unsigned sb = ((t & 0xFF800000u) + s.kc) | sign;  // 2^(e - k - 1075), signed
+    const float lo = __fmul_rn(lf, __uint_as_float(sb));
+    const bool ok = (hi32 & 0x7FF00000u) >= s.thr;
+    return dfv{ok ? __uint_as_float(hb) : 0.0f, ok ? lo : 0.0f};
+}
+
 // float x * 2^k as an exact double (x normal; zero, subnormal x and results below the
 // normal FP64 range give 0, results above it infinity)
 __device__ __forceinline__ double float_bits_to_double_shift(float x, int k) {

@@ -51,32 +51,6 @@ struct RegParams {
 // field of the high part, kc = -(k + 948) << 23 builds the low part's power of two, thr =
 // max(949 + k, 1) << 20: values whose scaled exponent is below 2^-74, zeros and subnormals
 // give 0 (the kernels' line-relative range).  Exactly the value of df_from_double_shift.
-struct SplitK {
-    unsigned kb, kc, thr;
-};
-
-__device__ __forceinline__ SplitK split_consts(int k) {
-    SplitK s;
-    s.kb = (unsigned)(-(k + 896)) << 23;
-    s.kc = (unsigned)(-(k + 948)) << 23;
-    s.thr = (unsigned)max(949 + k, 1) << 20;
-    return s;
-}
-
-__device__ __forceinline__ dfv df_split_line(double d, const SplitK& s) {
-    const unsigned lo32 = (unsigned)__double2loint(d);
-    const unsigned hi32 = (unsigned)__double2hiint(d);
-    const unsigned sign = hi32 & 0x80000000u;
-    // mantissa top 23 bits below the low 8 exponent bits: (hi32 << 3) | (lo32 >> 29)
-    const unsigned t = __funnelshift_l(lo32, hi32, 3);
-    const unsigned hb = (t + s.kb) | sign;  // exponent e - k - 896 in [53, 127] fits the field
-    const float lf = __uint2float_rn(lo32 & 0x1FFFFFFFu);
-    const unsigned sb = ((t & 0xFF800000u) + s.kc) | sign;  // 2^(e - k - 1075), signed
-    const float lo = __fmul_rn(lf, __uint_as_float(sb));
-    const bool ok = (hi32 & 0x7FF00000u) >= s.thr;
-    return dfv{ok ? __uint_as_float(hb) : 0.0f, ok ? lo : 0.0f};
-}
-
 // Row accessor of a chunk and its halos (r in [-H, M + H); constant after unrolling).
 template <int M, int H, class V>
 __device__ __forceinline__ V row_at(const V (&x)[M], const V (&hl)[H], const V (&hr)[H], int r) {

@@ -152,10 +152,11 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
                 mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
                 bad |= (unsigned)(mx == 2047);
                 if (lane == 0) lexp[l] = mx;
+                const SplitK sk = split_consts(mx - 1023);
     #pragma unroll
                 for (int u = 0; u < kStageRegs; u++) {
                     const int p = lane + 32 * u;
-                    if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], mx - 1023);
+                    if (u < U && p < ns) tile[main_pos(l, p)] = df_split_line(v[u], sk);
                 }
             }
         } else if ((ns + nth / L - 1) / (nth / L) > kStageRegs) {
@@ -188,9 +189,10 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
             if (l < nl) {
                 const int k = lexp[l] - 1023;
                 bad |= (unsigned)(lexp[l] == 2047);
+                const SplitK sk = split_consts(k);
                 for (int p = q0; p < ns; p += pstep) {
                     const int ps = main_pos(l, p);
-                    tile[ps] = df_from_double_shift(raw[ps], k);
+                    tile[ps] = df_split_line(raw[ps], sk);
                 }
             }
         } else {
@@ -213,10 +215,11 @@ __global__ void __launch_bounds__(NT, line_min_blocks(CIRC, M, ALIAS))
             if (l < nl) {
                 const int k = lexp[l] - 1023;
                 bad |= (unsigned)(lexp[l] == 2047);
+                const SplitK sk = split_consts(k);
     #pragma unroll
                 for (int u = 0; u < kStageRegs; u++) {
                     const int p = q0 + pstep * u;
-                    if (u < U && p < ns) tile[main_pos(l, p)] = df_from_double_shift(v[u], k);
+                    if (u < U && p < ns) tile[main_pos(l, p)] = df_split_line(v[u], sk);
                 }
             }
         }
