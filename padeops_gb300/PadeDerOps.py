@@ -4,7 +4,8 @@ igrid's z-operator facade over the staggered operators.  Scheme cd06: periodic o
 one periodic cd06stagg; non-periodic objects select one of nine cd06stagg objects per call
 from the boundary codes (bot, top), each -1 (odd), 0 (one-sided) or 1 (even).  Scheme fd02:
 the second-order staggered operators (staggOps.F90) with PadeDerOps' per-code choices.
-Scheme fourierColl needs a spectral object's z transforms and is not supported.  Arrays are
+Scheme fourierColl (periodic, nz a power of two): Fourier collocation along z, each mode
+multiplied by its factor (i k, -k^2, and the half-cell shifts e^{+-i k dz/2}).  Arrays are
 Fortran-ordered (x fastest): cell fields (n1, n2, nz), edge fields (n1, n2, nz + 1), real
 float64 or complex128, as CUDA torch tensors (asynchronous on the current stream) or host
 numpy arrays (staged by the library).  The x-y extents are taken from the arrays.

@@ -133,9 +133,30 @@ int pipe_chunks() {
     static const int n = [] {
         const char* e = std::getenv("PADE_PIPE_CHUNKS");
         const int v = e ? std::atoi(e) : 0;
-        return (v >= 1 && v <= kPipeChunks) ? v : 8;
+        return (v >= 1 && v <= kPipeChunks) ? v : 0;
     }();
     return n;
+}
+
+// Chunk boundaries of the host-buffer pipeline over `units` rows: equal chunks when
+// PADE_PIPE_CHUNKS sets a count, otherwise a ramp of weights 1 2 4 8 ... 8 4 2 1: a
+// synchronous call pays the first chunk's copy-in and the last chunk's compute and copy-out
+// alone, so those are small, while the middle chunks keep both copy directions busy.
+int pipe_bounds(long units, long* bounds) {
+    static const int kRamp[] = {1, 2, 4, 8, 8, 8, 8, 8, 8, 8, 8, 4, 2, 1};
+    const int fixed = pipe_chunks();
+    int nch = fixed ? fixed : (int)(sizeof(kRamp) / sizeof(kRamp[0]));
+    long wsum = 0;
+    for (int c = 0; c < nch; c++) wsum += fixed ? 1 : kRamp[c];
+    long acc = 0;
+    int out = 0;
+    bounds[0] = 0;
+    for (int c = 0; c < nch; c++) {
+        acc += fixed ? 1 : kRamp[c];
+        const long b = (units * acc + wsum - 1) / wsum;  // ceil: the last bound is units
+        if (b > bounds[out]) bounds[++out] = b;        // skip empty chunks of small inputs
+    }
+    return out;  // number of chunks
 }
 }  // namespace pade
 
@@ -165,8 +186,8 @@ int apply_host_pipelined(pade_op h, const DevicePlan& P, int path, const void* f
     const long nl = ls.nlines;
     const int mode = ls.fb != 0 ? 0 : (ls.fp == 1 ? 1 : 2);
     const long units = mode == 0 ? nl / ls.na : nl;  // b-rows or lines
-    const int nch = pipe_chunks();
-    const long per = (units + nch - 1) / nch;
+    long bounds[kPipeChunks + 1];
+    const int nch = pipe_bounds(units, bounds);
     const unsigned char* fh = static_cast<const unsigned char*>(f);
     unsigned char* oh = static_cast<unsigned char*>(out);
     unsigned char* fd = static_cast<unsigned char*>(h->stage_in);
@@ -174,9 +195,8 @@ int apply_host_pipelined(pade_op h, const DevicePlan& P, int path, const void* f
     if (cudaEventRecord(h->pstart, s) != cudaSuccess) return PS_ECUDA;
     for (int i = 0; i < 3; i++)
         if (cudaStreamWaitEvent(h->pipe[i], h->pstart, 0) != cudaSuccess) return PS_ECUDA;
-    int c = 0;
-    for (long u0 = 0; u0 < units; u0 += per, c++) {
-        const long u1 = std::min(units, u0 + per);
+    for (int c = 0; c < nch; c++) {
+        const long u0 = bounds[c], u1 = bounds[c + 1];
         LineSet cs = ls;
         size_t ioff = 0, ooff = 0;  // element offsets of the chunk
         if (mode == 0) {

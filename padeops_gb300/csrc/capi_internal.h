@@ -19,7 +19,7 @@ inline bool bc_valid(int bc) { return bc == 0 || bc == 1 || bc == -1; }
 inline int plan_key(int opcode, int bc1, int bcn) { return opcode * 16 + bcid(bc1) * 3 + bcid(bcn); }
 
 // chunks of the host-buffer copy-in / compute / copy-out pipeline (capi.cpp): at most
-// kPipeChunks; pipe_chunks() is the number used (8, or PADE_PIPE_CHUNKS as a tuning override)
+// kPipeChunks; a ramp of 14 chunks by default (pipe_bounds), or PADE_PIPE_CHUNKS equal ones (a tuning override)
 constexpr int kPipeChunks = 32;
 int pipe_chunks();
 
