@@ -3,6 +3,7 @@ field (the driver of the Nsight Compute captures summarised under profiles/).
 
     python bench_cases.py --family cd10 --opcode 1 --dir 1 --n 256 --other 256 320 --repeat 3 --path df
     python bench_cases.py --family dense --opcode 1 --dir 1 --n 256 --other 256 256 --repeat 3
+    python bench_cases.py --family dense --of cf90 --opcode 0 --dir 1 --n 256 --other 256 256 --repeat 3
     python bench_cases.py --family spectral --n 256 --repeat 3      # fft + ifft
     python bench_cases.py --family projection --n 256 --repeat 3
     python bench_cases.py --family les --n 128 --repeat 2           # TVD-RK3 steps
@@ -33,6 +34,7 @@ def main(argv=None):
     ap.add_argument("--bc", type=int, nargs=2, default=[0, 0])
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--path", default="df", choices=["df", "native", "fp32"])
+    ap.add_argument("--of", default="cd10", choices=["cd10", "cf90"], help="operator of the dense family")
     a = ap.parse_args(argv)
     import torch
 
@@ -80,12 +82,17 @@ def main(argv=None):
 
 
 def dense_case(a, torch, P, L):
-    """pade_dense_apply of a periodic cd10 operator (opcode 1 or 2) along a.dir."""
+    """pade_dense_apply of a periodic cd10 operator (opcode 1 or 2) or the periodic cf90
+    filter (opcode 0, residual form) along a.dir."""
     import ctypes
 
     n = a.n
-    o = P.cd10()
-    assert o.init(n, 2 * np.pi / n, True) == 0
+    if a.of == "cf90":
+        o = P.cf90()
+        assert o.init(n, True) == 0
+    else:
+        o = P.cd10()
+        assert o.init(n, 2 * np.pi / n, True) == 0
     na, nb = a.other
     total = n * na * nb
     g = torch.Generator(device="cuda").manual_seed(0)
@@ -98,7 +105,7 @@ def dense_case(a, torch, P, L):
                                          ctypes.c_void_p(out.data_ptr()), na, nb, 0, 0, s), "dense_apply")
 
     ms = _timed(torch, run, a.repeat)
-    print(f"dense cd10 op{a.opcode} dir{a.dir} n={n} lines={na}x{nb}: {ms:.4f} ms/app, "
+    print(f"dense {a.of} op{a.opcode} dir{a.dir} n={n} lines={na}x{nb}: {ms:.4f} ms/app, "
           f"{total / ms / 1e6:.1f} Gpts/s, {total * 16 / ms / 1e6:.1f} GB/s")
 
 
