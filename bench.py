@@ -815,7 +815,8 @@ def main():
     tr = traffic_per_launch()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": tr, "peak_source": src,
-            "kernel": "k_line (fixed-stencil double-float chunked scan), mean over the 9 launches",
+            "kernel": "k_lhalf (periodic cd10, x and y) and k_line (cf90, banded z): double-float chunked scans, "
+                      "mean over the 9 launches",
             "algorithmic_bytes_per_launch": npts * BYTES_PER_POINT,
             "per_launch_ms": {p[3]: round(float(v), 4) for p, v in zip(plan, per_launch)}}
     cb = None

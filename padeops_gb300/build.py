@@ -17,10 +17,10 @@ LIB = os.path.join(OUT_DIR, "libpadeops_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["operators.cpp", "plan.cpp", "chunkplan.cpp", "capi.cpp", "pade6stagg.cpp"]
 CUDA_SOURCES = ["kernels.cu", "kernels_df16.cu", "kernels_df32.cu", "kernels_f32.cu", "kernels_stencil.cu", "kernels_stencil_band.cu", "kernels_stencil_f32.cu",
-                "kernels_stencil_stagg.cu", "kernels_reg.cu", "noalloc.cu", "fft.cu", "fft_df.cu",
+                "kernels_stencil_stagg.cu", "kernels_reg.cu", "kernels_half.cu", "noalloc.cu", "fft.cu", "fft_df.cu",
                 "spectral.cu", "fourier_coll.cu", "poisson_wall.cu", "les.cu", "mlp.cu",
                 "dense_tc.cu"]
-HEADERS = ["operators.h", "plan.h", "chunkplan.h", "engine.h", "dfmath.cuh", "chunk_kernel.cuh", "stencil_kernel.cuh", "reg_kernel.cuh", "capi_internal.h",
+HEADERS = ["operators.h", "plan.h", "chunkplan.h", "engine.h", "dfmath.cuh", "chunk_kernel.cuh", "stencil_kernel.cuh", "reg_kernel.cuh", "half_kernel.cuh", "capi_internal.h",
            "fft.h", "spectral_internal.h", "tc_common.cuh"]
 
 

@@ -126,6 +126,10 @@ int launch_line(int shape, const StencilParams& c, const void* f, void* out, con
                 cudaStream_t s);
 int launch_line_f32(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                     unsigned* status, cudaStream_t s);
+// Half-chunk periodic line kernel (half_kernel.cuh), double-float: PS_ENOTSUP for the
+// shapes and sizes it does not take.
+int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                     unsigned* status, cudaStream_t s);
 // Register-resident periodic line kernel (reg_kernel.cuh): double-float (fp32 = 0, FP64
 // in and out) or FP32.  PS_ENOTSUP for shapes it does not instantiate.
 int launch_line_reg(int shape, const RegParams& c, int fp32, const void* f, void* out, const LineSet& ls,

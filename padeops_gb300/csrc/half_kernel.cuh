@@ -1,0 +1,481 @@
+// Half-chunk line kernel: periodic (circulant) lines in chunks of 32 rows, double-float
+// arithmetic in Blackwell's packed FP32x2 instructions.
+//
+// k_line runs one lane per 32-row chunk and spends most of its issue slots on the
+// double-float sums and products of the right-hand side, the two recurrences and the two
+// fundamental-solution corrections, one row at a time.  Here each lane splits its chunk
+// into two halves of 16 rows, A (rows 0..15) and B (rows 16..31), and runs the same
+// algorithm on both halves at once: rows j and j + 16 travel as the two components of
+// packed operands (`add/mul/fma.rn.f32x2`, each component rounded as the scalar
+// instruction, so every error-free transformation stays exact), which halves the
+// instructions of all five per-row phases.  The halves meet in the lane's chunk transfer
+// and in the corrections:
+//   * forward: both halves run the recurrence from a zero state; the chunk's outgoing state
+//     is B's end state plus A's end state propagated through B by the fundamental solutions
+//     of a 16-row block (the first 16 rows of those of a 32-row chunk); after the scan, A is
+//     corrected with the incoming state and B with A's corrected end state;
+//   * backward: the same from the bottom, with the backward fundamental solutions.
+// The lane scan, the ring wrap and every table are those of the 32-row chunk plan.
+//
+// Layout: a lane's input window holds rows -H .. 15 + H of half A beside rows 16 - H .. 31 + H
+// of half B as 16-byte pairs {h_r, h_r+16, l_r, l_r+16} (r = -H .. 15 + H), so one 128-bit
+// shared load gives both packed operands; rows 13 .. 18 (for H = 3) sit in two pairs.  Work
+// pairs overwrite the window pair H rows up, and the FP64 results of rows j and j + 16
+// overwrite work pair j as a double2, which the coalesced store reads back.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "stencil_kernel.cuh"
+
+namespace pade {
+
+// two double-float values: component x is half A's row, y half B's
+struct df2 {
+    float2 h, l;
+};
+
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __fadd2_rn(a, f2neg(b)); }
+
+__device__ __forceinline__ df2 d2_zero() { return df2{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
+__device__ __forceinline__ df2 d2_of(float4 v) { return df2{make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+__device__ __forceinline__ float4 d2_f4(df2 a) { return make_float4(a.h.x, a.h.y, a.l.x, a.l.y); }
+// a coefficient broadcast to both components ({h, h, l, l} in shared memory)
+__device__ __forceinline__ df2 d2_bcast(F2 c) { return df2{make_float2(c.h, c.h), make_float2(c.l, c.l)}; }
+__device__ __forceinline__ dfv d2_x(df2 a) { return dfv{a.h.x, a.l.x}; }
+__device__ __forceinline__ dfv d2_y(df2 a) { return dfv{a.h.y, a.l.y}; }
+__device__ __forceinline__ df2 d2_pack(dfv x, dfv y) { return df2{make_float2(x.h, y.h), make_float2(x.l, y.l)}; }
+__device__ __forceinline__ dfv d2c_scalar(float4 c) { return dfv{c.x, c.z}; }
+
+// df_add, df_norm and df_mul of dfmath.cuh, componentwise
+__device__ __forceinline__ df2 d2_add(df2 a, df2 b) {
+    const float2 s = f2add(a.h, b.h);
+    const float2 bb = f2sub(s, a.h);
+    const float2 e = f2add(f2sub(a.h, f2sub(s, bb)), f2sub(b.h, bb));
+    return df2{s, f2add(e, f2add(a.l, b.l))};
+}
+__device__ __forceinline__ df2 d2_neg(df2 a) { return df2{f2neg(a.h), f2neg(a.l)}; }
+__device__ __forceinline__ df2 d2_sub(df2 a, df2 b) { return d2_add(a, d2_neg(b)); }
+__device__ __forceinline__ df2 d2_norm(df2 a) {
+    const float2 s = f2add(a.h, a.l);
+    return df2{s, f2sub(a.l, f2sub(s, a.h))};
+}
+__device__ __forceinline__ df2 d2_mul(df2 a, df2 c) {
+    const float2 ph = __fmul2_rn(a.h, c.h);
+    float2 pe = __ffma2_rn(a.h, c.h, f2neg(ph));
+    pe = __ffma2_rn(a.h, c.l, pe);
+    pe = __ffma2_rn(a.l, c.h, pe);
+    return df2{ph, pe};
+}
+// base - c1 x1 - c2 x2 and acc + m0 v1 + m1 v2 (ArDF::fms2 / mac2, componentwise)
+__device__ __forceinline__ df2 d2_fms2(df2 base, df2 c1, df2 x1, df2 c2, df2 x2) {
+    return d2_norm(d2_sub(d2_sub(base, d2_mul(x1, c1)), d2_mul(x2, c2)));
+}
+__device__ __forceinline__ df2 d2_fms1(df2 base, df2 c1, df2 x1) { return d2_norm(d2_sub(base, d2_mul(x1, c1))); }
+__device__ __forceinline__ df2 d2_mac2(df2 acc, df2 m0, df2 v1, df2 m1, df2 v2) {
+    return d2_norm(d2_add(d2_add(acc, d2_mul(v1, m0)), d2_mul(v2, m1)));
+}
+__device__ __forceinline__ df2 d2_mac1(df2 acc, df2 m0, df2 v1) { return d2_norm(d2_add(acc, d2_mul(v1, m0))); }
+
+// right-hand side of rows (j, j + 16): the window pairs at p[-NP .. NP]
+template <int NP, bool SYM>
+__device__ __forceinline__ df2 half_stencil(const float4* p, const df2 (&c)[NP], df2 c0) {
+    df2 acc;
+    if constexpr (SYM) {
+        acc = d2_mul(d2_of(p[0]), c0);
+#pragma unroll
+        for (int k = 1; k <= NP; k++) acc = d2_add(acc, d2_mul(d2_add(d2_of(p[k]), d2_of(p[-k])), c[k - 1]));
+    } else {
+        acc = d2_mul(d2_sub(d2_of(p[1]), d2_of(p[-1])), c[0]);
+#pragma unroll
+        for (int k = 2; k <= NP; k++) acc = d2_add(acc, d2_mul(d2_sub(d2_of(p[k]), d2_of(p[-k])), c[k - 1]));
+    }
+    return d2_norm(acc);
+}
+
+constexpr int kHalf = 16;  // rows per half chunk
+
+// window pairs per lane (rows -H .. 15 + H of half A), padded to an odd count of 16-byte
+// units so the 8 lanes of a line in one quarter-warp read distinct banks
+__host__ __device__ constexpr int half_lane_stride(int np) { return (kHalf + 2 * np) | 1; }
+
+// 16-byte units per line: odd, so the 16 lines a strided warp instruction touches spread
+// over the banks (an even stride such as 8 x 23 = 184 puts all 16 on one bank)
+__host__ __device__ constexpr int half_line_stride(int p, int np) { return (p * half_lane_stride(np)) | 1; }
+
+// Largest line the kernel stages in registers: contiguous lines take ns / 32 rows per lane
+// (at most 8), strided lines ns / (threads per line) rows per thread (at most 32).
+constexpr int kHalfRowsContig = 8;
+constexpr int kHalfRowsStrided = 32;
+
+template <int Q, int NP, bool SYM>
+__global__ void __launch_bounds__(kLineThreadsCirc, 4)
+    k_lhalf(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
+            unsigned* __restrict__ status) {
+    using AR = ArDF;
+    using V = dfv;
+    constexpr int H = NP;
+    constexpr int SL = half_lane_stride(NP);  // 16-byte units per lane
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ns = cp.ns, P = cp.P, L = cp.L;
+    const int LT = half_line_stride(P, NP);                   // 16-byte units per line
+    float4* ctab = reinterpret_cast<float4*>(smem_raw);      // pf1, pf2 (row j), pb1, pb2 (distance d), 16 each
+    float4* tile = ctab + 4 * kHalf;                          // L lines x P lanes x SL
+    __shared__ int lexp[kLineThreadsCirc];
+    __shared__ long base_in[kLineThreadsCirc], base_out[kLineThreadsCirc];
+
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const long line0 = (long)blockIdx.x * L;
+    const int nl = (int)min((long)L, ls.nlines - line0);
+    if (tid < L) {
+        lexp[tid] = 0;
+        const long lg = line0 + tid;
+        const long a = lg % ls.na, b = lg / ls.na;
+        base_in[tid] = a * ls.fa + b * ls.fb;
+        base_out[tid] = a * ls.oa + b * ls.ob;
+    }
+    if (tid < 4 * kHalf) {
+        const int k = tid / kHalf, j = tid % kHalf;
+        const F2 c = (k < 2 ? cp.phf : cp.phb)[2 * j + (k & 1)];
+        ctab[tid] = make_float4(c.h, c.h, c.l, c.l);
+    }
+    __syncthreads();
+
+    // ---- A: stage each line scaled by 2^-(e_max - 1023); row q of chunk t goes to pair
+    // q % 16, component q / 16 of lane t's window ----
+    auto hpos = [&](int l, int p) -> int {  // float index of row p's high part
+        const int t = p >> 5, q = p & 31;
+        return ((l * LT + t * SL + H + (q & 15)) << 2) + (q >> 4);
+    };
+    float* tf = reinterpret_cast<float*>(tile);
+    unsigned bad = 0;
+    if (ls.fp == 1) {
+        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+        const int U = ns >> 5;
+        for (int l = warp; l < nl; l += nw) {
+            const double* src = f + base_in[l];
+            double v[kHalfRowsContig];
+            int mx = 0;
+#pragma unroll
+            for (int u = 0; u < kHalfRowsContig; u++) {
+                v[u] = u < U ? __ldg(src + lane + 32 * u) : 0.0;
+                mx = max(mx, bexp(v[u]));
+            }
+            mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
+            bad |= (unsigned)(mx == 2047);
+            if (lane == 0) lexp[l] = mx;
+            const SplitK sk = split_consts(mx - 1023);
+            float* lf = tf + hpos(l, lane);
+#pragma unroll
+            for (int u = 0; u < kHalfRowsContig; u++) {
+                if (u < U) {
+                    const dfv d = df_split_line(v[u], sk);
+                    lf[u * SL * 4] = d.h;
+                    lf[u * SL * 4 + 2] = d.l;
+                }
+            }
+        }
+    } else {
+        const int pstep = nth / L;
+        const int U = (ns + pstep - 1) / pstep;
+        const int l = tid % L, q0 = tid / L;
+        double v[kHalfRowsStrided];
+        int mx = 0;
+        if (l < nl) {
+            const double* src = f + base_in[l];
+#pragma unroll
+            for (int u = 0; u < kHalfRowsStrided; u++) {
+                const int p = q0 + pstep * u;
+                v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
+                mx = max(mx, bexp(v[u]));
+            }
+            atomicMax(&lexp[l], mx);
+        }
+        __syncthreads();
+        if (l < nl) {
+            const int mxl = lexp[l];
+            bad |= (unsigned)(mxl == 2047);
+            const SplitK sk = split_consts(mxl - 1023);
+#pragma unroll
+            for (int u = 0; u < kHalfRowsStrided; u++) {
+                const int p = q0 + pstep * u;
+                if (u < U && p < ns) {
+                    const dfv d = df_split_line(v[u], sk);
+                    const int o = hpos(l, p);
+                    tf[o] = d.h;
+                    tf[o + 2] = d.l;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    const int t = tid % cp.Pp, l = tid / cp.Pp;
+    const bool active = (l < nl) && (t < P);
+    float4* wp = tile + (size_t)l * LT + t * SL + H;  // pair r at wp[r], -H <= r < 16 + H
+    float* wf = reinterpret_cast<float*>(wp);
+
+    // ---- halo pairs: rows -H..-1 (previous chunk, around the ring) beside rows 16-H..15,
+    // and rows 16..15+H beside rows 32..31+H (next chunk) ----
+    if (active) {
+#pragma unroll
+        for (int h = 1; h <= H; h++) {
+            const int pm = t * 32 - h, pp = t * 32 + 31 + h;
+            const int om = hpos(l, pm < 0 ? pm + ns : pm), op = hpos(l, pp >= ns ? pp - ns : pp);
+            const int oa = hpos(l, t * 32 + 16 - h), ob = hpos(l, t * 32 + 15 + h);
+            float* lo = wf + 4 * (-h);          // pair -h
+            float* hi = wf + 4 * (15 + h);      // pair 15 + h
+            lo[0] = tf[om];
+            lo[2] = tf[om + 2];
+            lo[1] = tf[oa];
+            lo[3] = tf[oa + 2];
+            hi[0] = tf[ob];
+            hi[2] = tf[ob + 2];
+            hi[1] = tf[op];
+            hi[3] = tf[op + 2];
+        }
+    }
+    // the neighbouring lanes of a line (one warp) read this lane's first and last rows
+    // before its work pairs overwrite them
+    __syncwarp();
+
+    df2 cc[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) cc[k] = d2_bcast(cp.c[k]);
+    const df2 c0 = d2_bcast(cp.c0);
+    const df2 a1 = d2_bcast(cp.ca1), a2 = d2_bcast(cp.ca2);
+    const dfv a1s = AR::coef(cp.ca1), a2s = AR::coef(cp.ca2);
+    const int Pp = cp.Pp;
+
+    // ---- B: right-hand side and forward recurrence of both halves from zero states ----
+    df2 S1 = d2_zero(), S2 = d2_zero();
+    if (active) {
+#pragma unroll 4
+        for (int j = 0; j < kHalf; j++) {
+            const df2 r = half_stencil<NP, SYM>(wp + j, cc, c0);
+            const df2 y = (Q == 2) ? d2_fms2(r, a1, S1, a2, S2) : d2_fms1(r, a1, S1);
+            wp[j - H] = d2_f4(y);
+            S2 = S1;
+            S1 = y;
+        }
+    }
+    // the chunk's outgoing state: half B's end plus half A's end carried through half B
+    const dfv yA15 = d2_x(S1), yA14 = d2_x(S2);
+    V s1, s2 = AR::zero();
+    {
+        const dfv p15a = d2c_scalar(ctab[15]), p14a = d2c_scalar(ctab[14]);
+        if constexpr (Q == 2) {
+            const dfv p15b = d2c_scalar(ctab[kHalf + 15]), p14b = d2c_scalar(ctab[kHalf + 14]);
+            s1 = AR::mac2(d2_y(S1), p15a, yA15, p15b, yA14);
+            s2 = AR::mac2(d2_y(S2), p14a, yA15, p14b, yA14);
+        } else {
+            s1 = AR::mac1(d2_y(S1), p15a, yA15);
+        }
+    }
+    // ---- D: log-step scan of the chunk transfers (then the ring wrap) ----
+    for (int k = 0; k < cp.nsteps; k++) {
+        const unsigned dlt = 1u << k;
+        const V o1 = AR::shfl_up(s1, dlt, Pp);
+        const V o2 = (Q == 2) ? AR::shfl_up(s2, dlt, Pp) : AR::zero();
+        if (t >= (int)dlt) {
+            const F2* Fm = cp.fscan + ((size_t)t * kMaxSteps + k) * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(s1, AR::coef(Fm[0]), o1, AR::coef(Fm[1]), o2);
+                const V n2 = AR::mac2(s2, AR::coef(Fm[2]), o1, AR::coef(Fm[3]), o2);
+                s1 = n1;
+                s2 = n2;
+            } else {
+                s1 = AR::mac1(s1, AR::coef(Fm[0]), o1);
+            }
+        }
+    }
+    V i1 = AR::shfl_up(s1, 1, Pp);
+    V i2 = (Q == 2) ? AR::shfl_up(s2, 1, Pp) : AR::zero();
+    if (t == 0) {
+        i1 = AR::zero();
+        i2 = AR::zero();
+    }
+    {
+        const V E1 = AR::shfl_idx(s1, P - 1, Pp);
+        const V E2 = (Q == 2) ? AR::shfl_idx(s2, P - 1, Pp) : AR::zero();
+        if (t < P) {
+            const F2* Wm = cp.fwrap + (size_t)t * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(i1, AR::coef(Wm[0]), E1, AR::coef(Wm[1]), E2);
+                const V n2 = AR::mac2(i2, AR::coef(Wm[2]), E1, AR::coef(Wm[3]), E2);
+                i1 = n1;
+                i2 = n2;
+            } else {
+                i1 = AR::mac1(i1, AR::coef(Wm[0]), E1);
+            }
+        }
+    }
+    // incoming states: half A the chunk's, half B half A's corrected end rows 15 and 14
+    df2 I1, I2;
+    {
+        const dfv p15a = d2c_scalar(ctab[15]), p14a = d2c_scalar(ctab[14]);
+        if constexpr (Q == 2) {
+            const dfv p15b = d2c_scalar(ctab[kHalf + 15]), p14b = d2c_scalar(ctab[kHalf + 14]);
+            I1 = d2_pack(i1, AR::mac2(yA15, p15a, i1, p15b, i2));
+            I2 = d2_pack(i2, AR::mac2(yA14, p14a, i1, p14b, i2));
+        } else {
+            I1 = d2_pack(i1, AR::mac1(yA15, p15a, i1));
+            I2 = d2_zero();
+        }
+    }
+    // ---- E+F: forward correction and backward recurrence of both halves from zero states ----
+    df2 U1 = d2_zero(), U2 = d2_zero();
+    if (active) {
+#pragma unroll 4
+        for (int j = kHalf - 1; j >= 0; j--) {
+            const df2 p1 = d2_of(ctab[j]);
+            const df2 w = d2_of(wp[j - H]);
+            df2 y;
+            if constexpr (Q == 2) {
+                y = d2_mac2(w, p1, I1, d2_of(ctab[kHalf + j]), I2);
+            } else {
+                y = d2_mac1(w, p1, I1);
+            }
+            const df2 x = (Q == 2) ? d2_fms2(y, a1, U1, a2, U2) : d2_fms1(y, a1, U1);
+            wp[j - H] = d2_f4(x);
+            U2 = U1;
+            U1 = x;
+        }
+    }
+    // outgoing backward state (rows 0 and 1): half A's plus half B's rows 16, 17 carried up
+    const dfv xB0 = d2_y(U1), xB1 = d2_y(U2);
+    V u1, u2 = AR::zero();
+    {
+        const dfv q15a = d2c_scalar(ctab[2 * kHalf + 15]), q14a = d2c_scalar(ctab[2 * kHalf + 14]);
+        if constexpr (Q == 2) {
+            const dfv q15b = d2c_scalar(ctab[3 * kHalf + 15]), q14b = d2c_scalar(ctab[3 * kHalf + 14]);
+            u1 = AR::mac2(d2_x(U1), q15a, xB0, q15b, xB1);
+            u2 = AR::mac2(d2_x(U2), q14a, xB0, q14b, xB1);
+        } else {
+            u1 = AR::mac1(d2_x(U1), q15a, xB0);
+        }
+    }
+    // ---- G: reverse scan (then the ring wrap) ----
+    for (int k = 0; k < cp.nsteps; k++) {
+        const unsigned dlt = 1u << k;
+        const V o1 = AR::shfl_down(u1, dlt, Pp);
+        const V o2 = (Q == 2) ? AR::shfl_down(u2, dlt, Pp) : AR::zero();
+        if (t + (int)dlt < Pp) {
+            const F2* Bm = cp.bscan + ((size_t)t * kMaxSteps + k) * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(u1, AR::coef(Bm[0]), o1, AR::coef(Bm[1]), o2);
+                const V n2 = AR::mac2(u2, AR::coef(Bm[2]), o1, AR::coef(Bm[3]), o2);
+                u1 = n1;
+                u2 = n2;
+            } else {
+                u1 = AR::mac1(u1, AR::coef(Bm[0]), o1);
+            }
+        }
+    }
+    V j1 = AR::shfl_down(u1, 1, Pp);
+    V j2 = (Q == 2) ? AR::shfl_down(u2, 1, Pp) : AR::zero();
+    if (t >= P - 1) {
+        j1 = AR::zero();
+        j2 = AR::zero();
+    }
+    {
+        const V F1 = AR::shfl_idx(u1, 0, Pp);
+        const V F2v = (Q == 2) ? AR::shfl_idx(u2, 0, Pp) : AR::zero();
+        if (t < P) {
+            const F2* Wm = cp.bwrap + (size_t)t * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(j1, AR::coef(Wm[0]), F1, AR::coef(Wm[1]), F2v);
+                const V n2 = AR::mac2(j2, AR::coef(Wm[2]), F1, AR::coef(Wm[3]), F2v);
+                j1 = n1;
+                j2 = n2;
+            } else {
+                j1 = AR::mac1(j1, AR::coef(Wm[0]), F1);
+            }
+        }
+    }
+    // incoming backward states: half B the chunk's, half A half B's corrected rows 16, 17
+    df2 J1, J2;
+    {
+        const dfv q15a = d2c_scalar(ctab[2 * kHalf + 15]), q14a = d2c_scalar(ctab[2 * kHalf + 14]);
+        if constexpr (Q == 2) {
+            const dfv q15b = d2c_scalar(ctab[3 * kHalf + 15]), q14b = d2c_scalar(ctab[3 * kHalf + 14]);
+            J1 = d2_pack(AR::mac2(xB0, q15a, j1, q15b, j2), j1);
+            J2 = d2_pack(AR::mac2(xB1, q14a, j1, q14b, j2), j2);
+        } else {
+            J1 = d2_pack(AR::mac1(xB0, q15a, j1), j1);
+            J2 = d2_zero();
+        }
+    }
+    // ---- H+I: backward correction and FP64 assembly (rows j and j + 16 over work pair j) ----
+    // (Running this last correction in FP64 on the assembled values, two FMAs per row, was
+    // measured slower: 0.153 -> 0.166 ms per 256^3 launch along x; the whole CTA reaches the
+    // phase at once and the FP64 pipe saturates there.)
+    if (active) {
+        const int kl = lexp[l] - 1023;
+        double2* wd = reinterpret_cast<double2*>(wp - H);
+        if (kl >= -800 && kl <= 800) {
+            const unsigned kadd = (unsigned)(896 + kl) << 20;
+#pragma unroll 4
+            for (int j = 0; j < kHalf; j++) {
+                const int d = kHalf - 1 - j;
+                const df2 w = d2_of(wp[j - H]);
+                const df2 x = (Q == 2) ? d2_mac2(w, d2_of(ctab[2 * kHalf + d]), J1, d2_of(ctab[3 * kHalf + d]), J2)
+                                       : d2_mac1(w, d2_of(ctab[2 * kHalf + d]), J1);
+                wd[j] = make_double2(df_to_double_kadd(d2_x(x), kadd), df_to_double_kadd(d2_y(x), kadd));
+            }
+        } else {
+#pragma unroll 1
+            for (int j = 0; j < kHalf; j++) {
+                const int d = kHalf - 1 - j;
+                const df2 w = d2_of(wp[j - H]);
+                const df2 x = (Q == 2) ? d2_mac2(w, d2_of(ctab[2 * kHalf + d]), J1, d2_of(ctab[3 * kHalf + d]), J2)
+                                       : d2_mac1(w, d2_of(ctab[2 * kHalf + d]), J1);
+                wd[j] = make_double2(AR::store_scaled(d2_x(x), kl), AR::store_scaled(d2_y(x), kl));
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- J: coalesced stores; row q of chunk t is double 2 (q % 16) + q / 16 of its lane ----
+    const double* od = reinterpret_cast<const double*>(tile);
+    auto out_pos = [&](int ll, int p) -> int {
+        const int tt = p >> 5, q = p & 31;
+        return ((ll * LT + tt * SL) << 1) + 2 * (q & 15) + (q >> 4);
+    };
+    if (ls.op == 1) {
+        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+        for (int ll = warp; ll < nl; ll += nw) {
+            double* o = out + base_out[ll];
+            for (int p = lane; p < cp.nout; p += 32) o[p] = od[out_pos(ll, p < ns ? p : p - ns)];
+        }
+    } else {
+        const int ll = tid % L, pstep = nth / L;
+        if (ll < nl) {
+            double* o = out + base_out[ll];
+            for (int p = tid / L; p < cp.nout; p += pstep) o[(long)p * ls.op] = od[out_pos(ll, p < ns ? p : p - ns)];
+        }
+    }
+    if (bad) atomicOr(status, 1u);
+}
+
+template <int Q, int NP, bool SYM>
+int launch_lhalf_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
+                   cudaStream_t s) {
+    constexpr int NT = kLineThreadsCirc;
+    const long blocks = (ls.nlines + c.L - 1) / c.L;
+    const size_t smem = sizeof(float4) * (4 * kHalf + (size_t)c.L * half_line_stride(c.P, NP));
+    auto kern = k_lhalf<Q, NP, SYM>;
+    // the opt-in covers dynamic plus static shared memory (the per-line arrays, 2.5 KB)
+    if (smem + 4096 > 48 * 1024) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return PS_ECUDA;
+    }
+    kern<<<(unsigned)blocks, NT, smem, s>>>(c, (const double*)f, (double*)out, ls, status);
+    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+}
+
+int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                     unsigned* status, cudaStream_t s);
+
+}  // namespace pade

@@ -418,10 +418,12 @@ int DevicePlan::upload(const HostPlan& hp) {
 // ------------------------------------------------------------------------------------
 // Which periodic line kernel runs: the register-resident one for the FP32 path; for
 // double-float the register kernel only on tridiagonal operators along strided lines
-// (measured 5-7 % faster there), the shared-memory k_line otherwise (the unrolled
-// pentadiagonal double-float code stalls on instruction fetch; contiguous lines stage
-// faster through shared memory).  PADE_LINE_KERNEL (a tuning override): "reg" the register
-// kernel everywhere, "shared" k_line everywhere.
+// (measured 5-7 % faster there), otherwise the half-chunk kernel k_lhalf (packed FP32x2
+// arithmetic) where its shapes and sizes apply and the shared-memory k_line for the rest
+// (the unrolled pentadiagonal double-float code of the register kernel stalls on
+// instruction fetch; contiguous lines stage faster through shared memory).
+// PADE_LINE_KERNEL (a tuning override): "reg" the register kernel everywhere, "shared"
+// k_line everywhere.
 static int line_kernel_choice() {
     static const int v = [] {
         const char* e = std::getenv("PADE_LINE_KERNEL");
@@ -460,7 +462,13 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
             const int rc = launch_line_reg(sh, p.reg_params(), 0, f, out, ls, status, s);
             if (rc != PS_ENOTSUP) return rc;
         }
-        if (p.line_shape() != SHAPE_NONE) return launch_line(p.line_shape(), p.line_params(), f, out, ls, status, s);
+        if (sh != SHAPE_NONE) {
+            if (line_kernel_choice() != 2 && sh >= SHAPE_T2A && sh <= SHAPE_P3S) {
+                const int rc = launch_line_half(sh, p.line_params(), f, out, ls, status, s);
+                if (rc != PS_ENOTSUP) return rc;
+            }
+            return launch_line(sh, p.line_params(), f, out, ls, status, s);
+        }
         return h.M == 16 ? launch_chunk_m<ArDF, 16>(h, p.chunk_df(), f, out, ls, status, s)
                          : launch_chunk_m<ArDF, 32>(h, p.chunk_df(), f, out, ls, status, s);
     }

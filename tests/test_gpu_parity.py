@@ -124,6 +124,23 @@ def test_cd10_nonperiodic(oracle, bc1, bcn, dir, n):
             assert relerr(out, ref) < tol64(order, f, ref, dx), (order, path)
 
 
+@pytest.mark.parametrize("fam", ["cd06", "cd10"])
+@pytest.mark.parametrize("dir", [1, 2, 3])
+@pytest.mark.parametrize("n", [32, 96, 160, 224])
+def test_periodic_whole_chunks(oracle, fam, dir, n):
+    """Periodic lines of 1, 3, 5 and 7 chunks of 32 rows (the half-chunk line kernel: one
+    lane per line, idle lanes in the scan groups) over a ragged 7 x 5 set of lines."""
+    dx = 2 * np.pi / n
+    o = getattr(P, fam)()
+    assert o.init(n, dx, True) == 0
+    shape = shape_for(n, dir, (7, 5))
+    f = field(shape, 5)
+    for order in (1, 2):
+        out = run(o, order, dir, f, shape)
+        ref = getattr(oracle, fam)(f, dx, periodic=True, order=order, dir=dir)
+        assert relerr(out, ref) < tol64(order, f, ref, dx), order
+
+
 @pytest.mark.parametrize("periodic", [True, False])
 @pytest.mark.parametrize("bc1,bcn", list(itertools.product(BCS, BCS)))
 @pytest.mark.parametrize("dir", [1, 2, 3])
