@@ -103,6 +103,9 @@ class DevicePlan {
     int chunk_M() const { return ch_.M; }
     int line_shape() const { return line_shape_; }
     const StencilParams& line_params() const { return cline_; }
+    // the line kernel's parameters on the 16-row chunk plan when line_params() is a 32-row
+    // plan (null otherwise): the half-chunk kernel can take either
+    const StencilParams* half16_params() const { return half16_ ? &chalf16_ : nullptr; }
     // register-resident periodic kernel (chunks of 32 rows), when the line shape allows it
     bool reg_ok() const { return reg_ok_; }
     const RegParams& reg_params() const { return *creg_; }
@@ -116,6 +119,8 @@ class DevicePlan {
     ChunkParams cdf_{}, cf32_{};
     int line_shape_ = SHAPE_NONE;
     StencilParams cline_{};
+    StencilParams chalf16_{};
+    bool half16_ = false;
     bool reg_ok_ = false;
     RegParams* creg_ = nullptr;
 };

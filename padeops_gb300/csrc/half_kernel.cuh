@@ -22,6 +22,8 @@
 // shared load gives both packed operands; rows 13 .. 18 (for H = 3) sit in two pairs.  Work
 // pairs overwrite the window pair H rows up, and the FP64 results of rows j and j + 16
 // overwrite work pair j as a double2, which the coalesced store reads back.
+// The same runs on 16-row chunks split into halves of 8 (template M = 16, the 16-row chunk
+// plan's tables): half the shared memory and staging registers per thread.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -94,34 +96,37 @@ __device__ __forceinline__ df2 half_stencil(const float4* p, const df2 (&c)[NP],
     return d2_norm(acc);
 }
 
-constexpr int kHalf = 16;  // rows per half chunk
-
-// window pairs per lane (rows -H .. 15 + H of half A), padded to an odd count of 16-byte
-// units so the 8 lanes of a line in one quarter-warp read distinct banks
-__host__ __device__ constexpr int half_lane_stride(int np) { return (kHalf + 2 * np) | 1; }
+// window pairs per lane (rows -H .. HM - 1 + H of half A, HM = M / 2 rows per half),
+// padded to an odd count of 16-byte units so the 8 lanes of a line in one quarter-warp
+// read distinct banks
+__host__ __device__ constexpr int half_lane_stride(int hm, int np) { return (hm + 2 * np) | 1; }
 
 // 16-byte units per line: odd, so the 16 lines a strided warp instruction touches spread
 // over the banks (an even stride such as 8 x 23 = 184 puts all 16 on one bank)
-__host__ __device__ constexpr int half_line_stride(int p, int np) { return (p * half_lane_stride(np)) | 1; }
+__host__ __device__ constexpr int half_line_stride(int p, int hm, int np) {
+    return (p * half_lane_stride(hm, np)) | 1;
+}
 
 // Largest line the kernel stages in registers: contiguous lines take ns / 32 rows per lane
-// (at most 8), strided lines ns / (threads per line) rows per thread (at most 32).
+// (at most 8); strided lines one row per lane of the line and chunk row (at most M).
 constexpr int kHalfRowsContig = 8;
-constexpr int kHalfRowsStrided = 32;
 
-template <int Q, int NP, bool SYM>
-__global__ void __launch_bounds__(kLineThreadsCirc, 4)
+// M: chunk rows (32, or 16 for twice the resident lines per SM: half the shared memory and
+// registers per thread for a longer lane scan)
+template <int Q, int NP, bool SYM, int M>
+__global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     k_lhalf(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
             unsigned* __restrict__ status) {
     using AR = ArDF;
     using V = dfv;
     constexpr int H = NP;
-    constexpr int SL = half_lane_stride(NP);  // 16-byte units per lane
+    constexpr int HM = M / 2;                     // rows per half
+    constexpr int SL = half_lane_stride(HM, NP);  // 16-byte units per lane
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ns = cp.ns, P = cp.P, L = cp.L;
-    const int LT = half_line_stride(P, NP);                   // 16-byte units per line
-    float4* ctab = reinterpret_cast<float4*>(smem_raw);      // pf1, pf2 (row j), pb1, pb2 (distance d), 16 each
-    float4* tile = ctab + 4 * kHalf;                          // L lines x P lanes x SL
+    const int LT = half_line_stride(P, HM, NP);               // 16-byte units per line
+    float4* ctab = reinterpret_cast<float4*>(smem_raw);      // pf1, pf2 (row j), pb1, pb2 (distance d), HM each
+    float4* tile = ctab + 4 * HM;                             // L lines x P lanes x SL
     __shared__ int lexp[kLineThreadsCirc];
     __shared__ long base_in[kLineThreadsCirc], base_out[kLineThreadsCirc];
 
@@ -135,31 +140,31 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
         base_in[tid] = a * ls.fa + b * ls.fb;
         base_out[tid] = a * ls.oa + b * ls.ob;
     }
-    if (tid < 4 * kHalf) {
-        const int k = tid / kHalf, j = tid % kHalf;
+    if (tid < 4 * HM) {
+        const int k = tid / HM, j = tid % HM;
         const F2 c = (k < 2 ? cp.phf : cp.phb)[2 * j + (k & 1)];
         ctab[tid] = make_float4(c.h, c.h, c.l, c.l);
     }
     __syncthreads();
 
     // ---- A: stage each line scaled by 2^-(e_max - 1023); row q of chunk t goes to pair
-    // q % 16, component q / 16 of lane t's window ----
+    // q % HM, component q / HM of lane t's window ----
     auto hpos = [&](int l, int p) -> int {  // float index of row p's high part
-        const int t = p >> 5, q = p & 31;
-        return ((l * LT + t * SL + H + (q & 15)) << 2) + (q >> 4);
+        const int t = p / M, q = p % M;
+        return ((l * LT + t * SL + H + q % HM) << 2) + q / HM;
     };
     float* tf = reinterpret_cast<float*>(tile);
     unsigned bad = 0;
     if (ls.fp == 1) {
         const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
-        const int U = ns >> 5;
+        const int U = (ns + 31) >> 5;
         for (int l = warp; l < nl; l += nw) {
             const double* src = f + base_in[l];
             double v[kHalfRowsContig];
             int mx = 0;
 #pragma unroll
             for (int u = 0; u < kHalfRowsContig; u++) {
-                v[u] = u < U ? __ldg(src + lane + 32 * u) : 0.0;
+                v[u] = (u < U && lane + 32 * u < ns) ? __ldg(src + lane + 32 * u) : 0.0;
                 mx = max(mx, bexp(v[u]));
             }
             mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
@@ -169,10 +174,10 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
             float* lf = tf + hpos(l, lane);
 #pragma unroll
             for (int u = 0; u < kHalfRowsContig; u++) {
-                if (u < U) {
+                if (u < U && lane + 32 * u < ns) {
                     const dfv d = df_split_line(v[u], sk);
-                    lf[u * SL * 4] = d.h;
-                    lf[u * SL * 4 + 2] = d.l;
+                    lf[u * (32 / M) * SL * 4] = d.h;
+                    lf[u * (32 / M) * SL * 4 + 2] = d.l;
                 }
             }
         }
@@ -180,12 +185,12 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
         const int pstep = nth / L;
         const int U = (ns + pstep - 1) / pstep;
         const int l = tid % L, q0 = tid / L;
-        double v[kHalfRowsStrided];
+        double v[M];
         int mx = 0;
         if (l < nl) {
             const double* src = f + base_in[l];
 #pragma unroll
-            for (int u = 0; u < kHalfRowsStrided; u++) {
+            for (int u = 0; u < M; u++) {
                 const int p = q0 + pstep * u;
                 v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
                 mx = max(mx, bexp(v[u]));
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
             bad |= (unsigned)(mxl == 2047);
             const SplitK sk = split_consts(mxl - 1023);
 #pragma unroll
-            for (int u = 0; u < kHalfRowsStrided; u++) {
+            for (int u = 0; u < M; u++) {
                 const int p = q0 + pstep * u;
                 if (u < U && p < ns) {
                     const dfv d = df_split_line(v[u], sk);
@@ -213,19 +218,19 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
 
     const int t = tid % cp.Pp, l = tid / cp.Pp;
     const bool active = (l < nl) && (t < P);
-    float4* wp = tile + (size_t)l * LT + t * SL + H;  // pair r at wp[r], -H <= r < 16 + H
+    float4* wp = tile + (size_t)l * LT + t * SL + H;  // pair r at wp[r], -H <= r < HM + H
     float* wf = reinterpret_cast<float*>(wp);
 
-    // ---- halo pairs: rows -H..-1 (previous chunk, around the ring) beside rows 16-H..15,
-    // and rows 16..15+H beside rows 32..31+H (next chunk) ----
+    // ---- halo pairs: rows -H..-1 (previous chunk, around the ring) beside rows HM-H..HM-1,
+    // and rows HM..HM-1+H beside rows M..M-1+H (next chunk) ----
     if (active) {
 #pragma unroll
         for (int h = 1; h <= H; h++) {
-            const int pm = t * 32 - h, pp = t * 32 + 31 + h;
+            const int pm = t * M - h, pp = t * M + M - 1 + h;
             const int om = hpos(l, pm < 0 ? pm + ns : pm), op = hpos(l, pp >= ns ? pp - ns : pp);
-            const int oa = hpos(l, t * 32 + 16 - h), ob = hpos(l, t * 32 + 15 + h);
+            const int oa = hpos(l, t * M + HM - h), ob = hpos(l, t * M + HM - 1 + h);
             float* lo = wf + 4 * (-h);          // pair -h
-            float* hi = wf + 4 * (15 + h);      // pair 15 + h
+            float* hi = wf + 4 * (HM - 1 + h);  // pair HM - 1 + h
             lo[0] = tf[om];
             lo[2] = tf[om + 2];
             lo[1] = tf[oa];
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     df2 S1 = d2_zero(), S2 = d2_zero();
     if (active) {
 #pragma unroll 4
-        for (int j = 0; j < kHalf; j++) {
+        for (int j = 0; j < HM; j++) {
             const df2 r = half_stencil<NP, SYM>(wp + j, cc, c0);
             const df2 y = (Q == 2) ? d2_fms2(r, a1, S1, a2, S2) : d2_fms1(r, a1, S1);
             wp[j - H] = d2_f4(y);
@@ -264,9 +269,9 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     const dfv yA15 = d2_x(S1), yA14 = d2_x(S2);
     V s1, s2 = AR::zero();
     {
-        const dfv p15a = d2c_scalar(ctab[15]), p14a = d2c_scalar(ctab[14]);
+        const dfv p15a = d2c_scalar(ctab[HM - 1]), p14a = d2c_scalar(ctab[HM - 2]);
         if constexpr (Q == 2) {
-            const dfv p15b = d2c_scalar(ctab[kHalf + 15]), p14b = d2c_scalar(ctab[kHalf + 14]);
+            const dfv p15b = d2c_scalar(ctab[HM + HM - 1]), p14b = d2c_scalar(ctab[HM + HM - 2]);
             s1 = AR::mac2(d2_y(S1), p15a, yA15, p15b, yA14);
             s2 = AR::mac2(d2_y(S2), p14a, yA15, p14b, yA14);
         } else {
@@ -314,9 +319,9 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     // incoming states: half A the chunk's, half B half A's corrected end rows 15 and 14
     df2 I1, I2;
     {
-        const dfv p15a = d2c_scalar(ctab[15]), p14a = d2c_scalar(ctab[14]);
+        const dfv p15a = d2c_scalar(ctab[HM - 1]), p14a = d2c_scalar(ctab[HM - 2]);
         if constexpr (Q == 2) {
-            const dfv p15b = d2c_scalar(ctab[kHalf + 15]), p14b = d2c_scalar(ctab[kHalf + 14]);
+            const dfv p15b = d2c_scalar(ctab[HM + HM - 1]), p14b = d2c_scalar(ctab[HM + HM - 2]);
             I1 = d2_pack(i1, AR::mac2(yA15, p15a, i1, p15b, i2));
             I2 = d2_pack(i2, AR::mac2(yA14, p14a, i1, p14b, i2));
         } else {
@@ -328,12 +333,12 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     df2 U1 = d2_zero(), U2 = d2_zero();
     if (active) {
 #pragma unroll 4
-        for (int j = kHalf - 1; j >= 0; j--) {
+        for (int j = HM - 1; j >= 0; j--) {
             const df2 p1 = d2_of(ctab[j]);
             const df2 w = d2_of(wp[j - H]);
             df2 y;
             if constexpr (Q == 2) {
-                y = d2_mac2(w, p1, I1, d2_of(ctab[kHalf + j]), I2);
+                y = d2_mac2(w, p1, I1, d2_of(ctab[HM + j]), I2);
             } else {
                 y = d2_mac1(w, p1, I1);
             }
@@ -347,9 +352,9 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     const dfv xB0 = d2_y(U1), xB1 = d2_y(U2);
     V u1, u2 = AR::zero();
     {
-        const dfv q15a = d2c_scalar(ctab[2 * kHalf + 15]), q14a = d2c_scalar(ctab[2 * kHalf + 14]);
+        const dfv q15a = d2c_scalar(ctab[2 * HM + HM - 1]), q14a = d2c_scalar(ctab[2 * HM + HM - 2]);
         if constexpr (Q == 2) {
-            const dfv q15b = d2c_scalar(ctab[3 * kHalf + 15]), q14b = d2c_scalar(ctab[3 * kHalf + 14]);
+            const dfv q15b = d2c_scalar(ctab[3 * HM + HM - 1]), q14b = d2c_scalar(ctab[3 * HM + HM - 2]);
             u1 = AR::mac2(d2_x(U1), q15a, xB0, q15b, xB1);
             u2 = AR::mac2(d2_x(U2), q14a, xB0, q14b, xB1);
         } else {
@@ -397,9 +402,9 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     // incoming backward states: half B the chunk's, half A half B's corrected rows 16, 17
     df2 J1, J2;
     {
-        const dfv q15a = d2c_scalar(ctab[2 * kHalf + 15]), q14a = d2c_scalar(ctab[2 * kHalf + 14]);
+        const dfv q15a = d2c_scalar(ctab[2 * HM + HM - 1]), q14a = d2c_scalar(ctab[2 * HM + HM - 2]);
         if constexpr (Q == 2) {
-            const dfv q15b = d2c_scalar(ctab[3 * kHalf + 15]), q14b = d2c_scalar(ctab[3 * kHalf + 14]);
+            const dfv q15b = d2c_scalar(ctab[3 * HM + HM - 1]), q14b = d2c_scalar(ctab[3 * HM + HM - 2]);
             J1 = d2_pack(AR::mac2(xB0, q15a, j1, q15b, j2), j1);
             J2 = d2_pack(AR::mac2(xB1, q14a, j1, q14b, j2), j2);
         } else {
@@ -417,31 +422,31 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
         if (kl >= -800 && kl <= 800) {
             const unsigned kadd = (unsigned)(896 + kl) << 20;
 #pragma unroll 4
-            for (int j = 0; j < kHalf; j++) {
-                const int d = kHalf - 1 - j;
+            for (int j = 0; j < HM; j++) {
+                const int d = HM - 1 - j;
                 const df2 w = d2_of(wp[j - H]);
-                const df2 x = (Q == 2) ? d2_mac2(w, d2_of(ctab[2 * kHalf + d]), J1, d2_of(ctab[3 * kHalf + d]), J2)
-                                       : d2_mac1(w, d2_of(ctab[2 * kHalf + d]), J1);
+                const df2 x = (Q == 2) ? d2_mac2(w, d2_of(ctab[2 * HM + d]), J1, d2_of(ctab[3 * HM + d]), J2)
+                                       : d2_mac1(w, d2_of(ctab[2 * HM + d]), J1);
                 wd[j] = make_double2(df_to_double_kadd(d2_x(x), kadd), df_to_double_kadd(d2_y(x), kadd));
             }
         } else {
 #pragma unroll 1
-            for (int j = 0; j < kHalf; j++) {
-                const int d = kHalf - 1 - j;
+            for (int j = 0; j < HM; j++) {
+                const int d = HM - 1 - j;
                 const df2 w = d2_of(wp[j - H]);
-                const df2 x = (Q == 2) ? d2_mac2(w, d2_of(ctab[2 * kHalf + d]), J1, d2_of(ctab[3 * kHalf + d]), J2)
-                                       : d2_mac1(w, d2_of(ctab[2 * kHalf + d]), J1);
+                const df2 x = (Q == 2) ? d2_mac2(w, d2_of(ctab[2 * HM + d]), J1, d2_of(ctab[3 * HM + d]), J2)
+                                       : d2_mac1(w, d2_of(ctab[2 * HM + d]), J1);
                 wd[j] = make_double2(AR::store_scaled(d2_x(x), kl), AR::store_scaled(d2_y(x), kl));
             }
         }
     }
     __syncthreads();
 
-    // ---- J: coalesced stores; row q of chunk t is double 2 (q % 16) + q / 16 of its lane ----
+    // ---- J: coalesced stores; row q of chunk t is double 2 (q % HM) + q / HM of its lane ----
     const double* od = reinterpret_cast<const double*>(tile);
     auto out_pos = [&](int ll, int p) -> int {
-        const int tt = p >> 5, q = p & 31;
-        return ((ll * LT + tt * SL) << 1) + 2 * (q & 15) + (q >> 4);
+        const int tt = p / M, q = p % M;
+        return ((ll * LT + tt * SL) << 1) + 2 * (q % HM) + q / HM;
     };
     if (ls.op == 1) {
         const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
@@ -459,13 +464,13 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     if (bad) atomicOr(status, 1u);
 }
 
-template <int Q, int NP, bool SYM>
+template <int Q, int NP, bool SYM, int M>
 int launch_lhalf_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                    cudaStream_t s) {
     constexpr int NT = kLineThreadsCirc;
     const long blocks = (ls.nlines + c.L - 1) / c.L;
-    const size_t smem = sizeof(float4) * (4 * kHalf + (size_t)c.L * half_line_stride(c.P, NP));
-    auto kern = k_lhalf<Q, NP, SYM>;
+    const size_t smem = sizeof(float4) * (4 * (M / 2) + (size_t)c.L * half_line_stride(c.P, M / 2, NP));
+    auto kern = k_lhalf<Q, NP, SYM, M>;
     // the opt-in covers dynamic plus static shared memory (the per-line arrays, 2.5 KB)
     if (smem + 4096 > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

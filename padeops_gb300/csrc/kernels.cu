@@ -410,6 +410,26 @@ int DevicePlan::upload(const HostPlan& hp) {
         cline_.phf = own ? (const F2*)(lb + o_lk[4]) : cdf_.phf;
         cline_.phb = own ? (const F2*)(lb + o_lk[5]) : cdf_.phb;
     }
+    // the same centred periodic operator on the 16-row chunk plan, for the half-chunk kernel
+    half16_ = false;
+    if (line_shape_ >= SHAPE_T2A && line_shape_ <= SHAPE_P3S && cok_ && ch_.circ && cline_.alias && cline_.M == 32 &&
+        ch_.M == 16 && ch_.Pp >= 1 && kLineThreadsCirc % ch_.Pp == 0) {
+        chalf16_ = cline_;
+        chalf16_.M = 16;
+        chalf16_.ns = ch_.ns;
+        chalf16_.nout = ch_.nout;
+        chalf16_.P = ch_.P;
+        chalf16_.Pp = ch_.Pp;
+        chalf16_.nsteps = ch_.nsteps;
+        chalf16_.L = kLineThreadsCirc / ch_.Pp;
+        chalf16_.fscan = cdf_.fscan;
+        chalf16_.bscan = cdf_.bscan;
+        chalf16_.fwrap = cdf_.fwrap;
+        chalf16_.bwrap = cdf_.bwrap;
+        chalf16_.phf = cdf_.phf;
+        chalf16_.phb = cdf_.phb;
+        half16_ = true;
+    }
     return PS_OK;
 }
 
@@ -424,6 +444,19 @@ int DevicePlan::upload(const HostPlan& hp) {
 // instruction fetch; contiguous lines stage faster through shared memory).
 // PADE_LINE_KERNEL (a tuning override): "reg" the register kernel everywhere, "shared"
 // k_line everywhere.
+// Chunk length of the half-chunk kernel on lines that have both plans: PADE_HALF_CHUNK
+// (16 or 32, a tuning override); the default is the measured faster one.
+constexpr int kHalfChunkDefault = 32;
+static int half_chunk_choice() {
+    static const int v = [] {
+        const char* e = std::getenv("PADE_HALF_CHUNK");
+        if (e && std::atoi(e) == 16) return 16;
+        if (e && std::atoi(e) == 32) return 32;
+        return kHalfChunkDefault;
+    }();
+    return v;
+}
+
 static int line_kernel_choice() {
     static const int v = [] {
         const char* e = std::getenv("PADE_LINE_KERNEL");
@@ -464,7 +497,9 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
         }
         if (sh != SHAPE_NONE) {
             if (line_kernel_choice() != 2 && sh >= SHAPE_T2A && sh <= SHAPE_P3S) {
-                const int rc = launch_line_half(sh, p.line_params(), f, out, ls, status, s);
+                const StencilParams* h16 = p.half16_params();
+                const StencilParams& hc = (h16 && half_chunk_choice() == 16) ? *h16 : p.line_params();
+                const int rc = launch_line_half(sh, hc, f, out, ls, status, s);
                 if (rc != PS_ENOTSUP) return rc;
             }
             return launch_line(sh, p.line_params(), f, out, ls, status, s);

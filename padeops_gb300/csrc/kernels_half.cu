@@ -3,24 +3,31 @@
 
 namespace pade {
 
-// Periodic lines of whole 32-row chunks of the centred shapes with the input window reused;
-// PS_ENOTSUP for the rest (k_line runs those).
-int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
-                     unsigned* status, cudaStream_t s) {
-    if (!c.circ || !c.alias || c.M != 32 || c.xdup || c.ns % 32 != 0 || c.L < 1) return PS_ENOTSUP;
-    if (ls.fp == 1) {
-        if (c.ns / 32 > kHalfRowsContig) return PS_ENOTSUP;
-    } else {
-        const int pstep = kLineThreadsCirc / c.L;
-        if ((c.ns + pstep - 1) / pstep > kHalfRowsStrided) return PS_ENOTSUP;
-    }
+// Periodic lines of whole chunks (32 rows, or 16 with the 16-row plan's parameters) of the
+// centred shapes with the input window reused; PS_ENOTSUP for the rest (k_line runs those).
+template <int M>
+static int launch_half_m(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                         unsigned* status, cudaStream_t s) {
     switch (shape) {
-        case SHAPE_T2A: return launch_lhalf_t<1, 2, false>(c, f, out, ls, status, s);
-        case SHAPE_T2S: return launch_lhalf_t<1, 2, true>(c, f, out, ls, status, s);
-        case SHAPE_P3A: return launch_lhalf_t<2, 3, false>(c, f, out, ls, status, s);
-        case SHAPE_P3S: return launch_lhalf_t<2, 3, true>(c, f, out, ls, status, s);
+        case SHAPE_T2A: return launch_lhalf_t<1, 2, false, M>(c, f, out, ls, status, s);
+        case SHAPE_T2S: return launch_lhalf_t<1, 2, true, M>(c, f, out, ls, status, s);
+        case SHAPE_P3A: return launch_lhalf_t<2, 3, false, M>(c, f, out, ls, status, s);
+        case SHAPE_P3S: return launch_lhalf_t<2, 3, true, M>(c, f, out, ls, status, s);
         default: return PS_ENOTSUP;
     }
+}
+
+int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                     unsigned* status, cudaStream_t s) {
+    if (!c.circ || !c.alias || (c.M != 32 && c.M != 16) || c.xdup || c.ns % c.M != 0 || c.L < 1) return PS_ENOTSUP;
+    if (ls.fp == 1) {
+        if ((c.ns + 31) / 32 > kHalfRowsContig) return PS_ENOTSUP;
+    } else {
+        const int pstep = kLineThreadsCirc / c.L;
+        if ((c.ns + pstep - 1) / pstep > c.M) return PS_ENOTSUP;
+    }
+    return c.M == 32 ? launch_half_m<32>(shape, c, f, out, ls, status, s)
+                     : launch_half_m<16>(shape, c, f, out, ls, status, s);
 }
 
 }  // namespace pade

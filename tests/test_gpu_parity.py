@@ -126,10 +126,11 @@ def test_cd10_nonperiodic(oracle, bc1, bcn, dir, n):
 
 @pytest.mark.parametrize("fam", ["cd06", "cd10"])
 @pytest.mark.parametrize("dir", [1, 2, 3])
-@pytest.mark.parametrize("n", [32, 96, 160, 224])
+@pytest.mark.parametrize("n", [32, 48, 80, 96, 160, 224])
 def test_periodic_whole_chunks(oracle, fam, dir, n):
-    """Periodic lines of 1, 3, 5 and 7 chunks of 32 rows (the half-chunk line kernel: one
-    lane per line, idle lanes in the scan groups) over a ragged 7 x 5 set of lines."""
+    """Periodic lines of whole chunks for the half-chunk line kernel: 1, 3, 5 and 7 chunks of
+    32 rows (one lane per line, idle lanes in the scan groups) and 3 and 5 chunks of 16 rows
+    (lengths that are not multiples of 32), over a ragged 7 x 5 set of lines."""
     dx = 2 * np.pi / n
     o = getattr(P, fam)()
     assert o.init(n, dx, True) == 0
