@@ -106,6 +106,9 @@ class DevicePlan {
     // the line kernel's parameters on the 16-row chunk plan when line_params() is a 32-row
     // plan (null otherwise): the half-chunk kernel can take either
     const StencilParams* half16_params() const { return half16_ ? &chalf16_ : nullptr; }
+    // 32-row chunk parameters of a residual-form filter whose line_params() keep 16-row
+    // chunks for k_line (null otherwise)
+    const StencilParams* half32_params() const { return half32_ ? &chalf32_ : nullptr; }
     // register-resident periodic kernel (chunks of 32 rows), when the line shape allows it
     bool reg_ok() const { return reg_ok_; }
     const RegParams& reg_params() const { return *creg_; }
@@ -120,7 +123,9 @@ class DevicePlan {
     int line_shape_ = SHAPE_NONE;
     StencilParams cline_{};
     StencilParams chalf16_{};
+    StencilParams chalf32_{};
     bool half16_ = false;
+    bool half32_ = false;
     bool reg_ok_ = false;
     RegParams* creg_ = nullptr;
 };

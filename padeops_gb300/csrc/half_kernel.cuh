@@ -112,8 +112,10 @@ __host__ __device__ constexpr int half_line_stride(int p, int hm, int np) {
 constexpr int kHalfRowsContig = 8;
 
 // M: chunk rows (32, or 16 for twice the resident lines per SM: half the shared memory and
-// registers per thread for a longer lane scan)
-template <int Q, int NP, bool SYM, int M>
+// registers per thread for a longer lane scan).  RESID: a filter in residual form (cf90): the
+// solve gives x = A^-1 (A - B) f and the output is f - x, with f read again from the input
+// by the coalesced store (L2-resident by then), so the window can still be overwritten.
+template <int Q, int NP, bool SYM, int M, bool RESID>
 __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     k_lhalf(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
             unsigned* __restrict__ status) {
@@ -448,29 +450,38 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
         const int tt = p / M, q = p % M;
         return ((ll * LT + tt * SL) << 1) + 2 * (q % HM) + q / HM;
     };
+    // (residual form: each thread reads f at the points it writes, so an in-place call is safe)
     if (ls.op == 1) {
         const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
         for (int ll = warp; ll < nl; ll += nw) {
             double* o = out + base_out[ll];
-            for (int p = lane; p < cp.nout; p += 32) o[p] = od[out_pos(ll, p < ns ? p : p - ns)];
+            const double* fi = f + base_in[ll];
+            for (int p = lane; p < cp.nout; p += 32) {
+                const double x = od[out_pos(ll, p < ns ? p : p - ns)];
+                o[p] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
+            }
         }
     } else {
         const int ll = tid % L, pstep = nth / L;
         if (ll < nl) {
             double* o = out + base_out[ll];
-            for (int p = tid / L; p < cp.nout; p += pstep) o[(long)p * ls.op] = od[out_pos(ll, p < ns ? p : p - ns)];
+            const double* fi = f + base_in[ll];
+            for (int p = tid / L; p < cp.nout; p += pstep) {
+                const double x = od[out_pos(ll, p < ns ? p : p - ns)];
+                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
+            }
         }
     }
     if (bad) atomicOr(status, 1u);
 }
 
-template <int Q, int NP, bool SYM, int M>
+template <int Q, int NP, bool SYM, int M, bool RESID = false>
 int launch_lhalf_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                    cudaStream_t s) {
     constexpr int NT = kLineThreadsCirc;
     const long blocks = (ls.nlines + c.L - 1) / c.L;
     const size_t smem = sizeof(float4) * (4 * (M / 2) + (size_t)c.L * half_line_stride(c.P, M / 2, NP));
-    auto kern = k_lhalf<Q, NP, SYM, M>;
+    auto kern = k_lhalf<Q, NP, SYM, M, RESID>;
     // the opt-in covers dynamic plus static shared memory (the per-line arrays, 2.5 KB)
     if (smem + 4096 > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -270,6 +270,26 @@ int DevicePlan::upload(const HostPlan& hp) {
             line_shape_ = shape;
         }
     }
+    // residual-form filters (cf90) keep 16-row chunks for k_line; the half-chunk kernel
+    // takes 32-row chunks, with tables of their own
+    size_t o_h32[6] = {0, 0, 0, 0, 0, 0};
+    ChunkPlanHost h32;
+    bool h32_ok = false;
+    if (line_shape_ == SHAPE_P4S && cline_.M == 16 && cline_.resid && ch_.circ && d.ns % 32 == 0 &&
+        build_chunk_plan(hp, 32, h32) == PS_OK && h32.ok && kLineThreadsCirc % h32.Pp == 0) {
+        auto put = [&](const std::vector<double>& src) {
+            std::vector<F2> o(src.size());
+            for (size_t k = 0; k < src.size(); k++) o[k] = split(src[k]);
+            return A.put(o.data(), o.size() * sizeof(F2));
+        };
+        o_h32[0] = put(h32.fscan);
+        o_h32[1] = put(h32.bscan);
+        o_h32[2] = put(h32.fwrap);
+        o_h32[3] = put(h32.bwrap);
+        o_h32[4] = put(h32.phf);
+        o_h32[5] = put(h32.phb);
+        h32_ok = true;
+    }
     // register-resident periodic kernel: whole chunks of 32 rows, a power-of-two number of
     // lanes per line; coefficients and fundamental solutions travel in the kernel parameters
     size_t o_rg[4] = {0, 0, 0, 0};
@@ -410,6 +430,24 @@ int DevicePlan::upload(const HostPlan& hp) {
         cline_.phf = own ? (const F2*)(lb + o_lk[4]) : cdf_.phf;
         cline_.phb = own ? (const F2*)(lb + o_lk[5]) : cdf_.phb;
     }
+    half32_ = false;
+    if (h32_ok) {
+        chalf32_ = cline_;
+        chalf32_.M = 32;
+        chalf32_.ns = h32.ns;
+        chalf32_.nout = h32.nout;
+        chalf32_.P = h32.P;
+        chalf32_.Pp = h32.Pp;
+        chalf32_.nsteps = h32.nsteps;
+        chalf32_.L = kLineThreadsCirc / h32.Pp;
+        chalf32_.fscan = (const F2*)(base + o_h32[0]);
+        chalf32_.bscan = (const F2*)(base + o_h32[1]);
+        chalf32_.fwrap = (const F2*)(base + o_h32[2]);
+        chalf32_.bwrap = (const F2*)(base + o_h32[3]);
+        chalf32_.phf = (const F2*)(base + o_h32[4]);
+        chalf32_.phb = (const F2*)(base + o_h32[5]);
+        half32_ = true;
+    }
     // the same centred periodic operator on the 16-row chunk plan, for the half-chunk kernel
     half16_ = false;
     if (line_shape_ >= SHAPE_T2A && line_shape_ <= SHAPE_P3S && cok_ && ch_.circ && cline_.alias && cline_.M == 32 &&
@@ -496,10 +534,13 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
             if (rc != PS_ENOTSUP) return rc;
         }
         if (sh != SHAPE_NONE) {
-            if (line_kernel_choice() != 2 && sh >= SHAPE_T2A && sh <= SHAPE_P3S) {
+            if (line_kernel_choice() != 2 && sh >= SHAPE_T2A && sh <= SHAPE_P4S) {
                 const StencilParams* h16 = p.half16_params();
-                const StencilParams& hc = (h16 && half_chunk_choice() == 16) ? *h16 : p.line_params();
-                const int rc = launch_line_half(sh, hc, f, out, ls, status, s);
+                const StencilParams* h32 = p.half32_params();
+                const StencilParams* hc = &p.line_params();
+                if (h16 && half_chunk_choice() == 16) hc = h16;
+                if (h32 && half_chunk_choice() == 32) hc = h32;
+                const int rc = launch_line_half(sh, *hc, f, out, ls, status, s);
                 if (rc != PS_ENOTSUP) return rc;
             }
             return launch_line(sh, p.line_params(), f, out, ls, status, s);
