@@ -151,9 +151,9 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
 
     // ---- A: stage each line scaled by 2^-(e_max - 1023); row q of chunk t goes to pair
     // q % HM, component q / HM of lane t's window ----
-    auto hpos = [&](int l, int p) -> int {  // float index of row p's high part
-        const int t = p / M, q = p % M;
-        return ((l * LT + t * SL + H + q % HM) << 2) + q / HM;
+    auto hpos = [&](int l, int p) -> int {  // float index of row p's high part (p >= 0)
+        const unsigned t = (unsigned)p / M, q = (unsigned)p % M;
+        return ((l * LT + (int)t * SL + H + (int)(q % HM)) << 2) + (int)(q / HM);
     };
     float* tf = reinterpret_cast<float*>(tile);
     unsigned bad = 0;
@@ -447,8 +447,8 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     // ---- J: coalesced stores; row q of chunk t is double 2 (q % HM) + q / HM of its lane ----
     const double* od = reinterpret_cast<const double*>(tile);
     auto out_pos = [&](int ll, int p) -> int {
-        const int tt = p / M, q = p % M;
-        return ((ll * LT + tt * SL) << 1) + 2 * (q % HM) + q / HM;
+        const unsigned tt = (unsigned)p / M, q = (unsigned)p % M;
+        return ((ll * LT + (int)tt * SL) << 1) + 2 * (int)(q % HM) + (int)(q / HM);
     };
     // (residual form: each thread reads f at the points it writes, so an in-place call is safe)
     if (ls.op == 1) {
