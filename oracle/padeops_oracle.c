@@ -500,6 +500,56 @@ static void penta_solve(const double *P, int n, double *y, long ys) {
 #undef Y
 }
 
+/* The same two solves on nb lines at once: line j of the block at y + j, rows ys apart.  The
+ * reference's y and z solves (SolveYPenta1/2, SolveZPenta1/2, SolveYLU*, cd10.F90:751-899,
+ * 951-1090; cf90.F90:460-600) run each statement over a whole row of lines (array syntax over
+ * x); this restatement does the same, with every line's operations in the per-line order,
+ * so the results equal penta_solve / penta_cyclic_solve bit for bit. */
+enum { ORACLE_BLOCK = 16 };
+
+static void penta_solve_blk(const double *P, int n, double *y, long ys, int nb) {
+#define Y(i) y[((long)(i) - 1) * ys + j]
+    for (int j = 0; j < nb; j++) Y(2) = Y(2) - T(P, 2, 8) * Y(1);
+    for (int i = 3; i <= n; i++)
+        for (int j = 0; j < nb; j++) Y(i) = Y(i) - T(P, i, 9) * Y(i - 2) - T(P, i, 8) * Y(i - 1);
+    for (int j = 0; j < nb; j++) Y(n) = Y(n) * T(P, n, 7);
+    for (int j = 0; j < nb; j++) Y(n - 1) = Y(n - 1) * T(P, n - 1, 7) - T(P, n - 1, 10) * Y(n);
+    for (int i = n - 2; i >= 1; i--)
+        for (int j = 0; j < nb; j++)
+            Y(i) = Y(i) * T(P, i, 7) - Y(i + 2) * T(P, i, 5) * T(P, i, 7) - Y(i + 1) * T(P, i, 10);
+#undef Y
+}
+
+static void penta_cyclic_solve_blk(const double *LU, int n, double *y, long ys, int nb) {
+#define Y(i) y[((long)(i) - 1) * ys + j]
+    double sum1[ORACLE_BLOCK], sum2[ORACLE_BLOCK];
+    for (int j = 0; j < nb; j++) {
+        Y(2) = Y(2) - T(LU, 2, 1) * Y(1);
+        sum1[j] = T(LU, 1, 3) * Y(1) + T(LU, 2, 3) * Y(2);
+        sum2[j] = T(LU, 1, 4) * Y(1) + T(LU, 2, 4) * Y(2);
+    }
+    for (int i = 3; i <= n - 2; i++)
+        for (int j = 0; j < nb; j++) {
+            Y(i) = Y(i) - T(LU, i, 1) * Y(i - 1) - T(LU, i, 2) * Y(i - 2);
+            sum1[j] = sum1[j] + T(LU, i, 3) * Y(i);
+            sum2[j] = sum2[j] + T(LU, i, 4) * Y(i);
+        }
+    for (int j = 0; j < nb; j++) {
+        Y(n - 1) = Y(n - 1) - sum1[j];
+        Y(n) = (Y(n) - sum2[j] - T(LU, n - 1, 4) * Y(n - 1)) * T(LU, n, 5);
+        Y(n - 1) = (Y(n - 1) - T(LU, n - 1, 9) * Y(n)) * T(LU, n - 1, 5);
+        Y(n - 2) = (Y(n - 2) - T(LU, n - 2, 8) * Y(n - 1) - T(LU, n - 2, 9) * Y(n)) * T(LU, n - 2, 5);
+        Y(n - 3) = (Y(n - 3) - T(LU, n - 3, 6) * Y(n - 2) - T(LU, n - 3, 8) * Y(n - 1) - T(LU, n - 3, 9) * Y(n)) *
+                   T(LU, n - 3, 5);
+    }
+    for (int i = n - 4; i >= 1; i--)
+        for (int j = 0; j < nb; j++)
+            Y(i) = (Y(i) - T(LU, i, 6) * Y(i + 1) - T(LU, i, 7) * Y(i + 2) - T(LU, i, 8) * Y(n - 1) -
+                    T(LU, i, 9) * Y(n)) *
+                   T(LU, i, 5);
+#undef Y
+}
+
 /* index of bc in {0, 1, -1} -> 0..2, used to address the 9 precomputed factorisations */
 static int bcidx(int bc) { return bc == 0 ? 0 : (bc == 1 ? 1 : 2); }
 static int bc_ok(int bc) { return bc == 0 || bc == 1 || bc == -1; }
@@ -1433,6 +1483,24 @@ static void for_lines(int dir, const int *sin, const int *sout, const double *f,
     }
 }
 
+/* Blocks of nb lines that are consecutive in memory (y and z lines: consecutive x), for the
+ * blocked solves: right-hand sides line by line (the block's rows stay in cache), then one
+ * solve over the whole block. */
+typedef void (*block_fn)(const void *ctx, const double *f, long fs, double *g, long gs, int nb);
+
+static void for_line_blocks(int dir, const int *s, const double *f, double *g, block_fn fn, const void *ctx) {
+    long fps, las, lbs, fla_n;
+    long nl = lines_of(dir, s[0], s[1], s[2], &fps, &fla_n, &las, &lbs);
+    if (nl <= 0 || fla_n <= 0) return;
+    const long nbpa = (fla_n + ORACLE_BLOCK - 1) / ORACLE_BLOCK, nblk = nbpa * (nl / fla_n);
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < nblk; k++) {
+        const long b = k / nbpa, a0 = (k % nbpa) * ORACLE_BLOCK;
+        const int nb = (int)(fla_n - a0 < ORACLE_BLOCK ? fla_n - a0 : ORACLE_BLOCK);
+        fn(ctx, f + a0 * las + b * lbs, fps, g + a0 * las + b * lbs, fps, nb);
+    }
+}
+
 typedef struct { const cd06_t *o; int order; } cd06_ctx;
 static void cd06_fn(const void *c, const double *f, long fs, double *g, long gs) {
     const cd06_ctx *x = c;
@@ -1460,6 +1528,26 @@ static void cd10_fn(const void *c, const double *f, long fs, double *g, long gs)
     cd10_line(x->o, x->order, f, fs, g, gs, x->bc1, x->bcn);
 }
 
+/* cd10 on a block of nb consecutive lines (y, z): the reference's SolveY* / SolveZ* shape */
+static void cd10_blk_fn(const void *c, const double *f, long fs, double *g, long gs, int nb) {
+    const cd10_ctx *x = c;
+    const cd10_t *o = x->o;
+    if (o->n == 1) {
+        for (int j = 0; j < nb; j++) g[j] = 0.0;
+        return;
+    }
+    for (int j = 0; j < nb; j++) {
+        if (x->order == 1) cd10_rhs_d1(o, f + j, fs, g + j, gs, x->bc1, x->bcn);
+        else cd10_rhs_d2(o, f + j, fs, g + j, gs, x->bc1, x->bcn);
+    }
+    if (o->periodic) {
+        penta_cyclic_solve_blk(x->order == 1 ? o->LU1 : o->LU2, o->n, g, gs, nb);
+    } else {
+        const int id = bcidx(x->bc1) * 3 + bcidx(x->bcn);
+        penta_solve_blk(x->order == 1 ? o->penta1[id] : o->penta2[id], o->n, g, gs, nb);
+    }
+}
+
 ORACLE_API int oracle_cd10(int n, double dx, int periodic, int bc1, int bcn, int order, int dir, const double *f,
                            double *df, int n1, int n2, int n3) {
     if (!bc_ok(bc1) || !bc_ok(bcn)) return 324;
@@ -1468,7 +1556,8 @@ ORACLE_API int oracle_cd10(int n, double dx, int periodic, int bc1, int bcn, int
     if (ierr) { cd10_free(&o); return ierr; }
     int s[3] = {n1, n2, n3};
     cd10_ctx c = {&o, order, bc1, bcn};
-    for_lines(dir, s, s, f, df, cd10_fn, &c);
+    if (dir == 1) for_lines(dir, s, s, f, df, cd10_fn, &c);
+    else for_line_blocks(dir, s, f, df, cd10_blk_fn, &c);
     cd10_free(&o);
     return 0;
 }
@@ -1479,6 +1568,19 @@ static void cf90_fn(const void *c, const double *f, long fs, double *g, long gs)
     cf90_line(x->o, f, fs, g, gs, x->bc1, x->bcn);
 }
 
+/* cf90 on a block of nb consecutive lines (y, z) */
+static void cf90_blk_fn(const void *c, const double *f, long fs, double *g, long gs, int nb) {
+    const cf90_ctx *x = c;
+    const cf90_t *o = x->o;
+    if (o->n == 1) {
+        for (int j = 0; j < nb; j++) g[j] = f[j];
+        return;
+    }
+    for (int j = 0; j < nb; j++) cf90_rhs(o, f + j, fs, g + j, gs, x->bc1, x->bcn);
+    if (o->periodic) penta_cyclic_solve_blk(o->LU, o->n, g, gs, nb);
+    else penta_solve_blk(o->penta[bcidx(x->bc1) * 3 + bcidx(x->bcn)], o->n, g, gs, nb);
+}
+
 ORACLE_API int oracle_cf90(int n, int periodic, int bc1, int bcn, int dir, const double *f, double *ff, int n1,
                            int n2, int n3) {
     if (!bc_ok(bc1) || !bc_ok(bcn)) return 324;
@@ -1487,7 +1589,8 @@ ORACLE_API int oracle_cf90(int n, int periodic, int bc1, int bcn, int dir, const
     if (ierr) { cf90_free(&o); return ierr; }
     int s[3] = {n1, n2, n3};
     cf90_ctx c = {&o, bc1, bcn};
-    for_lines(dir, s, s, f, ff, cf90_fn, &c);
+    if (dir == 1) for_lines(dir, s, s, f, ff, cf90_fn, &c);
+    else for_line_blocks(dir, s, f, ff, cf90_blk_fn, &c);
     cf90_free(&o);
     return 0;
 }
