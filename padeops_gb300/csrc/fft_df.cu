@@ -41,34 +41,46 @@ namespace pade {
 
 namespace {
 
-struct cdf {
-    dfv r, i;
-};
+// A complex double-float value, packed for the FP32x2 instructions: the real and imaginary
+// parts are the two components of one df2 (h = (re_hi, im_hi), l = (re_lo, im_lo)), so a
+// complex sum, difference or real scaling is one packed double-float operation, and a
+// twiddle product two packed products and one packed sum.  Every component is rounded as
+// the scalar double-float code rounds it (the same operations in the same order), so the
+// results are those of the unpacked form.
+using cdf = df2;
+__device__ __forceinline__ dfv cre(cdf a) { return d2_x(a); }
+__device__ __forceinline__ dfv cim(cdf a) { return d2_y(a); }
+__device__ __forceinline__ cdf mkc(dfv re, dfv im) { return d2_pack(re, im); }
+__device__ __forceinline__ cdf czero() { return d2_zero(); }
 
-__device__ __forceinline__ cdf ldc(const float4* s, int idx) {
-    const float4 v = s[idx];
-    return cdf{dfv{v.x, v.y}, dfv{v.z, v.w}};
+// shared memory holds a value as {re_hi, im_hi, re_lo, im_lo}
+__device__ __forceinline__ cdf ldc(const float4* s, int idx) { return d2_of(s[idx]); }
+__device__ __forceinline__ void stc(float4* s, int idx, cdf c) { s[idx] = d2_f4(c); }
+
+__device__ __forceinline__ cdf cadd(cdf a, cdf b) { return d2_norm(d2_add(a, b)); }
+__device__ __forceinline__ cdf csub(cdf a, cdf b) { return d2_norm(d2_sub(a, b)); }
+
+// (im, re): the swap behind the cross terms of a complex product
+__device__ __forceinline__ cdf cswap(cdf a) {
+    return cdf{make_float2(a.h.y, a.h.x), make_float2(a.l.y, a.l.x)};
 }
-__device__ __forceinline__ void stc(float4* s, int idx, cdf c) { s[idx] = make_float4(c.r.h, c.r.l, c.i.h, c.i.l); }
 
-__device__ __forceinline__ cdf cadd(cdf a, cdf b) { return cdf{df_norm(df_add(a.r, b.r)), df_norm(df_add(a.i, b.i))}; }
-__device__ __forceinline__ cdf csub(cdf a, cdf b) { return cdf{df_norm(df_sub(a.r, b.r)), df_norm(df_sub(a.i, b.i))}; }
-
-// a * w (w a twiddle (c_hi, c_lo, s_hi, s_lo)); conj uses c - i s
+// a * w (w a twiddle (c_hi, c_lo, s_hi, s_lo)); conj uses c - i s.  With wi the imaginary
+// part used: (re, im) * (wr, wr) + (im, re) * (-wi, wi) = (re wr - im wi, im wr + re wi).
 __device__ __forceinline__ cdf cmulw(cdf a, float4 w, bool conj) {
-    const dfv wr{w.x, w.y};
-    const dfv wi = conj ? dfv{-w.z, -w.w} : dfv{w.z, w.w};
-    const dfv rr = df_sub(df_mul(a.r, wr), df_mul(a.i, wi));
-    const dfv ii = df_add(df_mul(a.r, wi), df_mul(a.i, wr));
-    return cdf{df_norm(rr), df_norm(ii)};
+    const float sh = conj ? -w.z : w.z, sl = conj ? -w.w : w.w;
+    const cdf p1 = d2_mul(a, cdf{make_float2(w.x, w.x), make_float2(w.y, w.y)});
+    const cdf p2 = d2_mul(cswap(a), cdf{make_float2(-sh, sh), make_float2(-sl, sl)});
+    return d2_norm(d2_add(p1, p2));
 }
 
 // -i a (forward), +i a (backward): exact
 __device__ __forceinline__ cdf mul_mi(cdf a, bool conj) {
-    return conj ? cdf{df_neg(a.i), a.r} : cdf{a.i, df_neg(a.r)};
+    return conj ? cdf{make_float2(-a.h.y, a.h.x), make_float2(-a.l.y, a.l.x)}
+                : cdf{make_float2(a.h.y, -a.h.x), make_float2(a.l.y, -a.l.x)};
 }
 
-__device__ __forceinline__ cdf cscale(cdf a, dfv m) { return cdf{df_norm(df_mul(a.r, m)), df_norm(df_mul(a.i, m))}; }
+__device__ __forceinline__ cdf cscale(cdf a, dfv m) { return d2_norm(d2_mul(a, d2_bcast(m))); }
 
 // W^t for t < 3N/4 from the table of t < N/2 (= nh): W^(t + N/2) = -W^t
 __device__ __forceinline__ float4 twiddle_ext(const float4* __restrict__ twg, int t, int nh) {
@@ -232,12 +244,12 @@ __device__ __forceinline__ void dit_df(float4* x, int nl, int logn, int lsd, con
 // c * 2^k as FP64: d(h) + d(l) with the shift on the exponent bits when |k| <= 800 (exact,
 // the same value as shifting the sum), else the checked shift of the sum
 __device__ __noinline__ double2 cstore_checked(cdf c, int k) {  // out of line: rare, keeps kernels small
-    return make_double2(shift_up(df_to_double(c.r), k), shift_up(df_to_double(c.i), k));
+    return make_double2(shift_up(df_to_double(cre(c)), k), shift_up(df_to_double(cim(c)), k));
 }
 __device__ __forceinline__ double2 cstore(cdf c, int k) {
     if (k >= -800 && k <= 800) {  // both parts scaled on their exponent bits, no range checks
         const unsigned kadd = (unsigned)(896 + k) << 20;
-        return make_double2(df_to_double_kadd(c.r, kadd), df_to_double_kadd(c.i, kadd));
+        return make_double2(df_to_double_kadd(cre(c), kadd), df_to_double_kadd(cim(c), kadd));
     }
     return cstore_checked(c, k);
 }
@@ -363,7 +375,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
         const int k = emax[e >> logn] - 1023;
         const int i = e + (e >> logn);
         const double2 v = smd[i];
-        stc(smf, i, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
+        stc(smf, i, mkc(df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)));
     }
     __syncthreads();
 
@@ -379,7 +391,7 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
             const int i = lxi[l], j = lyj[l];
             if (KIND == FK_DEALIAS) {
                 const bool keep = keep_ij[l] && fabs(ex.kc[f]) < ex.cut_c;
-                if (!keep) stc(smf, se, cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}});
+                if (!keep) stc(smf, se, czero());
             } else {
                 double m;
                 if (ex.mtab) {
@@ -435,9 +447,10 @@ __global__ void __launch_bounds__(256) k_fft_df(const void* in, void* out, const
     }
 }
 
-__device__ __forceinline__ cdf cconj(cdf a) { return cdf{a.r, df_neg(a.i)}; }
+__device__ __forceinline__ cdf cconj(cdf a) { return cdf{make_float2(a.h.x, -a.h.y), make_float2(a.l.x, -a.l.y)}; }
 __device__ __forceinline__ cdf chalf(cdf a) {
-    return cdf{dfv{0.5f * a.r.h, 0.5f * a.r.l}, dfv{0.5f * a.i.h, 0.5f * a.i.l}};
+    const float2 half = make_float2(0.5f, 0.5f);
+    return cdf{__fmul2_rn(a.h, half), __fmul2_rn(a.l, half)};
 }
 
 // Real transforms along x lines (fp == 1) of N = 2^logN points through one complex transform
@@ -513,13 +526,13 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
         const int k = emax[e >> logM] - 1023;
         const double2 v = smd[e];
-        stc(smf, e, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
+        stc(smf, e, mkc(df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)));
     }
     if (!R2C) {
         for (int l = threadIdx.x; l < nl; l += blockDim.x) {
             const int k = emax[l] - 1023;
             const double2 v = xlast_raw[l];
-            stc(xlast, l, cdf{df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)});
+            stc(xlast, l, mkc(df_from_double_shift(v.x, k), df_from_double_shift(v.y, k)));
         }
     }
     __syncthreads();
@@ -543,10 +556,10 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             if (k < M) {
                 t = cmulw(df, tw[k], false);
             } else {
-                t = cdf{df_neg(df.r), df_neg(df.i)};  // W^M = -1
+                t = d2_neg(df);  // W^M = -1
             }
             // X = (sm - i t) / 2, -i t = (t.i, -t.r)
-            cdf X = chalf(cdf{df_norm(df_add(sm.r, t.i)), df_norm(df_sub(sm.i, t.r))});
+            cdf X = chalf(cadd(sm, mul_mi(t, false)));
             if (use_scale_df) X = cscale(X, sdf);
             reinterpret_cast<double2*>(out)[lbout[l] + k] = cstore(X, emax[l] - 1023 + scale_exp);
         }
@@ -565,13 +578,13 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
                 const cdf sm = cadd(xk, c2);
                 cdf d = csub(xk, c2);
                 if (k > 0) d = cmulw(d, tw[k], true);
-                stc(smf, ik, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+                stc(smf, ik, cadd(sm, mul_mi(d, true)));  // sm + i d
             }
             if (k > 0) {  // Z'[k2], k2 = M - k in (M/2, M)
                 const cdf c1 = cconj(xk);
                 const cdf sm = cadd(xk2, c1);
                 const cdf d = cmulw(csub(xk2, c1), tw[k2], true);
-                stc(smf, ik2, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+                stc(smf, ik2, cadd(sm, mul_mi(d, true)));
             }
         }
         // k = M/2 pairs with itself: conj(W^(M/2)) = i
@@ -581,8 +594,8 @@ __global__ void __launch_bounds__(256) k_fft_df_real(const void* in, void* out, 
             const cdf c = cconj(x);
             const cdf sm = cadd(x, c);
             cdf d = csub(x, c);
-            d = cdf{df_neg(d.i), d.r};  // i * d
-            stc(smf, ih, cdf{df_norm(df_sub(sm.r, d.i)), df_norm(df_add(sm.i, d.r))});
+            d = mul_mi(d, true);  // i * d
+            stc(smf, ih, cadd(sm, mul_mi(d, true)));
         }
         __syncthreads();
         dif_df(smf, nl, logM, M, tw, true, 1);  // backward, bit-reversed
@@ -690,10 +703,10 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256(const void* in, void* out,
     cdf a[16];
 #pragma unroll
     for (int p1 = 0; p1 < 16; p1++) {
-        a[p1] = cdf{df_from_double_shift(v[p1].x, ke), df_from_double_shift(v[p1].y, ke)};
+        a[p1] = mkc(df_from_double_shift(v[p1].x, ke), df_from_double_shift(v[p1].y, ke));
         if (MUL == MUL_IK_A || MUL == MUL_IK_P) {  // i k x in double-float (the FP64 products ran on the FP64 pipe)
             const dfv k = kdf[MUL == MUL_IK_A ? l : 16 * p1 + j];
-            a[p1] = cdf{df_neg(df_norm(df_mul(a[p1].i, k))), df_norm(df_mul(a[p1].r, k))};
+            a[p1] = mul_mi(cscale(a[p1], k), true);
         }
     }
     // ---- DFT over p1, twiddles and exchange; then the DFT over j.  One copy of the DFT code
@@ -783,7 +796,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256_fk(const void* in, void* o
     const int ke = emax[l] - 1023;
     cdf a[16];
 #pragma unroll
-    for (int p1 = 0; p1 < 16; p1++) a[p1] = cdf{df_from_double_shift(v[p1].x, ke), df_from_double_shift(v[p1].y, ke)};
+    for (int p1 = 0; p1 < 16; p1++) a[p1] = mkc(df_from_double_shift(v[p1].x, ke), df_from_double_shift(v[p1].y, ke));
     // ---- forward (stages 0, 1), multiplier, backward (stages 2, 3): one copy of the DFT code
 #pragma unroll 1
     for (int st = 0; st < 4; st++) {
@@ -795,7 +808,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df256_fk(const void* in, void* o
             for (int k2 = 0; k2 < 16 && act; k2++) {
                 const int f = j + 16 * k2;
                 if (KIND == FK_DEALIAS) {
-                    if (!(keep_ij[l] && fabs(ex.kc[f]) < ex.cut_c)) a[k2] = cdf{dfv{0.0f, 0.0f}, dfv{0.0f, 0.0f}};
+                    if (!(keep_ij[l] && fabs(ex.kc[f]) < ex.cut_c)) a[k2] = czero();
                 } else {
                     const double m = ex.mtab ? ex.mtab[lg * 256 + brev(f, 8)]
                                              : fk_mult_call<KIND>(ex.ka[lxi[l]], ex.kb[lyj[l]], ex.kc[f],
@@ -855,7 +868,7 @@ __device__ __forceinline__ double dstore(dfv a, int k) {
 }
 // X split at line scale 2^k (the rare path of the derivative pair, out of line)
 __device__ __noinline__ cdf split_at(double2 x, int k) {
-    return cdf{df_from_double_shift(x.x, k), df_from_double_shift(x.y, k)};
+    return mkc(df_from_double_shift(x.x, k), df_from_double_shift(x.y, k));
 }
 
 template <bool DERIV>  // Y = i km X (DERIV) or the second half spectrum in2
@@ -942,8 +955,8 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
                 xi2 = dfv{xi0.h * shf, xi0.l * shf};
             } else {
                 const cdf x2 = split_at(v[p1], ke2);
-                xr2 = x2.r;
-                xi2 = x2.i;
+                xr2 = cre(x2);
+                xi2 = cim(x2);
             }
             yr = df_neg(df_norm(df_mul(xi2, k)));           // Re(i k X) (from the stored X)
             yi = edge ? df_zero() : df_norm(df_mul(xr2, k));  // Im(i k X)
@@ -952,8 +965,8 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
             yr = df_from_double_shift(w.x, ke2);
             yi = edge ? df_zero() : df_from_double_shift(w.y, ke2);
         }
-        a[p1] = qp <= 128 ? cdf{df_norm(df_sub(xr, yi)), df_norm(df_add(xi, yr))}
-                          : cdf{df_norm(df_add(xr, yi)), df_norm(df_sub(yr, xi))};
+        a[p1] = qp <= 128 ? mkc(df_norm(df_sub(xr, yi)), df_norm(df_add(xi, yr)))
+                          : mkc(df_norm(df_add(xr, yi)), df_norm(df_sub(yr, xi)));
     }
     // ---- backward four-step (one copy of the DFT code for both stages)
 #pragma unroll 1
@@ -979,8 +992,8 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_c2r_pair256(const double2* __
             cdf c = a[k2];
             if (use_scale_df) c = cscale(c, sdf);
             const long o = (long)(j + 16 * k2) * ls.op;
-            d1[o] = dstore(c.r, ks);
-            d2[o] = dstore(c.i, ks2);
+            d1[o] = dstore(cre(c), ks);
+            d2[o] = dstore(cim(c), ks2);
         }
     }
 }
@@ -1029,7 +1042,7 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_r2c_pair256(const double* __r
     const int ke1 = emax1[l] - 1023, ke2 = emax2[l] - 1023;
     cdf a[16];
 #pragma unroll
-    for (int p1 = 0; p1 < 16; p1++) a[p1] = cdf{df_from_double_shift(v[p1].x, ke1), df_from_double_shift(v[p1].y, ke2)};
+    for (int p1 = 0; p1 < 16; p1++) a[p1] = mkc(df_from_double_shift(v[p1].x, ke1), df_from_double_shift(v[p1].y, ke2));
 #pragma unroll 1
     for (int stage = 0; stage < 2; stage++) {
         dft16(a, false, tw);
@@ -1052,8 +1065,10 @@ __global__ void __launch_bounds__(256, 2) k_fft_df_r2c_pair256(const double* __r
         const int ks1 = ke1 + scale_exp, ks2 = ke2 + scale_exp;
         for (int k = j; k <= 128; k += 16) {
             const cdf zk = ldc(smf, l * LSD + k), zn = ldc(smf, l * LSD + ((256 - k) & 255));
-            cdf x1 = chalf(cdf{df_norm(df_add(zk.r, zn.r)), df_norm(df_sub(zk.i, zn.i))});
-            cdf x2 = chalf(cdf{df_norm(df_add(zk.i, zn.i)), df_norm(df_sub(zn.r, zk.r))});
+            // X1 = (zk + conj zn) / 2, X2 = -i (zk - conj zn) / 2
+            const cdf czn = cconj(zn);
+            cdf x1 = chalf(cadd(zk, czn));
+            cdf x2 = chalf(mul_mi(csub(zk, czn), false));
             if (use_scale_df) {
                 x1 = cscale(x1, sdf);
                 x2 = cscale(x2, sdf);

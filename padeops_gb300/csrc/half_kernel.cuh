@@ -31,54 +31,8 @@
 
 namespace pade {
 
-// two double-float values: component x is half A's row, y half B's
-struct df2 {
-    float2 h, l;
-};
-
-__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __fadd2_rn(a, f2neg(b)); }
-
-__device__ __forceinline__ df2 d2_zero() { return df2{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
-__device__ __forceinline__ df2 d2_of(float4 v) { return df2{make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
-__device__ __forceinline__ float4 d2_f4(df2 a) { return make_float4(a.h.x, a.h.y, a.l.x, a.l.y); }
-// a coefficient broadcast to both components ({h, h, l, l} in shared memory)
-__device__ __forceinline__ df2 d2_bcast(F2 c) { return df2{make_float2(c.h, c.h), make_float2(c.l, c.l)}; }
-__device__ __forceinline__ dfv d2_x(df2 a) { return dfv{a.h.x, a.l.x}; }
-__device__ __forceinline__ dfv d2_y(df2 a) { return dfv{a.h.y, a.l.y}; }
-__device__ __forceinline__ df2 d2_pack(dfv x, dfv y) { return df2{make_float2(x.h, y.h), make_float2(x.l, y.l)}; }
-__device__ __forceinline__ dfv d2c_scalar(float4 c) { return dfv{c.x, c.z}; }
-
-// df_add, df_norm and df_mul of dfmath.cuh, componentwise
-__device__ __forceinline__ df2 d2_add(df2 a, df2 b) {
-    const float2 s = f2add(a.h, b.h);
-    const float2 bb = f2sub(s, a.h);
-    const float2 e = f2add(f2sub(a.h, f2sub(s, bb)), f2sub(b.h, bb));
-    return df2{s, f2add(e, f2add(a.l, b.l))};
-}
-__device__ __forceinline__ df2 d2_neg(df2 a) { return df2{f2neg(a.h), f2neg(a.l)}; }
-__device__ __forceinline__ df2 d2_sub(df2 a, df2 b) { return d2_add(a, d2_neg(b)); }
-__device__ __forceinline__ df2 d2_norm(df2 a) {
-    const float2 s = f2add(a.h, a.l);
-    return df2{s, f2sub(a.l, f2sub(s, a.h))};
-}
-__device__ __forceinline__ df2 d2_mul(df2 a, df2 c) {
-    const float2 ph = __fmul2_rn(a.h, c.h);
-    float2 pe = __ffma2_rn(a.h, c.h, f2neg(ph));
-    pe = __ffma2_rn(a.h, c.l, pe);
-    pe = __ffma2_rn(a.l, c.h, pe);
-    return df2{ph, pe};
-}
-// base - c1 x1 - c2 x2 and acc + m0 v1 + m1 v2 (ArDF::fms2 / mac2, componentwise)
-__device__ __forceinline__ df2 d2_fms2(df2 base, df2 c1, df2 x1, df2 c2, df2 x2) {
-    return d2_norm(d2_sub(d2_sub(base, d2_mul(x1, c1)), d2_mul(x2, c2)));
-}
-__device__ __forceinline__ df2 d2_fms1(df2 base, df2 c1, df2 x1) { return d2_norm(d2_sub(base, d2_mul(x1, c1))); }
-__device__ __forceinline__ df2 d2_mac2(df2 acc, df2 m0, df2 v1, df2 m1, df2 v2) {
-    return d2_norm(d2_add(d2_add(acc, d2_mul(v1, m0)), d2_mul(v2, m1)));
-}
-__device__ __forceinline__ df2 d2_mac1(df2 acc, df2 m0, df2 v1) { return d2_norm(d2_add(acc, d2_mul(v1, m0))); }
+// a plan coefficient broadcast to both components
+__device__ __forceinline__ df2 d2_bcast(F2 c) { return d2_bcast(dfv{c.h, c.l}); }
 
 // right-hand side of rows (j, j + 16): the window pairs at p[-NP .. NP]
 template <int NP, bool SYM>
