@@ -409,15 +409,20 @@ __global__ void k_clip_neg(double* __restrict__ x, long n) {
     }
 }
 
-// tau = -2 nu Sij(idx)  (sgsmod_igrid.F90:188-193)
+// tau = -2 nu Sij(idx)  (sgsmod_igrid.F90:188-193), in double-float like the kernels above:
+// its two FP64 operations per value had kept it at 106 us per 256^3 launch against ~80 us
+// of HBM traffic
 __global__ void k_tau(Ptr9 d, int idx, const double* __restrict__ nu, double* __restrict__ out, long n) {
-    // off-diagonal: 2 nu * (0.5 (a + b)) is nu * (a + b) exactly (power-of-two scalings), two
-    // FP64 instructions instead of four (the kernel runs at the FP64 issue rate)
+    // off-diagonal: 2 nu * (0.5 (a + b)) is nu * (a + b) exactly (power-of-two scalings)
     const int ia = idx == 1 ? 1 : (idx == 2 ? 2 : 5), ib = idx == 1 ? 3 : (idx == 2 ? 6 : 7);
     if (idx == 1 || idx == 2 || idx == 4) {
-        GRID_STRIDE(e, n) { out[e] = -mul(nu[e], add(d.p[ia][e], d.p[ib][e])); }
+        GRID_STRIDE(e, n) {
+            const dfv s = df_norm(df_add(dsp(d.p[ia][e]), dsp(d.p[ib][e])));
+            out[e] = -dfo(df_mul(dsp(nu[e]), s));
+        }
     } else {
-        GRID_STRIDE(e, n) { out[e] = -mul(2.0 * nu[e], sij(d.p, idx, e)); }
+        const int id = idx == 0 ? 0 : (idx == 3 ? 4 : 8);
+        GRID_STRIDE(e, n) { out[e] = -dfo(df_mul(dscale(dsp(nu[e]), 2.0f), dsp(d.p[id][e]))); }
     }
 }
 
