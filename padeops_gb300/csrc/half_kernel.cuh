@@ -34,11 +34,23 @@ namespace pade {
 // a plan coefficient broadcast to both components
 __device__ __forceinline__ df2 d2_bcast(F2 c) { return d2_bcast(dfv{c.h, c.l}); }
 
-// right-hand side of rows (j, j + 16): the window pairs at p[-NP .. NP]
-template <int NP, bool SYM>
+// right-hand side of rows (j, j + 16): the window pairs at p[-NP .. NP]; pairs k = 1..NP at
+// offsets (k, -k) about the row (STG = 0), or about a half point: (k, 1 - k) (STG = +1, edges
+// to cells) or (k - 1, -k) (STG = -1, cells to edges), in k_line's operation order
+template <int NP, bool SYM, int STG = 0>
 __device__ __forceinline__ df2 half_stencil(const float4* p, const df2 (&c)[NP], df2 c0) {
     df2 acc;
-    if constexpr (SYM) {
+    if constexpr (STG != 0) {
+        constexpr int sh = STG > 0 ? 0 : -1;
+        acc = SYM ? d2_mul(d2_add(d2_of(p[1 + sh]), d2_of(p[sh])), c[0])
+                  : d2_mul(d2_sub(d2_of(p[1 + sh]), d2_of(p[sh])), c[0]);
+#pragma unroll
+        for (int k = 2; k <= NP; k++) {
+            const df2 d = SYM ? d2_add(d2_of(p[k + sh]), d2_of(p[1 - k + sh]))
+                              : d2_sub(d2_of(p[k + sh]), d2_of(p[1 - k + sh]));
+            acc = d2_add(acc, d2_mul(d, c[k - 1]));
+        }
+    } else if constexpr (SYM) {
         acc = d2_mul(d2_of(p[0]), c0);
 #pragma unroll
         for (int k = 1; k <= NP; k++) acc = d2_add(acc, d2_mul(d2_add(d2_of(p[k]), d2_of(p[-k])), c[k - 1]));
@@ -69,7 +81,10 @@ constexpr int kHalfRowsContig = 8;
 // registers per thread for a longer lane scan).  RESID: a filter in residual form (cf90): the
 // solve gives x = A^-1 (A - B) f and the output is f - x, with f read again from the input
 // by the coalesced store (L2-resident by then), so the window can still be overwritten.
-template <int Q, int NP, bool SYM, int M, bool RESID>
+// STG: the staggered cd06stagg shapes (+1 edges to cells, -1 cells to edges; with xdup the
+// stored edge n + 1 is read as the first row above the top, as the reference's periodic RHS
+// reads it, cd06stagg.F90:319, 544)
+template <int Q, int NP, bool SYM, int M, bool RESID, int STG = 0>
 __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     k_lhalf(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
             unsigned* __restrict__ status) {
@@ -195,6 +210,15 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
             hi[2] = tf[ob + 2];
             hi[1] = tf[op];
             hi[3] = tf[op + 2];
+            if constexpr (STG > 0) {
+                if (pp == ns && cp.xdup) {
+                    const double v = __ldg(f + base_in[l] + (long)ns * ls.fp);
+                    bad |= (unsigned)(bexp(v) == 2047);
+                    const dfv d = df_from_double_shift(v, lexp[l] - 1023);
+                    hi[1] = d.h;
+                    hi[3] = d.l;
+                }
+            }
         }
     }
     // the neighbouring lanes of a line (one warp) read this lane's first and last rows
@@ -214,7 +238,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     if (active) {
 #pragma unroll 4
         for (int j = 0; j < HM; j++) {
-            const df2 r = half_stencil<NP, SYM>(wp + j, cc, c0);
+            const df2 r = half_stencil<NP, SYM, STG>(wp + j, cc, c0);
             const df2 y = (Q == 2) ? d2_fms2(r, a1, S1, a2, S2) : d2_fms1(r, a1, S1);
             wp[j - H] = d2_f4(y);
             S2 = S1;
@@ -429,13 +453,13 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     if (bad) atomicOr(status, 1u);
 }
 
-template <int Q, int NP, bool SYM, int M, bool RESID = false>
+template <int Q, int NP, bool SYM, int M, bool RESID = false, int STG = 0>
 int launch_lhalf_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
                    cudaStream_t s) {
     constexpr int NT = kLineThreadsCirc;
     const long blocks = (ls.nlines + c.L - 1) / c.L;
     const size_t smem = sizeof(float4) * (4 * (M / 2) + (size_t)c.L * half_line_stride(c.P, M / 2, NP));
-    auto kern = k_lhalf<Q, NP, SYM, M, RESID>;
+    auto kern = k_lhalf<Q, NP, SYM, M, RESID, STG>;
     // the opt-in covers dynamic plus static shared memory (the per-line arrays, 2.5 KB)
     if (smem + 4096 > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -474,14 +474,6 @@ int DevicePlan::upload(const HostPlan& hp) {
 // ------------------------------------------------------------------------------------
 // launch
 // ------------------------------------------------------------------------------------
-// Which periodic line kernel runs: the register-resident one for the FP32 path; for
-// double-float the register kernel only on tridiagonal operators along strided lines
-// (measured 5-7 % faster there), otherwise the half-chunk kernel k_lhalf (packed FP32x2
-// arithmetic) where its shapes and sizes apply and the shared-memory k_line for the rest
-// (the unrolled pentadiagonal double-float code of the register kernel stalls on
-// instruction fetch; contiguous lines stage faster through shared memory).
-// PADE_LINE_KERNEL (a tuning override): "reg" the register kernel everywhere, "shared"
-// k_line everywhere.
 // Chunk length of the half-chunk kernel on lines that have both plans: PADE_HALF_CHUNK
 // (16 or 32, a tuning override); the default is the measured faster one.
 constexpr int kHalfChunkDefault = 32;
@@ -495,11 +487,21 @@ static int half_chunk_choice() {
     return v;
 }
 
+// Which periodic line kernel runs: the register-resident one for the FP32 path; for
+// double-float the half-chunk kernel k_lhalf (packed FP32x2 arithmetic) wherever its shapes
+// and sizes apply (it measured faster than both others: cd10 x/y 7-11 %, cf90 6-15 % against
+// k_line, the staggered z operators ~10 % against the register kernel), else the register
+// kernel for tridiagonal operators along strided lines (5-7 % faster than k_line there), else
+// the shared-memory k_line (the unrolled pentadiagonal double-float code of the register
+// kernel stalls on instruction fetch; contiguous lines stage faster through shared memory).
+// PADE_LINE_KERNEL (a tuning override): "reg" the register kernel everywhere, "shared"
+// k_line everywhere, "half" k_lhalf wherever it applies (no register kernel).
 static int line_kernel_choice() {
     static const int v = [] {
         const char* e = std::getenv("PADE_LINE_KERNEL");
         if (e && std::strcmp(e, "reg") == 0) return 1;
         if (e && std::strcmp(e, "shared") == 0) return 2;
+        if (e && std::strcmp(e, "half") == 0) return 3;
         return 0;
     }();
     return v;
@@ -529,20 +531,21 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
     if (path == PATH_DF) {
         const int sh = p.line_shape();
         const bool tri = sh == SHAPE_T2A || sh == SHAPE_T2S || sh >= SHAPE_T2A_E2C;
-        if (p.reg_ok() && (line_kernel_choice() == 1 || (line_kernel_choice() == 0 && tri && ls.fp != 1))) {
+        const int choice = line_kernel_choice();
+        if ((choice == 0 || choice == 3) && sh >= SHAPE_T2A && sh <= SHAPE_T2S_C2E) {
+            const StencilParams* h16 = p.half16_params();
+            const StencilParams* h32 = p.half32_params();
+            const StencilParams* hc = &p.line_params();
+            if (h16 && half_chunk_choice() == 16) hc = h16;
+            if (h32 && half_chunk_choice() == 32) hc = h32;
+            const int rc = launch_line_half(sh, *hc, f, out, ls, status, s);
+            if (rc != PS_ENOTSUP) return rc;
+        }
+        if (p.reg_ok() && (choice == 1 || (choice == 0 && tri && ls.fp != 1))) {
             const int rc = launch_line_reg(sh, p.reg_params(), 0, f, out, ls, status, s);
             if (rc != PS_ENOTSUP) return rc;
         }
         if (sh != SHAPE_NONE) {
-            if (line_kernel_choice() != 2 && sh >= SHAPE_T2A && sh <= SHAPE_P4S) {
-                const StencilParams* h16 = p.half16_params();
-                const StencilParams* h32 = p.half32_params();
-                const StencilParams* hc = &p.line_params();
-                if (h16 && half_chunk_choice() == 16) hc = h16;
-                if (h32 && half_chunk_choice() == 32) hc = h32;
-                const int rc = launch_line_half(sh, *hc, f, out, ls, status, s);
-                if (rc != PS_ENOTSUP) return rc;
-            }
             return launch_line(sh, p.line_params(), f, out, ls, status, s);
         }
         return h.M == 16 ? launch_chunk_m<ArDF, 16>(h, p.chunk_df(), f, out, ls, status, s)

@@ -3,9 +3,9 @@
 
 namespace pade {
 
-// Periodic lines of whole chunks (32 rows, or 16 with the 16-row plan's parameters) of the
-// centred shapes: the derivatives (window reused) and cf90 in residual form; PS_ENOTSUP for
-// the rest (k_line runs those).
+// Periodic lines of whole chunks (32 rows, or 16 with the 16-row plan's parameters): the
+// centred derivatives (window reused), cf90 in residual form and (32-row chunks) the
+// staggered cd06stagg shapes; PS_ENOTSUP for the rest (k_line runs those).
 template <int M>
 static int launch_half_m(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                          unsigned* status, cudaStream_t s) {
@@ -15,13 +15,26 @@ static int launch_half_m(int shape, const StencilParams& c, const void* f, void*
         case SHAPE_P3A: return launch_lhalf_t<2, 3, false, M>(c, f, out, ls, status, s);
         case SHAPE_P3S: return launch_lhalf_t<2, 3, true, M>(c, f, out, ls, status, s);
         case SHAPE_P4S: return c.resid ? launch_lhalf_t<2, 4, true, M, true>(c, f, out, ls, status, s) : PS_ENOTSUP;
-        default: return PS_ENOTSUP;
+        default: break;
     }
+    if constexpr (M == 32) {  // the staggered shapes run in chunks of 32 only
+        switch (shape) {
+            case SHAPE_T2A_E2C: return launch_lhalf_t<1, 2, false, 32, false, 1>(c, f, out, ls, status, s);
+            case SHAPE_T2S_E2C: return launch_lhalf_t<1, 2, true, 32, false, 1>(c, f, out, ls, status, s);
+            case SHAPE_T2A_C2E: return launch_lhalf_t<1, 2, false, 32, false, -1>(c, f, out, ls, status, s);
+            case SHAPE_T2S_C2E: return launch_lhalf_t<1, 2, true, 32, false, -1>(c, f, out, ls, status, s);
+            default: break;
+        }
+    }
+    return PS_ENOTSUP;
 }
 
 int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                      unsigned* status, cudaStream_t s) {
-    if (!c.circ || (c.M != 32 && c.M != 16) || c.xdup || c.ns % c.M != 0 || c.L < 1) return PS_ENOTSUP;
+    const bool stagg = shape >= SHAPE_T2A_E2C && shape <= SHAPE_T2S_C2E;
+    if (!c.circ || (c.M != 32 && c.M != 16) || (c.xdup && !(shape == SHAPE_T2A_E2C || shape == SHAPE_T2S_E2C)) ||
+        c.ns % c.M != 0 || c.L < 1 || (stagg && c.M != 32))
+        return PS_ENOTSUP;
     if (c.alias == (shape == SHAPE_P4S) || (shape == SHAPE_P4S && (!c.resid || c.nout != c.ns))) return PS_ENOTSUP;
     if (ls.fp == 1) {
         if ((c.ns + 31) / 32 > kHalfRowsContig) return PS_ENOTSUP;

@@ -7,8 +7,8 @@ chunks).  The library picks per path, operator and line (FP32: the register kern
 double-float: the register kernel for tridiagonal operators along strided lines, k_lhalf
 for the centred derivatives and cf90 where it applies, k_line otherwise), so the regular
 parity tests see each kernel only on the cases it is picked for.  Here the periodic parity
-tests run again with each choice forced (PADE_LINE_KERNEL = reg / shared, PADE_HALF_CHUNK =
-16; read once per process, so in a fresh process), at the same tolerances.
+tests run again with each choice forced (PADE_LINE_KERNEL = reg / shared / half,
+PADE_HALF_CHUNK = 16; read once per process, so in a fresh process), at the same tolerances.
 """
 import os
 import subprocess
@@ -22,7 +22,7 @@ SELECT = ("cd06 or cd10_periodic or cf90 or stagg_periodic or fp32_path or bench
           "periodic_whole_chunks")
 
 
-@pytest.mark.parametrize("kernel", ["reg", "shared", "half16"])
+@pytest.mark.parametrize("kernel", ["reg", "shared", "half", "half16"])
 def test_periodic_parity_with_each_line_kernel(native_lib, kernel):
     env = dict(os.environ)
     if kernel == "half16":
