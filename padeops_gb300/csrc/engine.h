@@ -83,6 +83,8 @@ struct StencilParams {
     const F2* bwrap;
     const F2* phf;    // circulant: kLineM x 2 per chunk position; banded: ns x 2 per row
     const F2* phb;
+    const void* hpair;  // banded half-chunk kernel: the leading lanes', last lane's and interior tables (float4)
+    int hnf;            // banded half-chunk kernel: leading lanes with tables of their own
 };
 
 struct RegParams;  // reg_kernel.cuh
@@ -109,6 +111,9 @@ class DevicePlan {
     // 32-row chunk parameters of a residual-form filter whose line_params() keep 16-row
     // chunks for k_line (null otherwise)
     const StencilParams* half32_params() const { return half32_ ? &chalf32_ : nullptr; }
+    // banded lines whose per-row tables are one interior pattern between the two end lanes:
+    // the banded half-chunk kernel's parameters (null otherwise)
+    const StencilParams* half_band_params() const { return halfb_ ? &chalfb_ : nullptr; }
     // register-resident periodic kernel (chunks of 32 rows), when the line shape allows it
     bool reg_ok() const { return reg_ok_; }
     const RegParams& reg_params() const { return *creg_; }
@@ -124,8 +129,10 @@ class DevicePlan {
     StencilParams cline_{};
     StencilParams chalf16_{};
     StencilParams chalf32_{};
+    StencilParams chalfb_{};
     bool half16_ = false;
     bool half32_ = false;
+    bool halfb_ = false;
     bool reg_ok_ = false;
     RegParams* creg_ = nullptr;
 };
@@ -140,6 +147,10 @@ int launch_line_f32(int shape, const StencilParams& c, const void* f, void* out,
 // shapes and sizes it does not take.
 int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                      unsigned* status, cudaStream_t s);
+// Banded half-chunk line kernel (half_kernel.cuh), double-float: PS_ENOTSUP for the shapes
+// and sizes it does not take.
+int launch_line_half_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                          unsigned* status, cudaStream_t s);
 // Register-resident periodic line kernel (reg_kernel.cuh): double-float (fp32 = 0, FP64
 // in and out) or FP32.  PS_ENOTSUP for shapes it does not instantiate.
 int launch_line_reg(int shape, const RegParams& c, int fp32, const void* f, void* out, const LineSet& ls,

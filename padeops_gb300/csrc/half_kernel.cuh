@@ -469,7 +469,407 @@ int launch_lhalf_t(const StencilParams& c, const void* f, void* out, const LineS
     return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
 }
 
+
+// ------------------------------------------------------------------------------------
+// Banded (non-periodic) lines: the same pairing on the 16-row chunk plan, two chunks per
+// lane (chunk 2t is half A, chunk 2t + 1 half B); the plan's own log-step scan is kept, its
+// step 0 (chunk 2t + 1 after chunk 2t) inside the lane and steps k >= 1 across lanes
+// 2^(k-1) apart.  The nine per-row tables (g, a1, a2, b1, b2, pf1, pf2, pb1, pb2) of a banded
+// line differ from row to row only near its ends: the LU factors and the chunk fundamental
+// solutions converge to a fixed pattern some rows in from the top (within the first lane for
+// cd10, three lanes for cf90, whose matrix is nearly singular at the Nyquist mode) and change
+// again only in the closure rows at the bottom.  The plan finds the fewest leading lanes NF
+// after which every interior lane's rows equal the last interior lane's within 2^-50 of each
+// table's largest value (far below the double-float representation) and ships NF + 2 blocks
+// in pair layout: the NF leading lanes' rows, the last lane's and the interior pattern,
+// {h(row j), h(row 16 + j), l(row j), l(row 16 + j)} per table and j; 2.3 KB each in shared
+// memory instead of 18 KB of per-row tables, which did not fit beside the windows.  The edge rows (one-sided closures) are summed in FP64 from
+// the FP64 input as in k_line and replace the stencil in their component; halo rows beyond
+// the line ends are zero.
+// ------------------------------------------------------------------------------------
+constexpr int kHalf = 16;  // rows per half of a 32-row chunk
+constexpr int kHalfBandTables = 9;
+constexpr int kHalfBandBlock = kHalfBandTables * kHalf;  // float4 per block (first, last, interior)
+
+template <int Q, int NP, bool SYM, bool RESID>
+__global__ void __launch_bounds__(kLineThreadsCirc, 4)
+    k_lhalf_band(const StencilParams cp, const double* __restrict__ f, double* __restrict__ out, const LineSet ls,
+                 unsigned* __restrict__ status) {
+    using AR = ArDF;
+    using V = dfv;
+    constexpr int H = NP, M = 32, HM = kHalf;
+    constexpr int SL = half_lane_stride(HM, NP);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int ns = cp.ns, L = cp.L;
+    const int PL = ns / M;         // lanes per line
+    const int PLp = cp.Pp >> 1;    // lanes per line, padded to a power of two
+    const int LT = half_line_stride(PL, HM, NP);
+    const int ne = cp.nlo + cp.nhi, ehi = ns - cp.nhi;
+    const int NF = cp.hnf;                                   // leading lanes with tables of their own
+    float4* btab = reinterpret_cast<float4*>(smem_raw);     // NF leading lanes, last lane, interior
+    float4* tile = btab + (NF + 2) * kHalfBandBlock;        // L lines x PL lanes x SL
+    V* edge = reinterpret_cast<V*>(tile + (size_t)L * LT);  // L x ne edge-row right-hand sides
+    long* base_in = reinterpret_cast<long*>(edge + (size_t)L * ne);
+    long* base_out = base_in + L;
+    int* lexp = reinterpret_cast<int*>(base_out + L);
+
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const long line0 = (long)blockIdx.x * L;
+    const int nl = (int)min((long)L, ls.nlines - line0);
+    for (int i = tid; i < L; i += nth) {
+        lexp[i] = 0;
+        const long lg = line0 + i;
+        const long a = lg % ls.na, b = lg / ls.na;
+        base_in[i] = a * ls.fa + b * ls.fb;
+        base_out[i] = a * ls.oa + b * ls.ob;
+    }
+    {
+        const float4* __restrict__ g = reinterpret_cast<const float4*>(cp.hpair);
+        for (int i = tid; i < (NF + 2) * kHalfBandBlock; i += nth) btab[i] = __ldg(g + i);
+    }
+    __syncthreads();
+
+    auto hpos = [&](int l, int p) -> int {  // float index of row p's high part (p >= 0)
+        const unsigned t = (unsigned)p / M, q = (unsigned)p % M;
+        return ((l * LT + (int)t * SL + H + (int)(q % HM)) << 2) + (int)(q / HM);
+    };
+    float* tf = reinterpret_cast<float*>(tile);
+    unsigned bad = 0;
+    // ---- A: staging, as for periodic lines ----
+    if (ls.fp == 1) {
+        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+        const int U = (ns + 31) >> 5;
+        for (int l = warp; l < nl; l += nw) {
+            const double* src = f + base_in[l];
+            double v[kHalfRowsContig];
+            int mx = 0;
+#pragma unroll
+            for (int u = 0; u < kHalfRowsContig; u++) {
+                v[u] = (u < U && lane + 32 * u < ns) ? __ldg(src + lane + 32 * u) : 0.0;
+                mx = max(mx, bexp(v[u]));
+            }
+            mx = (int)__reduce_max_sync(0xffffffffu, (unsigned)mx);
+            bad |= (unsigned)(mx == 2047);
+            if (lane == 0) lexp[l] = mx;
+            const SplitK sk = split_consts(mx - 1023);
+            float* lf = tf + hpos(l, lane);
+#pragma unroll
+            for (int u = 0; u < kHalfRowsContig; u++) {
+                if (u < U && lane + 32 * u < ns) {
+                    const dfv d = df_split_line(v[u], sk);
+                    lf[u * SL * 4] = d.h;
+                    lf[u * SL * 4 + 2] = d.l;
+                }
+            }
+        }
+    } else {
+        const int pstep = nth / L;
+        const int U = (ns + pstep - 1) / pstep;
+        const int l = tid % L, q0 = tid / L;
+        double v[M];
+        int mx = 0;
+        if (l < nl) {
+            const double* src = f + base_in[l];
+#pragma unroll
+            for (int u = 0; u < M; u++) {
+                const int p = q0 + pstep * u;
+                v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
+                mx = max(mx, bexp(v[u]));
+            }
+            atomicMax(&lexp[l], mx);
+        }
+        __syncthreads();
+        if (l < nl) {
+            const int mxl = lexp[l];
+            bad |= (unsigned)(mxl == 2047);
+            const SplitK sk = split_consts(mxl - 1023);
+#pragma unroll
+            for (int u = 0; u < M; u++) {
+                const int p = q0 + pstep * u;
+                if (u < U && p < ns) {
+                    const dfv d = df_split_line(v[u], sk);
+                    const int o = hpos(l, p);
+                    tf[o] = d.h;
+                    tf[o + 2] = d.l;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    const int t = tid % PLp, l = tid / PLp;
+    const bool active = (l < nl) && (t < PL);
+    // this lane's tables: its own (leading lanes), the last lane's, or the interior pattern
+    const float4* tb = btab + (t < NF ? t : (t >= PL - 1 ? NF : NF + 1)) * kHalfBandBlock;
+    auto tab = [&](int k, int j) -> df2 { return d2_of(tb[k * HM + j]); };
+    float4* wp = tile + (size_t)l * LT + t * SL + H;
+    float* wf = reinterpret_cast<float*>(wp);
+
+    // ---- halo pairs (zero beyond the line ends) ----
+    if (active) {
+#pragma unroll
+        for (int h = 1; h <= H; h++) {
+            const int pm = t * M - h, pp = t * M + M - 1 + h;
+            const int oa = hpos(l, t * M + HM - h), ob = hpos(l, t * M + HM - 1 + h);
+            float* lo = wf + 4 * (-h);
+            float* hi = wf + 4 * (HM - 1 + h);
+            if (pm >= 0) {
+                const int om = hpos(l, pm);
+                lo[0] = tf[om];
+                lo[2] = tf[om + 2];
+            } else {
+                lo[0] = 0.0f;
+                lo[2] = 0.0f;
+            }
+            lo[1] = tf[oa];
+            lo[3] = tf[oa + 2];
+            hi[0] = tf[ob];
+            hi[2] = tf[ob + 2];
+            if (pp < ns) {
+                const int op = hpos(l, pp);
+                hi[1] = tf[op];
+                hi[3] = tf[op + 2];
+            } else {
+                hi[1] = 0.0f;
+                hi[3] = 0.0f;
+            }
+        }
+    }
+    // ---- edge rows: one-sided right-hand sides in FP64 from the FP64 input, each input
+    // scaled by the line's power of two first (exact) ----
+    for (int it = tid; it < nl * ne; it += nth) {
+        const int ll = it / ne, e = it - ll * ne;
+        const double* src = f + base_in[ll];
+        const double sc = scalbn(1.0, 1023 - lexp[ll]);
+        double acc = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < cp.tw; k++) {
+            const int idx = __ldg(cp.tidx + e * cp.tw + k);
+            acc = __fma_rn(__ldg(cp.tcd + e * cp.tw + k), __dmul_rn(__ldg(src + (long)idx * ls.fp), sc), acc);
+        }
+        edge[it] = df_from_double_shift(acc, 0);
+    }
+    // the neighbouring lanes have read this lane's first and last rows, the edge rows are
+    // complete
+    __syncthreads();
+
+    df2 cc[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) cc[k] = d2_bcast(cp.c[k]);
+    const df2 c0 = d2_bcast(cp.c0);
+
+    // ---- B: right-hand side (edge rows in their component), row scale g, forward
+    // recurrence of both halves from zero states ----
+    df2 S1 = d2_zero(), S2 = d2_zero();
+    if (active) {
+        const int iA0 = t * M, iB0 = t * M + HM;
+#pragma unroll 4
+        for (int j = 0; j < HM; j++) {
+            df2 r = half_stencil<NP, SYM>(wp + j, cc, c0);
+            if (iA0 + j < cp.nlo) {
+                const V e = edge[l * ne + iA0 + j];
+                r.h.x = e.h;
+                r.l.x = e.l;
+            }
+            if (iB0 + j >= ehi) {
+                const V e = edge[l * ne + cp.nlo + (iB0 + j - ehi)];
+                r.h.y = e.h;
+                r.l.y = e.l;
+            }
+            r = d2_mul(r, tab(0, j));
+            const df2 y = (Q == 2) ? d2_fms2(r, tab(1, j), S1, tab(2, j), S2) : d2_fms1(r, tab(1, j), S1);
+            wp[j - H] = d2_f4(y);
+            S2 = S1;
+            S1 = y;
+        }
+    }
+    // ---- D: the plan's scan over 16-row chunks; step 0 (chunk 2t + 1 after chunk 2t) in the lane ----
+    const dfv yA15 = d2_x(S1), yA14 = d2_x(S2);
+    V s1, s2 = AR::zero();
+    {
+        const F2* Fm = cp.fscan + ((size_t)(2 * t + 1) * kMaxSteps) * 4;
+        if constexpr (Q == 2) {
+            s1 = AR::mac2(d2_y(S1), AR::coef(Fm[0]), yA15, AR::coef(Fm[1]), yA14);
+            s2 = AR::mac2(d2_y(S2), AR::coef(Fm[2]), yA15, AR::coef(Fm[3]), yA14);
+        } else {
+            s1 = AR::mac1(d2_y(S1), AR::coef(Fm[0]), yA15);
+        }
+    }
+    for (int k = 1; k < cp.nsteps; k++) {
+        const unsigned dlt = 1u << (k - 1);
+        const V o1 = AR::shfl_up(s1, dlt, PLp);
+        const V o2 = (Q == 2) ? AR::shfl_up(s2, dlt, PLp) : AR::zero();
+        if (t >= (int)dlt) {
+            const F2* Fm = cp.fscan + ((size_t)(2 * t + 1) * kMaxSteps + k) * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(s1, AR::coef(Fm[0]), o1, AR::coef(Fm[1]), o2);
+                const V n2 = AR::mac2(s2, AR::coef(Fm[2]), o1, AR::coef(Fm[3]), o2);
+                s1 = n1;
+                s2 = n2;
+            } else {
+                s1 = AR::mac1(s1, AR::coef(Fm[0]), o1);
+            }
+        }
+    }
+    V i1 = AR::shfl_up(s1, 1, PLp);
+    V i2 = (Q == 2) ? AR::shfl_up(s2, 1, PLp) : AR::zero();
+    if (t == 0) {
+        i1 = AR::zero();
+        i2 = AR::zero();
+    }
+    // incoming states: half A the lane's, half B half A's corrected rows 15 and 14
+    df2 I1, I2;
+    {
+        const df2 p15 = tab(5, HM - 1), p14 = tab(5, HM - 2);
+        if constexpr (Q == 2) {
+            const df2 q15 = tab(6, HM - 1), q14 = tab(6, HM - 2);
+            I1 = d2_pack(i1, AR::mac2(yA15, d2_x(p15), i1, d2_x(q15), i2));
+            I2 = d2_pack(i2, AR::mac2(yA14, d2_x(p14), i1, d2_x(q14), i2));
+        } else {
+            I1 = d2_pack(i1, AR::mac1(yA15, d2_x(p15), i1));
+            I2 = d2_zero();
+        }
+    }
+    // ---- E+F: forward correction and backward recurrence of both halves ----
+    df2 U1 = d2_zero(), U2 = d2_zero();
+    if (active) {
+#pragma unroll 4
+        for (int j = HM - 1; j >= 0; j--) {
+            const df2 w = d2_of(wp[j - H]);
+            const df2 y = (Q == 2) ? d2_mac2(w, tab(5, j), I1, tab(6, j), I2) : d2_mac1(w, tab(5, j), I1);
+            const df2 x = (Q == 2) ? d2_fms2(y, tab(3, j), U1, tab(4, j), U2) : d2_fms1(y, tab(3, j), U1);
+            wp[j - H] = d2_f4(x);
+            U2 = U1;
+            U1 = x;
+        }
+    }
+    // ---- G: the plan's reverse scan; step 0 (chunk 2t before chunk 2t + 1) in the lane ----
+    const dfv xB0 = d2_y(U1), xB1 = d2_y(U2);
+    V u1, u2 = AR::zero();
+    {
+        const F2* Bm = cp.bscan + ((size_t)(2 * t) * kMaxSteps) * 4;
+        if constexpr (Q == 2) {
+            u1 = AR::mac2(d2_x(U1), AR::coef(Bm[0]), xB0, AR::coef(Bm[1]), xB1);
+            u2 = AR::mac2(d2_x(U2), AR::coef(Bm[2]), xB0, AR::coef(Bm[3]), xB1);
+        } else {
+            u1 = AR::mac1(d2_x(U1), AR::coef(Bm[0]), xB0);
+        }
+    }
+    for (int k = 1; k < cp.nsteps; k++) {
+        const unsigned dlt = 1u << (k - 1);
+        const V o1 = AR::shfl_down(u1, dlt, PLp);
+        const V o2 = (Q == 2) ? AR::shfl_down(u2, dlt, PLp) : AR::zero();
+        if (t + (int)dlt < PLp) {
+            const F2* Bm = cp.bscan + ((size_t)(2 * t) * kMaxSteps + k) * 4;
+            if constexpr (Q == 2) {
+                const V n1 = AR::mac2(u1, AR::coef(Bm[0]), o1, AR::coef(Bm[1]), o2);
+                const V n2 = AR::mac2(u2, AR::coef(Bm[2]), o1, AR::coef(Bm[3]), o2);
+                u1 = n1;
+                u2 = n2;
+            } else {
+                u1 = AR::mac1(u1, AR::coef(Bm[0]), o1);
+            }
+        }
+    }
+    V j1 = AR::shfl_down(u1, 1, PLp);
+    V j2 = (Q == 2) ? AR::shfl_down(u2, 1, PLp) : AR::zero();
+    if (t >= PL - 1) {
+        j1 = AR::zero();
+        j2 = AR::zero();
+    }
+    // incoming backward states: half B the lane's, half A half B's corrected rows 0 and 1
+    df2 J1, J2;
+    {
+        const df2 q0 = tab(7, 0), q1 = tab(7, 1);
+        if constexpr (Q == 2) {
+            const df2 r0 = tab(8, 0), r1 = tab(8, 1);
+            J1 = d2_pack(AR::mac2(xB0, d2_y(q0), j1, d2_y(r0), j2), j1);
+            J2 = d2_pack(AR::mac2(xB1, d2_y(q1), j1, d2_y(r1), j2), j2);
+        } else {
+            J1 = d2_pack(AR::mac1(xB0, d2_y(q0), j1), j1);
+            J2 = d2_zero();
+        }
+    }
+    // ---- H+I: backward correction and FP64 assembly (rows j and j + 16 over work pair j) ----
+    if (active) {
+        const int kl = lexp[l] - 1023;
+        double2* wd = reinterpret_cast<double2*>(wp - H);
+        if (kl >= -800 && kl <= 800) {
+            const unsigned kadd = (unsigned)(896 + kl) << 20;
+#pragma unroll 4
+            for (int j = 0; j < HM; j++) {
+                const df2 w = d2_of(wp[j - H]);
+                const df2 x = (Q == 2) ? d2_mac2(w, tab(7, j), J1, tab(8, j), J2) : d2_mac1(w, tab(7, j), J1);
+                wd[j] = make_double2(df_to_double_kadd(d2_x(x), kadd), df_to_double_kadd(d2_y(x), kadd));
+            }
+        } else {
+#pragma unroll 1
+            for (int j = 0; j < HM; j++) {
+                const df2 w = d2_of(wp[j - H]);
+                const df2 x = (Q == 2) ? d2_mac2(w, tab(7, j), J1, tab(8, j), J2) : d2_mac1(w, tab(7, j), J1);
+                wd[j] = make_double2(AR::store_scaled(d2_x(x), kl), AR::store_scaled(d2_y(x), kl));
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- J: coalesced stores (residual form: f - x, f read again) ----
+    const double* od = reinterpret_cast<const double*>(tile);
+    auto out_pos = [&](int ll, int p) -> int {
+        const unsigned tt = (unsigned)p / M, q = (unsigned)p % M;
+        return ((ll * LT + (int)tt * SL) << 1) + 2 * (int)(q % HM) + (int)(q / HM);
+    };
+    if (ls.op == 1) {
+        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+        for (int ll = warp; ll < nl; ll += nw) {
+            double* o = out + base_out[ll];
+            const double* fi = f + base_in[ll];
+            for (int p = lane; p < ns; p += 32) {
+                const double x = od[out_pos(ll, p)];
+                o[p] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
+            }
+        }
+    } else {
+        const int ll = tid % L, pstep = nth / L;
+        if (ll < nl) {
+            double* o = out + base_out[ll];
+            const double* fi = f + base_in[ll];
+            for (int p = tid / L; p < ns; p += pstep) {
+                const double x = od[out_pos(ll, p)];
+                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
+            }
+        }
+    }
+    if (bad) atomicOr(status, 1u);
+}
+
+// dynamic shared memory of k_lhalf_band: tables, windows, edge rows, per-line arrays
+inline size_t lhalf_band_smem(const StencilParams& c, int np) {
+    const size_t tabs = sizeof(float4) * (size_t)(c.hnf + 2) * kHalfBandBlock;
+    const size_t tile = sizeof(float4) * (size_t)c.L * half_line_stride(c.ns / 32, kHalf, np);
+    const size_t edge = sizeof(dfv) * (size_t)c.L * (c.nlo + c.nhi);
+    const size_t lines = (2 * sizeof(long) + sizeof(int)) * (size_t)c.L;
+    return tabs + tile + ((edge + 7) & ~(size_t)7) + lines;
+}
+
+template <int Q, int NP, bool SYM, bool RESID = false>
+int launch_lhalf_band_t(const StencilParams& c, const void* f, void* out, const LineSet& ls, unsigned* status,
+                        cudaStream_t s) {
+    constexpr int NT = kLineThreadsCirc;
+    const long blocks = (ls.nlines + c.L - 1) / c.L;
+    const size_t smem = lhalf_band_smem(c, NP);
+    auto kern = k_lhalf_band<Q, NP, SYM, RESID>;
+    if (smem + 1024 > 48 * 1024) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return PS_ECUDA;
+    }
+    kern<<<(unsigned)blocks, NT, smem, s>>>(c, (const double*)f, (double*)out, ls, status);
+    return cudaGetLastError() == cudaSuccess ? PS_OK : PS_ECUDA;
+}
+
 int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                      unsigned* status, cudaStream_t s);
+int launch_line_half_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                          unsigned* status, cudaStream_t s);
 
 }  // namespace pade

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 
@@ -290,6 +291,62 @@ int DevicePlan::upload(const HostPlan& hp) {
         o_h32[5] = put(h32.phb);
         h32_ok = true;
     }
+    // the banded half-chunk kernel's tables: the NF leading lanes' rows, the last lane's and
+    // the interior pattern (the last interior lane's), each per table k (g a1 a2 b1 b2 pf1 pf2
+    // pb1 pb2) and pair j as {h(j), h(16 + j), l(j), l(16 + j)} of the lane's 32 rows; NF is the
+    // fewest leading lanes after which every interior lane equals the pattern within 2^-50 of
+    // the table's largest value (at most 3, else k_line keeps the operator)
+    size_t o_hb = 0;
+    int hb_nf = -1;
+    // (the residual-form cf90 measured slower there than on k_line: its wider window, five
+    // table blocks and the re-read of f leave three CTAs per SM; 0.349 against 0.301 ms per
+    // 256^3 launch along z; so the derivatives only)
+    if (line_shape_ >= SHAPE_T2A && line_shape_ <= SHAPE_P3S && !ch_.circ && cline_.M == 16 && ch_.M == 16 &&
+        d.ns % 32 == 0 && d.nout == d.ns && ch_.nlo <= 16 && ch_.nhi <= 16 && ch_.Pp >= 2 &&
+        kLineThreadsCirc % (ch_.Pp / 2) == 0 && ch_.rc.size() >= (size_t)d.ns * 5 &&
+        ch_.phf.size() >= (size_t)d.ns * 2 && ch_.phb.size() >= (size_t)d.ns * 2) {
+        const int ns = d.ns, PL = ns / 32, tp = std::max(PL - 2, 0);
+        auto val = [&](int k, int r) -> double {
+            return k < 5 ? ch_.rc[(size_t)r * 5 + k]
+                         : (k < 7 ? ch_.phf[(size_t)r * 2 + (k - 5)] : ch_.phb[(size_t)r * 2 + (k - 7)]);
+        };
+        double tol[9];
+        for (int k = 0; k < 9; k++) {
+            double mx = 0.0;
+            for (int r = 0; r < ns; r++) mx = std::max(mx, std::fabs(val(k, r)));
+            tol[k] = std::ldexp(mx, -50);
+        }
+        auto lane_is_pattern = [&](int t) {
+            for (int k = 0; k < 9; k++)
+                for (int j = 0; j < 32; j++)
+                    if (!(std::fabs(val(k, 32 * t + j) - val(k, 32 * tp + j)) <= tol[k])) return false;
+            return true;
+        };
+        int nf = std::max(1, std::min(PL - 1, 1));  // the first lane always has its own tables
+        while (nf < PL - 1 && !lane_is_pattern(nf)) nf++;
+        bool ok = nf <= 3;
+        for (int t = nf; t < PL - 1 && ok; t++) ok = lane_is_pattern(t);
+        if (ok) {
+            const int nb = nf + 2;
+            std::vector<int> base_row(nb);
+            for (int b = 0; b < nf; b++) base_row[b] = 32 * b;
+            base_row[nf] = ns - 32;
+            base_row[nf + 1] = 32 * tp;
+            std::vector<float> tb((size_t)nb * 9 * 16 * 4);
+            for (int b = 0; b < nb; b++)
+                for (int k = 0; k < 9; k++)
+                    for (int j = 0; j < 16; j++) {
+                        const F2 a = split(val(k, base_row[b] + j)), c = split(val(k, base_row[b] + 16 + j));
+                        float* q = &tb[(((size_t)b * 9 + k) * 16 + j) * 4];
+                        q[0] = a.h;
+                        q[1] = c.h;
+                        q[2] = a.l;
+                        q[3] = c.l;
+                    }
+            o_hb = A.put(tb.data(), tb.size() * sizeof(float));
+            hb_nf = nf;
+        }
+    }
     // register-resident periodic kernel: whole chunks of 32 rows, a power-of-two number of
     // lanes per line; coefficients and fundamental solutions travel in the kernel parameters
     size_t o_rg[4] = {0, 0, 0, 0};
@@ -430,6 +487,14 @@ int DevicePlan::upload(const HostPlan& hp) {
         cline_.phf = own ? (const F2*)(lb + o_lk[4]) : cdf_.phf;
         cline_.phb = own ? (const F2*)(lb + o_lk[5]) : cdf_.phb;
     }
+    halfb_ = false;
+    if (hb_nf >= 1) {
+        chalfb_ = cline_;
+        chalfb_.L = kLineThreadsCirc / (ch_.Pp / 2);
+        chalfb_.hpair = base + o_hb;
+        chalfb_.hnf = hb_nf;
+        halfb_ = true;
+    }
     half32_ = false;
     if (h32_ok) {
         chalf32_ = cline_;
@@ -532,6 +597,10 @@ int launch_lines(const DevicePlan& p, int path, const void* f, void* out, const 
         const int sh = p.line_shape();
         const bool tri = sh == SHAPE_T2A || sh == SHAPE_T2S || sh >= SHAPE_T2A_E2C;
         const int choice = line_kernel_choice();
+        if ((choice == 0 || choice == 3) && sh >= SHAPE_T2A && sh <= SHAPE_P4S && p.half_band_params()) {
+            const int rc = launch_line_half_band(sh, *p.half_band_params(), f, out, ls, status, s);
+            if (rc != PS_ENOTSUP) return rc;
+        }
         if ((choice == 0 || choice == 3) && sh >= SHAPE_T2A && sh <= SHAPE_T2S_C2E) {
             const StencilParams* h16 = p.half16_params();
             const StencilParams* h32 = p.half32_params();

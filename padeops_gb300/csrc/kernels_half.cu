@@ -46,4 +46,27 @@ int launch_line_half(int shape, const StencilParams& c, const void* f, void* out
                      : launch_half_m<16>(shape, c, f, out, ls, status, s);
 }
 
+// Banded lines of whole 32-row chunks (two 16-row chunks of the plan per lane) whose tables
+// passed the plan's interior check (hpair set).
+int launch_line_half_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
+                          unsigned* status, cudaStream_t s) {
+    if (c.circ || c.M != 16 || !c.hpair || c.hnf < 1 || c.hnf > 3 || c.ns % 32 != 0 || c.nout != c.ns || c.L < 1 ||
+        c.nlo > 16 || c.nhi > 16)
+        return PS_ENOTSUP;
+    if (!c.alias) return PS_ENOTSUP;
+    if (ls.fp == 1) {
+        if ((c.ns + 31) / 32 > kHalfRowsContig) return PS_ENOTSUP;
+    } else {
+        const int pstep = kLineThreadsCirc / c.L;
+        if ((c.ns + pstep - 1) / pstep > 32) return PS_ENOTSUP;
+    }
+    switch (shape) {
+        case SHAPE_T2A: return launch_lhalf_band_t<1, 2, false>(c, f, out, ls, status, s);
+        case SHAPE_T2S: return launch_lhalf_band_t<1, 2, true>(c, f, out, ls, status, s);
+        case SHAPE_P3A: return launch_lhalf_band_t<2, 3, false>(c, f, out, ls, status, s);
+        case SHAPE_P3S: return launch_lhalf_band_t<2, 3, true>(c, f, out, ls, status, s);
+        default: return PS_ENOTSUP;  // the residual-form cf90 stays on k_line (measured faster there)
+    }
+}
+
 }  // namespace pade

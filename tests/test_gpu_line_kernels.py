@@ -19,7 +19,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SELECT = ("cd06 or cd10_periodic or cf90 or stagg_periodic or fp32_path or bench_scale or range_free or "
-          "periodic_whole_chunks")
+          "periodic_whole_chunks or banded_whole_chunks")
 
 
 @pytest.mark.parametrize("kernel", ["reg", "shared", "half", "half16"])

@@ -142,6 +142,29 @@ def test_periodic_whole_chunks(oracle, fam, dir, n):
         assert relerr(out, ref) < tol64(order, f, ref, dx), order
 
 
+@pytest.mark.parametrize("bc1,bcn", list(itertools.product(BCS, BCS)))
+@pytest.mark.parametrize("dir", [1, 3])
+@pytest.mark.parametrize("n", [64, 96, 160, 256])
+def test_banded_whole_chunks(oracle, bc1, bcn, dir, n):
+    """Non-periodic lines of 2, 3, 5 and 8 chunks of 32 rows (the banded half-chunk kernel for
+    the derivatives: the leading and the last lanes with their own tables, the interior lanes
+    on the shared pattern; cf90 stays on k_line), cd10 d1 / d2 and cf90, every bc pair, a
+    ragged set of lines."""
+    shape = shape_for(n, dir, (7, 5) if n > 64 else (12, 10))
+    f = field(shape, 6)
+    dx = 1.0 / (n - 1)
+    o = P.cd10()
+    assert o.init(n, dx, False) == 0
+    for order in (1, 2):
+        out = run(o, order, dir, f, shape, bc1, bcn)
+        ref = oracle.cd10(f, dx, periodic=False, bc1=bc1, bcn=bcn, order=order, dir=dir)
+        assert relerr(out, ref) < tol64(order, f, ref, dx), order
+    c = P.cf90()
+    assert c.init(n, False) == 0
+    out = run(c, 0, dir, f, shape, bc1, bcn)
+    assert relerr(out, oracle.cf90(f, periodic=False, bc1=bc1, bcn=bcn, dir=dir)) < 1e-12
+
+
 @pytest.mark.parametrize("periodic", [True, False])
 @pytest.mark.parametrize("bc1,bcn", list(itertools.product(BCS, BCS)))
 @pytest.mark.parametrize("dir", [1, 2, 3])
