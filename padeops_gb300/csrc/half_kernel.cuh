@@ -153,18 +153,25 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
             }
         }
     } else {
+        // strided lines by pairs: thread q0 of a line loads both rows of pairs k = q0 + pstep i,
+        // rows p = (k / HM) M + k % HM and p + HM, and writes each pair with one 16-byte store
+        // (the lines of a quarter-warp on distinct banks; ns is a multiple of M, and
+        // ceil(ns / pstep) <= M gives every pair a thread)
         const int pstep = nth / L;
-        const int U = (ns + pstep - 1) / pstep;
+        const int nk = ns >> 1;
         const int l = tid % L, q0 = tid / L;
         double v[M];
         int mx = 0;
         if (l < nl) {
             const double* src = f + base_in[l];
 #pragma unroll
-            for (int u = 0; u < M; u++) {
-                const int p = q0 + pstep * u;
-                v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
-                mx = max(mx, bexp(v[u]));
+            for (int i = 0; i < HM; i++) {
+                const int k = q0 + pstep * i;
+                const int p = (k / HM) * M + k % HM;
+                const bool ok = k < nk;
+                v[2 * i] = ok ? __ldg(src + (long)p * ls.fp) : 0.0;
+                v[2 * i + 1] = ok ? __ldg(src + (long)(p + HM) * ls.fp) : 0.0;
+                mx = max(mx, max(bexp(v[2 * i]), bexp(v[2 * i + 1])));
             }
             atomicMax(&lexp[l], mx);
         }
@@ -173,14 +180,13 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
             const int mxl = lexp[l];
             bad |= (unsigned)(mxl == 2047);
             const SplitK sk = split_consts(mxl - 1023);
+            float4* lt = tile + (size_t)l * LT + H;
 #pragma unroll
-            for (int u = 0; u < M; u++) {
-                const int p = q0 + pstep * u;
-                if (u < U && p < ns) {
-                    const dfv d = df_split_line(v[u], sk);
-                    const int o = hpos(l, p);
-                    tf[o] = d.h;
-                    tf[o + 2] = d.l;
+            for (int i = 0; i < HM; i++) {
+                const int k = q0 + pstep * i;
+                if (k < nk) {
+                    const dfv a = df_split_line(v[2 * i], sk), b = df_split_line(v[2 * i + 1], sk);
+                    lt[(k / HM) * SL + k % HM] = make_float4(a.h, b.h, a.l, b.l);
                 }
             }
         }
@@ -490,6 +496,10 @@ int launch_lhalf_t(const StencilParams& c, const void* f, void* out, const LineS
 constexpr int kHalf = 16;  // rows per half of a 32-row chunk
 constexpr int kHalfBandTables = 9;
 constexpr int kHalfBandBlock = kHalfBandTables * kHalf;  // float4 per block (first, last, interior)
+// blocks sit one 16-byte unit further apart in shared memory than their size: the lanes of a
+// line read the same (table, row) of up to NF + 2 different blocks at once, and a stride that
+// is a multiple of 128 bytes put all of them on the same banks (one wavefront per block)
+constexpr int kHalfBandBlockStride = kHalfBandBlock + 1;
 
 template <int Q, int NP, bool SYM, bool RESID>
 __global__ void __launch_bounds__(kLineThreadsCirc, 4)
@@ -507,7 +517,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     const int ne = cp.nlo + cp.nhi, ehi = ns - cp.nhi;
     const int NF = cp.hnf;                                   // leading lanes with tables of their own
     float4* btab = reinterpret_cast<float4*>(smem_raw);     // NF leading lanes, last lane, interior
-    float4* tile = btab + (NF + 2) * kHalfBandBlock;        // L lines x PL lanes x SL
+    float4* tile = btab + (NF + 2) * kHalfBandBlockStride;  // L lines x PL lanes x SL
     V* edge = reinterpret_cast<V*>(tile + (size_t)L * LT);  // L x ne edge-row right-hand sides
     long* base_in = reinterpret_cast<long*>(edge + (size_t)L * ne);
     long* base_out = base_in + L;
@@ -525,7 +535,8 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     }
     {
         const float4* __restrict__ g = reinterpret_cast<const float4*>(cp.hpair);
-        for (int i = tid; i < (NF + 2) * kHalfBandBlock; i += nth) btab[i] = __ldg(g + i);
+        for (int i = tid; i < (NF + 2) * kHalfBandBlock; i += nth)
+            btab[(i / kHalfBandBlock) * kHalfBandBlockStride + i % kHalfBandBlock] = __ldg(g + i);
     }
     __syncthreads();
 
@@ -563,18 +574,25 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
             }
         }
     } else {
+        // strided lines by pairs: thread q0 of a line loads both rows of pairs k = q0 + pstep i,
+        // rows p = (k / HM) M + k % HM and p + HM, and writes each pair with one 16-byte store
+        // (the lines of a quarter-warp on distinct banks; ns is a multiple of M, and
+        // ceil(ns / pstep) <= M gives every pair a thread)
         const int pstep = nth / L;
-        const int U = (ns + pstep - 1) / pstep;
+        const int nk = ns >> 1;
         const int l = tid % L, q0 = tid / L;
         double v[M];
         int mx = 0;
         if (l < nl) {
             const double* src = f + base_in[l];
 #pragma unroll
-            for (int u = 0; u < M; u++) {
-                const int p = q0 + pstep * u;
-                v[u] = (u < U && p < ns) ? __ldg(src + (long)p * ls.fp) : 0.0;
-                mx = max(mx, bexp(v[u]));
+            for (int i = 0; i < HM; i++) {
+                const int k = q0 + pstep * i;
+                const int p = (k / HM) * M + k % HM;
+                const bool ok = k < nk;
+                v[2 * i] = ok ? __ldg(src + (long)p * ls.fp) : 0.0;
+                v[2 * i + 1] = ok ? __ldg(src + (long)(p + HM) * ls.fp) : 0.0;
+                mx = max(mx, max(bexp(v[2 * i]), bexp(v[2 * i + 1])));
             }
             atomicMax(&lexp[l], mx);
         }
@@ -583,14 +601,13 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
             const int mxl = lexp[l];
             bad |= (unsigned)(mxl == 2047);
             const SplitK sk = split_consts(mxl - 1023);
+            float4* lt = tile + (size_t)l * LT + H;
 #pragma unroll
-            for (int u = 0; u < M; u++) {
-                const int p = q0 + pstep * u;
-                if (u < U && p < ns) {
-                    const dfv d = df_split_line(v[u], sk);
-                    const int o = hpos(l, p);
-                    tf[o] = d.h;
-                    tf[o + 2] = d.l;
+            for (int i = 0; i < HM; i++) {
+                const int k = q0 + pstep * i;
+                if (k < nk) {
+                    const dfv a = df_split_line(v[2 * i], sk), b = df_split_line(v[2 * i + 1], sk);
+                    lt[(k / HM) * SL + k % HM] = make_float4(a.h, b.h, a.l, b.l);
                 }
             }
         }
@@ -600,7 +617,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     const int t = tid % PLp, l = tid / PLp;
     const bool active = (l < nl) && (t < PL);
     // this lane's tables: its own (leading lanes), the last lane's, or the interior pattern
-    const float4* tb = btab + (t < NF ? t : (t >= PL - 1 ? NF : NF + 1)) * kHalfBandBlock;
+    const float4* tb = btab + (t < NF ? t : (t >= PL - 1 ? NF : NF + 1)) * kHalfBandBlockStride;
     auto tab = [&](int k, int j) -> df2 { return d2_of(tb[k * HM + j]); };
     float4* wp = tile + (size_t)l * LT + t * SL + H;
     float* wf = reinterpret_cast<float*>(wp);
@@ -845,7 +862,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
 
 // dynamic shared memory of k_lhalf_band: tables, windows, edge rows, per-line arrays
 inline size_t lhalf_band_smem(const StencilParams& c, int np) {
-    const size_t tabs = sizeof(float4) * (size_t)(c.hnf + 2) * kHalfBandBlock;
+    const size_t tabs = sizeof(float4) * (size_t)(c.hnf + 2) * kHalfBandBlockStride;
     const size_t tile = sizeof(float4) * (size_t)c.L * half_line_stride(c.ns / 32, kHalf, np);
     const size_t edge = sizeof(dfv) * (size_t)c.L * (c.nlo + c.nhi);
     const size_t lines = (2 * sizeof(long) + sizeof(int)) * (size_t)c.L;
