@@ -817,7 +817,7 @@ def main():
     tr = traffic_per_launch()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": tr, "peak_source": src,
-            "kernel": "k_lhalf (periodic cd10, x and y) and k_line (cf90, banded z): double-float chunked scans, "
+            "kernel": "k_lhalf (periodic lines, x and y) and k_lhalf_band (banded z): double-float chunked scans, "
                       "mean over the 9 launches",
             "algorithmic_bytes_per_launch": npts * BYTES_PER_POINT,
             "per_launch_ms": {p[3]: round(float(v), 4) for p, v in zip(plan, per_launch)}}

@@ -34,30 +34,29 @@ namespace pade {
 // a plan coefficient broadcast to both components
 __device__ __forceinline__ df2 d2_bcast(F2 c) { return d2_bcast(dfv{c.h, c.l}); }
 
-// right-hand side of rows (j, j + 16): the window pairs at p[-NP .. NP]; pairs k = 1..NP at
-// offsets (k, -k) about the row (STG = 0), or about a half point: (k, 1 - k) (STG = +1, edges
-// to cells) or (k - 1, -k) (STG = -1, cells to edges), in k_line's operation order
-template <int NP, bool SYM, int STG = 0>
-__device__ __forceinline__ df2 half_stencil(const float4* p, const df2 (&c)[NP], df2 c0) {
+// right-hand side of rows (j, j + 16) from the window pairs p(-NP) .. p(NP) (p(k): pair j + k
+// as packed operands); pairs k = 1..NP at offsets (k, -k) about the row (STG = 0), or about a
+// half point: (k, 1 - k) (STG = +1, edges to cells) or (k - 1, -k) (STG = -1, cells to
+// edges), in k_line's operation order
+template <int NP, bool SYM, int STG = 0, class W>
+__device__ __forceinline__ df2 half_stencil(const W& p, const df2 (&c)[NP], df2 c0) {
     df2 acc;
     if constexpr (STG != 0) {
         constexpr int sh = STG > 0 ? 0 : -1;
-        acc = SYM ? d2_mul(d2_add(d2_of(p[1 + sh]), d2_of(p[sh])), c[0])
-                  : d2_mul(d2_sub(d2_of(p[1 + sh]), d2_of(p[sh])), c[0]);
+        acc = SYM ? d2_mul(d2_add(p(1 + sh), p(sh)), c[0]) : d2_mul(d2_sub(p(1 + sh), p(sh)), c[0]);
 #pragma unroll
         for (int k = 2; k <= NP; k++) {
-            const df2 d = SYM ? d2_add(d2_of(p[k + sh]), d2_of(p[1 - k + sh]))
-                              : d2_sub(d2_of(p[k + sh]), d2_of(p[1 - k + sh]));
+            const df2 d = SYM ? d2_add(p(k + sh), p(1 - k + sh)) : d2_sub(p(k + sh), p(1 - k + sh));
             acc = d2_add(acc, d2_mul(d, c[k - 1]));
         }
     } else if constexpr (SYM) {
-        acc = d2_mul(d2_of(p[0]), c0);
+        acc = d2_mul(p(0), c0);
 #pragma unroll
-        for (int k = 1; k <= NP; k++) acc = d2_add(acc, d2_mul(d2_add(d2_of(p[k]), d2_of(p[-k])), c[k - 1]));
+        for (int k = 1; k <= NP; k++) acc = d2_add(acc, d2_mul(d2_add(p(k), p(-k)), c[k - 1]));
     } else {
-        acc = d2_mul(d2_sub(d2_of(p[1]), d2_of(p[-1])), c[0]);
+        acc = d2_mul(d2_sub(p(1), p(-1)), c[0]);
 #pragma unroll
-        for (int k = 2; k <= NP; k++) acc = d2_add(acc, d2_mul(d2_sub(d2_of(p[k]), d2_of(p[-k])), c[k - 1]));
+        for (int k = 2; k <= NP; k++) acc = d2_add(acc, d2_mul(d2_sub(p(k), p(-k)), c[k - 1]));
     }
     return d2_norm(acc);
 }
@@ -196,35 +195,30 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     const int t = tid % cp.Pp, l = tid / cp.Pp;
     const bool active = (l < nl) && (t < P);
     float4* wp = tile + (size_t)l * LT + t * SL + H;  // pair r at wp[r], -H <= r < HM + H
-    float* wf = reinterpret_cast<float*>(wp);
 
     // ---- halo pairs: rows -H..-1 (previous chunk, around the ring) beside rows HM-H..HM-1,
     // and rows HM..HM-1+H beside rows M..M-1+H (next chunk) ----
+    // (row -h is component B of the previous lane's pair HM - h, row HM - h component A of
+    // this lane's; row HM - 1 + h component B of this lane's pair h - 1, row M - 1 + h
+    // component A of the next lane's: two 16-byte loads and one store per halo pair)
     if (active) {
+        const float4* wprev = tile + (size_t)l * LT + (t == 0 ? P - 1 : t - 1) * SL + H;
+        const float4* wnext = tile + (size_t)l * LT + (t == P - 1 ? 0 : t + 1) * SL + H;
 #pragma unroll
         for (int h = 1; h <= H; h++) {
-            const int pm = t * M - h, pp = t * M + M - 1 + h;
-            const int om = hpos(l, pm < 0 ? pm + ns : pm), op = hpos(l, pp >= ns ? pp - ns : pp);
-            const int oa = hpos(l, t * M + HM - h), ob = hpos(l, t * M + HM - 1 + h);
-            float* lo = wf + 4 * (-h);          // pair -h
-            float* hi = wf + 4 * (HM - 1 + h);  // pair HM - 1 + h
-            lo[0] = tf[om];
-            lo[2] = tf[om + 2];
-            lo[1] = tf[oa];
-            lo[3] = tf[oa + 2];
-            hi[0] = tf[ob];
-            hi[2] = tf[ob + 2];
-            hi[1] = tf[op];
-            hi[3] = tf[op + 2];
+            const float4 pv = wprev[HM - h], oa = wp[HM - h], ob = wp[h - 1], nx = wnext[h - 1];
+            wp[-h] = make_float4(pv.y, oa.x, pv.w, oa.z);
+            float4 hi = make_float4(ob.y, nx.x, ob.w, nx.z);
             if constexpr (STG > 0) {
-                if (pp == ns && cp.xdup) {
+                if (t == P - 1 && h == 1 && cp.xdup) {
                     const double v = __ldg(f + base_in[l] + (long)ns * ls.fp);
                     bad |= (unsigned)(bexp(v) == 2047);
                     const dfv d = df_from_double_shift(v, lexp[l] - 1023);
-                    hi[1] = d.h;
-                    hi[3] = d.l;
+                    hi.y = d.h;
+                    hi.w = d.l;
                 }
             }
+            wp[HM - 1 + h] = hi;
         }
     }
     // the neighbouring lanes of a line (one warp) read this lane's first and last rows
@@ -244,7 +238,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     if (active) {
 #pragma unroll 4
         for (int j = 0; j < HM; j++) {
-            const df2 r = half_stencil<NP, SYM, STG>(wp + j, cc, c0);
+            const df2 r = half_stencil<NP, SYM, STG>([&](int k) { return d2_of(wp[j + k]); }, cc, c0);
             const df2 y = (Q == 2) ? d2_fms2(r, a1, S1, a2, S2) : d2_fms1(r, a1, S1);
             wp[j - H] = d2_f4(y);
             S2 = S1;
@@ -446,14 +440,20 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
             }
         }
     } else {
+        // strided lines by pairs, as staged: rows p and p + HM of pair k from one 16-byte load
         const int ll = tid % L, pstep = nth / L;
         if (ll < nl) {
             double* o = out + base_out[ll];
             const double* fi = f + base_in[ll];
-            for (int p = tid / L; p < cp.nout; p += pstep) {
-                const double x = od[out_pos(ll, p < ns ? p : p - ns)];
-                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
+            const double2* od2 = reinterpret_cast<const double2*>(tile) + (size_t)ll * LT;
+            for (int k = tid / L; k < (ns >> 1); k += pstep) {
+                const int p = (k / HM) * M + k % HM;
+                const double2 x = od2[(k / HM) * SL + k % HM];
+                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x.x) : x.x;
+                o[(long)(p + HM) * ls.op] = RESID ? __dsub_rn(fi[(long)(p + HM) * ls.fp], x.y) : x.y;
             }
+            // rows past the line's end (an output longer than the line repeats its first rows)
+            for (int p = ns + tid / L; p < cp.nout; p += pstep) o[(long)p * ls.op] = od[out_pos(ll, p - ns)];
         }
     }
     if (bad) atomicOr(status, 1u);
@@ -620,36 +620,18 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     const float4* tb = btab + (t < NF ? t : (t >= PL - 1 ? NF : NF + 1)) * kHalfBandBlockStride;
     auto tab = [&](int k, int j) -> df2 { return d2_of(tb[k * HM + j]); };
     float4* wp = tile + (size_t)l * LT + t * SL + H;
-    float* wf = reinterpret_cast<float*>(wp);
 
     // ---- halo pairs (zero beyond the line ends) ----
     if (active) {
+        const float4* wprev = tile + (size_t)l * LT + (t - 1) * SL + H;  // read only when t > 0
+        const float4* wnext = tile + (size_t)l * LT + (t + 1) * SL + H;  // read only when t < PL - 1
+        const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
         for (int h = 1; h <= H; h++) {
-            const int pm = t * M - h, pp = t * M + M - 1 + h;
-            const int oa = hpos(l, t * M + HM - h), ob = hpos(l, t * M + HM - 1 + h);
-            float* lo = wf + 4 * (-h);
-            float* hi = wf + 4 * (HM - 1 + h);
-            if (pm >= 0) {
-                const int om = hpos(l, pm);
-                lo[0] = tf[om];
-                lo[2] = tf[om + 2];
-            } else {
-                lo[0] = 0.0f;
-                lo[2] = 0.0f;
-            }
-            lo[1] = tf[oa];
-            lo[3] = tf[oa + 2];
-            hi[0] = tf[ob];
-            hi[2] = tf[ob + 2];
-            if (pp < ns) {
-                const int op = hpos(l, pp);
-                hi[1] = tf[op];
-                hi[3] = tf[op + 2];
-            } else {
-                hi[1] = 0.0f;
-                hi[3] = 0.0f;
-            }
+            const float4 pv = t > 0 ? wprev[HM - h] : z4, oa = wp[HM - h], ob = wp[h - 1];
+            const float4 nx = t < PL - 1 ? wnext[h - 1] : z4;
+            wp[-h] = make_float4(pv.y, oa.x, pv.w, oa.z);
+            wp[HM - 1 + h] = make_float4(ob.y, nx.x, ob.w, nx.z);
         }
     }
     // ---- edge rows: one-sided right-hand sides in FP64 from the FP64 input, each input
@@ -682,7 +664,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
         const int iA0 = t * M, iB0 = t * M + HM;
 #pragma unroll 4
         for (int j = 0; j < HM; j++) {
-            df2 r = half_stencil<NP, SYM>(wp + j, cc, c0);
+            df2 r = half_stencil<NP, SYM>([&](int k) { return d2_of(wp[j + k]); }, cc, c0);
             if (iA0 + j < cp.nlo) {
                 const V e = edge[l * ne + iA0 + j];
                 r.h.x = e.h;
@@ -847,13 +829,17 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
             }
         }
     } else {
+        // strided lines by pairs, as staged
         const int ll = tid % L, pstep = nth / L;
         if (ll < nl) {
             double* o = out + base_out[ll];
             const double* fi = f + base_in[ll];
-            for (int p = tid / L; p < ns; p += pstep) {
-                const double x = od[out_pos(ll, p)];
-                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
+            const double2* od2 = reinterpret_cast<const double2*>(tile) + (size_t)ll * LT;
+            for (int k = tid / L; k < (ns >> 1); k += pstep) {
+                const int p = (k / HM) * M + k % HM;
+                const double2 x = od2[(k / HM) * SL + k % HM];
+                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x.x) : x.x;
+                o[(long)(p + HM) * ls.op] = RESID ? __dsub_rn(fi[(long)(p + HM) * ls.fp], x.y) : x.y;
             }
         }
     }

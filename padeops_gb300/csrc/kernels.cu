@@ -298,10 +298,7 @@ int DevicePlan::upload(const HostPlan& hp) {
     // the table's largest value (at most 3, else k_line keeps the operator)
     size_t o_hb = 0;
     int hb_nf = -1;
-    // (the residual-form cf90 measured slower there than on k_line: its wider window, five
-    // table blocks and the re-read of f leave three CTAs per SM; 0.349 against 0.301 ms per
-    // 256^3 launch along z; so the derivatives only)
-    if (line_shape_ >= SHAPE_T2A && line_shape_ <= SHAPE_P3S && !ch_.circ && cline_.M == 16 && ch_.M == 16 &&
+    if (line_shape_ >= SHAPE_T2A && line_shape_ <= SHAPE_P4S && !ch_.circ && cline_.M == 16 && ch_.M == 16 &&
         d.ns % 32 == 0 && d.nout == d.ns && ch_.nlo <= 16 && ch_.nhi <= 16 && ch_.Pp >= 2 &&
         kLineThreadsCirc % (ch_.Pp / 2) == 0 && ch_.rc.size() >= (size_t)d.ns * 5 &&
         ch_.phf.size() >= (size_t)d.ns * 2 && ch_.phb.size() >= (size_t)d.ns * 2) {

@@ -53,7 +53,7 @@ int launch_line_half_band(int shape, const StencilParams& c, const void* f, void
     if (c.circ || c.M != 16 || !c.hpair || c.hnf < 1 || c.hnf > 3 || c.ns % 32 != 0 || c.nout != c.ns || c.L < 1 ||
         c.nlo > 16 || c.nhi > 16)
         return PS_ENOTSUP;
-    if (!c.alias) return PS_ENOTSUP;
+    if (c.alias == (shape == SHAPE_P4S) || (shape == SHAPE_P4S && !c.resid)) return PS_ENOTSUP;
     if (ls.fp == 1) {
         if ((c.ns + 31) / 32 > kHalfRowsContig) return PS_ENOTSUP;
     } else {
@@ -65,7 +65,8 @@ int launch_line_half_band(int shape, const StencilParams& c, const void* f, void
         case SHAPE_T2S: return launch_lhalf_band_t<1, 2, true>(c, f, out, ls, status, s);
         case SHAPE_P3A: return launch_lhalf_band_t<2, 3, false>(c, f, out, ls, status, s);
         case SHAPE_P3S: return launch_lhalf_band_t<2, 3, true>(c, f, out, ls, status, s);
-        default: return PS_ENOTSUP;  // the residual-form cf90 stays on k_line (measured faster there)
+        case SHAPE_P4S: return launch_lhalf_band_t<2, 4, true, true>(c, f, out, ls, status, s);
+        default: return PS_ENOTSUP;
     }
 }
 
