@@ -76,6 +76,85 @@ __host__ __device__ constexpr int half_line_stride(int p, int hm, int np) {
 // (at most 8); strided lines one row per lane of the line and chunk row (at most M).
 constexpr int kHalfRowsContig = 8;
 
+// J: coalesced stores of a CTA's lines from the FP64 results in the windows (rows j and
+// j + HM of a lane as the double2 over its work pair j: row q of chunk t is double
+// 2 (q % HM) + q / HM of its lane); strided lines by pairs, as staged.  An output longer than
+// the line (nout > ns) repeats its first rows.  Residual form (nout = ns): f - x, each thread
+// reading f at the points it writes (so an in-place call is safe), all of its loads issued
+// before its first subtraction instead of one L2 round trip per row.
+template <int M, bool RESID>
+__device__ __forceinline__ void half_store(const float4* tile, int LT, int SL, int nl, int L, int ns, int nout,
+                                           const double* __restrict__ f, double* __restrict__ out,
+                                           const long* base_in, const long* base_out, const LineSet& ls) {
+    constexpr int HM = M / 2;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const double* od = reinterpret_cast<const double*>(tile);
+    auto out_pos = [&](int ll, int p) -> int {
+        const unsigned tt = (unsigned)p / M, q = (unsigned)p % M;
+        return ((ll * LT + (int)tt * SL) << 1) + 2 * (int)(q % HM) + (int)(q / HM);
+    };
+    if (ls.op == 1) {
+        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
+        for (int ll = warp; ll < nl; ll += nw) {
+            double* o = out + base_out[ll];
+            if constexpr (RESID) {
+                const double* fi = f + base_in[ll];
+                double fv[kHalfRowsContig];
+#pragma unroll
+                for (int u = 0; u < kHalfRowsContig; u++) {
+                    const int p = lane + 32 * u;
+                    fv[u] = p < ns ? fi[(long)p * ls.fp] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < kHalfRowsContig; u++) {
+                    const int p = lane + 32 * u;
+                    if (p < ns) o[p] = __dsub_rn(fv[u], od[out_pos(ll, p)]);
+                }
+                for (int p = lane + 32 * kHalfRowsContig; p < ns; p += 32)
+                    o[p] = __dsub_rn(fi[(long)p * ls.fp], od[out_pos(ll, p)]);
+            } else {
+                for (int p = lane; p < nout; p += 32) o[p] = od[out_pos(ll, p < ns ? p : p - ns)];
+            }
+        }
+    } else {
+        const int ll = tid % L, pstep = nth / L, k0 = tid / L, nk = ns >> 1;
+        if (ll < nl) {
+            double* o = out + base_out[ll];
+            const double2* od2 = reinterpret_cast<const double2*>(tile) + (size_t)ll * LT;
+            if constexpr (RESID) {
+                // pstep * HM >= nk: HM pairs per thread cover the line
+                const double* fi = f + base_in[ll];
+                double2 fv[HM];
+#pragma unroll
+                for (int i = 0; i < HM; i++) {
+                    const int k = k0 + pstep * i;
+                    const int p = (k / HM) * M + k % HM;
+                    fv[i] = k < nk ? make_double2(fi[(long)p * ls.fp], fi[(long)(p + HM) * ls.fp])
+                                   : make_double2(0.0, 0.0);
+                }
+#pragma unroll
+                for (int i = 0; i < HM; i++) {
+                    const int k = k0 + pstep * i;
+                    if (k < nk) {
+                        const int p = (k / HM) * M + k % HM;
+                        const double2 x = od2[(k / HM) * SL + k % HM];
+                        o[(long)p * ls.op] = __dsub_rn(fv[i].x, x.x);
+                        o[(long)(p + HM) * ls.op] = __dsub_rn(fv[i].y, x.y);
+                    }
+                }
+            } else {
+                for (int k = k0; k < nk; k += pstep) {
+                    const int p = (k / HM) * M + k % HM;
+                    const double2 x = od2[(k / HM) * SL + k % HM];
+                    o[(long)p * ls.op] = x.x;
+                    o[(long)(p + HM) * ls.op] = x.y;
+                }
+                for (int p = ns + k0; p < nout; p += pstep) o[(long)p * ls.op] = od[out_pos(ll, p - ns)];
+            }
+        }
+    }
+}
+
 // M: chunk rows (32, or 16 for twice the resident lines per SM: half the shared memory and
 // registers per thread for a longer lane scan).  RESID: a filter in residual form (cf90): the
 // solve gives x = A^-1 (A - B) f and the output is f - x, with f read again from the input
@@ -422,40 +501,8 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     }
     __syncthreads();
 
-    // ---- J: coalesced stores; row q of chunk t is double 2 (q % HM) + q / HM of its lane ----
-    const double* od = reinterpret_cast<const double*>(tile);
-    auto out_pos = [&](int ll, int p) -> int {
-        const unsigned tt = (unsigned)p / M, q = (unsigned)p % M;
-        return ((ll * LT + (int)tt * SL) << 1) + 2 * (int)(q % HM) + (int)(q / HM);
-    };
-    // (residual form: each thread reads f at the points it writes, so an in-place call is safe)
-    if (ls.op == 1) {
-        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
-        for (int ll = warp; ll < nl; ll += nw) {
-            double* o = out + base_out[ll];
-            const double* fi = f + base_in[ll];
-            for (int p = lane; p < cp.nout; p += 32) {
-                const double x = od[out_pos(ll, p < ns ? p : p - ns)];
-                o[p] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
-            }
-        }
-    } else {
-        // strided lines by pairs, as staged: rows p and p + HM of pair k from one 16-byte load
-        const int ll = tid % L, pstep = nth / L;
-        if (ll < nl) {
-            double* o = out + base_out[ll];
-            const double* fi = f + base_in[ll];
-            const double2* od2 = reinterpret_cast<const double2*>(tile) + (size_t)ll * LT;
-            for (int k = tid / L; k < (ns >> 1); k += pstep) {
-                const int p = (k / HM) * M + k % HM;
-                const double2 x = od2[(k / HM) * SL + k % HM];
-                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x.x) : x.x;
-                o[(long)(p + HM) * ls.op] = RESID ? __dsub_rn(fi[(long)(p + HM) * ls.fp], x.y) : x.y;
-            }
-            // rows past the line's end (an output longer than the line repeats its first rows)
-            for (int p = ns + tid / L; p < cp.nout; p += pstep) o[(long)p * ls.op] = od[out_pos(ll, p - ns)];
-        }
-    }
+    // ---- J: coalesced stores ----
+    half_store<M, RESID>(tile, LT, SL, nl, L, ns, cp.nout, f, out, base_in, base_out, ls);
     if (bad) atomicOr(status, 1u);
 }
 
@@ -640,11 +687,22 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
         const int ll = it / ne, e = it - ll * ne;
         const double* src = f + base_in[ll];
         const double sc = scalbn(1.0, 1023 - lexp[ll]);
+        const int* ti = cp.tidx + e * cp.tw;
+        const double* tc = cp.tcd + e * cp.tw;
         double acc = 0.0;
-#pragma unroll 1
-        for (int k = 0; k < cp.tw; k++) {
-            const int idx = __ldg(cp.tidx + e * cp.tw + k);
-            acc = __fma_rn(__ldg(cp.tcd + e * cp.tw + k), __dmul_rn(__ldg(src + (long)idx * ls.fp), sc), acc);
+        // the taps' loads in groups of 8 ahead of the (ordered) FMA chain
+        for (int k0 = 0; k0 < cp.tw; k0 += 8) {
+            double xv[8], cv[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const bool ok = k0 + u < cp.tw;
+                const int idx = ok ? __ldg(ti + k0 + u) : 0;
+                cv[u] = ok ? __ldg(tc + k0 + u) : 0.0;
+                xv[u] = ok ? __ldg(src + (long)idx * ls.fp) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (k0 + u < cp.tw) acc = __fma_rn(cv[u], __dmul_rn(xv[u], sc), acc);
         }
         edge[it] = df_from_double_shift(acc, 0);
     }
@@ -812,37 +870,8 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     }
     __syncthreads();
 
-    // ---- J: coalesced stores (residual form: f - x, f read again) ----
-    const double* od = reinterpret_cast<const double*>(tile);
-    auto out_pos = [&](int ll, int p) -> int {
-        const unsigned tt = (unsigned)p / M, q = (unsigned)p % M;
-        return ((ll * LT + (int)tt * SL) << 1) + 2 * (int)(q % HM) + (int)(q / HM);
-    };
-    if (ls.op == 1) {
-        const int warp = tid >> 5, lane = tid & 31, nw = nth >> 5;
-        for (int ll = warp; ll < nl; ll += nw) {
-            double* o = out + base_out[ll];
-            const double* fi = f + base_in[ll];
-            for (int p = lane; p < ns; p += 32) {
-                const double x = od[out_pos(ll, p)];
-                o[p] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x) : x;
-            }
-        }
-    } else {
-        // strided lines by pairs, as staged
-        const int ll = tid % L, pstep = nth / L;
-        if (ll < nl) {
-            double* o = out + base_out[ll];
-            const double* fi = f + base_in[ll];
-            const double2* od2 = reinterpret_cast<const double2*>(tile) + (size_t)ll * LT;
-            for (int k = tid / L; k < (ns >> 1); k += pstep) {
-                const int p = (k / HM) * M + k % HM;
-                const double2 x = od2[(k / HM) * SL + k % HM];
-                o[(long)p * ls.op] = RESID ? __dsub_rn(fi[(long)p * ls.fp], x.x) : x.x;
-                o[(long)(p + HM) * ls.op] = RESID ? __dsub_rn(fi[(long)(p + HM) * ls.fp], x.y) : x.y;
-            }
-        }
-    }
+    // ---- J: coalesced stores (residual form: f - x) ----
+    half_store<M, RESID>(tile, LT, SL, nl, L, ns, ns, f, out, base_in, base_out, ls);
     if (bad) atomicOr(status, 1u);
 }
 
