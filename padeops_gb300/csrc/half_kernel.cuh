@@ -76,6 +76,29 @@ __host__ __device__ constexpr int half_line_stride(int p, int hm, int np) {
 // (at most 8); strided lines one row per lane of the line and chunk row (at most M).
 constexpr int kHalfRowsContig = 8;
 
+// A lane's coefficients of scan step k (4 for two-term recurrences, 1 otherwise), loaded for
+// every step the lane takes part in before the scan starts: one round trip to L1 / L2 instead
+// of one per step; the entries of skipped steps are neither read nor used.
+template <int Q>
+struct ScanCoefs {
+    static constexpr int NE = Q == 2 ? 4 : 1;
+    F2 m[kMaxSteps][NE];
+    __device__ __forceinline__ void load(const F2* tab, int row, int k0, int nsteps, unsigned take) {
+#pragma unroll
+        for (int k = 0; k < kMaxSteps; k++) {
+#pragma unroll
+            for (int e = 0; e < NE; e++) m[k][e] = F2{0.0f, 0.0f};
+            if (k >= k0 && k < nsteps && ((take >> k) & 1u)) {
+#pragma unroll
+                for (int e = 0; e < NE; e++) {
+                    const float2 v = __ldg(reinterpret_cast<const float2*>(tab) + ((size_t)row * kMaxSteps + k) * 4 + e);
+                    m[k][e] = F2{v.x, v.y};
+                }
+            }
+        }
+    }
+};
+
 // J: coalesced stores of a CTA's lines from the FP64 results in the windows (rows j and
 // j + HM of a lane as the double2 over its work pair j: row q of chunk t is double
 // 2 (q % HM) + q / HM of its lane); strided lines by pairs, as staged.  An output longer than
@@ -338,12 +361,20 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
         }
     }
     // ---- D: log-step scan of the chunk transfers (then the ring wrap) ----
-    for (int k = 0; k < cp.nsteps; k++) {
+    ScanCoefs<Q> fsc;
+    {
+        unsigned take = 0;  // steps k with t >= 2^k
+        for (int k = 0; k < kMaxSteps; k++) take |= (t >= (1 << k) ? 1u : 0u) << k;
+        fsc.load(cp.fscan, t, 0, cp.nsteps, take);
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxSteps; k++) {
+        if (k >= cp.nsteps) break;
         const unsigned dlt = 1u << k;
         const V o1 = AR::shfl_up(s1, dlt, Pp);
         const V o2 = (Q == 2) ? AR::shfl_up(s2, dlt, Pp) : AR::zero();
         if (t >= (int)dlt) {
-            const F2* Fm = cp.fscan + ((size_t)t * kMaxSteps + k) * 4;
+            const F2* Fm = fsc.m[k];
             if constexpr (Q == 2) {
                 const V n1 = AR::mac2(s1, AR::coef(Fm[0]), o1, AR::coef(Fm[1]), o2);
                 const V n2 = AR::mac2(s2, AR::coef(Fm[2]), o1, AR::coef(Fm[3]), o2);
@@ -421,12 +452,20 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
         }
     }
     // ---- G: reverse scan (then the ring wrap) ----
-    for (int k = 0; k < cp.nsteps; k++) {
+    ScanCoefs<Q> bsc;
+    {
+        unsigned take = 0;  // steps k with t + 2^k < Pp
+        for (int k = 0; k < kMaxSteps; k++) take |= (t + (1 << k) < Pp ? 1u : 0u) << k;
+        bsc.load(cp.bscan, t, 0, cp.nsteps, take);
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxSteps; k++) {
+        if (k >= cp.nsteps) break;
         const unsigned dlt = 1u << k;
         const V o1 = AR::shfl_down(u1, dlt, Pp);
         const V o2 = (Q == 2) ? AR::shfl_down(u2, dlt, Pp) : AR::zero();
         if (t + (int)dlt < Pp) {
-            const F2* Bm = cp.bscan + ((size_t)t * kMaxSteps + k) * 4;
+            const F2* Bm = bsc.m[k];
             if constexpr (Q == 2) {
                 const V n1 = AR::mac2(u1, AR::coef(Bm[0]), o1, AR::coef(Bm[1]), o2);
                 const V n2 = AR::mac2(u2, AR::coef(Bm[2]), o1, AR::coef(Bm[3]), o2);
@@ -743,8 +782,14 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     // ---- D: the plan's scan over 16-row chunks; step 0 (chunk 2t + 1 after chunk 2t) in the lane ----
     const dfv yA15 = d2_x(S1), yA14 = d2_x(S2);
     V s1, s2 = AR::zero();
+    ScanCoefs<Q> fsc;
     {
-        const F2* Fm = cp.fscan + ((size_t)(2 * t + 1) * kMaxSteps) * 4;
+        unsigned take = 1u;  // step 0 in the lane, steps k >= 1 with t >= 2^(k-1)
+        for (int k = 1; k < kMaxSteps; k++) take |= (t >= (1 << (k - 1)) ? 1u : 0u) << k;
+        fsc.load(cp.fscan, 2 * t + 1, 0, cp.nsteps, take);
+    }
+    {
+        const F2* Fm = fsc.m[0];
         if constexpr (Q == 2) {
             s1 = AR::mac2(d2_y(S1), AR::coef(Fm[0]), yA15, AR::coef(Fm[1]), yA14);
             s2 = AR::mac2(d2_y(S2), AR::coef(Fm[2]), yA15, AR::coef(Fm[3]), yA14);
@@ -752,12 +797,14 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
             s1 = AR::mac1(d2_y(S1), AR::coef(Fm[0]), yA15);
         }
     }
-    for (int k = 1; k < cp.nsteps; k++) {
+#pragma unroll
+    for (int k = 1; k < kMaxSteps; k++) {
+        if (k >= cp.nsteps) break;
         const unsigned dlt = 1u << (k - 1);
         const V o1 = AR::shfl_up(s1, dlt, PLp);
         const V o2 = (Q == 2) ? AR::shfl_up(s2, dlt, PLp) : AR::zero();
         if (t >= (int)dlt) {
-            const F2* Fm = cp.fscan + ((size_t)(2 * t + 1) * kMaxSteps + k) * 4;
+            const F2* Fm = fsc.m[k];
             if constexpr (Q == 2) {
                 const V n1 = AR::mac2(s1, AR::coef(Fm[0]), o1, AR::coef(Fm[1]), o2);
                 const V n2 = AR::mac2(s2, AR::coef(Fm[2]), o1, AR::coef(Fm[3]), o2);
@@ -803,8 +850,14 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     // ---- G: the plan's reverse scan; step 0 (chunk 2t before chunk 2t + 1) in the lane ----
     const dfv xB0 = d2_y(U1), xB1 = d2_y(U2);
     V u1, u2 = AR::zero();
+    ScanCoefs<Q> bsc;
     {
-        const F2* Bm = cp.bscan + ((size_t)(2 * t) * kMaxSteps) * 4;
+        unsigned take = 1u;  // step 0 in the lane, steps k >= 1 with t + 2^(k-1) < PLp
+        for (int k = 1; k < kMaxSteps; k++) take |= (t + (1 << (k - 1)) < PLp ? 1u : 0u) << k;
+        bsc.load(cp.bscan, 2 * t, 0, cp.nsteps, take);
+    }
+    {
+        const F2* Bm = bsc.m[0];
         if constexpr (Q == 2) {
             u1 = AR::mac2(d2_x(U1), AR::coef(Bm[0]), xB0, AR::coef(Bm[1]), xB1);
             u2 = AR::mac2(d2_x(U2), AR::coef(Bm[2]), xB0, AR::coef(Bm[3]), xB1);
@@ -812,12 +865,14 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
             u1 = AR::mac1(d2_x(U1), AR::coef(Bm[0]), xB0);
         }
     }
-    for (int k = 1; k < cp.nsteps; k++) {
+#pragma unroll
+    for (int k = 1; k < kMaxSteps; k++) {
+        if (k >= cp.nsteps) break;
         const unsigned dlt = 1u << (k - 1);
         const V o1 = AR::shfl_down(u1, dlt, PLp);
         const V o2 = (Q == 2) ? AR::shfl_down(u2, dlt, PLp) : AR::zero();
         if (t + (int)dlt < PLp) {
-            const F2* Bm = cp.bscan + ((size_t)(2 * t) * kMaxSteps + k) * 4;
+            const F2* Bm = bsc.m[k];
             if constexpr (Q == 2) {
                 const V n1 = AR::mac2(u1, AR::coef(Bm[0]), o1, AR::coef(Bm[1]), o2);
                 const V n2 = AR::mac2(u2, AR::coef(Bm[2]), o1, AR::coef(Bm[3]), o2);
