@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
     // ---- E+F: forward correction and backward recurrence of both halves from zero states ----
     df2 U1 = d2_zero(), U2 = d2_zero();
     if (active) {
-#pragma unroll 4
+#pragma unroll 2
         for (int j = HM - 1; j >= 0; j--) {
             const df2 p1 = d2_of(ctab[j]);
             const df2 w = d2_of(wp[j - H]);
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
         double2* wd = reinterpret_cast<double2*>(wp - H);
         if (kl >= -800 && kl <= 800) {
             const unsigned kadd = (unsigned)(896 + kl) << 20;
-#pragma unroll 4
+#pragma unroll 2
             for (int j = 0; j < HM; j++) {
                 const int d = HM - 1 - j;
                 const df2 w = d2_of(wp[j - H]);
@@ -838,7 +838,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
     // ---- E+F: forward correction and backward recurrence of both halves ----
     df2 U1 = d2_zero(), U2 = d2_zero();
     if (active) {
-#pragma unroll 4
+#pragma unroll 2
         for (int j = HM - 1; j >= 0; j--) {
             const df2 w = d2_of(wp[j - H]);
             const df2 y = (Q == 2) ? d2_mac2(w, tab(5, j), I1, tab(6, j), I2) : d2_mac1(w, tab(5, j), I1);
@@ -909,7 +909,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
         double2* wd = reinterpret_cast<double2*>(wp - H);
         if (kl >= -800 && kl <= 800) {
             const unsigned kadd = (unsigned)(896 + kl) << 20;
-#pragma unroll 4
+#pragma unroll 2
             for (int j = 0; j < HM; j++) {
                 const df2 w = d2_of(wp[j - H]);
                 const df2 x = (Q == 2) ? d2_mac2(w, tab(7, j), J1, tab(8, j), J2) : d2_mac1(w, tab(7, j), J1);
