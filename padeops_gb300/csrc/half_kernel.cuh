@@ -140,7 +140,10 @@ __device__ __forceinline__ void half_store(const float4* tile, int LT, int SL, i
             }
         }
     } else {
+        // row offsets in 32 bits (the launchers check that they fit)
         const int ll = tid % L, pstep = nth / L, k0 = tid / L, nk = ns >> 1;
+        const int fs = (int)ls.fp, os = (int)ls.op;
+        (void)fs;
         if (ll < nl) {
             double* o = out + base_out[ll];
             const double2* od2 = reinterpret_cast<const double2*>(tile) + (size_t)ll * LT;
@@ -152,7 +155,7 @@ __device__ __forceinline__ void half_store(const float4* tile, int LT, int SL, i
                 for (int i = 0; i < HM; i++) {
                     const int k = k0 + pstep * i;
                     const int p = (k / HM) * M + k % HM;
-                    fv[i] = k < nk ? make_double2(fi[(long)p * ls.fp], fi[(long)(p + HM) * ls.fp])
+                    fv[i] = k < nk ? make_double2(fi[p * fs], fi[(p + HM) * fs])
                                    : make_double2(0.0, 0.0);
                 }
 #pragma unroll
@@ -161,18 +164,18 @@ __device__ __forceinline__ void half_store(const float4* tile, int LT, int SL, i
                     if (k < nk) {
                         const int p = (k / HM) * M + k % HM;
                         const double2 x = od2[(k / HM) * SL + k % HM];
-                        o[(long)p * ls.op] = __dsub_rn(fv[i].x, x.x);
-                        o[(long)(p + HM) * ls.op] = __dsub_rn(fv[i].y, x.y);
+                        o[p * os] = __dsub_rn(fv[i].x, x.x);
+                        o[(p + HM) * os] = __dsub_rn(fv[i].y, x.y);
                     }
                 }
             } else {
                 for (int k = k0; k < nk; k += pstep) {
                     const int p = (k / HM) * M + k % HM;
                     const double2 x = od2[(k / HM) * SL + k % HM];
-                    o[(long)p * ls.op] = x.x;
-                    o[(long)(p + HM) * ls.op] = x.y;
+                    o[p * os] = x.x;
+                    o[(p + HM) * os] = x.y;
                 }
-                for (int p = ns + k0; p < nout; p += pstep) o[(long)p * ls.op] = od[out_pos(ll, p - ns)];
+                for (int p = ns + k0; p < nout; p += pstep) o[p * os] = od[out_pos(ll, p - ns)];
             }
         }
     }
@@ -261,6 +264,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
         const int pstep = nth / L;
         const int nk = ns >> 1;
         const int l = tid % L, q0 = tid / L;
+        const int fs = (int)ls.fp;  // row offsets in 32 bits (the launchers check that they fit)
         double v[M];
         int mx = 0;
         if (l < nl) {
@@ -270,8 +274,8 @@ __global__ void __launch_bounds__(kLineThreadsCirc, M == 32 ? 4 : 5)
                 const int k = q0 + pstep * i;
                 const int p = (k / HM) * M + k % HM;
                 const bool ok = k < nk;
-                v[2 * i] = ok ? __ldg(src + (long)p * ls.fp) : 0.0;
-                v[2 * i + 1] = ok ? __ldg(src + (long)(p + HM) * ls.fp) : 0.0;
+                v[2 * i] = ok ? __ldg(src + p * fs) : 0.0;
+                v[2 * i + 1] = ok ? __ldg(src + (p + HM) * fs) : 0.0;
                 mx = max(mx, max(bexp(v[2 * i]), bexp(v[2 * i + 1])));
             }
             atomicMax(&lexp[l], mx);
@@ -667,6 +671,7 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
         const int pstep = nth / L;
         const int nk = ns >> 1;
         const int l = tid % L, q0 = tid / L;
+        const int fs = (int)ls.fp;  // row offsets in 32 bits (the launchers check that they fit)
         double v[M];
         int mx = 0;
         if (l < nl) {
@@ -676,8 +681,8 @@ __global__ void __launch_bounds__(kLineThreadsCirc, 4)
                 const int k = q0 + pstep * i;
                 const int p = (k / HM) * M + k % HM;
                 const bool ok = k < nk;
-                v[2 * i] = ok ? __ldg(src + (long)p * ls.fp) : 0.0;
-                v[2 * i + 1] = ok ? __ldg(src + (long)(p + HM) * ls.fp) : 0.0;
+                v[2 * i] = ok ? __ldg(src + p * fs) : 0.0;
+                v[2 * i + 1] = ok ? __ldg(src + (p + HM) * fs) : 0.0;
                 mx = max(mx, max(bexp(v[2 * i]), bexp(v[2 * i + 1])));
             }
             atomicMax(&lexp[l], mx);

@@ -1,4 +1,7 @@
 // Instantiations of the half-chunk line kernel (half_kernel.cuh) and its dispatcher.
+#include <algorithm>
+#include <cstdlib>
+
 #include "half_kernel.cuh"
 
 namespace pade {
@@ -29,8 +32,16 @@ static int launch_half_m(int shape, const StencilParams& c, const void* f, void*
     return PS_ENOTSUP;
 }
 
+// The half-chunk kernels address the rows of strided lines with 32-bit offsets.
+static bool half_offsets_fit(const StencilParams& c, const LineSet& ls) {
+    const long rows = (long)std::max(c.ns, c.nout) + 1;
+    const long st = std::max(std::labs(ls.fp), std::labs(ls.op));
+    return rows * st <= 2147483647L;
+}
+
 int launch_line_half(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                      unsigned* status, cudaStream_t s) {
+    if (!half_offsets_fit(c, ls)) return PS_ENOTSUP;
     const bool stagg = shape >= SHAPE_T2A_E2C && shape <= SHAPE_T2S_C2E;
     if (!c.circ || (c.M != 32 && c.M != 16) || (c.xdup && !(shape == SHAPE_T2A_E2C || shape == SHAPE_T2S_E2C)) ||
         c.ns % c.M != 0 || c.L < 1 || (stagg && c.M != 32))
@@ -50,6 +61,7 @@ int launch_line_half(int shape, const StencilParams& c, const void* f, void* out
 // passed the plan's interior check (hpair set).
 int launch_line_half_band(int shape, const StencilParams& c, const void* f, void* out, const LineSet& ls,
                           unsigned* status, cudaStream_t s) {
+    if (!half_offsets_fit(c, ls)) return PS_ENOTSUP;
     if (c.circ || c.M != 16 || !c.hpair || c.hnf < 1 || c.hnf > 3 || c.ns % 32 != 0 || c.nout != c.ns || c.L < 1 ||
         c.nlo > 16 || c.nhi > 16)
         return PS_ENOTSUP;
