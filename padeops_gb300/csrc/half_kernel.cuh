@@ -122,11 +122,12 @@ __device__ __forceinline__ void half_store(const float4* tile, int LT, int SL, i
             double* o = out + base_out[ll];
             if constexpr (RESID) {
                 const double* fi = f + base_in[ll];
+                const int fs = (int)ls.fp;  // 32-bit row offsets (the launchers check that they fit)
                 double fv[kHalfRowsContig];
 #pragma unroll
                 for (int u = 0; u < kHalfRowsContig; u++) {
                     const int p = lane + 32 * u;
-                    fv[u] = p < ns ? fi[(long)p * ls.fp] : 0.0;
+                    fv[u] = p < ns ? fi[p * fs] : 0.0;
                 }
 #pragma unroll
                 for (int u = 0; u < kHalfRowsContig; u++) {
@@ -134,7 +135,7 @@ __device__ __forceinline__ void half_store(const float4* tile, int LT, int SL, i
                     if (p < ns) o[p] = __dsub_rn(fv[u], od[out_pos(ll, p)]);
                 }
                 for (int p = lane + 32 * kHalfRowsContig; p < ns; p += 32)
-                    o[p] = __dsub_rn(fi[(long)p * ls.fp], od[out_pos(ll, p)]);
+                    o[p] = __dsub_rn(fi[p * fs], od[out_pos(ll, p)]);
             } else {
                 for (int p = lane; p < nout; p += 32) o[p] = od[out_pos(ll, p < ns ? p : p - ns)];
             }
