@@ -580,9 +580,9 @@ int launch_lhalf_t(const StencilParams& c, const void* f, void* out, const LineS
 // table's largest value (far below the double-float representation) and ships NF + 2 blocks
 // in pair layout: the NF leading lanes' rows, the last lane's and the interior pattern,
 // {h(row j), h(row 16 + j), l(row j), l(row 16 + j)} per table and j; 2.3 KB each in shared
-// memory instead of 18 KB of per-row tables, which did not fit beside the windows.  The edge rows (one-sided closures) are summed in FP64 from
-// the FP64 input as in k_line and replace the stencil in their component; halo rows beyond
-// the line ends are zero.
+// memory instead of 18 KB of per-row tables, which did not fit beside the windows.  The edge
+// rows (one-sided closures) are summed in FP64 from the FP64 input as in k_line and replace
+// the stencil in their component; halo rows beyond the line ends are zero.
 // ------------------------------------------------------------------------------------
 constexpr int kHalf = 16;  // rows per half of a 32-row chunk
 constexpr int kHalfBandTables = 9;
